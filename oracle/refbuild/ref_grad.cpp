@@ -1,0 +1,96 @@
+// Oracle driver around the reference trainer's model (test infrastructure only).
+//
+// Usage: ref-grad MODEL CFG [WEIGHTS]
+//   Prints, as one JSON object per line:
+//     {"coeffs": [...]}                               MLMTPR::Coeff() (the trained parameter vector)
+//     {"cfg": c, "energy": E, "forces": [...], "stresses": [[...]], "site_energies": [...]}
+//                                                     from MLMTPR::CalcEFS (dev_src/mtpr.cpp:8779)
+//     {"cfg": c, "grad": [...]}                       AccumulateEFSCombinationGrad
+//                                                     (src/basic_mlip.cpp:421, dev_src/mtpr.cpp:9188)
+//
+// Usage: ref-grad --write MODEL OUT VALUES
+//   Loads MODEL, replaces its parameter vector by the whitespace-separated VALUES (same length
+//   and order as Coeff()), and saves it with MLMTPR::Save, so that the written .sus2 is in the
+//   reference's own serialisation.
+//
+//   WEIGHTS holds, per configuration, "n" then n rows "ene_w fx fy fz" then 3 rows of the
+//   3x3 stress weight; the gradient is accumulated from zero for each configuration.
+#include "mtpr.h"
+#include "configuration.h"
+#include <cstdio>
+#include <string>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+static void vec(const double* v, int n) {
+  std::printf("[");
+  for (int i = 0; i < n; ++i) std::printf(i ? ",%.17g" : "%.17g", v[i]);
+  std::printf("]");
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) { std::fprintf(stderr, "usage: ref-grad MODEL CFG [WEIGHTS]\n"); return 2; }
+  try {
+  if (std::string(argv[1]) == "--write") {
+    if (argc != 5) { std::fprintf(stderr, "usage: ref-grad --write MODEL OUT VALUES\n"); return 2; }
+    MLMTPR mtpr(argv[2]);
+    std::ifstream vf(argv[4]);
+    std::vector<double> v;
+    double x;
+    while (vf >> x) v.push_back(x);
+    if ((int)v.size() != mtpr.CoeffCount()) { std::fprintf(stderr, "expected %d values, got %zu\n", mtpr.CoeffCount(), v.size()); return 3; }
+    for (int i = 0; i < mtpr.CoeffCount(); ++i) mtpr.Coeff()[i] = v[i];
+    mtpr.DistributeCoeffs();
+    mtpr.Save(argv[3]);
+    return 0;
+  }
+  MLMTPR mtpr(argv[1]);
+  std::printf("{\"coeffs\": ");
+  vec(mtpr.Coeff(), mtpr.CoeffCount());
+  std::printf("}\n");
+  std::ifstream in(argv[2]);
+  std::ifstream wf;
+  if (argc > 3) wf.open(argv[3]);
+  Configuration cfg;
+  int c = 0;
+  while (cfg.Load(in)) {
+    Configuration eval = cfg;
+    mtpr.CalcEFS(eval);
+    const int n = eval.size();
+    std::printf("{\"cfg\": %d, \"energy\": %.17g, \"forces\": [", c, eval.energy);
+    for (int i = 0; i < n; ++i) {
+      if (i) std::printf(",");
+      double f[3] = {eval.force(i)[0], eval.force(i)[1], eval.force(i)[2]};
+      vec(f, 3);
+    }
+    std::printf("], \"stresses\": [");
+    for (int a = 0; a < 3; ++a) {
+      if (a) std::printf(",");
+      double s[3] = {eval.stresses[a][0], eval.stresses[a][1], eval.stresses[a][2]};
+      vec(s, 3);
+    }
+    std::printf("], \"site_energies\": ");
+    vec(eval.cal_se.data(), (int)eval.cal_se.size());
+    std::printf("}\n");
+    if (wf.is_open()) {
+      int m = 0;
+      wf >> m;
+      if (m != n) { std::fprintf(stderr, "weights size mismatch\n"); return 3; }
+      std::vector<double> ew(n);
+      std::vector<Vector3> fw(n);
+      Matrix3 sw;
+      for (int i = 0; i < n; ++i) wf >> ew[i] >> fw[i][0] >> fw[i][1] >> fw[i][2];
+      for (int a = 0; a < 3; ++a) for (int b = 0; b < 3; ++b) wf >> sw[a][b];
+      std::vector<double> grad(mtpr.CoeffCount(), 0.0);
+      Configuration g = cfg;
+      mtpr.AccumulateEFSCombinationGrad(g, ew, fw, sw, grad);
+      std::printf("{\"cfg\": %d, \"grad\": ", c);
+      vec(grad.data(), (int)grad.size());
+      std::printf("}\n");
+    }
+    ++c;
+  }
+  } catch (const MlipException& e) { std::fprintf(stderr, "reference error: %s\n", e.What()); return 1; }
+  return 0;
+}

@@ -1,0 +1,202 @@
+#!/usr/bin/env python3
+"""Regenerate the committed golden fixtures from the reference implementation.
+
+Runs only where the reference checkout and its oracle builds exist
+(``make -C oracle ref REF=<reference>`` then ``make -C oracle _ref/ref-grad``).
+Everything it writes lands under ``tests/golden/``; the tests and the GPU
+checks read those files and never the reference itself.
+
+Outputs
+  two_cutoff/        the reference's own FP64 two-cutoff fixtures, copied byte for byte
+                     (interfaces/lammps/tests/fixtures/two_cutoff/{fixtures_v2,fixtures_hi_l})
+  models/*.sus2      benchmark topologies written by the reference's ``init-sh`` (grouped YAML
+                     front end, src/mlp/grouped_input.cpp) with seeded parameters
+                     (superlinear_gb300.synth.random_vector) and checked to load back
+                     bit-exactly through the reference trainer
+  frames/*.cfg       seeded geometries
+  efs/*.json         E / F / virial / site energies from the reference embedded engine
+                     (interfaces/lammps/tests/embedded_efs.cpp, one domain)
+  grad/*.json        dTheta of sum_i eW_i E_i + sum_e w_e . dE/dd_e from the reference trainer's
+                     AccumulateEFSCombinationGrad (src/basic_mlip.cpp:421, dev_src/mtpr.cpp:9188)
+                     for seeded random weights, plus the trainer's own CalcEFS
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from superlinear_gb300.sus2_format import read_sus2, write_sus2  # noqa: E402
+from superlinear_gb300.synth import (diamond, fields_to_vector, random_vector,  # noqa: E402
+                                     training_frames, vector_to_fields, write_cfg, lattice_frame)
+
+# (name, yaml model block, (parameter seed, radial scale, readout scale))
+MODELS = {
+    "static_l3k4o2": ("static-radial", dict(elements="[C]", l_max=3, radial_channels=4, neighbor_cutoff=5.0,
+                      interaction=dict(channels=2, body_order=4, channel_coupling="cross")), (11, 3.0, 5.0)),
+    "effect_l3k4r2o2": ("coordination-effect", dict(species_count=2, l_max=3, radial_channels=4, neighbor_cutoff=5.0,
+                        coordination=dict(channels=2, body_order=4, channel_coupling="cross"),
+                        interaction=dict(channels=2, body_order=4, channel_coupling="diagonal")), (12, 5.0, 8.0)),
+    "effect_l4k8r2o3": ("coordination-effect", dict(species_count=2, l_max=4, radial_channels=8, neighbor_cutoff=5.5,
+                        coordination=dict(channels=2, body_order=4, channel_coupling="cross"),
+                        interaction=dict(channels=3, body_order=4, channel_coupling="diagonal")), (13, 3.0, 8.0)),
+    # small two-species Static model used by the fast tests
+    "static_l2k3o2_c2": ("static-radial", dict(species_count=2, l_max=2, radial_channels=3, neighbor_cutoff=4.5,
+                         interaction=dict(channels=2, body_order=4, channel_coupling="cross")), (14, 5.0, 20.0)),
+}
+
+
+def yaml_for(kind, spec, out):
+    lines = ["schema_version: 1", "model:", f"  kind: {kind}"]
+    for key in ("elements", "species_count", "l_max", "radial_channels", "neighbor_cutoff"):
+        if key in spec:
+            lines.append(f"  {key}: {spec[key]}")
+    lines += ["  radial:", "    basis: chebyshev-sss", "    basis_size: 8", "    warp_sharing: K"]
+    for group in ("coordination", "interaction"):
+        if group in spec:
+            lines.append(f"  {group}:")
+            lines += [f"    {k}: {v}" for k, v in spec[group].items()]
+    lines += ["  readout:", "    element_mode: per-element", "output:", f"  model: {out}"]
+    return "\n".join(lines) + "\n"
+
+
+def run(cmd, **kw):
+    r = subprocess.run(cmd, capture_output=True, text=True, **kw)
+    if r.returncode:
+        raise RuntimeError(f"{cmd[0]} failed: {r.stderr[-2000:]}")
+    return r.stdout
+
+
+def frames_for(name):
+    """Seeded geometries per model: (label, [frames])."""
+    if name == "static_l3k4o2":
+        return [("diamond64_s05", [diamond(2, sigma=0.05, seed=101)]),
+                ("diamond64_s15", [diamond(2, sigma=0.15, seed=102)])]
+    if name == "static_l2k3o2_c2":
+        rng = np.random.default_rng(103)
+        return [("mixed", [lattice_frame("fcc", (2, 2, 1), 3.4, 0.12, rng, type_prob=0.5, species=2),
+                           lattice_frame("bcc", (2, 2, 2), 2.9, 0.12, rng, type_prob=0.5, species=2)])]
+    if name == "effect_l3k4r2o2":
+        return [("train4", training_frames(4, 8, 64, 3.0, 4.2, 0.1, seed=104, species=2))]
+    if name == "effect_l4k8r2o3":
+        return [("diamond64_c2", [diamond(2, sigma=0.1, seed=105, species=2, type_prob=0.5)])]
+    raise KeyError(name)
+
+
+def weights_for(frames, seed):
+    """Seeded loss-derivative weights (per-atom energy weight, per-atom force weight, 3x3 stress)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for fr in frames:
+        n = fr.natoms
+        ew = np.full(n, rng.uniform(0.5, 1.5))
+        fw = rng.normal(0, 1.0, (n, 3))
+        sw = rng.normal(0, 0.2, (3, 3))
+        out.append((ew, fw, sw))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--reference", default=os.environ.get("SUS2_REFERENCE", "/root/reference"))
+    ap.add_argument("--oracle", default=os.path.join(REPO, "oracle", "_ref"))
+    args = ap.parse_args()
+    emb = os.path.join(args.oracle, "embedded-efs")
+    mlp = os.path.join(args.oracle, "mlp-sus2")
+    refgrad = os.path.join(args.oracle, "ref-grad")
+    for tool in (emb, mlp, refgrad):
+        if not os.path.exists(tool):
+            sys.exit(f"missing {tool}: build it with make -C oracle ref _ref/ref-grad")
+
+    # 1. the reference's own golden fixtures
+    src = os.path.join(args.reference, "interfaces/lammps/tests/fixtures/two_cutoff")
+    dst = os.path.join(HERE, "two_cutoff")
+    manifest = {}
+    for sub in ("fixtures_v2", "fixtures_hi_l"):
+        os.makedirs(os.path.join(dst, sub), exist_ok=True)
+        for fn in sorted(os.listdir(os.path.join(src, sub))):
+            if fn.startswith("adaptive"):
+                continue  # Adaptive family is outside this path
+            shutil.copyfile(os.path.join(src, sub, fn), os.path.join(dst, sub, fn))
+            manifest[f"{sub}/{fn}"] = hashlib.sha256(open(os.path.join(dst, sub, fn), "rb").read()).hexdigest()
+
+    for sub in ("models", "frames", "efs", "grad"):
+        os.makedirs(os.path.join(HERE, sub), exist_ok=True)
+
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, (kind, spec, (seed, rscale, oscale)) in MODELS.items():
+            ypath = os.path.join(tmp, f"{name}.yaml")
+            topo = os.path.join(tmp, f"{name}.sus2")
+            with open(ypath, "w") as fh:
+                fh.write(yaml_for(kind, spec, f"{name}.sus2"))
+            run([mlp, "init-sh", ypath], cwd=tmp)
+            # 2. parameters: reference Save of the topology, then our seeded vector, then verify
+            fields = read_sus2(topo)
+            vec = random_vector(fields, seed, rscale, oscale)
+            vfile = os.path.join(tmp, "v.txt")
+            np.savetxt(vfile, vec)
+            saved = os.path.join(tmp, f"{name}_saved.sus2")
+            run([refgrad, "--write", topo, saved, vfile])
+            fields = read_sus2(saved)
+            vector_to_fields(fields, vec)
+            model = os.path.join(HERE, "models", f"{name}.sus2")
+            write_sus2(model, fields)
+            back = json.loads(run([refgrad, model, "/dev/null"]).splitlines()[0])["coeffs"]
+            assert np.array_equal(np.asarray(back), vec), f"{name}: reference did not load the written vector"
+            assert np.array_equal(fields_to_vector(read_sus2(model)), vec)
+            manifest[f"models/{name}.sus2"] = hashlib.sha256(open(model, "rb").read()).hexdigest()
+
+            for label, frames in frames_for(name):
+                cfg = os.path.join(HERE, "frames", f"{name}__{label}.cfg")
+                write_cfg(cfg, frames)
+                # 3. embedded engine E/F/virial, one frame at a time
+                records = []
+                for k, fr in enumerate(frames):
+                    one = os.path.join(tmp, "one.cfg")
+                    write_cfg(one, [fr])
+                    out = run([emb, model, one, "1", "direct"])
+                    line = next(l for l in out.splitlines() if l.startswith("NATIVE_EFS_JSON"))
+                    rec = json.loads(line.split(" ", 1)[1])
+                    rec["config"] = k
+                    records.append(rec)
+                with open(os.path.join(HERE, "efs", f"{name}__{label}.json"), "w") as fh:
+                    json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
+                               "source": "reference embedded engine (embedded_efs.cpp, domains=1, direct)",
+                               "records": records}, fh)
+                # 4. trainer gradient for seeded weights
+                wts = weights_for(frames, seed + 1000)
+                wfile = os.path.join(tmp, "w.txt")
+                with open(wfile, "w") as fh:
+                    for ew, fw, sw in wts:
+                        fh.write(f"{len(ew)}\n")
+                        for i in range(len(ew)):
+                            fh.write("%.17g %.17g %.17g %.17g\n" % (ew[i], *fw[i]))
+                        for row in sw:
+                            fh.write("%.17g %.17g %.17g\n" % tuple(row))
+                lines = [json.loads(l) for l in run([refgrad, model, cfg, wfile]).splitlines()]
+                efs = [l for l in lines if "energy" in l]
+                grads = [l["grad"] for l in lines if "grad" in l]
+                with open(os.path.join(HERE, "grad", f"{name}__{label}.json"), "w") as fh:
+                    json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
+                               "source": "reference trainer MLMTPR::CalcEFS + AccumulateEFSCombinationGrad",
+                               "weights": [{"energy": ew.tolist(), "force": fw.tolist(), "stress": sw.tolist()}
+                                           for ew, fw, sw in wts],
+                               "trainer_efs": efs, "grad": grads}, fh)
+                print(name, label, "frames", len(frames), "atoms", [f.natoms for f in frames])
+    with open(os.path.join(HERE, "manifest.json"), "w") as fh:
+        json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()
