@@ -1,0 +1,95 @@
+/*
+ * sus2g.h -- C ABI of the GB300 SUS2-SH descriptor -> energy -> force / virial / parameter-gradient
+ * engine.  Plain pointers and sizes only; every function returns 0 on success or a positive error
+ * code, with the message available from sus2g_last_error() (thread-local).  No C++ exceptions
+ * cross this boundary (the reference converts its exceptions to LAMMPS errors at the same seam,
+ * interfaces/lammps/ML-SUS2/pair_sus2_embedded.cpp:311-313).
+ *
+ * Reference interfaces each entry point replaces are cited as file:line within the reference
+ * project (hu-yanxiao/superlinear).
+ *
+ * Units are the reference's (metal): A, eV, eV/A; virial components are ordered
+ * (xx, yy, zz, xy, xz, yz) and equal the reference's plus_stress / Result::virial
+ * (sus2_sl_kernel.cpp:545-546): W = -sum_edges d (x) dE/dd.
+ */
+#ifndef SUS2G_H
+#define SUS2G_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SUS2G_FP64 0 /* plain FP64 evaluation */
+#define SUS2G_FP32 1 /* FP32 bulk (radial, Y_lm, moments, contractions) with FP64 reductions */
+
+typedef struct sus2g_model_s* sus2g_model;
+typedef struct sus2g_engine_s* sus2g_engine;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* sus2g_last_error(void);
+/* ABI version (major * 100 + minor). */
+int sus2g_abi_version(void);
+
+/* ---- model (.sus2) --------------------------------------------------------------------------
+ * Replaces LAMMPS_NS::SUS2SL::Model::load + Model::validate
+ * (interfaces/lammps/ML-SUS2/sus2_sl_model.cpp:174-257, 258-453) and the trainer's
+ * MLMTPR::Load (dev_src/mtpr.cpp:4490) for the Static and Effect families. */
+int sus2g_model_load(const char* path, sus2g_model* out);
+void sus2g_model_free(sus2g_model model);
+/* dims[16] = {species C, l_max L, k_max K, basis B, radial funcs F, moments M, basics NB,
+ *             products P, scalars S, gate scalars Q, gated, param count, outer rank, gate rank,
+ *             split cutoff, 0}.
+ * Replaces the Model / Kernel dimension accessors (sus2_sl_model.h:13-18, sus2_sl_kernel.h:24-31). */
+int sus2g_model_dims(sus2g_model model, int* dims16);
+/* Neighbour cutoff max_dist (Model::cutoff, sus2_sl_model.cpp:154-159; ZBL is outside this path). */
+int sus2g_model_cutoff(sus2g_model model, double* cutoff);
+/* Trainable parameter vector in the reference trainer's order
+ * (MLMTPR::CoeffCount / Coeff, dev_src/mtpr.h:1340-1347; layout DistributeCoeffs, :1358-1470). */
+int sus2g_model_param_count(sus2g_model model, int* count);
+int sus2g_model_get_params(sus2g_model model, double* out, int n);
+int sus2g_model_set_params(sus2g_model model, const double* in, int n);
+
+/* ---- engine -----------------------------------------------------------------------------------
+ * Replaces SUS2SL::Kernel(const Model&) (sus2_sl_kernel.cpp:45-106): binds a model to one CUDA
+ * device in FP64 (SUS2G_FP64) or FP32-bulk (SUS2G_FP32) form.  The engine snapshots the model's
+ * parameters; call sus2g_engine_update_params after sus2g_model_set_params. */
+int sus2g_engine_create(sus2g_model model, int device, int precision, sus2g_engine* out);
+void sus2g_engine_free(sus2g_engine engine);
+int sus2g_engine_update_params(sus2g_engine engine, sus2g_model model);
+/* Use a caller CUDA stream (cudaStream_t passed as void*; NULL restores the engine's own). */
+int sus2g_engine_set_stream(sus2g_engine engine, void* cuda_stream);
+/* Kernels launched by the engine since the last call to this function. */
+int sus2g_engine_take_launch_count(sus2g_engine engine, int* count);
+/* Number of directed edges of the last evaluation. */
+int sus2g_engine_edge_count(sus2g_engine engine, long long* count);
+
+/* ---- E / F / virial of periodic frames (trainer calc-efs path) ----------------------------------
+ * Replaces MLMTPR::CalcEFS(Configuration&) (dev_src/mtpr.cpp:8779-8956) including its
+ * Neighborhoods build (src/neighborhoods.cpp:358-415) for a batch of frames.
+ *   nframes, natoms[nframes]      frame sizes; atoms of all frames concatenated
+ *   cells[9*nframes]              host, rows are the lattice vectors (Configuration::lattice)
+ *   positions[3*N], types[N]      Cartesian positions (A) and species 0..C-1
+ *   energy[nframes], forces[3*N], virial[6*nframes], site_energy[N]   outputs (any may be NULL)
+ * _host: positions/types/outputs are host memory (copied inside the call, synchronous).
+ * _device: positions/types/outputs are device memory on the engine's stream (asynchronous). */
+int sus2g_calc_efs_host(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                        const double* positions, const int* types, double* energy, double* forces,
+                        double* virial, double* site_energy);
+int sus2g_calc_efs_device(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                          const double* positions, const int* types, double* energy, double* forces,
+                          double* virial, double* site_energy);
+
+/* ---- E / F / virial of a caller edge list (pair_style sus2/embedded compute contract) ----------
+ * Replaces SUS2SL::Kernel::begin / outer / finish (sus2_sl_kernel.cpp:381-562) as called by
+ * PairSUS2Embedded::compute (pair_sus2_embedded.cpp:250-314) with a single domain: nowned centre
+ * atoms 0..nowned-1, nall >= nowned atoms in total, types[nall], directed edges (ei, ej, d = x_j - x_i).
+ * Outputs energy (sum of owned site energies), site_energy[nowned], forces[3*nall] (including
+ * ghost contributions, to be reverse-communicated by the caller), virial[6].  Host buffers. */
+int sus2g_efs_edges_host(sus2g_engine engine, int nowned, int nall, const int* types, int nedges,
+                         const int* ei, const int* ej, const double* d, double* energy, double* site_energy,
+                         double* forces, double* virial);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SUS2G_H */

@@ -1,0 +1,138 @@
+"""ctypes wrapper of the CPU FP64 oracle (``oracle/_build/libsus2_oracle.so``).
+
+TEST INFRASTRUCTURE ONLY: used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py`` as the checker / reported baseline.  The product path never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libsus2_oracle.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def build() -> str:
+    """Compile the oracle with the Makefile next to this file (g++, OpenMP)."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "port"], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        L.orc_load.restype = ctypes.c_void_p
+        L.orc_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int]
+        L.orc_free.argtypes = [ctypes.c_void_p]
+        L.orc_param_count.argtypes = [ctypes.c_void_p]
+        L.orc_get_params.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_set_params.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_efs.restype = ctypes.c_longlong
+        L.orc_efs.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_int,
+                              ctypes.c_char_p, ctypes.c_int]
+        L.orc_efs_edges.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp,
+                                    _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
+        L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
+                               ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class OracleModel:
+    """FP64 CPU evaluation of one ``.sus2`` model."""
+
+    def __init__(self, path: str):
+        err = ctypes.create_string_buffer(512)
+        self._h = lib().orc_load(path.encode(), err, 512)
+        if not self._h:
+            raise ValueError(err.value.decode())
+        self.nparams = lib().orc_param_count(self._h)
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_free(self._h)
+            self._h = None
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparams)
+        lib().orc_get_params(self._h, _d(out))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        assert p.size == self.nparams
+        lib().orc_set_params(self._h, _d(p))
+
+    def efs(self, cell, pos, types, threads: int = 1):
+        """One periodic frame -> (energy, forces[n,3], virial6, site[n], n_edges)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        n = types.size
+        e = np.zeros(1)
+        f = np.zeros((n, 3))
+        v = np.zeros(6)
+        s = np.zeros(n)
+        err = ctypes.create_string_buffer(512)
+        ne = lib().orc_efs(self._h, n, _d(cell), _d(pos), _i(types), _d(e), _d(f), _d(v), _d(s), threads, err, 512)
+        if ne < 0:
+            raise RuntimeError(err.value.decode())
+        return float(e[0]), f, v, s, int(ne)
+
+    def efs_edges(self, nowned, types, ei, ej, d):
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        ei = np.ascontiguousarray(ei, dtype=np.int32)
+        ej = np.ascontiguousarray(ej, dtype=np.int32)
+        d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1, 3)
+        nall = types.size
+        e = np.zeros(1)
+        f = np.zeros((nall, 3))
+        v = np.zeros(6)
+        s = np.zeros(nowned)
+        err = ctypes.create_string_buffer(512)
+        rc = lib().orc_efs_edges(self._h, nowned, nall, _i(types), ei.size, _i(ei), _i(ej), _d(d), _d(e), _d(f),
+                                 _d(v), _d(s), err, 512)
+        if rc:
+            raise RuntimeError(err.value.decode())
+        return float(e[0]), f, v, s
+
+    def grad(self, cell, pos, types, ew, fw, sw) -> np.ndarray:
+        """d/dtheta of sum_i ew_i E_i + sum_e (fw_i - fw_j + sw d_e) . dE/dd_e (one frame)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        ew = np.ascontiguousarray(ew, dtype=np.float64)
+        fw = np.ascontiguousarray(fw, dtype=np.float64).reshape(-1, 3)
+        sw = np.ascontiguousarray(sw, dtype=np.float64).reshape(9)
+        g = np.zeros(self.nparams)
+        err = ctypes.create_string_buffer(512)
+        if lib().orc_grad(self._h, types.size, _d(cell), _d(pos), _i(types), _d(ew), _d(fw), _d(sw), _d(g), err, 512):
+            raise RuntimeError(err.value.decode())
+        return g
+
+
+def virial6_to_matrix(v):
+    """(xx, yy, zz, xy, xz, yz) -> symmetric 3x3 (the reference harness's virial layout)."""
+    return np.array([[v[0], v[3], v[4]], [v[3], v[1], v[5]], [v[4], v[5], v[2]]])

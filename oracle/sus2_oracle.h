@@ -1,0 +1,35 @@
+/* CPU FP64 restatement of the SUS2-SH E / F / virial path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This is the oracle the GPU engine is checked against.  It is never linked into, loaded by or
+ * called from the product path; only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline use it.  It is pinned against the reference implementation through the committed
+ * golden fixtures in tests/golden/ (reference embedded engine and trainer outputs).
+ */
+#ifndef SUS2_ORACLE_H
+#define SUS2_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* Loads a .sus2 model; returns NULL and writes a message into err on failure. */
+void* orc_load(const char* path, char* err, int errlen);
+void orc_free(void* model);
+int orc_param_count(void* model);
+int orc_get_params(void* model, double* out);
+int orc_set_params(void* model, const double* in);
+/* One periodic frame: cell rows are lattice vectors.  Outputs energy, forces[3n], virial[6]
+ * (xx, yy, zz, xy, xz, yz), site energies[n] (any may be NULL).  threads <= 0: all cores.
+ * Returns the number of directed edges, or -1 on error (message in err). */
+long long orc_efs(void* model, int n, const double* cell, const double* pos, const int* types, double* energy,
+                  double* forces, double* virial, double* site, int threads, char* err, int errlen);
+/* Caller edge list (single domain, owned centres 0..nowned-1 of nall atoms). */
+int orc_efs_edges(void* model, int nowned, int nall, const int* types, int nedges, const int* ei, const int* ej,
+                  const double* d, double* energy, double* forces, double* virial, double* site, char* err, int errlen);
+/* Parameter gradient of  sum_i ew_i E_i + sum_i fw_i . F_i + sum_ab sw_ab S_ab  where F are forces and
+ * S = -sum_e d (x) dE/dd the 3x3 virial; accumulates into grad[param_count].  Uses the image-scan
+ * edges of one periodic frame.  Returns 0 or -1. */
+int orc_grad(void* model, int n, const double* cell, const double* pos, const int* types, const double* ew,
+             const double* fw, const double* sw, double* grad, char* err, int errlen);
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,239 @@
+// extern "C" boundary (include/sus2g.h): argument checks, host<->device staging, error codes.
+#include "../../include/sus2g.h"
+
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+#include "model.h"
+
+struct sus2g_model_s {
+  sus2g::Model model;
+};
+struct sus2g_engine_s {
+  std::unique_ptr<sus2g::Engine> engine;
+  int launches = 0;
+};
+
+namespace {
+thread_local std::string g_error;
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    g_error.clear();
+    return 0;
+  } catch (const sus2g::Error& e) {
+    g_error = e.what();
+    return e.code > 0 ? e.code : 1;
+  } catch (const std::bad_alloc&) {
+    g_error = "out of host memory";
+    return 9;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return 1;
+  }
+}
+
+void need(bool ok, const char* what) {
+  if (!ok) throw sus2g::Error(1, std::string("invalid argument: ") + what);
+}
+
+void cuda(cudaError_t e, const char* where) {
+  if (e != cudaSuccess) throw sus2g::Error(10, std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e));
+}
+
+// Device staging buffer owned by the call.
+struct Stage {
+  void* p = nullptr;
+  explicit Stage(size_t n) { if (n) cuda(cudaMalloc(&p, n), "staging allocation"); }
+  ~Stage() { if (p) cudaFree(p); }
+  template <typename T> T* as() { return static_cast<T*>(p); }
+};
+
+long long total_atoms(int nframes, const int* natoms) {
+  long long n = 0;
+  for (int f = 0; f < nframes; ++f) {
+    need(natoms[f] >= 0, "natoms must be non-negative");
+    n += natoms[f];
+  }
+  need(n < (1LL << 31), "too many atoms");
+  return n;
+}
+}  // namespace
+
+extern "C" {
+
+const char* sus2g_last_error(void) { return g_error.c_str(); }
+int sus2g_abi_version(void) { return 100; }
+
+int sus2g_model_load(const char* path, sus2g_model* out) {
+  return guarded([&] {
+    need(path && out, "path/out");
+    auto m = std::make_unique<sus2g_model_s>();
+    m->model.load(path);
+    *out = m.release();
+  });
+}
+
+void sus2g_model_free(sus2g_model model) { delete model; }
+
+int sus2g_model_dims(sus2g_model h, int* d) {
+  return guarded([&] {
+    need(h && d, "model/dims");
+    const auto& m = h->model;
+    const int v[16] = {m.C, m.L, m.K, m.B, m.F, m.M, m.NB, m.P, m.S, m.Q, m.gated ? 1 : 0, m.param_count(),
+                       m.outer_rank, m.gate_rank, m.split ? 1 : 0, 0};
+    std::memcpy(d, v, sizeof(v));
+  });
+}
+
+int sus2g_model_cutoff(sus2g_model h, double* c) {
+  return guarded([&] { need(h && c, "model/cutoff"); *c = h->model.max_dist; });
+}
+
+int sus2g_model_param_count(sus2g_model h, int* n) {
+  return guarded([&] { need(h && n, "model/count"); *n = h->model.param_count(); });
+}
+
+int sus2g_model_get_params(sus2g_model h, double* out, int n) {
+  return guarded([&] {
+    need(h && out, "model/out");
+    need(n == h->model.param_count(), "parameter count mismatch");
+    h->model.get_params(out);
+  });
+}
+
+int sus2g_model_set_params(sus2g_model h, const double* in, int n) {
+  return guarded([&] {
+    need(h && in, "model/in");
+    need(n == h->model.param_count(), "parameter count mismatch");
+    h->model.set_params(in);
+  });
+}
+
+int sus2g_engine_create(sus2g_model model, int device, int precision, sus2g_engine* out) {
+  return guarded([&] {
+    need(model && out, "model/out");
+    auto e = std::make_unique<sus2g_engine_s>();
+    e->engine = std::make_unique<sus2g::Engine>(model->model, device, precision);
+    *out = e.release();
+  });
+}
+
+void sus2g_engine_free(sus2g_engine e) { delete e; }
+
+int sus2g_engine_update_params(sus2g_engine e, sus2g_model model) {
+  return guarded([&] {
+    need(e && model, "engine/model");
+    need(model->model.param_count() == e->engine->model().param_count(), "model layout differs from the engine's");
+    auto fresh = std::make_unique<sus2g::Engine>(model->model, e->engine->device(), e->engine->precision());
+    e->engine = std::move(fresh);
+  });
+}
+
+int sus2g_engine_set_stream(sus2g_engine e, void* stream) {
+  return guarded([&] { need(e, "engine"); e->engine->set_stream(static_cast<cudaStream_t>(stream)); });
+}
+
+int sus2g_engine_take_launch_count(sus2g_engine e, int* count) {
+  return guarded([&] {
+    need(e && count, "engine/count");
+    *count = e->engine->last_launches();
+    e->engine->reset_launch_count();
+  });
+}
+
+int sus2g_engine_edge_count(sus2g_engine e, long long* count) {
+  return guarded([&] { need(e && count, "engine/count"); *count = e->engine->nedges(); });
+}
+
+int sus2g_calc_efs_device(sus2g_engine e, int nframes, const int* natoms, const double* cells,
+                          const double* positions, const int* types, double* energy, double* forces,
+                          double* virial, double* site_energy) {
+  return guarded([&] {
+    need(e && nframes >= 0 && (nframes == 0 || (natoms && cells)), "engine/frames");
+    const long long n = total_atoms(nframes, natoms);
+    need(n == 0 || (positions && types), "positions/types");
+    auto& eng = *e->engine;
+    eng.build_edges(nframes, natoms, cells, positions, types);
+    eng.efs(energy, forces, virial, site_energy);
+    eng.check_device_error();
+  });
+}
+
+int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const double* cells,
+                        const double* positions, const int* types, double* energy, double* forces,
+                        double* virial, double* site_energy) {
+  return guarded([&] {
+    need(e && nframes >= 0 && (nframes == 0 || (natoms && cells)), "engine/frames");
+    const long long n = total_atoms(nframes, natoms);
+    need(n == 0 || (positions && types), "positions/types");
+    auto& eng = *e->engine;
+    for (long long i = 0; i < n; ++i)
+      need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Stage pos(sizeof(double) * 3 * n), typ(sizeof(int) * n);
+    Stage out_e(sizeof(double) * nframes), out_f(sizeof(double) * 3 * n), out_v(sizeof(double) * 6 * nframes),
+        out_s(sizeof(double) * n);
+    if (n) {
+      cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
+      cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
+    }
+    eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
+    eng.efs(energy ? out_e.as<double>() : nullptr, forces ? out_f.as<double>() : nullptr,
+            virial ? out_v.as<double>() : nullptr, site_energy ? out_s.as<double>() : nullptr);
+    eng.check_device_error();
+    if (energy && nframes) cuda(cudaMemcpyAsync(energy, out_e.p, sizeof(double) * nframes, cudaMemcpyDeviceToHost, s), "energy copy");
+    if (forces && n) cuda(cudaMemcpyAsync(forces, out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "force copy");
+    if (virial && nframes) cuda(cudaMemcpyAsync(virial, out_v.p, sizeof(double) * 6 * nframes, cudaMemcpyDeviceToHost, s), "virial copy");
+    if (site_energy && n) cuda(cudaMemcpyAsync(site_energy, out_s.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "site copy");
+    cuda(cudaStreamSynchronize(s), "stream synchronize");
+  });
+}
+
+int sus2g_efs_edges_host(sus2g_engine e, int nowned, int nall, const int* types, int nedges, const int* ei,
+                         const int* ej, const double* d, double* energy, double* site_energy, double* forces,
+                         double* virial) {
+  return guarded([&] {
+    need(e && nowned >= 0 && nall >= nowned && nedges >= 0, "engine/layout");
+    need(nall == 0 || types, "types");
+    need(nedges == 0 || (ei && ej && d), "edges");
+    auto& eng = *e->engine;
+    for (int i = 0; i < nall; ++i) need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
+    const double rc2 = eng.model().max_dist * eng.model().max_dist;
+    for (long long q = 0; q < nedges; ++q) {
+      need(ei[q] >= 0 && ei[q] < nowned && ej[q] >= 0 && ej[q] < nall, "edge atom index out of range");
+      const double r2 = d[3 * q] * d[3 * q] + d[3 * q + 1] * d[3 * q + 1] + d[3 * q + 2] * d[3 * q + 2];
+      need(r2 > 0 && r2 < 1e300, "edge with zero or non-finite length");
+      (void)rc2;
+    }
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Stage typ(sizeof(int) * nall), di(sizeof(int) * nedges), dj(sizeof(int) * nedges), dd(sizeof(double) * 3 * nedges);
+    Stage out_e(sizeof(double)), out_f(sizeof(double) * 3 * nall), out_v(sizeof(double) * 6), out_s(sizeof(double) * nowned);
+    if (nall) cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * nall, cudaMemcpyHostToDevice, s), "types copy");
+    if (nedges) {
+      cuda(cudaMemcpyAsync(di.p, ei, sizeof(int) * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+      cuda(cudaMemcpyAsync(dj.p, ej, sizeof(int) * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+      cuda(cudaMemcpyAsync(dd.p, d, sizeof(double) * 3 * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+    }
+    eng.set_edges(nowned, nall, typ.as<int>(), nedges, di.as<int>(), dj.as<int>(), dd.as<double>());
+    eng.efs(out_e.as<double>(), forces ? out_f.as<double>() : nullptr, out_v.as<double>(),
+            site_energy ? out_s.as<double>() : nullptr);
+    eng.check_device_error();
+    if (energy) cuda(cudaMemcpyAsync(energy, out_e.p, sizeof(double), cudaMemcpyDeviceToHost, s), "energy copy");
+    if (forces && nall) cuda(cudaMemcpyAsync(forces, out_f.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s), "force copy");
+    if (virial) cuda(cudaMemcpyAsync(virial, out_v.p, sizeof(double) * 6, cudaMemcpyDeviceToHost, s), "virial copy");
+    if (site_energy && nowned) cuda(cudaMemcpyAsync(site_energy, out_s.p, sizeof(double) * nowned, cudaMemcpyDeviceToHost, s), "site copy");
+    cuda(cudaStreamSynchronize(s), "stream synchronize");
+  });
+}
+
+}  // extern "C"

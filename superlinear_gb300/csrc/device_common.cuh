@@ -1,0 +1,95 @@
+// Device-side tables and helpers shared by the SUS2 GPU kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sus2g {
+
+constexpr int kWarp = 32;
+constexpr int kMaxK = 8;        // radial channels a warp-per-atom pass keeps in registers
+constexpr int kMaxB = 16;       // Chebyshev basis size kept in registers
+
+// Device error codes recorded by kernels (first error wins); the host turns them into messages.
+enum DeviceError : int {
+  kErrNone = 0,
+  kErrEdgeCapacity = 1,   // a neighbour list exceeded the capacity the builder planned for
+  kErrImageRange = 2,     // periodic image index outside the packed range
+  kErrReverseEdge = 3,    // a directed edge had no reverse partner
+  kErrBadDistance = 4,    // zero or non-finite edge length
+};
+
+__device__ __forceinline__ void record_error(int* flag, int code) {
+  if (flag) atomicCAS(flag, 0, code);
+}
+
+// Edge geometry record (dx, dy, dz, r) in the compute precision.
+struct __align__(16) EdgeF { float x, y, z, w; };
+struct __align__(32) EdgeD { double x, y, z, w; };
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { using type = EdgeF; };
+template <> struct Vec4<double> { using type = EdgeD; };
+
+// Per-pass tables: the outer (energy) pass and the Effect gate pass share this layout.
+template <typename Real>
+struct PassTables {
+  const Real* coeff;      // F x B Chebyshev coefficients of R_mu
+  const Real* scal;       // warp: slope at [2 sb C^2 + pair], shift at [(2 sb + 1) C^2 + pair]
+  const Real* wcenter;    // C x F centre factor  (tau or gate type)
+  const Real* wsource;    // C x F source factor  (tau or gate type)
+  const Real* wadd;       // C x F Effect additive factor alpha (outer pass of gated models), else null
+  // ranked K contraction, forward grouped by destination node
+  int ndst;
+  const int* dst_node;    // [ndst]
+  const int* dst_begin;   // [ndst + 1]
+  const int* dst_src;     // basic index
+  const Real* dst_w;
+  // reverse grouped by basic index
+  const int* src_begin;   // [NB + 1]
+  const int* src_dst;
+  const Real* src_w;
+  // per-atom product graph schedule (see model.cpp build_schedule)
+  int levels;
+  const int* level_begin;   // [levels + 1]
+  const int* out_nodes;
+  const int* out_begin;
+  const int* fprod_a;
+  const int* fprod_b;
+  const Real* fprod_c;
+  const int* rlevel_begin;  // [levels + 1] (levels >= 1; level 0 holds sources)
+  const int* in_nodes;
+  const int* in_begin;
+  const int* rprod_out;
+  const int* rprod_other;
+  const Real* rprod_c;
+};
+
+template <typename Real>
+struct DevModel {
+  int C, L, K, B, F, H, M, NB, S, Q, nblk, scaling_mode;
+  Real rmax, rang, scaling;
+  int split, poly, cutoff_p, gated, species_readout;
+  const int* basic_of;      // K x H canonical (k, l*l+l+m) -> basic index, -1 when absent
+  PassTables<Real> outer, gate;
+  const Real* linear;       // readout weights (S or C x S)
+  const double* species;    // C
+  const double* shift;      // C
+  const int* scalar_map;    // S
+  const Real* gate_wmat;    // F x Q gate projection h = W g
+  const int* gate_nodes;    // Q
+};
+
+__device__ __forceinline__ int warp_lane() { return threadIdx.x & (kWarp - 1); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Warp index of the scaling block for radial function (k, l) (sus2_sl_kernel.cpp:198).
+__device__ __forceinline__ int scaling_block(int mode, int k, int l, int Lp) {
+  return mode == 2 ? k : (mode == 1 ? l : (mode == 0 ? 0 : k * Lp + l));
+}
+
+}  // namespace sus2g

@@ -1,0 +1,735 @@
+// Host orchestration of the GPU engine: device tables, edge building, pass launches, force gather
+// and per-frame reductions.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+
+#include "neighbors.cuh"
+#include "pass_launch.h"
+
+namespace sus2g {
+
+#define SUS2G_CUDA(call)                                                                      \
+  do {                                                                                        \
+    cudaError_t err__ = (call);                                                               \
+    if (err__ != cudaSuccess)                                                                 \
+      throw Error(10, std::string("CUDA error: ") + cudaGetErrorString(err__) + " at " #call); \
+  } while (0)
+
+void DevBuf::ensure(size_t n) {
+  if (n <= bytes && ptr) return;
+  release();
+  const size_t want = std::max<size_t>(n, 256);
+  SUS2G_CUDA(cudaMalloc(&ptr, want));
+  bytes = want;
+}
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+// ------------------------------------------------------------------------------------------------
+// edge building kernels
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+__global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) frame_of[i] = f;
+}
+
+__global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
+                            int* bin_of, int* bin_count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (!fp.use_bins) { bin_of[i] = -1; return; }
+  int b[3];
+  for (int q = 0; q < 3; ++q) {
+    const double s = pos[3 * i] * fp.inv[q] + pos[3 * i + 1] * fp.inv[3 + q] + pos[3 * i + 2] * fp.inv[6 + q];
+    const double w = s - floor(s);
+    b[q] = min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1);
+  }
+  const int bin = fp.bin0 + (b[0] * fp.nb[1] + b[1]) * fp.nb[2] + b[2];
+  bin_of[i] = bin;
+  atomicAdd(bin_count + bin, 1);
+}
+
+__global__ void k_bin_fill(const int* bin_of, int natoms, const int* bin_start, int* cursor, int* bin_atoms) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  const int bin = bin_of[i];
+  if (bin < 0) return;
+  bin_atoms[bin_start[bin] + atomicAdd(cursor + bin, 1)] = i;
+}
+
+// Atom order inside a bin is made deterministic (ascending index).
+__global__ void k_bin_sort(const int* bin_start, int nbins, int* bin_atoms) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  int* a = bin_atoms + bin_start[b];
+  const int n = bin_start[b + 1] - bin_start[b];
+  for (int i = 1; i < n; ++i) {
+    const int x = a[i];
+    int j = i - 1;
+    while (j >= 0 && a[j] > x) { a[j + 1] = a[j]; --j; }
+    a[j + 1] = x;
+  }
+}
+
+__global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
+                             const int* bin_start, const int* bin_atoms, int* counts, int* error) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  int n = 0;
+  enumerate_edges(i, plans[frame_of[i]], pos, rc2, bin_start, bin_atoms, error,
+                  [&](int, int, int, int, double, double, double, double) { ++n; });
+  counts[i] = n;
+}
+
+template <typename Real>
+__global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
+                            const int* bin_start, const int* bin_atoms, const int* row, int* nbr,
+                            typename Vec4<Real>::type* d4, unsigned long long* key, int* error) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= natoms) return;
+  int e = row[i];
+  const int end = row[i + 1];
+  enumerate_edges(i, plans[frame_of[i]], pos, rc2, bin_start, bin_atoms, error,
+                  [&](int j, int a, int b, int c, double x, double y, double z, double r2) {
+                    if (e >= end) { record_error(error, kErrEdgeCapacity); return; }
+                    nbr[e] = j;
+                    typename Vec4<Real>::type v;
+                    v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
+                    d4[e] = v;
+                    key[e] = edge_key(j, a, b, c);
+                    ++e;
+                  });
+}
+
+// Sort one centre's edges by key (warp per centre, rank sort; keys within a centre are unique).
+template <typename Real>
+__global__ void k_edge_sort(const int* row, int natoms, const unsigned long long* key_in, const int* nbr_in,
+                            const typename Vec4<Real>::type* d4_in, unsigned long long* key_out, int* nbr_out,
+                            typename Vec4<Real>::type* d4_out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x & 31;
+  if (warp >= natoms) return;
+  const int e0 = row[warp], e1 = row[warp + 1];
+  for (int e = e0 + lane; e < e1; e += kWarp) {
+    const unsigned long long k = key_in[e];
+    int rank = 0;
+    for (int q = e0; q < e1; ++q) rank += key_in[q] < k;
+    key_out[e0 + rank] = k;
+    nbr_out[e0 + rank] = nbr_in[e];
+    d4_out[e0 + rank] = d4_in[e];
+  }
+}
+
+__global__ void k_reverse(const int* row, const int* nbr, const unsigned long long* key, long long nedges, int* rev,
+                          const int* centre_of_edge_unused, int natoms, int* error) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= nedges) return;
+  // centre of e: binary search in row
+  int lo = 0, hi = natoms;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (row[mid] <= e) lo = mid; else hi = mid;
+  }
+  const int i = lo, j = nbr[e];
+  const unsigned long long k = key[e];
+  const int n0 = static_cast<int>((k >> 14) & 127) - 64, n1 = static_cast<int>((k >> 7) & 127) - 64,
+            n2 = static_cast<int>(k & 127) - 64;
+  const unsigned long long want = edge_key(i, -n0, -n1, -n2);
+  int a = row[j], b = row[j + 1] - 1, found = -1;
+  while (a <= b) {
+    const int mid = (a + b) >> 1;
+    const unsigned long long km = key[mid];
+    if (km == want) { found = mid; break; }
+    if (km < want) a = mid + 1; else b = mid - 1;
+  }
+  if (found < 0) record_error(error, kErrReverseEdge);
+  rev[e] = found < 0 ? static_cast<int>(e) : found;
+}
+
+// F_i = sum over i's edges of (g_e - g_rev(e)), FP64 accumulation, warp per atom.
+template <typename Real>
+__global__ void k_force_gather(const int* row, const int* rev, const Real* g, int natoms, double* force) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x & 31;
+  if (warp >= natoms) return;
+  double f[3] = {0, 0, 0};
+  for (int e = row[warp] + lane; e < row[warp + 1]; e += kWarp) {
+    const int r = rev[e];
+    for (int c = 0; c < 3; ++c) f[c] += double(g[3 * (size_t)e + c]) - double(g[3 * (size_t)r + c]);
+  }
+  for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
+  if (lane == 0)
+    for (int c = 0; c < 3; ++c) force[3 * (size_t)warp + c] = f[c];
+}
+
+// Caller-supplied edges: F_i += g_e, F_j -= g_e with FP64 atomics (forces zeroed beforehand).
+template <typename Real>
+__global__ void k_force_scatter(const int* ei, const int* nbr, const Real* g, long long n, double* force) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int i = ei[e], j = nbr[e];
+  for (int c = 0; c < 3; ++c) {
+    const double v = double(g[3 * e + c]);
+    atomicAdd(force + 3 * (size_t)i + c, v);
+    atomicAdd(force + 3 * (size_t)j + c, -v);
+  }
+}
+
+// Caller-supplied edges: hbar_j[mu] += per-edge contribution (stored at the edge itself).
+template <typename Real>
+__global__ void k_hbar_scatter(const int* nbr, const Real* hc, long long n, int F, double* hbar) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n * F) return;
+  const long long e = t / F;
+  const int mu = static_cast<int>(t - e * F);
+  atomicAdd(hbar + (size_t)nbr[e] * F + mu, double(hc[t]));
+}
+
+__global__ void k_centre_of_edge(const int* row, int ncentres, int* ei) {
+  const int i = blockIdx.x;
+  if (i >= ncentres) return;
+  for (int e = row[i] + threadIdx.x; e < row[i + 1]; e += blockDim.x) ei[e] = i;
+}
+
+__global__ void k_iota(int* v, long long n) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < n) v[e] = static_cast<int>(e);
+}
+
+// Per-frame energy and virial: one block per frame, fixed-order tree reduction.
+__global__ void k_frame_reduce(const FramePlan* plans, int nframes, const double* site, const double* vir_atom,
+                               double* energy, double* virial) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  __shared__ double sh[7][256];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) {
+    acc[0] += site[i];
+    for (int c = 0; c < 6; ++c) acc[1 + c] += vir_atom[6 * (size_t)i + c];
+  }
+  for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (energy) energy[f] = sh[0][0];
+    if (virial)
+      for (int c = 0; c < 6; ++c) virial[6 * f + c] = sh[1 + c][0];
+  }
+}
+
+// Caller-provided edges (owned centres, LAMMPS layout): count per centre.
+__global__ void k_count_centres(const int* ei, long long n, int* counts, int nowned, int* error) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int i = ei[e];
+  if (i < 0 || i >= nowned) { record_error(error, kErrEdgeCapacity); return; }
+  atomicAdd(counts + i, 1);
+}
+
+template <typename Real>
+__global__ void k_scatter_user_edges(const int* ei, const int* ej, const double* d, long long n, const int* row,
+                                     int* cursor, int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key,
+                                     int nall, int* error) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  const int i = ei[e], j = ej[e];
+  if (i < 0 || j < 0 || j >= nall) { record_error(error, kErrEdgeCapacity); return; }
+  const double x = d[3 * e], y = d[3 * e + 1], z = d[3 * e + 2];
+  const double r2 = x * x + y * y + z * z;
+  if (!(r2 > 0) || !isfinite(r2)) record_error(error, kErrBadDistance);
+  const int p = row[i] + atomicAdd(cursor + i, 1);
+  nbr[p] = j;
+  typename Vec4<Real>::type v;
+  v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
+  d4[p] = v;
+  // Order key: neighbour, then the caller's edge index (unique, deterministic).
+  key[p] = (static_cast<unsigned long long>(j) << 32) | static_cast<unsigned long long>(e & 0xffffffffLL);
+}
+
+void exclusive_scan_host_sync(const int* d_counts, int n, int* d_row, cudaStream_t s, long long* total) {
+  std::vector<int> h(n);
+  if (n) SUS2G_CUDA(cudaMemcpyAsync(h.data(), d_counts, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  SUS2G_CUDA(cudaStreamSynchronize(s));
+  std::vector<int> r(n + 1);
+  long long acc = 0;
+  for (int i = 0; i < n; ++i) {
+    r[i] = static_cast<int>(acc);
+    acc += h[i];
+    if (acc > 2000000000LL) throw Error(5, "edge count exceeds 2^31");
+  }
+  r[n] = static_cast<int>(acc);
+  SUS2G_CUDA(cudaMemcpyAsync(d_row, r.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, s));
+  SUS2G_CUDA(cudaStreamSynchronize(s));
+  *total = acc;
+}
+
+void invert3(const double* c, double* inv) {
+  // inverse of the row matrix c (rows = lattice vectors)
+  const double det = c[0] * (c[4] * c[8] - c[5] * c[7]) - c[1] * (c[3] * c[8] - c[5] * c[6]) + c[2] * (c[3] * c[7] - c[4] * c[6]);
+  if (!(std::fabs(det) > 0) || !std::isfinite(det)) throw Error(4, "invalid (singular) cell");
+  const double id = 1.0 / det;
+  inv[0] = (c[4] * c[8] - c[5] * c[7]) * id;
+  inv[1] = (c[2] * c[7] - c[1] * c[8]) * id;
+  inv[2] = (c[1] * c[5] - c[2] * c[4]) * id;
+  inv[3] = (c[5] * c[6] - c[3] * c[8]) * id;
+  inv[4] = (c[0] * c[8] - c[2] * c[6]) * id;
+  inv[5] = (c[2] * c[3] - c[0] * c[5]) * id;
+  inv[6] = (c[3] * c[7] - c[4] * c[6]) * id;
+  inv[7] = (c[1] * c[6] - c[0] * c[7]) * id;
+  inv[8] = (c[0] * c[4] - c[1] * c[3]) * id;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// model tables
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+struct Packer {
+  std::vector<int> ints;
+  std::vector<double> reals;
+  int add_int(const std::vector<int>& v) { int o = static_cast<int>(ints.size()); ints.insert(ints.end(), v.begin(), v.end()); return o; }
+  int add_real(const std::vector<double>& v) { int o = static_cast<int>(reals.size()); reals.insert(reals.end(), v.begin(), v.end()); return o; }
+};
+
+struct PassOffsets {
+  int coeff, scal, wc, ws, wa;
+  int ndst, dst_node, dst_begin, dst_src, dst_w, src_begin, src_dst, src_w;
+  int levels, level_begin, out_nodes, out_begin, fa, fb, fc, rlevel_begin, in_nodes, in_begin, rout, rother, rc;
+};
+
+PassOffsets pack_pass(const Model& m, bool gate, Packer& pk) {
+  PassOffsets o{};
+  const int C = m.C, F = m.F, B = m.B;
+  std::vector<double> coeff(static_cast<size_t>(F) * B);
+  const bool own_radial = gate && m.gate_shared_radial;
+  for (int mu = 0; mu < F; ++mu)
+    for (int b = 0; b < B; ++b)
+      coeff[static_cast<size_t>(mu) * B + b] = own_radial ? m.gate_radial[static_cast<size_t>(mu) * B + b]
+                                                          : m.radial[static_cast<size_t>(mu) * (B + C) + b];
+  o.coeff = pk.add_real(coeff);
+  o.scal = pk.add_real(gate && m.gate_decoupled ? m.gate_scal : m.scal);
+  std::vector<double> wc(static_cast<size_t>(C) * F), wa(static_cast<size_t>(C) * F, 0.0);
+  for (int t = 0; t < C; ++t)
+    for (int mu = 0; mu < F; ++mu) {
+      const size_t idx = static_cast<size_t>(t) * F + mu;
+      wc[idx] = gate ? m.gate_type[idx] : m.radial[static_cast<size_t>(mu) * (B + C) + B + t];
+      if (!gate && m.gated) wa[idx] = m.gate_add[idx];
+    }
+  o.wc = pk.add_real(wc);
+  o.ws = o.wc;
+  o.wa = pk.add_real(wa);
+  // contraction
+  const auto& rows = gate ? m.gate_rows : m.outer_rows;
+  const auto& w = gate ? m.gate_w : m.outer_w;
+  std::vector<int> dsts;
+  for (const auto& r : rows) dsts.push_back(r.dst);
+  std::sort(dsts.begin(), dsts.end());
+  dsts.erase(std::unique(dsts.begin(), dsts.end()), dsts.end());
+  std::vector<int> dst_begin{0}, dst_src, src_begin{0}, src_dst;
+  std::vector<double> dst_w, src_w;
+  for (int d : dsts) {
+    for (const auto& r : rows)
+      if (r.dst == d) { dst_src.push_back(r.src); dst_w.push_back(r.widx < 0 ? 1.0 : w[r.widx]); }
+    dst_begin.push_back(static_cast<int>(dst_src.size()));
+  }
+  for (int b = 0; b < m.NB; ++b) {
+    for (const auto& r : rows)
+      if (r.src == b) { src_dst.push_back(r.dst); src_w.push_back(r.widx < 0 ? 1.0 : w[r.widx]); }
+    src_begin.push_back(static_cast<int>(src_dst.size()));
+  }
+  o.ndst = static_cast<int>(dsts.size());
+  o.dst_node = pk.add_int(dsts);
+  o.dst_begin = pk.add_int(dst_begin);
+  o.dst_src = pk.add_int(dst_src);
+  o.dst_w = pk.add_real(dst_w);
+  o.src_begin = pk.add_int(src_begin);
+  o.src_dst = pk.add_int(src_dst);
+  o.src_w = pk.add_real(src_w);
+  // graph
+  const GraphSchedule& g = gate ? m.gate_graph : m.outer_graph;
+  o.levels = g.levels;
+  o.level_begin = pk.add_int(g.level_begin);
+  o.out_nodes = pk.add_int(g.out_nodes);
+  o.out_begin = pk.add_int(g.out_begin);
+  std::vector<int> fa, fb;
+  std::vector<double> fc;
+  for (int p : g.fprod) { fa.push_back(m.products[p].a); fb.push_back(m.products[p].b); fc.push_back(m.products[p].c); }
+  o.fa = pk.add_int(fa);
+  o.fb = pk.add_int(fb);
+  o.fc = pk.add_real(fc);
+  o.rlevel_begin = pk.add_int(g.rlevel_begin);
+  o.in_nodes = pk.add_int(g.in_nodes);
+  o.in_begin = pk.add_int(g.in_begin);
+  o.rout = pk.add_int(g.rprod_out);
+  o.rother = pk.add_int(g.rprod_other);
+  o.rc = pk.add_real(g.rprod_c);
+  return o;
+}
+
+template <typename Real>
+PassTables<Real> bind_pass(const PassOffsets& o, const int* I, const Real* R) {
+  PassTables<Real> t{};
+  t.coeff = R + o.coeff; t.scal = R + o.scal; t.wcenter = R + o.wc; t.wsource = R + o.ws; t.wadd = R + o.wa;
+  t.ndst = o.ndst; t.dst_node = I + o.dst_node; t.dst_begin = I + o.dst_begin; t.dst_src = I + o.dst_src; t.dst_w = R + o.dst_w;
+  t.src_begin = I + o.src_begin; t.src_dst = I + o.src_dst; t.src_w = R + o.src_w;
+  t.levels = o.levels; t.level_begin = I + o.level_begin; t.out_nodes = I + o.out_nodes; t.out_begin = I + o.out_begin;
+  t.fprod_a = I + o.fa; t.fprod_b = I + o.fb; t.fprod_c = R + o.fc;
+  t.rlevel_begin = I + o.rlevel_begin; t.in_nodes = I + o.in_nodes; t.in_begin = I + o.in_begin;
+  t.rprod_out = I + o.rout; t.rprod_other = I + o.rother; t.rprod_c = R + o.rc;
+  return t;
+}
+
+}  // namespace
+
+Engine::Engine(const Model& model, int device, int precision) : model_(model), device_(device), precision_(precision) {
+  if (precision != kFP64 && precision != kFP32) throw Error(1, "precision must be 0 (FP64) or 1 (FP32 bulk)");
+  SUS2G_CUDA(cudaSetDevice(device));
+  SUS2G_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
+  SUS2G_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
+  stream_ = own_stream_;
+  SUS2G_CUDA(upload_pass_constants<float>());
+  SUS2G_CUDA(upload_pass_constants<double>());
+  // scalar readout and gate nodes are written with plain stores; duplicates would race
+  auto unique = [](std::vector<int> v) { std::sort(v.begin(), v.end()); return std::adjacent_find(v.begin(), v.end()) == v.end(); };
+  if (!unique(model_.scalar_map)) throw Error(3, "SUS2 model: duplicate entries in alpha_moment_mapping");
+  if (model_.gated && !unique(model_.gate_nodes)) throw Error(3, "SUS2 model: duplicate gate scalar moments");
+  if (model_.K > kMaxK) throw Error(3, "SUS2 model: sh_k_max above 8 is not supported by the GPU engine");
+  plans_ = new std::vector<FramePlan>();
+  error_.ensure(sizeof(int));
+  SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
+  upload_model();
+}
+
+Engine::~Engine() {
+  delete plans_;
+  delete static_cast<char*>(dev_model_);
+  if (own_stream_) cudaStreamDestroy(own_stream_);
+}
+
+template <typename Real>
+void Engine::upload_tables() {
+  const Model& m = model_;
+  Packer pk;
+  std::vector<int> basic_of(static_cast<size_t>(m.K) * m.H, -1);
+  for (int b = 0; b < m.NB; ++b) {
+    const auto& q = m.basic[b];
+    basic_of[static_cast<size_t>(q[0]) * m.H + q[1] * q[1] + q[1] + q[2]] = b;
+  }
+  const int o_basic = pk.add_int(basic_of);
+  PassOffsets po = pack_pass(m, false, pk);
+  PassOffsets pg = m.gated ? pack_pass(m, true, pk) : po;
+  const int o_lin = pk.add_real(m.linear);
+  const int o_map = pk.add_int(m.scalar_map);
+  std::vector<double> wmat;
+  std::vector<int> nodes = m.gate_nodes;
+  if (m.gated) {
+    wmat.resize(static_cast<size_t>(m.F) * m.Q);
+    for (int mu = 0; mu < m.F; ++mu)
+      for (int q = 0; q < m.Q; ++q) wmat[static_cast<size_t>(mu) * m.Q + q] = m.gate_weight(mu, q);
+  }
+  const int o_wmat = pk.add_real(wmat);
+  const int o_nodes = pk.add_int(nodes);
+  std::vector<double> dbl(m.species);
+  dbl.insert(dbl.end(), m.shift.begin(), m.shift.end());
+
+  std::vector<Real> reals(pk.reals.begin(), pk.reals.end());
+  if (pk.ints.empty()) pk.ints.push_back(0);
+  if (reals.empty()) reals.push_back(Real(0));
+  tab_int_.ensure(sizeof(int) * pk.ints.size());
+  tab_real_.ensure(sizeof(Real) * reals.size());
+  tab_dbl_.ensure(sizeof(double) * dbl.size());
+  SUS2G_CUDA(cudaMemcpy(tab_int_.ptr, pk.ints.data(), sizeof(int) * pk.ints.size(), cudaMemcpyHostToDevice));
+  SUS2G_CUDA(cudaMemcpy(tab_real_.ptr, reals.data(), sizeof(Real) * reals.size(), cudaMemcpyHostToDevice));
+  SUS2G_CUDA(cudaMemcpy(tab_dbl_.ptr, dbl.data(), sizeof(double) * dbl.size(), cudaMemcpyHostToDevice));
+  const int* I = tab_int_.as<int>();
+  const Real* R = tab_real_.as<Real>();
+  auto* dm = new DevModel<Real>();
+  dm->C = m.C; dm->L = m.L; dm->K = m.K; dm->B = m.B; dm->F = m.F; dm->H = m.H; dm->M = m.M; dm->NB = m.NB;
+  dm->S = m.S; dm->Q = m.Q; dm->nblk = m.nblk; dm->scaling_mode = m.scaling_mode;
+  dm->rmax = Real(m.max_dist); dm->rang = Real(m.angular); dm->scaling = Real(m.scaling);
+  dm->split = m.split; dm->poly = m.poly_cutoff; dm->cutoff_p = m.cutoff_p; dm->gated = m.gated;
+  dm->species_readout = m.species_readout;
+  dm->basic_of = I + o_basic;
+  dm->outer = bind_pass<Real>(po, I, R);
+  dm->gate = bind_pass<Real>(pg, I, R);
+  dm->linear = R + o_lin;
+  dm->species = tab_dbl_.as<double>();
+  dm->shift = tab_dbl_.as<double>() + m.C;
+  dm->scalar_map = I + o_map;
+  dm->gate_wmat = R + o_wmat;
+  dm->gate_nodes = I + o_nodes;
+  delete static_cast<char*>(dev_model_);
+  dev_model_ = reinterpret_cast<char*>(dm);
+}
+
+void Engine::upload_model() {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (precision_ == kFP32) upload_tables<float>();
+  else upload_tables<double>();
+}
+
+void Engine::check_device_error() {
+  int h = 0;
+  SUS2G_CUDA(cudaMemcpyAsync(&h, error_.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  if (h) {
+    SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
+    static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
+                                "periodic image index outside [-64, 63]", "a directed edge has no reverse partner",
+                                "zero or non-finite edge length"};
+    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 5 ? msg[h] : "unknown"));
+  }
+}
+
+void Engine::build_edges(int nframes, const int* frame_natoms, const double* cells, const double* d_pos,
+                         const int* d_types) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (nframes < 0) throw Error(1, "negative frame count");
+  const double rc = model_.max_dist, rc2 = rc * rc;
+  std::vector<FramePlan>& plans = *plans_;
+  plans.assign(nframes, FramePlan{});
+  int a = 0, bins = 0;
+  for (int f = 0; f < nframes; ++f) {
+    FramePlan& fp = plans[f];
+    if (frame_natoms[f] < 0) throw Error(1, "negative atom count");
+    std::memcpy(fp.cell, cells + 9 * f, sizeof(fp.cell));
+    invert3(fp.cell, fp.inv);
+    double width[3];
+    for (int q = 0; q < 3; ++q) {
+      // |column q of inv| = 1 / perpendicular width of the cell along reciprocal direction q
+      const double n = std::sqrt(fp.inv[q] * fp.inv[q] + fp.inv[3 + q] * fp.inv[3 + q] + fp.inv[6 + q] * fp.inv[6 + q]);
+      fp.reach[q] = rc * n;
+      width[q] = 1.0 / n;
+    }
+    fp.a0 = a;
+    fp.a1 = a + frame_natoms[f];
+    a = fp.a1;
+    fp.use_bins = frame_natoms[f] > 512 && width[0] >= 3 * rc && width[1] >= 3 * rc && width[2] >= 3 * rc;
+    fp.bin0 = bins;
+    if (fp.use_bins) {
+      for (int q = 0; q < 3; ++q) fp.nb[q] = std::max(3, std::min(512, static_cast<int>(width[q] / rc)));
+      bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
+    }
+  }
+  natoms_ = ncentres_ = a;
+  nframes_ = nframes;
+  d_types_ = d_types;
+  user_edges_ = false;
+  cudaStream_t s = stream_;
+  plan_.ensure(sizeof(FramePlan) * std::max(1, nframes));
+  if (nframes) SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
+  frame_of_.ensure(sizeof(int) * std::max(1, a));
+  counts_.ensure(sizeof(int) * (a + 1));
+  row_.ensure(sizeof(int) * (a + 1));
+  bin_count_.ensure(sizeof(int) * (bins + 1));
+  bin_start_.ensure(sizeof(int) * (bins + 1));
+  bin_cursor_.ensure(sizeof(int) * (bins + 1));
+  bin_atoms_.ensure(sizeof(int) * std::max(1, a));
+  DevBuf bin_of;  // per-call temporary
+  bin_of.ensure(sizeof(int) * std::max(1, a));
+  if (nframes) { k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>()); ++launches_; }
+  if (bins) {
+    SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
+    SUS2G_CUDA(cudaMemsetAsync(bin_cursor_.ptr, 0, sizeof(int) * (bins + 1), s));
+    k_bin_count<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, bin_of.as<int>(), bin_count_.as<int>());
+    long long tot = 0;
+    exclusive_scan_host_sync(bin_count_.as<int>(), bins, bin_start_.as<int>(), s, &tot);
+    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(), bin_atoms_.as<int>());
+    k_bin_sort<<<(bins + 127) / 128, 128, 0, s>>>(bin_start_.as<int>(), bins, bin_atoms_.as<int>());
+    launches_ += 3;
+  }
+  if (a) {
+    k_edge_count<<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
+                                                   bin_start_.as<int>(), bin_atoms_.as<int>(), counts_.as<int>(), error_.as<int>());
+    ++launches_;
+  }
+  long long total = 0;
+  exclusive_scan_host_sync(counts_.as<int>(), a, row_.as<int>(), s, &total);
+  nedges_ = total;
+  const size_t E = std::max<long long>(1, total);
+  const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
+  nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);
+  rev_.ensure(sizeof(int) * E);
+  d4_.ensure(rsz * E); tmp_d4_.ensure(rsz * E);
+  key_.ensure(sizeof(unsigned long long) * E); tmp_key_.ensure(sizeof(unsigned long long) * E);
+  if (a) {
+    if (precision_ == kFP32)
+      k_edge_fill<float><<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2, bin_start_.as<int>(),
+          bin_atoms_.as<int>(), row_.as<int>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), tmp_key_.as<unsigned long long>(), error_.as<int>());
+    else
+      k_edge_fill<double><<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2, bin_start_.as<int>(),
+          bin_atoms_.as<int>(), row_.as<int>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), tmp_key_.as<unsigned long long>(), error_.as<int>());
+    ++launches_;
+  }
+  finalize_edges();
+}
+
+void Engine::finalize_edges() {
+  cudaStream_t s = stream_;
+  const int a = ncentres_;
+  if (a) {
+    const int blocks = (a * kWarp + 255) / 256;
+    if (precision_ == kFP32)
+      k_edge_sort<float><<<blocks, 256, 0, s>>>(row_.as<int>(), a, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+                                                  tmp_d4_.as<EdgeF>(), key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeF>());
+    else
+      k_edge_sort<double><<<blocks, 256, 0, s>>>(row_.as<int>(), a, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+                                                   tmp_d4_.as<EdgeD>(), key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
+    ++launches_;
+  }
+  if (nedges_ && user_edges_) {
+    k_iota<<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(rev_.as<int>(), nedges_);
+    ei_.ensure(sizeof(int) * nedges_);
+    k_centre_of_edge<<<a, 128, 0, s>>>(row_.as<int>(), a, ei_.as<int>());
+    launches_ += 2;
+  } else if (nedges_) {
+    k_reverse<<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(row_.as<int>(), nbr_.as<int>(), key_.as<unsigned long long>(),
+                                                                           nedges_, rev_.as<int>(), nullptr, a, error_.as<int>());
+    ++launches_;
+  }
+}
+
+void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j, const double* d_d) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (nowned < 0 || nall < nowned || nedges < 0) throw Error(1, "invalid atom layout");
+  cudaStream_t s = stream_;
+  ncentres_ = nowned;
+  natoms_ = nall;
+  nframes_ = 1;
+  d_types_ = d_types;
+  user_edges_ = true;
+  std::vector<FramePlan>& plans = *plans_;
+  plans.assign(1, FramePlan{});
+  plans[0].a0 = 0;
+  plans[0].a1 = nowned;
+  plan_.ensure(sizeof(FramePlan));
+  SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan), cudaMemcpyHostToDevice, s));
+  counts_.ensure(sizeof(int) * (nowned + 1));
+  row_.ensure(sizeof(int) * (nall + 1));
+  SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (nowned + 1), s));
+  if (nedges) {
+    k_count_centres<<<(nedges + 255) / 256, 256, 0, s>>>(d_i, nedges, counts_.as<int>(), nowned, error_.as<int>());
+    ++launches_;
+  }
+  long long total = 0;
+  exclusive_scan_host_sync(counts_.as<int>(), nowned, row_.as<int>(), s, &total);
+  nedges_ = total;
+  const size_t E = std::max<long long>(1, total);
+  const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
+  nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);
+  rev_.ensure(sizeof(int) * E);
+  d4_.ensure(rsz * E); tmp_d4_.ensure(rsz * E);
+  key_.ensure(sizeof(unsigned long long) * E); tmp_key_.ensure(sizeof(unsigned long long) * E);
+  DevBuf cursor;
+  cursor.ensure(sizeof(int) * (nowned + 1));
+  SUS2G_CUDA(cudaMemsetAsync(cursor.ptr, 0, sizeof(int) * (nowned + 1), s));
+  if (nedges) {
+    if (precision_ == kFP32)
+      k_scatter_user_edges<float><<<(nedges + 255) / 256, 256, 0, s>>>(d_i, d_j, d_d, nedges, row_.as<int>(), cursor.as<int>(),
+          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), tmp_key_.as<unsigned long long>(), nall, error_.as<int>());
+    else
+      k_scatter_user_edges<double><<<(nedges + 255) / 256, 256, 0, s>>>(d_i, d_j, d_d, nedges, row_.as<int>(), cursor.as<int>(),
+          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), tmp_key_.as<unsigned long long>(), nall, error_.as<int>());
+    ++launches_;
+  }
+  // rows of ghost atoms are empty
+  if (nall > nowned) {
+    std::vector<int> tail(nall - nowned, static_cast<int>(total));
+    SUS2G_CUDA(cudaMemcpyAsync(row_.as<int>() + nowned + 1, tail.data(), sizeof(int) * tail.size(), cudaMemcpyHostToDevice, s));
+    SUS2G_CUDA(cudaStreamSynchronize(s));
+  }
+  finalize_edges();
+}
+
+template <typename Real>
+void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
+  const Model& m = model_;
+  cudaStream_t s = stream_;
+  const int N = natoms_;
+  const size_t E = std::max<long long>(1, nedges_);
+  g_.ensure(sizeof(Real) * 3 * E);
+  site_.ensure(sizeof(double) * std::max(1, N));
+  vir_atom_.ensure(sizeof(double) * 6 * std::max(1, N));
+  SUS2G_CUDA(cudaMemsetAsync(site_.ptr, 0, sizeof(double) * std::max(1, N), s));
+  SUS2G_CUDA(cudaMemsetAsync(vir_atom_.ptr, 0, sizeof(double) * 6 * std::max(1, N), s));
+  PassArgs<Real> a{};
+  a.dm = *static_cast<DevModel<Real>*>(dev_model_);
+  a.natoms = ncentres_;
+  a.types = d_types_;
+  a.row = row_.as<int>();
+  a.nbr = nbr_.as<int>();
+  a.rev = rev_.as<int>();
+  a.d4 = static_cast<const typename Vec4<Real>::type*>(d4_.ptr);
+  a.g = g_.as<Real>();
+  a.site_energy = site_.as<double>();
+  a.virial = vir_atom_.as<double>();
+  a.error = error_.as<int>();
+  if (!m.gated) {
+    launches_ += launch_atom_pass<Real>(m.L, kModeStatic, a, sm_count_, s);
+  } else {
+    hsig_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F);
+    hcontrib_.ensure(sizeof(Real) * E * m.F);
+    gmom_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.M);
+    a.hsig = hsig_.as<Real>();
+    a.hcontrib = hcontrib_.as<Real>();
+    a.gmom = gmom_.as<Real>();
+    if (ncentres_ != natoms_) throw Error(1, "Effect models on a ghost layout need the forward gate exchange (not in this call)");
+    launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
+    launches_ += launch_atom_pass<Real>(m.L, kModeOuter, a, sm_count_, s);
+    if (user_edges_) {
+      hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
+      SUS2G_CUDA(cudaMemsetAsync(hbar_atom_.ptr, 0, sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F, s));
+      if (nedges_) {
+        const long long n = nedges_ * m.F;
+        k_hbar_scatter<Real><<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(nbr_.as<int>(), hcontrib_.as<Real>(), nedges_, m.F, hbar_atom_.as<double>());
+        ++launches_;
+      }
+      a.hbar_atom = hbar_atom_.as<double>();
+    }
+    launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
+  }
+  if (d_forces && N) {
+    if (user_edges_) {
+      SUS2G_CUDA(cudaMemsetAsync(d_forces, 0, sizeof(double) * 3 * N, s));
+      if (nedges_) {
+        k_force_scatter<Real><<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(ei_.as<int>(), nbr_.as<int>(), g_.as<Real>(), nedges_, d_forces);
+        ++launches_;
+      }
+    } else {
+      k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), rev_.as<int>(), g_.as<Real>(), ncentres_, d_forces);
+      ++launches_;
+    }
+  }
+  if (nframes_) {
+    k_frame_reduce<<<nframes_, 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, site_.as<double>(), vir_atom_.as<double>(), d_energy, d_virial);
+    ++launches_;
+  }
+  if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
+}
+
+void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site);
+  else run_efs<double>(d_energy, d_forces, d_virial, d_site);
+}
+
+}  // namespace sus2g

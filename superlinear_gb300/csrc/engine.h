@@ -1,0 +1,104 @@
+// GPU engine for one SUS2-SH model on one device: owns the device tables, the per-step buffers and
+// the CUDA stream work of an E / F / virial (and, for training, parameter-gradient) evaluation.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "model.h"
+
+namespace sus2g {
+
+enum Precision : int { kFP64 = 0, kFP32 = 1 };
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n);
+  void release();
+  template <typename T> T* as() const { return static_cast<T*>(ptr); }
+  ~DevBuf() { release(); }
+};
+
+struct FramePlan;
+
+class Engine {
+ public:
+  Engine(const Model& model, int device, int precision);
+  ~Engine();
+  Engine(const Engine&) = delete;
+  Engine& operator=(const Engine&) = delete;
+
+  const Model& model() const { return model_; }
+  int precision() const { return precision_; }
+  int device() const { return device_; }
+  cudaStream_t stream() const { return stream_; }
+  void set_stream(cudaStream_t s) { stream_ = s ? s : own_stream_; }
+
+  // Re-upload parameters after Model::set_params.
+  void upload_model();
+
+  // --- geometry -----------------------------------------------------------------------------
+  // Periodic frames: cells (row lattice vectors, 9 doubles each) live on the host, positions
+  // (double [N][3]) and types (int [N]) on the device.  Builds the CSR edge list on stream().
+  void build_edges(int nframes, const int* frame_natoms, const double* cells, const double* d_pos,
+                   const int* d_types);
+  // Caller-supplied directed edges (LAMMPS-style owned centres; device arrays).  nowned centres,
+  // nall atoms; edges need not be sorted; rev is computed from (i, j, d) pairing.
+  void set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j,
+                 const double* d_d);
+
+  // --- evaluation ---------------------------------------------------------------------------
+  // E / F / virial for the current edges.  Outputs (device, double): per-frame energy [nframes],
+  // forces [natoms][3], per-frame virial [nframes][6] in (xx, yy, zz, xy, xz, yz), site energies
+  // [natoms]; any output may be null.
+  void efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+
+  int natoms() const { return natoms_; }
+  int nframes() const { return nframes_; }
+  long long nedges() const { return nedges_; }
+  // number of kernels launched by the last build_edges + efs (for launch accounting)
+  int last_launches() const { return launches_; }
+  void reset_launch_count() { launches_ = 0; }
+  // Raises if a kernel recorded an error (synchronises the stream).
+  void check_device_error();
+
+  // internal buffers exposed for the tests / parameter-gradient pass
+  const int* d_row() const { return row_.as<int>(); }
+  const int* d_nbr() const { return nbr_.as<int>(); }
+  const int* d_rev() const { return rev_.as<int>(); }
+
+ private:
+  template <typename Real> void upload_tables();
+  template <typename Real> void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  void finalize_edges();
+
+  Model model_;
+  int device_ = 0, precision_ = kFP32;
+  cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
+  int sm_count_ = 0;
+  int launches_ = 0;
+
+  // model tables (both precisions are packed into one buffer each)
+  DevBuf tab_int_, tab_real_, tab_dbl_;
+  void* dev_model_ = nullptr;  // host copy of DevModel<Real>
+
+  // geometry
+  int natoms_ = 0, nframes_ = 0, ncentres_ = 0;
+  long long nedges_ = 0;
+  std::vector<FramePlan>* plans_ = nullptr;
+  DevBuf plan_, frame_of_, frame_begin_, types_copy_;
+  DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
+  DevBuf bin_count_, bin_start_, bin_atoms_, bin_cursor_;
+  const int* d_types_ = nullptr;
+  bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
+  DevBuf ei_, hbar_atom_;
+  // step buffers
+  DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_;
+  DevBuf scratch_;
+};
+
+}  // namespace sus2g
