@@ -30,7 +30,7 @@ namespace sus2g {
 // includes this header owns a copy and fills it once per device through sph_norm_upload().
 static __constant__ double c_sph_norm[64];
 
-inline cudaError_t sph_norm_upload() {
+static inline cudaError_t sph_norm_upload() {
   double n[64] = {0};
   const double pi = 3.14159265358979323846;
   for (int l = 0; l <= 6; ++l)

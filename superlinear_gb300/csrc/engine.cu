@@ -421,7 +421,8 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
 
 Engine::~Engine() {
   delete plans_;
-  delete static_cast<char*>(dev_model_);
+  if (precision_ == kFP32) delete static_cast<DevModel<float>*>(dev_model_);
+  else delete static_cast<DevModel<double>*>(dev_model_);
   if (own_stream_) cudaStreamDestroy(own_stream_);
 }
 
@@ -477,8 +478,8 @@ void Engine::upload_tables() {
   dm->scalar_map = I + o_map;
   dm->gate_wmat = R + o_wmat;
   dm->gate_nodes = I + o_nodes;
-  delete static_cast<char*>(dev_model_);
-  dev_model_ = reinterpret_cast<char*>(dm);
+  delete static_cast<DevModel<Real>*>(dev_model_);
+  dev_model_ = dm;
 }
 
 void Engine::upload_model() {

@@ -1,0 +1,152 @@
+"""Python host API over the C ABI: models, engines and E / F / virial evaluation.
+
+Mirrors the reference's call surface for this path:
+  * ``Model(path)``                    ~ SUS2SL::Model::load / MLMTPR::Load (.sus2)
+  * ``Engine.calc_efs(frames)``        ~ MLMTPR::CalcEFS over a batch of periodic frames (calc-efs)
+  * ``Engine.efs_edges(...)``          ~ SUS2SL::Kernel begin/outer/finish as called by
+                                         PairSUS2Embedded::compute (sus2/embedded)
+Errors raise ``Sus2Error`` with the library's message, as the reference raises on invalid input.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import Sus2Error, check, load
+
+__all__ = ["Model", "Engine", "Sus2Error", "FP64", "FP32"]
+
+FP64 = 0
+FP32 = 1
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+DIM_NAMES = ("C", "L", "K", "B", "F", "M", "NB", "P", "S", "Q", "gated", "nparams", "outer_rank", "gate_rank",
+             "split", "reserved")
+
+
+class Model:
+    """A loaded ``.sus2`` SUS2-SH model (host tables)."""
+
+    def __init__(self, path: str):
+        lib = load()
+        h = ctypes.c_void_p()
+        check(lib.sus2g_model_load(str(path).encode(), ctypes.byref(h)))
+        self._h = h
+        self.path = str(path)
+        d = (ctypes.c_int * 16)()
+        check(lib.sus2g_model_dims(h, d))
+        self.dims = dict(zip(DIM_NAMES, list(d)))
+        c = ctypes.c_double()
+        check(lib.sus2g_model_cutoff(h, ctypes.byref(c)))
+        self.cutoff = c.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            load().sus2g_model_free(h)
+            self._h = None
+
+    @property
+    def nparams(self) -> int:
+        return self.dims["nparams"]
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.nparams)
+        check(load().sus2g_model_get_params(self._h, _d(out), out.size))
+        return out
+
+    def set_params(self, values) -> None:
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        check(load().sus2g_model_set_params(self._h, _d(v), v.size))
+
+
+class Engine:
+    """A model bound to one CUDA device in FP64 (``FP64``) or FP32-bulk (``FP32``) form."""
+
+    def __init__(self, model: Model, device: int = 0, precision: int = FP32):
+        self.model = model
+        h = ctypes.c_void_p()
+        check(load().sus2g_engine_create(model._h, int(device), int(precision), ctypes.byref(h)))
+        self._h = h
+        self.precision = precision
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            load().sus2g_engine_free(h)
+            self._h = None
+
+    def update_params(self) -> None:
+        check(load().sus2g_engine_update_params(self._h, self.model._h))
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(load().sus2g_engine_set_stream(self._h, ctypes.c_void_p(stream_ptr or 0)))
+
+    def take_launch_count(self) -> int:
+        n = ctypes.c_int()
+        check(load().sus2g_engine_take_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def edge_count(self) -> int:
+        n = ctypes.c_longlong()
+        check(load().sus2g_engine_edge_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    # -- periodic frames ------------------------------------------------------------------------
+    @staticmethod
+    def pack_frames(frames):
+        natoms = np.array([f.natoms for f in frames], dtype=np.int32)
+        cells = np.ascontiguousarray(np.stack([f.cell for f in frames]) if frames else np.zeros((0, 3, 3)),
+                                     dtype=np.float64)
+        pos = np.ascontiguousarray(np.concatenate([f.positions for f in frames]) if frames else np.zeros((0, 3)),
+                                   dtype=np.float64)
+        types = np.ascontiguousarray(np.concatenate([f.types for f in frames]) if frames else np.zeros(0),
+                                     dtype=np.int32)
+        return natoms, cells, pos, types
+
+    def calc_efs(self, frames):
+        """Host arrays in and out: returns (energy[nf], forces[N,3], virial[nf,6], site[N])."""
+        natoms, cells, pos, types = self.pack_frames(frames)
+        nf, n = natoms.size, int(natoms.sum())
+        e = np.zeros(nf)
+        f = np.zeros((n, 3))
+        v = np.zeros((nf, 6))
+        s = np.zeros(n)
+        check(load().sus2g_calc_efs_host(self._h, nf, _i(natoms), _d(cells), _d(pos), _i(types), _d(e), _d(f),
+                                         _d(v), _d(s)))
+        return e, f, v, s
+
+    def calc_efs_device(self, natoms, cells, pos_ptr: int, types_ptr: int, energy_ptr: int = 0, forces_ptr: int = 0,
+                        virial_ptr: int = 0, site_ptr: int = 0) -> None:
+        """Device pointers (e.g. ``tensor.data_ptr()``) for positions/types/outputs; host natoms/cells."""
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        cells = np.ascontiguousarray(cells, dtype=np.float64)
+        vp = ctypes.c_void_p
+        check(load().sus2g_calc_efs_device(self._h, natoms.size, _i(natoms), _d(cells), vp(pos_ptr), vp(types_ptr),
+                                           vp(energy_ptr), vp(forces_ptr), vp(virial_ptr), vp(site_ptr)))
+
+    # -- caller edge list (pair_style sus2/embedded) --------------------------------------------
+    def efs_edges(self, nowned: int, types, ei, ej, d):
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        ei = np.ascontiguousarray(ei, dtype=np.int32)
+        ej = np.ascontiguousarray(ej, dtype=np.int32)
+        d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1, 3)
+        nall = types.size
+        e = np.zeros(1)
+        s = np.zeros(nowned)
+        f = np.zeros((nall, 3))
+        v = np.zeros(6)
+        check(load().sus2g_efs_edges_host(self._h, int(nowned), nall, _i(types), ei.size, _i(ei), _i(ej), _d(d),
+                                          _d(e), _d(s), _d(f), _d(v)))
+        return float(e[0]), s, f, v

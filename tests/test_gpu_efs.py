@@ -1,0 +1,222 @@
+"""GPU E / F / virial parity through the C ABI (FP64 plain and FP32 bulk).
+
+Bars (BASELINE the benchmark spec): FP64 plain within 1e-10 relative (tol * (1 + max|a|,|b|)) of the
+reference's values; FP32 bulk within 1e-5 eV/A on forces and 1e-6 eV/atom on energy of the FP64
+oracle; exact edge sets; deterministic results.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_json, rel_err, two_cutoff_cases, virial6_to_matrix
+from superlinear_gb300.synth import diamond, lattice_frame, read_cfg, training_frames, Frame
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_FORCE = 1e-5      # eV/A, absolute
+FP32_ENERGY = 1e-6     # eV/atom, absolute
+
+
+@pytest.fixture(scope="module")
+def lib(engine_lib):
+    import superlinear_gb300 as sg
+    return sg
+
+
+def engines(sg, path):
+    m = sg.Model(path)
+    return m, sg.Engine(m, 0, sg.FP64), sg.Engine(m, 0, sg.FP32)
+
+
+def check_fp32(e32, f32, e64, f64, natoms):
+    assert np.max(np.abs(np.asarray(f32) - np.asarray(f64))) <= FP32_FORCE
+    assert np.max(np.abs(np.asarray(e32) - np.asarray(e64)) / np.maximum(natoms, 1)) <= FP32_ENERGY
+
+
+@pytest.mark.parametrize("model,geom,ref", two_cutoff_cases(), ids=lambda p: os.path.basename(p))
+def test_two_cutoff_reference_fixtures(lib, model, geom, ref):
+    m, g64, g32 = engines(lib, model)
+    frames = read_cfg(geom)
+    data = load_json(ref)
+    sel = [frames[r["config"]] for r in data["records"]]
+    e, f, v, s = g64.calc_efs(sel)
+    e32, f32, v32, s32 = g32.calc_efs(sel)
+    off = 0
+    for k, rec in enumerate(data["records"]):
+        n = sel[k].natoms
+        assert rel_err(e[k], rec["energy"]) < FP64_TOL
+        assert rel_err(f[off:off + n], rec["forces"]) < FP64_TOL
+        assert rel_err(virial6_to_matrix(v[k]), rec["plus_stress"]) < FP64_TOL
+        check_fp32(e32[k], f32[off:off + n], e[k], f[off:off + n], n)
+        off += n
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "efs", "*.json"))),
+                         ids=os.path.basename)
+def test_embedded_engine_goldens(lib, golden, path):
+    data = load_json(path)
+    m, g64, g32 = engines(lib, os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    e, f, v, s = g64.calc_efs(frames)
+    e32, f32, v32, s32 = g32.calc_efs(frames)
+    off = 0
+    for k, rec in enumerate(data["records"]):
+        n = frames[k].natoms
+        assert rel_err(e[k], rec["energy"]) < FP64_TOL
+        assert rel_err(f[off:off + n], rec["forces"]) < FP64_TOL
+        assert rel_err(virial6_to_matrix(v[k]), rec["virial"]) < FP64_TOL
+        assert rel_err(s[off:off + n], rec["site_energies"]) < FP64_TOL
+        check_fp32(e32[k], f32[off:off + n], e[k], f[off:off + n], n)
+        off += n
+
+
+def test_batch_of_uneven_frames_matches_oracle(lib, oracle_lib, golden):
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    frames = training_frames(24, 8, 216, 3.0, 4.2, 0.1, seed=77)
+    e, f, v, s = g64.calc_efs(frames)
+    e32, f32, v32, s32 = g32.calc_efs(frames)
+    off = 0
+    edges = 0
+    for k, fr in enumerate(frames):
+        eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+        edges += ne
+        n = fr.natoms
+        assert rel_err(e[k], eo) < FP64_TOL
+        assert rel_err(f[off:off + n], fo) < FP64_TOL
+        assert rel_err(v[k], vo) < FP64_TOL
+        check_fp32(e32[k], f32[off:off + n], eo, fo, n)
+        off += n
+    assert g64.edge_count() == edges
+
+
+def test_large_static_box_cell_list_matches_oracle(lib, oracle_lib, golden):
+    """4,096-atom diamond (the E/F/virial benchmark box): cell-list edges, exact edge set."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    fr = diamond(8, sigma=0.08, seed=2)
+    e, f, v, s = g64.calc_efs([fr])
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+    assert g64.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    check_fp32(e32[0], f32, eo, fo, fr.natoms)
+
+
+def test_triclinic_cell(lib, oracle_lib, golden):
+    path = os.path.join(golden, "models", "static_l2k3o2_c2.sus2")
+    m, g64, _ = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    rng = np.random.default_rng(4)
+    cell = np.array([[5.1, 0.0, 0.0], [1.3, 4.7, 0.0], [0.7, -0.9, 5.6]])
+    pos = rng.uniform(0, 1, (11, 3)) @ cell
+    fr = Frame(cell, pos, rng.integers(0, 2, 11))
+    e, f, v, s = g64.calc_efs([fr])
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types)
+    assert g64.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
+
+
+def test_effect_l4k8_large_box_fp32_vs_fp64(lib, golden):
+    """Effect L4/K8/R2/O3 on a 1,728-atom two-species diamond: FP32 bulk within the force bound."""
+    path = os.path.join(golden, "models", "effect_l4k8r2o3.sus2")
+    m, g64, g32 = engines(lib, path)
+    fr = diamond(6, sigma=0.1, seed=9, species=2, type_prob=0.5)
+    e, f, v, s = g64.calc_efs([fr])
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    check_fp32(e32[0], f32, e[0], f, fr.natoms)
+
+
+def test_edge_list_api_with_ghosts_matches_oracle(lib, oracle_lib, golden):
+    """pair_style-style call: owned centres + ghost atoms, caller edges (Static)."""
+    path = os.path.join(golden, "models", "static_l2k3o2_c2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    rng = np.random.default_rng(8)
+    nall, nowned = 40, 25
+    x = rng.uniform(0, 9, (nall, 3))
+    types = rng.integers(0, 2, nall)
+    ei, ej, d = [], [], []
+    for i in range(nowned):
+        for j in range(nall):
+            if i != j:
+                dd = x[j] - x[i]
+                if dd @ dd < m.cutoff ** 2:
+                    ei.append(i); ej.append(j); d.append(dd)
+    e, s, f, v = g64.efs_edges(nowned, types, ei, ej, d)
+    eo, fo, vo, so = om.efs_edges(nowned, types, ei, ej, d)
+    assert rel_err(e, eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v, vo) < FP64_TOL
+    assert rel_err(s, so) < FP64_TOL
+    e32, s32, f32, v32 = g32.efs_edges(nowned, types, ei, ej, d)
+    check_fp32(e32, f32, eo, fo, nowned)
+
+
+def test_edge_list_api_effect_single_domain(lib, oracle_lib, golden):
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    m, g64, _ = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    fr = training_frames(1, 30, 64, 3.2, 3.8, 0.1, seed=5)[0]
+    # periodic edges of the frame from the oracle's own enumeration order is not exposed; build here
+    inv = np.linalg.inv(fr.cell)
+    ei, ej, d = [], [], []
+    for i in range(fr.natoms):
+        for j in range(fr.natoms):
+            for a in range(-2, 3):
+                for b in range(-2, 3):
+                    for c in range(-2, 3):
+                        if i == j and a == b == c == 0:
+                            continue
+                        dd = fr.positions[j] - fr.positions[i] + np.array([a, b, c]) @ fr.cell
+                        if dd @ dd < m.cutoff ** 2:
+                            ei.append(i); ej.append(j); d.append(dd)
+    e, s, f, v = g64.efs_edges(fr.natoms, fr.types, ei, ej, d)
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types)
+    assert len(ei) == ne
+    assert rel_err(e, eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v, vo) < FP64_TOL
+
+
+def test_deterministic_and_batch_invariant(lib, golden):
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    frames = training_frames(6, 8, 120, 3.0, 4.2, 0.1, seed=12)
+    for g in (g64, g32):
+        a = g.calc_efs(frames)
+        b = g.calc_efs(frames)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+        single = g.calc_efs(frames[2:3])
+        off = sum(fr.natoms for fr in frames[:2])
+        assert np.array_equal(single[1], a[1][off:off + frames[2].natoms])
+        assert single[0][0] == a[0][2]
+
+
+def test_empty_and_isolated_frames(lib, golden):
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    e, f, v, s = g64.calc_efs([])
+    assert e.size == 0 and f.size == 0
+    lone = Frame(np.eye(3) * 30.0, [[1.0, 2.0, 3.0]], [0])
+    far = Frame(np.eye(3) * 30.0, [[1.0, 1.0, 1.0], [20.0, 20.0, 20.0]], [0, 0])
+    e, f, v, s = g64.calc_efs([lone, far])
+    params = m.params()
+    # no neighbours: site energy = species + shift (readout of empty moments), forces zero
+    assert np.allclose(s, params[m.nparams - m.dims["S"] - 1] + params[0], rtol=0, atol=1e-14)
+    assert np.all(f == 0) and np.all(v == 0)
+
+
+def test_invalid_inputs_raise(lib, golden):
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, _ = engines(lib, path)
+    bad = Frame(np.eye(3) * 10.0, [[0, 0, 0], [1.5, 0, 0]], [0, 3])
+    with pytest.raises(lib.Sus2Error):
+        g64.calc_efs([bad])
+    singular = Frame(np.zeros((3, 3)), [[0, 0, 0]], [0])
+    with pytest.raises(lib.Sus2Error):
+        g64.calc_efs([singular])
+    with pytest.raises(lib.Sus2Error):
+        lib.Engine(m, 0, 7)

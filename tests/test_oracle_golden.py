@@ -1,0 +1,79 @@
+"""The CPU oracle is pinned against the reference's own outputs (CPU only).
+
+* two-cutoff FP64 fixtures shipped with the reference (independent PyTorch float64 values),
+* the reference embedded engine on the benchmark model families (tests/golden/efs),
+* the reference trainer's AccumulateEFSCombinationGrad parameter gradients (tests/golden/grad).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_json, rel_err, two_cutoff_cases, virial6_to_matrix
+from superlinear_gb300.synth import read_cfg
+
+
+@pytest.mark.parametrize("model,geom,ref", two_cutoff_cases(), ids=lambda p: os.path.basename(p))
+def test_two_cutoff_fixtures(oracle_lib, model, geom, ref):
+    m = oracle_lib.OracleModel(model)
+    frames = read_cfg(geom)
+    data = load_json(ref)
+    for rec in data["records"]:
+        fr = frames[rec["config"]]
+        e, f, v, s, _ = m.efs(fr.cell, fr.positions, fr.types)
+        assert rel_err(e, rec["energy"]) < 1e-12
+        assert rel_err(f, rec["forces"]) < 1e-12
+        assert rel_err(virial6_to_matrix(v), rec["plus_stress"]) < 1e-12
+
+
+def efs_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "efs", "*.json")))
+
+
+@pytest.mark.parametrize("path", efs_cases(), ids=os.path.basename)
+def test_embedded_engine_goldens(oracle_lib, golden, path):
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    for rec in data["records"]:
+        fr = frames[rec["config"]]
+        e, f, v, s, _ = m.efs(fr.cell, fr.positions, fr.types)
+        assert rel_err(e, rec["energy"]) < 1e-12
+        assert rel_err(f, rec["forces"]) < 1e-12
+        assert rel_err(virial6_to_matrix(v), rec["virial"]) < 1e-12
+        assert rel_err(s, rec["site_energies"]) < 1e-12
+
+
+def grad_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "grad", "*.json")))
+
+
+@pytest.mark.parametrize("path", grad_cases(), ids=os.path.basename)
+def test_trainer_gradient_goldens(oracle_lib, golden, path):
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    for fr, w, ref, tr in zip(frames, data["weights"], data["grad"], data["trainer_efs"]):
+        g = m.grad(fr.cell, fr.positions, fr.types, w["energy"], w["force"], w["stress"])
+        ref = np.asarray(ref)
+        assert np.linalg.norm(g - ref) <= 1e-12 * np.linalg.norm(ref)
+        e, f, v, s, _ = m.efs(fr.cell, fr.positions, fr.types)
+        assert rel_err(e, tr["energy"]) < 1e-12 and rel_err(f, tr["forces"]) < 1e-12
+
+
+def test_oracle_rejects_missing_model(oracle_lib, tmp_path):
+    with pytest.raises(ValueError):
+        oracle_lib.OracleModel(str(tmp_path / "missing.sus2"))
+
+
+def test_oracle_planted_error_is_detected(oracle_lib, golden):
+    """A mistake planted in the oracle's inputs (one coefficient) moves the result off the golden."""
+    data = load_json(os.path.join(golden, "efs", "static_l3k4o2__diamond64_s05.json"))
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    p = m.params()
+    p[20] += 1e-3
+    m.set_params(p)
+    fr = read_cfg(os.path.join(golden, "frames", data["frames"]))[0]
+    e, f, *_ = m.efs(fr.cell, fr.positions, fr.types)
+    assert rel_err(f, data["records"][0]["forces"]) > 1e-9
