@@ -1,0 +1,389 @@
+#!/usr/bin/env python3
+"""Benchmark of the SUS2-SH E / F / virial hot path on one GB300 (one JSON line on stdout).
+
+Workload (the configuration the headline metric is quoted on): Static L3/K4/O2 carbon model,
+4,096-atom periodic diamond (8x8x8 conventional cells, a = 3.567 A, seeded Gaussian
+displacements sigma = 0.08 A), cutoff 5.0 A.  One step = one MD-step evaluation: build the
+directed edge list from positions on the GPU, then energy, forces and virial (FP32 bulk with
+FP64 reductions; the FP64 plain path is timed alongside).  The inputs are smaller than L2, so L2 is flushed
+(a 256 MiB write) between timed steps, outside the step's events.
+
+--impl reference times the CPU reference path on the host cores instead: the FP64 CPU
+restatement of the reference algorithm (the reference's own sources do not travel to the GPU
+machine), all host threads, E/F/virial per step on the same frame.
+
+Multi-GPU: the path runs on one GPU; with --gpus N each rank runs an independent replica of the
+same workload (replicas only, no collective) and rank 0 reports the sum of rank throughputs
+timed as max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "atom-steps/s E/F/virial; train loss+grad frames/s; FP32-bulk vs FP64, 1 GB300"
+MODEL = os.path.join(ROOT, "tests", "golden", "models", "static_l3k4o2.sus2")
+EFFECT_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l4k8r2o3.sus2")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+
+
+def workload(cells: int = 8):
+    from superlinear_gb300.synth import diamond
+    return diamond(cells, a=3.567, sigma=0.08, seed=2)
+
+
+# ------------------------------------------------------------------------------------------------
+# algorithmic flop model (per edge and per atom), counting FMA as 2 and tanh / sqrt / div as 1
+# ------------------------------------------------------------------------------------------------
+def pass_flops(d, edges, atoms):
+    """Forward + reverse of one per-atom pass (Static outer pass, or each Effect pass)."""
+    H = (d["L"] + 1) ** 2
+    K, B, F, NB = d["K"], d["B"], d["F"], d["NB"]
+    nblk = K  # warp sharing K in the benchmark models
+    fwd = 6 + 12 * H + nblk * (3 * B + 10) + 2 * F * B + 4 * NB
+    rev = 6 + 42 * H + nblk * (7 * B + 15) + 4 * F * B + 24 * NB + 18
+    per_atom = 2 * 4 * max(d["outer_rank"], 1) * H * K + 9 * d["P"] + 4 * d["S"]
+    return edges * (fwd + rev) + atoms * per_atom
+
+
+def algorithmic_bytes(d, edges, atoms, real_bytes=4):
+    """Bytes one Static pass must move: per edge the neighbour index, the edge record (d, r) and
+    the written dE/dd; per atom the type, row offsets, site energy and virial."""
+    return edges * (4 + 4 * real_bytes + 3 * real_bytes) + atoms * (4 + 4 + 8 + 48)
+
+
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in self.rows:
+            for name, val in zip(names, r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def read_traffic(key):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, or None."""
+    try:
+        with open(TRAFFIC) as fh:
+            for line in fh:
+                parts = line.split()
+                if len(parts) >= 2 and parts[0] == key:
+                    return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------------------------------------
+def cpu_sample(frame, threads, min_seconds=8.0, max_evals=50):
+    """Time the oracle port on the frame: E/F/virial compute per evaluation (edge build reported
+    separately), repeated until min_seconds of CPU work."""
+    import oracle as orc
+    m = orc.OracleModel(MODEL)
+    evals, compute, edges_t = 0, 0.0, 0.0
+    t0 = time.perf_counter()
+    while evals == 0 or (evals < max_evals and (time.perf_counter() - t0) < min_seconds):
+        _, ne, te, tc = m.efs_timed(frame.cell, frame.positions, frame.types, threads=threads)
+        compute += tc
+        edges_t += te
+        evals += 1
+    return evals, compute, edges_t
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    import oracle as orc
+    orc.build()
+    frame = workload()
+    threads = os.cpu_count() or 1
+    # warmup
+    for _ in range(max(0, args.warmup)):
+        cpu_sample(frame, threads, min_seconds=0.0, max_evals=1)
+    times = []
+    edge_times = []
+    for _ in range(args.steps):
+        n, tc, te = cpu_sample(frame, threads, min_seconds=0.0, max_evals=1)
+        times.append(tc)
+        edge_times.append(te)
+    ms = 1e3 * float(np.mean(times))
+    value = frame.natoms / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "static_l3k4o2_diamond4096", "atoms": frame.natoms, "cutoff": 5.0,
+                   "cells": "8x8x8", "sigma": 0.08},
+        "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full E/F/virial evaluations of the 4,096-atom frame; "
+                                   f"edge build excluded (mean {1e3 * float(np.mean(edge_times)):.1f} ms, O(N^2) "
+                                   f"image scan like the reference's Neighborhoods)"},
+        "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    import superlinear_gb300 as sg
+    rank, world, local = dist_info()
+    device = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    frame = workload(args.cells)
+    n = frame.natoms
+    dev = torch.device("cuda", device)
+    model = sg.Model(MODEL)
+    stream = torch.cuda.current_stream()
+    pos = torch.tensor(frame.positions, device=dev)
+    typ = torch.tensor(frame.types, device=dev)
+    E = torch.zeros(1, dtype=torch.float64, device=dev)
+    F = torch.zeros(n, 3, dtype=torch.float64, device=dev)
+    V = torch.zeros(1, 6, dtype=torch.float64, device=dev)
+    natoms = np.array([n], np.int32)
+    cells = frame.cell.reshape(1, 9).copy()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def make(prec):
+        eng = sg.Engine(model, device, prec)
+        eng.set_stream(stream.cuda_stream)
+        return eng
+
+    def step(eng):
+        eng.calc_efs_device(natoms, cells, pos.data_ptr(), typ.data_ptr(), E.data_ptr(), F.data_ptr(), V.data_ptr(), 0)
+
+    def timed(eng, steps, warmup, sampler=None):
+        for _ in range(warmup):
+            step(eng)
+        torch.cuda.synchronize()
+        eng.take_launch_count()
+        eng.set_timing(True)
+        eng.take_stage_times()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.start()
+        total = 0.0
+        for _ in range(steps):
+            flush.fill_(1.0)  # L2 flush between timed steps (not timed)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step(eng)
+            b.record(stream)
+            b.synchronize()
+            total += a.elapsed_time(b)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        stages = eng.take_stage_times()
+        eng.set_timing(False)
+        launches = eng.take_launch_count()
+        return total / steps, stages, launches, clocks
+
+    eng32 = make(sg.FP32)
+    sampler = ClockSampler(device) if rank == 0 and not args.profile_only else None
+    ms32, st32, launches, clocks = timed(eng32, args.steps, args.warmup, sampler)
+    edges = eng32.edge_count()
+    if args.profile_only:
+        print(json.dumps({"profile_only": True, "atoms": n, "edges": edges, "ms_per_step": ms32,
+                          "stages_ms": {k: v[0] / max(1, v[1]) for k, v in st32.items() if v[1]}}), flush=True)
+        return 0
+    eng64 = make(sg.FP64)
+    ms64, st64, _, _ = timed(eng64, max(3, args.steps // 2), args.warmup)
+
+    # e2e through the C ABI with host buffers (copies in and out inside the timed region)
+    for _ in range(args.warmup):
+        eng32.calc_efs([frame])
+    torch.cuda.synchronize()
+    calls = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        eng32.calc_efs([frame])
+        calls.append(time.perf_counter() - t1)
+    e2e_ms = 1e3 * float(np.mean(calls))
+
+    # max over ranks
+    t_rank = torch.tensor([ms32, ms64, e2e_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
+    ms32, ms64, e2e_ms = (float(x) for x in t_rank.cpu())
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    d = model.dims
+    pass_ms = st32["outer"][0] / max(1, st32["outer"][1])
+    flops = pass_flops(d, edges, n)
+    peaks = {}
+    try:
+        with open(PEAKS) as fh:
+            peaks = json.load(fh)
+    except OSError:
+        pass
+    sm_mhz = (clocks or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sm_count = torch.cuda.get_device_properties(device).multi_processor_count
+    fp32_peak = sm_count * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    achieved = flops / (pass_ms / 1e3) / 1e12
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    abytes = algorithmic_bytes(d, edges, n)
+    traffic = read_traffic("static_pass_diamond4096_fp32")
+    # CPU baseline (oracle port, all host cores, bounded sample)
+    threads = os.cpu_count() or 1
+    nev, tc, te = cpu_sample(frame, threads, min_seconds=10.0, max_evals=40)
+    cpu_value = frame.natoms * nev / tc
+
+    # Effect L4/K8/R2/O3 at 110,592 atoms (the large-system configuration), FP32 and FP64
+    extra = {}
+    if not args.skip_effect:
+        from superlinear_gb300.synth import diamond
+        fr4 = diamond(24, a=3.567, sigma=0.1, seed=4, species=2, type_prob=0.5)
+        m4 = sg.Model(EFFECT_MODEL)
+        p4 = torch.tensor(fr4.positions, device=dev)
+        t4 = torch.tensor(fr4.types, device=dev)
+        F4 = torch.zeros(fr4.natoms, 3, dtype=torch.float64, device=dev)
+        c4 = fr4.cell.reshape(1, 9).copy()
+        n4 = np.array([fr4.natoms], np.int32)
+        for prec, key, reps in ((sg.FP32, "fp32", 5), (sg.FP64, "fp64", 2)):
+            e4 = sg.Engine(m4, device, prec)
+            e4.set_stream(stream.cuda_stream)
+            e4.calc_efs_device(n4, c4, p4.data_ptr(), t4.data_ptr(), E.data_ptr(), F4.data_ptr(), V.data_ptr(), 0)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                e4.calc_efs_device(n4, c4, p4.data_ptr(), t4.data_ptr(), E.data_ptr(), F4.data_ptr(), V.data_ptr(), 0)
+            b.record(stream)
+            b.synchronize()
+            ms = a.elapsed_time(b) / reps
+            extra[key] = {"ms_per_step": ms, "atom_steps_per_s": fr4.natoms / (ms / 1e3), "edges": e4.edge_count()}
+            del e4
+        extra["fp32_over_fp64"] = extra["fp64"]["ms_per_step"] / extra["fp32"]["ms_per_step"]
+
+    line = {
+        "metric": METRIC, "value": n * world / (ms32 / 1e3), "unit": "atom-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "static_l3k4o2_diamond4096", "model": "Static L3/K4/O2 (1 species, C)", "atoms": n,
+                   "edges": edges, "cutoff": 5.0, "cells": "8x8x8", "a": 3.567, "sigma": 0.08,
+                   "step": "GPU edge build + energy/forces/virial", "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "fp64_plain": {"ms_per_step": ms64, "value": n / (ms64 / 1e3), "fp32_over_fp64": ms64 / ms32},
+        "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in st32.items() if v[1]},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak,
+                     "peak_source": f"nominal FP32 FMA rate {sm_count} SMs x 128 lanes x 2 flop x sm_max_mhz "
+                                    "(MEASURED_PEAKS.json holds no FP32 CUDA-core peak)",
+                     "kernel": "atom_pass_kernel (Static, forward + adjoint)", "kernel_ms": pass_ms,
+                     "flops_per_launch": flops,
+                     "hbm": {"achieved": abytes / (pass_ms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": abytes / (pass_ms / 1e3) / 1e9 / hbm_peak, "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
+                     "traffic": traffic},
+        "cpu_baseline": {"value": cpu_value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{nev} E/F/virial evaluations of the same 4,096-atom frame by the FP64 CPU "
+                                   f"restatement on {threads} threads, edge build excluded "
+                                   f"({1e3 * te / max(nev, 1):.1f} ms each)"},
+        "e2e": {"value": n / (e2e_ms / 1e3), "unit": "atom-steps/s",
+                "h2d_bytes_per_step": n * 3 * 8 + n * 4 + 9 * 8,
+                "d2h_bytes_per_step": 8 + n * 3 * 8 + 6 * 8 + n * 8, "ms_per_step": e2e_ms,
+                "api": "sus2g_calc_efs_host (C ABI, host buffers)"},
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "effect_l4k8r2o3_110592": extra or None,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-effect", action="store_true", help="skip the 110,592-atom Effect measurement")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="only the FP32 timed steps (for ncu captures); prints a short JSON line")
+    ap.add_argument("--cells", type=int, default=8, help="diamond cells per edge (8 -> the 4,096-atom workload)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

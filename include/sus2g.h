@@ -62,6 +62,13 @@ int sus2g_engine_set_stream(sus2g_engine engine, void* cuda_stream);
 int sus2g_engine_take_launch_count(sus2g_engine engine, int* count);
 /* Number of directed edges of the last evaluation. */
 int sus2g_engine_edge_count(sus2g_engine engine, long long* count);
+/* Stage timer (CUDA events on the engine's stream), the counterpart of the reference's
+ * profile_every stage timers and Kernel::outer_profile (pair_sus2_embedded.cpp:261-264,320-361;
+ * sus2_sl_kernel.h:33-35).  Stages: 0 edge build, 1 Static/outer pass, 2 gate forward pass,
+ * 3 gate reverse pass, 4 force gather + per-frame reductions.  take_stage_times synchronises and
+ * returns milliseconds[8] and event-pair counts[8] accumulated since the previous call. */
+int sus2g_engine_set_timing(sus2g_engine engine, int enabled);
+int sus2g_engine_take_stage_times(sus2g_engine engine, double* ms8, int* counts8);
 
 /* ---- E / F / virial of periodic frames (trainer calc-efs path) ----------------------------------
  * Replaces MLMTPR::CalcEFS(Configuration&) (dev_src/mtpr.cpp:8779-8956) including its

@@ -44,6 +44,9 @@ def lib():
         L.orc_efs.restype = ctypes.c_longlong
         L.orc_efs.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_int,
                               ctypes.c_char_p, ctypes.c_int]
+        L.orc_efs_timed.restype = ctypes.c_longlong
+        L.orc_efs_timed.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_int,
+                                    _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_efs_edges.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp,
                                     _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
@@ -100,6 +103,23 @@ class OracleModel:
         if ne < 0:
             raise RuntimeError(err.value.decode())
         return float(e[0]), f, v, s, int(ne)
+
+    def efs_timed(self, cell, pos, types, threads: int = 0):
+        """One frame; returns (energy, n_edges, edge_build_seconds, compute_seconds)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        n = types.size
+        e = np.zeros(1)
+        f = np.zeros((n, 3))
+        v = np.zeros(6)
+        sec = np.zeros(2)
+        err = ctypes.create_string_buffer(512)
+        ne = lib().orc_efs_timed(self._h, n, _d(cell), _d(pos), _i(types), _d(e), _d(f), _d(v), None, threads,
+                                 _d(sec), err, 512)
+        if ne < 0:
+            raise RuntimeError(err.value.decode())
+        return float(e[0]), int(ne), float(sec[0]), float(sec[1])
 
     def efs_edges(self, nowned, types, ei, ej, d):
         types = np.ascontiguousarray(types, dtype=np.int32)

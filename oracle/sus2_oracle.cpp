@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
@@ -235,7 +236,7 @@ void harmonics(const V3& d, int L, vector<double>& Y, vector<double>& dY) {
   const double u[3] = {d[0] / r, d[1] / r, d[2] / r};
   const double pi = std::acos(-1.0);
   std::complex<double> w(u[0], u[1]);
-  vector<std::complex<double>> pw(L + 1);
+  std::complex<double> pw[8];
   pw[0] = 1.0;
   for (int m = 1; m <= L; ++m) pw[m] = pw[m - 1] * w;
   for (int m = 0; m <= L; ++m) {
@@ -251,9 +252,17 @@ void harmonics(const V3& d, int L, vector<double>& Y, vector<double>& dY) {
         dp = ((2 * l - 1) * (pm1 + u[2] * dm1) - (l + m - 1) * dm2) / (l - m);
       }
       pm2 = pm1; pm1 = p; dm2 = dm1; dm1 = dp;
-      double ratio = 1;
-      for (int a = l - m + 1; a <= l + m; ++a) ratio /= a;
-      const double n = std::sqrt((2 * l + 1) * ratio / (4 * pi)) * (m ? std::sqrt(2.0) : 1.0);
+      static const std::array<double, 64> norms = [pi] {
+        std::array<double, 64> t{};
+        for (int ll = 0; ll <= 6; ++ll)
+          for (int mm = 0; mm <= ll; ++mm) {
+            double ratio = 1;
+            for (int a = ll - mm + 1; a <= ll + mm; ++a) ratio /= a;
+            t[hidx(ll, mm)] = std::sqrt((2 * ll + 1) * ratio / (4 * pi)) * (mm ? std::sqrt(2.0) : 1.0);
+          }
+        return t;
+      }();
+      const double n = norms[hidx(l, m)];
       // extension values and grad_u
       std::complex<double> t = pw[m];
       std::complex<double> tx = m ? double(m) * pw[m - 1] : std::complex<double>(0);   // d/dux (ux+i uy)^m
@@ -274,7 +283,7 @@ void harmonics(const V3& d, int L, vector<double>& Y, vector<double>& dY) {
 // Chebyshev radial basis with envelope: values v, d/dr, d/dslope, d2/dslope dr, d/dshift, d2/dshift dr.
 struct Rad { double v[16], r[16], s[16], sr[16], g[16], gr[16]; };
 
-void radial(const Model& m, double r, double slope, double shift, double rc, Rad& o) {
+void radial(const Model& m, double r, double slope, double shift, double rc, Rad& o, bool param_derivs = true) {
   double f, fd;
   if (r >= rc) { f = 0; fd = 0; }
   else if (!m.poly) { f = (r - rc) * (r - rc); fd = 2 * (r - rc); }
@@ -290,6 +299,22 @@ void radial(const Model& m, double r, double slope, double shift, double rc, Rad
   const double xi = std::tanh(slope * (r - shift) / 2), e = 1 - xi * xi;
   const double xr = e * slope / 2, xs = e * (r - shift) / 2, xg = -e * slope / 2;
   const double xrs = e / 2 - xi * xs * slope, xrg = -xi * xg * slope;
+  if (!param_derivs) {  // values and d/dr only (E / F / virial)
+    double T0 = 1, T1 = xi, D0 = 0, D1 = 1;
+    for (int b = 0; b < m.B; ++b) {
+      double T, D;
+      if (b == 0) { T = T0; D = D0; }
+      else if (b == 1) { T = T1; D = D1; }
+      else {
+        T = 2 * xi * T1 - T0;
+        D = 2 * T1 + 2 * xi * D1 - D0;
+        T0 = T1; T1 = T; D0 = D1; D1 = D;
+      }
+      o.v[b] = f * T;
+      o.r[b] = fd * T + f * D * xr;
+    }
+    return;
+  }
   // T_b(xi), T_b', T_b''
   double T[16], D[16], DD[16];
   T[0] = 1; D[0] = 0; DD[0] = 0;
@@ -324,7 +349,8 @@ vector<Edge> image_edges(int n, const double* cell, const double* pos, double rc
   for (auto& row : inv) for (auto& x : row) x /= det;
   double reach[3];
   for (int q = 0; q < 3; ++q) { double s = 0; for (int a = 0; a < 3; ++a) s += inv[a][q] * inv[a][q]; reach[q] = rc * std::sqrt(s); }
-  vector<Edge> out;
+  vector<vector<Edge>> per(n);
+#pragma omp parallel for schedule(dynamic, 16)
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       V3 d{}, f{};
@@ -339,9 +365,11 @@ vector<Edge> image_edges(int n, const double* cell, const double* pos, double rc
             V3 v = d;
             double r2 = 0;
             for (int q = 0; q < 3; ++q) { v[q] += a * c[0][q] + b * c[1][q] + cc * c[2][q]; r2 += v[q] * v[q]; }
-            if (r2 < rc * rc) out.push_back({i, j, v});
+            if (r2 < rc * rc) per[i].push_back({i, j, v});
           }
     }
+  vector<Edge> out;
+  for (auto& p : per) out.insert(out.end(), p.begin(), p.end());
   return out;
 }
 
@@ -391,7 +419,7 @@ struct EdgeEval {
   vector<Rad> rad;               // per mu (raw basis derivatives)
 };
 
-void eval_edge(const Model& m, const Pass& p, const Edge& e, int ti, int tj, EdgeEval& ev) {
+void eval_edge(const Model& m, const Pass& p, const Edge& e, int ti, int tj, EdgeEval& ev, bool param_derivs = true) {
   const int Lp = m.L + 1, C = m.C;
   ev.r = std::sqrt(e.d[0] * e.d[0] + e.d[1] * e.d[1] + e.d[2] * e.d[2]);
   for (int q = 0; q < 3; ++q) ev.u[q] = e.d[q] / ev.r;
@@ -402,14 +430,14 @@ void eval_edge(const Model& m, const Pass& p, const Edge& e, int ti, int tj, Edg
   }
   ev.R.assign(m.F, 0.0);
   ev.Rd.assign(m.F, 0.0);
-  ev.rad.assign(m.F, Rad{});
+  if (ev.rad.size() != static_cast<size_t>(m.F)) ev.rad.resize(m.F);  // entries are rewritten below when used
   for (int k = 0; k < m.K; ++k)
     for (int l = 0; l < Lp; ++l) {
       if (l > 0 && !ang) continue;
       const int mu = k * Lp + l, sb = sblock(m, k, l), pair = ti * C + tj;
       const double slope = (*p.scal)[2 * sb * C * C + pair], shift = (*p.scal)[(2 * sb + 1) * C * C + pair];
       const double rc = (l > 0 && m.split) ? m.rang : m.rmax;
-      radial(m, ev.r, slope, shift, rc, ev.rad[mu]);
+      radial(m, ev.r, slope, shift, rc, ev.rad[mu], param_derivs);
       double a = 0, ad = 0;
       for (int b = 0; b < m.B; ++b) {
         const double c = (*p.coeff)[static_cast<size_t>(mu) * p.stride + b];
@@ -519,7 +547,7 @@ void evaluate(const Ctx& cx, int ncentres, Result& res, int threads) {
       for (int e = cx.row[i]; e < cx.row[i + 1]; ++e) {
         const Edge& ed = cx.edges[e];
         const int ti = cx.types[ed.i], tj = cx.types[ed.j];
-        eval_edge(m, pg, ed, ti, tj, ev);
+        eval_edge(m, pg, ed, ti, tj, ev, false);
         for (int b = 0; b < m.NB; ++b) {
           const int mu = basic_mu(m, b);
           v[b] += wfac(m, pg, ti, mu) * wfac(m, pg, tj, mu) * ev.R[mu] * ev.Y[basic_h(m, b)];
@@ -543,7 +571,7 @@ void evaluate(const Ctx& cx, int ncentres, Result& res, int threads) {
     for (int e = cx.row[i]; e < cx.row[i + 1]; ++e) {
       const Edge& ed = cx.edges[e];
       const int tj = cx.types[ed.j];
-      eval_edge(m, po, ed, ti, tj, ev);
+      eval_edge(m, po, ed, ti, tj, ev, false);
       for (int b = 0; b < m.NB; ++b) {
         const int mu = basic_mu(m, b);
         double x3 = wfac(m, po, tj, mu);
@@ -564,7 +592,7 @@ void evaluate(const Ctx& cx, int ncentres, Result& res, int threads) {
     for (int e = cx.row[i]; e < cx.row[i + 1]; ++e) {
       const Edge& ed = cx.edges[e];
       const int tj = cx.types[ed.j];
-      eval_edge(m, po, ed, ti, tj, ev);
+      eval_edge(m, po, ed, ti, tj, ev, false);
       V3 g{0, 0, 0};
       for (int b = 0; b < m.NB; ++b) {
         const int mu = basic_mu(m, b), hh = basic_h(m, b);
@@ -599,7 +627,7 @@ void evaluate(const Ctx& cx, int ncentres, Result& res, int threads) {
       for (int e = cx.row[i]; e < cx.row[i + 1]; ++e) {
         const Edge& ed = cx.edges[e];
         const int tj = cx.types[ed.j];
-        eval_edge(m, pg, ed, ti, tj, ev);
+        eval_edge(m, pg, ed, ti, tj, ev, false);
         for (int b = 0; b < m.NB; ++b) {
           const int mu = basic_mu(m, b), hh = basic_h(m, b);
           const double adj = lam[b] * wfac(m, pg, ti, mu) * wfac(m, pg, tj, mu);
@@ -900,19 +928,33 @@ int orc_set_params(void* mp, const double* in) {
 
 long long orc_efs(void* mp, int n, const double* cell, const double* pos, const int* types, double* energy,
                   double* forces, double* virial, double* site, int threads, char* err, int errlen) {
+  return orc_efs_timed(mp, n, cell, pos, types, energy, forces, virial, site, threads, nullptr, err, errlen);
+}
+
+long long orc_efs_timed(void* mp, int n, const double* cell, const double* pos, const int* types, double* energy,
+                        double* forces, double* virial, double* site, int threads, double* seconds, char* err,
+                        int errlen) {
   try {
     const Model& m = *static_cast<Model*>(mp);
 #ifdef _OPENMP
     if (threads <= 0) threads = omp_get_max_threads();
+    omp_set_num_threads(threads);
 #else
     threads = 1;
 #endif
+    const auto t0 = std::chrono::steady_clock::now();
     Ctx cx = make_ctx(m, n, cell, pos, types);
+    const auto t1 = std::chrono::steady_clock::now();
     Result res;
     evaluate(cx, n, res, threads);
     if (energy) *energy = res.energy;
     if (site) std::copy(res.site.begin(), res.site.end(), site);
     finish(cx, res, forces, virial);
+    const auto t2 = std::chrono::steady_clock::now();
+    if (seconds) {
+      seconds[0] = std::chrono::duration<double>(t1 - t0).count();
+      seconds[1] = std::chrono::duration<double>(t2 - t1).count();
+    }
     return static_cast<long long>(cx.edges.size());
   } catch (const std::exception& e) {
     set_err(err, errlen, e.what());

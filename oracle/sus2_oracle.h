@@ -21,6 +21,10 @@ int orc_set_params(void* model, const double* in);
  * Returns the number of directed edges, or -1 on error (message in err). */
 long long orc_efs(void* model, int n, const double* cell, const double* pos, const int* types, double* energy,
                   double* forces, double* virial, double* site, int threads, char* err, int errlen);
+/* Same, also returning seconds[2] = {edge build, E/F/virial compute}. */
+long long orc_efs_timed(void* model, int n, const double* cell, const double* pos, const int* types, double* energy,
+                        double* forces, double* virial, double* site, int threads, double* seconds, char* err,
+                        int errlen);
 /* Caller edge list (single domain, owned centres 0..nowned-1 of nall atoms). */
 int orc_efs_edges(void* model, int nowned, int nall, const int* types, int nedges, const int* ei, const int* ej,
                   const double* d, double* energy, double* forces, double* virial, double* site, char* err, int errlen);

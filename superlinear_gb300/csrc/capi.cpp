@@ -48,11 +48,10 @@ void cuda(cudaError_t e, const char* where) {
   if (e != cudaSuccess) throw sus2g::Error(10, std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e));
 }
 
-// Device staging buffer owned by the call.
-struct Stage {
-  void* p = nullptr;
-  explicit Stage(size_t n) { if (n) cuda(cudaMalloc(&p, n), "staging allocation"); }
-  ~Stage() { if (p) cudaFree(p); }
+// Engine-owned, grow-only device staging buffer for host arrays.
+struct Slot {
+  void* p;
+  Slot(sus2g::Engine& e, int slot, size_t n) : p(e.io(slot, n)) {}
   template <typename T> T* as() { return static_cast<T*>(p); }
 };
 
@@ -153,6 +152,14 @@ int sus2g_engine_edge_count(sus2g_engine e, long long* count) {
   return guarded([&] { need(e && count, "engine/count"); *count = e->engine->nedges(); });
 }
 
+int sus2g_engine_set_timing(sus2g_engine e, int enabled) {
+  return guarded([&] { need(e, "engine"); e->engine->set_timing(enabled != 0); });
+}
+
+int sus2g_engine_take_stage_times(sus2g_engine e, double* ms, int* counts) {
+  return guarded([&] { need(e, "engine"); e->engine->take_stage_times(ms, counts); });
+}
+
 int sus2g_calc_efs_device(sus2g_engine e, int nframes, const int* natoms, const double* cells,
                           const double* positions, const int* types, double* energy, double* forces,
                           double* virial, double* site_energy) {
@@ -179,9 +186,9 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
       need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
     cudaStream_t s = eng.stream();
     cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
-    Stage pos(sizeof(double) * 3 * n), typ(sizeof(int) * n);
-    Stage out_e(sizeof(double) * nframes), out_f(sizeof(double) * 3 * n), out_v(sizeof(double) * 6 * nframes),
-        out_s(sizeof(double) * n);
+    Slot pos(eng, 0, sizeof(double) * 3 * n), typ(eng, 1, sizeof(int) * n);
+    Slot out_e(eng, 2, sizeof(double) * nframes), out_f(eng, 3, sizeof(double) * 3 * n),
+        out_v(eng, 4, sizeof(double) * 6 * nframes), out_s(eng, 5, sizeof(double) * n);
     if (n) {
       cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
       cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
@@ -216,8 +223,10 @@ int sus2g_efs_edges_host(sus2g_engine e, int nowned, int nall, const int* types,
     }
     cudaStream_t s = eng.stream();
     cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
-    Stage typ(sizeof(int) * nall), di(sizeof(int) * nedges), dj(sizeof(int) * nedges), dd(sizeof(double) * 3 * nedges);
-    Stage out_e(sizeof(double)), out_f(sizeof(double) * 3 * nall), out_v(sizeof(double) * 6), out_s(sizeof(double) * nowned);
+    Slot typ(eng, 0, sizeof(int) * nall), di(eng, 1, sizeof(int) * nedges), dj(eng, 2, sizeof(int) * nedges),
+        dd(eng, 3, sizeof(double) * 3 * nedges);
+    Slot out_e(eng, 4, sizeof(double)), out_f(eng, 5, sizeof(double) * 3 * nall), out_v(eng, 6, sizeof(double) * 6),
+        out_s(eng, 7, sizeof(double) * nowned);
     if (nall) cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * nall, cudaMemcpyHostToDevice, s), "types copy");
     if (nedges) {
       cuda(cudaMemcpyAsync(di.p, ei, sizeof(int) * nedges, cudaMemcpyHostToDevice, s), "edge copy");

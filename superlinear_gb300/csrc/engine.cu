@@ -46,17 +46,23 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
 }
 
 __global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
-                            int* bin_of, int* bin_count) {
+                            int* bin_of, int* bin_count, AtomFrac* frac, AtomOff* off) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
   if (!fp.use_bins) { bin_of[i] = -1; return; }
-  int b[3];
+  int b[3], o[3];
+  float w32[3];
   for (int q = 0; q < 3; ++q) {
     const double s = pos[3 * i] * fp.inv[q] + pos[3 * i + 1] * fp.inv[3 + q] + pos[3 * i + 2] * fp.inv[6 + q];
-    const double w = s - floor(s);
+    const double fl = floor(s);
+    const double w = s - fl;
+    o[q] = static_cast<int>(fl);
+    w32[q] = static_cast<float>(w);
     b[q] = min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1);
   }
+  frac[i] = AtomFrac{w32[0], w32[1], w32[2], 0};
+  off[i] = AtomOff{o[0], o[1], o[2], 0};
   const int bin = fp.bin0 + (b[0] * fp.nb[1] + b[1]) * fp.nb[2] + b[2];
   bin_of[i] = bin;
   atomicAdd(bin_count + bin, 1);
@@ -84,34 +90,84 @@ __global__ void k_bin_sort(const int* bin_start, int nbins, int* bin_atoms) {
   }
 }
 
+// Image-scan frames: one thread per centre (cell-list frames are left to the warp kernels).
 __global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                             const int* bin_start, const int* bin_atoms, int* counts, int* error) {
+                             const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                             const AtomOff* off, int* counts, int* error) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (fp.use_bins) return;
   int n = 0;
-  enumerate_edges(i, plans[frame_of[i]], pos, rc2, bin_start, bin_atoms, error,
+  enumerate_edges(i, 0, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
                   [&](int, int, int, int, double, double, double, double) { ++n; });
   counts[i] = n;
 }
 
 template <typename Real>
+__device__ __forceinline__ void write_edge(int e, int j, int a, int b, int c, double x, double y, double z, double r2,
+                                           int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key) {
+  nbr[e] = j;
+  typename Vec4<Real>::type v;
+  v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
+  d4[e] = v;
+  key[e] = edge_key(j, a, b, c);
+}
+
+template <typename Real>
 __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                            const int* bin_start, const int* bin_atoms, const int* row, int* nbr,
-                            typename Vec4<Real>::type* d4, unsigned long long* key, int* error) {
+                            const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                            const AtomOff* off, const int* row, int* nbr, typename Vec4<Real>::type* d4,
+                            unsigned long long* key, int* error) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (fp.use_bins) return;
   int e = row[i];
   const int end = row[i + 1];
-  enumerate_edges(i, plans[frame_of[i]], pos, rc2, bin_start, bin_atoms, error,
+  enumerate_edges(i, 0, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
                   [&](int j, int a, int b, int c, double x, double y, double z, double r2) {
                     if (e >= end) { record_error(error, kErrEdgeCapacity); return; }
-                    nbr[e] = j;
-                    typename Vec4<Real>::type v;
-                    v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
-                    d4[e] = v;
-                    key[e] = edge_key(j, a, b, c);
-                    ++e;
+                    write_edge<Real>(e++, j, a, b, c, x, y, z, r2, nbr, d4, key);
                   });
+}
+
+// Cell-list frames: one warp per centre over the flattened 27-bin candidate list.
+__global__ void k_edge_count_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
+                                  double rc2, const int* bin_start, const int* bin_atoms, const int* bin_of,
+                                  const AtomFrac* frac, const AtomOff* off, int* counts, int* error) {
+  const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
+  if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (!fp.use_bins) return;
+  int n = 0;
+  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
+                 [&](unsigned mask, bool, int, int, int, int, double, double, double, double) { n += __popc(mask); });
+  if ((threadIdx.x & 31) == 0) counts[i] = n;
+}
+
+template <typename Real>
+__global__ void k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
+                                 double rc2, const int* bin_start, const int* bin_atoms, const int* bin_of,
+                                 const AtomFrac* frac, const AtomOff* off, const int* row, int* nbr,
+                                 typename Vec4<Real>::type* d4, unsigned long long* key, int* error) {
+  const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
+  if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (!fp.use_bins) return;
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  int cursor = row[i];
+  const int end = row[i + 1];
+  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
+                 [&](unsigned mask, bool ok, int j, int a, int b, int c, double x, double y, double z, double r2) {
+                   if (ok) {
+                     const int e = cursor + __popc(mask & below);
+                     if (e < end) write_edge<Real>(e, j, a, b, c, x, y, z, r2, nbr, d4, key);
+                     else record_error(error, kErrEdgeCapacity);
+                   }
+                   cursor += __popc(mask);
+                 });
 }
 
 // Sort one centre's edges by key (warp per centre, rank sort; keys within a centre are unique).
@@ -261,6 +317,35 @@ __global__ void k_scatter_user_edges(const int* ei, const int* ej, const double*
   d4[p] = v;
   // Order key: neighbour, then the caller's edge index (unique, deterministic).
   key[p] = (static_cast<unsigned long long>(j) << 32) | static_cast<unsigned long long>(e & 0xffffffffLL);
+}
+
+// Exclusive scan of n counts into row[0..n] on the device (one block; each thread scans a
+// contiguous chunk, then the chunk totals are scanned in shared memory).  Totals above 2^31 - 1
+// are flagged.
+__global__ void k_exclusive_scan(const int* counts, int n, int* row, int* error) {
+  __shared__ long long part[1024];
+  const int t = threadIdx.x, T = blockDim.x;
+  const long long chunk = (static_cast<long long>(n) + T - 1) / T;
+  const long long a = t * chunk, b = min(static_cast<long long>(n), a + chunk);
+  long long s = 0;
+  for (long long i = a; i < b; ++i) s += counts[i];
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < T; off <<= 1) {
+    const long long v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long run = part[t] - s;
+  for (long long i = a; i < b; ++i) {
+    row[i] = static_cast<int>(run);
+    run += counts[i];
+  }
+  if (t == T - 1) {
+    if (part[t] > 2147483647LL) record_error(error, kErrEdgeCapacity);
+    row[n] = static_cast<int>(min(part[t], 2147483647LL));
+  }
 }
 
 void exclusive_scan_host_sync(const int* d_counts, int n, int* d_row, cudaStream_t s, long long* total) {
@@ -414,6 +499,7 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   if (model_.gated && !unique(model_.gate_nodes)) throw Error(3, "SUS2 model: duplicate gate scalar moments");
   if (model_.K > kMaxK) throw Error(3, "SUS2 model: sh_k_max above 8 is not supported by the GPU engine");
   plans_ = new std::vector<FramePlan>();
+  SUS2G_CUDA(cudaMallocHost(&host_total_, sizeof(int)));
   error_.ensure(sizeof(int));
   SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
   upload_model();
@@ -421,6 +507,8 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
 
 Engine::~Engine() {
   delete plans_;
+  if (host_total_) cudaFreeHost(host_total_);
+  for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
   if (precision_ == kFP32) delete static_cast<DevModel<float>*>(dev_model_);
   else delete static_cast<DevModel<double>*>(dev_model_);
   if (own_stream_) cudaStreamDestroy(own_stream_);
@@ -501,6 +589,55 @@ void Engine::check_device_error() {
   }
 }
 
+cudaEvent_t Engine::take_event() {
+  if (event_next_ == event_pool_.size()) {
+    cudaEvent_t e;
+    SUS2G_CUDA(cudaEventCreate(&e));
+    event_pool_.push_back(e);
+  }
+  return event_pool_[event_next_++];
+}
+
+void Engine::mark_begin(int stage) {
+  if (!timing_) return;
+  open_stage_ = stage;
+  open_event_ = take_event();
+  SUS2G_CUDA(cudaEventRecord(open_event_, stream_));
+}
+
+void Engine::mark_end() {
+  if (!timing_ || open_stage_ < 0) return;
+  cudaEvent_t e = take_event();
+  SUS2G_CUDA(cudaEventRecord(e, stream_));
+  marks_.push_back({open_stage_, {open_event_, e}});
+  open_stage_ = -1;
+}
+
+void Engine::set_timing(bool on) {
+  timing_ = on;
+  marks_.clear();
+  event_next_ = 0;
+  for (int i = 0; i < 8; ++i) { stage_ms_[i] = 0; stage_count_[i] = 0; }
+}
+
+void Engine::take_stage_times(double* ms, int* counts) {
+  SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  for (const auto& m : marks_) {
+    float t = 0;
+    SUS2G_CUDA(cudaEventElapsedTime(&t, m.second.first, m.second.second));
+    stage_ms_[m.first] += t;
+    stage_count_[m.first] += 1;
+  }
+  marks_.clear();
+  event_next_ = 0;
+  for (int i = 0; i < 8; ++i) {
+    if (ms) ms[i] = stage_ms_[i];
+    if (counts) counts[i] = stage_count_[i];
+    stage_ms_[i] = 0;
+    stage_count_[i] = 0;
+  }
+}
+
 void Engine::build_edges(int nframes, const int* frame_natoms, const double* cells, const double* d_pos,
                          const int* d_types) {
   SUS2G_CUDA(cudaSetDevice(device_));
@@ -509,6 +646,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   std::vector<FramePlan>& plans = *plans_;
   plans.assign(nframes, FramePlan{});
   int a = 0, bins = 0;
+  bins_frames_ = 0;
   for (int f = 0; f < nframes; ++f) {
     FramePlan& fp = plans[f];
     if (frame_natoms[f] < 0) throw Error(1, "negative atom count");
@@ -527,7 +665,15 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     fp.use_bins = frame_natoms[f] > 512 && width[0] >= 3 * rc && width[1] >= 3 * rc && width[2] >= 3 * rc;
     fp.bin0 = bins;
     if (fp.use_bins) {
+      ++bins_frames_;
       for (int q = 0; q < 3; ++q) fp.nb[q] = std::max(3, std::min(512, static_cast<int>(width[q] / rc)));
+      // FP32 prefilter: |error of r^2| <= 2 r_c |error of d|, with |error of d| bounded by the
+      // rounding of the wrapped fractions (< 2^-24 each, three terms) times the cell row norms
+      double rows = 0;
+      for (int q = 0; q < 3; ++q)
+        rows += std::sqrt(fp.cell[3 * q] * fp.cell[3 * q] + fp.cell[3 * q + 1] * fp.cell[3 * q + 1] + fp.cell[3 * q + 2] * fp.cell[3 * q + 2]);
+      fp.band = 2.0 * rc * (4.0 * 6.0e-8 * rows) * 4.0 + 1e-6;
+      for (int q = 0; q < 9; ++q) fp.cellf[q] = static_cast<float>(fp.cell[q]);
       bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
     }
   }
@@ -536,6 +682,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   d_types_ = d_types;
   user_edges_ = false;
   cudaStream_t s = stream_;
+  mark_begin(0);
   plan_.ensure(sizeof(FramePlan) * std::max(1, nframes));
   if (nframes) SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
   frame_of_.ensure(sizeof(int) * std::max(1, a));
@@ -545,26 +692,44 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   bin_start_.ensure(sizeof(int) * (bins + 1));
   bin_cursor_.ensure(sizeof(int) * (bins + 1));
   bin_atoms_.ensure(sizeof(int) * std::max(1, a));
-  DevBuf bin_of;  // per-call temporary
+  DevBuf& bin_of = bin_of_;
   bin_of.ensure(sizeof(int) * std::max(1, a));
   if (nframes) { k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>()); ++launches_; }
   if (bins) {
     SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
     SUS2G_CUDA(cudaMemsetAsync(bin_cursor_.ptr, 0, sizeof(int) * (bins + 1), s));
-    k_bin_count<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, bin_of.as<int>(), bin_count_.as<int>());
-    long long tot = 0;
-    exclusive_scan_host_sync(bin_count_.as<int>(), bins, bin_start_.as<int>(), s, &tot);
-    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(), bin_atoms_.as<int>());
-    k_bin_sort<<<(bins + 127) / 128, 128, 0, s>>>(bin_start_.as<int>(), bins, bin_atoms_.as<int>());
-    launches_ += 3;
-  }
-  if (a) {
-    k_edge_count<<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
-                                                   bin_start_.as<int>(), bin_atoms_.as<int>(), counts_.as<int>(), error_.as<int>());
+    frac_.ensure(sizeof(AtomFrac) * a);
+    off_.ensure(sizeof(AtomOff) * a);
+    k_bin_count<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, bin_of.as<int>(),
+                                               bin_count_.as<int>(), frac_.as<AtomFrac>(), off_.as<AtomOff>());
+    k_exclusive_scan<<<1, 1024, 0, s>>>(bin_count_.as<int>(), bins, bin_start_.as<int>(), error_.as<int>());
     ++launches_;
+    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(), bin_atoms_.as<int>());
+    launches_ += 2;
   }
-  long long total = 0;
-  exclusive_scan_host_sync(counts_.as<int>(), a, row_.as<int>(), s, &total);
+  const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
+  const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);
+  if (a) {
+    SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
+    if (bins) {
+      k_edge_count_bins<<<warp_blocks, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
+                                                    bin_start_.as<int>(), bin_atoms_.as<int>(), bin_of.as<int>(),
+                                                    frac_.as<AtomFrac>(), off_.as<AtomOff>(), counts_.as<int>(), error_.as<int>());
+      ++launches_;
+    }
+    if (bins_frames_ < nframes) {
+      k_edge_count<<<thread_blocks, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
+                                                 bin_start_.as<int>(), bin_atoms_.as<int>(), bin_of.as<int>(), frac_.as<AtomFrac>(),
+                                                 off_.as<AtomOff>(), counts_.as<int>(), error_.as<int>());
+      ++launches_;
+    }
+  }
+  k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
+  ++launches_;
+  // the only host synchronisation of the build: the edge total sizes the edge arrays
+  SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SUS2G_CUDA(cudaStreamSynchronize(s));
+  const long long total = *host_total_;
   nedges_ = total;
   const size_t E = std::max<long long>(1, total);
   const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
@@ -573,15 +738,27 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   d4_.ensure(rsz * E); tmp_d4_.ensure(rsz * E);
   key_.ensure(sizeof(unsigned long long) * E); tmp_key_.ensure(sizeof(unsigned long long) * E);
   if (a) {
-    if (precision_ == kFP32)
-      k_edge_fill<float><<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2, bin_start_.as<int>(),
-          bin_atoms_.as<int>(), row_.as<int>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), tmp_key_.as<unsigned long long>(), error_.as<int>());
-    else
-      k_edge_fill<double><<<(a + 127) / 128, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2, bin_start_.as<int>(),
-          bin_atoms_.as<int>(), row_.as<int>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), tmp_key_.as<unsigned long long>(), error_.as<int>());
-    ++launches_;
+    const FramePlan* P = plan_.as<FramePlan>();
+    const int* F = frame_of_.as<int>();
+    const int *BS = bin_start_.as<int>(), *BA = bin_atoms_.as<int>(), *BO = bin_of.as<int>();
+    const AtomFrac* FR = frac_.as<AtomFrac>();
+    const AtomOff* OF = off_.as<AtomOff>();
+    unsigned long long* KY = tmp_key_.as<unsigned long long>();
+    if (precision_ == kFP32) {
+      if (bins) k_edge_fill_bins<float><<<warp_blocks, 256, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                                    tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
+      if (bins_frames_ < nframes) k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                                                 tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
+    } else {
+      if (bins) k_edge_fill_bins<double><<<warp_blocks, 256, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                                     tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
+      if (bins_frames_ < nframes) k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                                                  tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
+    }
+    launches_ += (bins ? 1 : 0) + (bins_frames_ < nframes ? 1 : 0);
   }
   finalize_edges();
+  mark_end();
 }
 
 void Engine::finalize_edges() {
@@ -685,7 +862,9 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   a.virial = vir_atom_.as<double>();
   a.error = error_.as<int>();
   if (!m.gated) {
+    mark_begin(1);
     launches_ += launch_atom_pass<Real>(m.L, kModeStatic, a, sm_count_, s);
+    mark_end();
   } else {
     hsig_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F);
     hcontrib_.ensure(sizeof(Real) * E * m.F);
@@ -694,8 +873,12 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     a.hcontrib = hcontrib_.as<Real>();
     a.gmom = gmom_.as<Real>();
     if (ncentres_ != natoms_) throw Error(1, "Effect models on a ghost layout need the forward gate exchange (not in this call)");
+    mark_begin(2);
     launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
+    mark_end();
+    mark_begin(1);
     launches_ += launch_atom_pass<Real>(m.L, kModeOuter, a, sm_count_, s);
+    mark_end();
     if (user_edges_) {
       hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
       SUS2G_CUDA(cudaMemsetAsync(hbar_atom_.ptr, 0, sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F, s));
@@ -706,8 +889,11 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       }
       a.hbar_atom = hbar_atom_.as<double>();
     }
+    mark_begin(3);
     launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
+    mark_end();
   }
+  mark_begin(4);
   if (d_forces && N) {
     if (user_edges_) {
       SUS2G_CUDA(cudaMemsetAsync(d_forces, 0, sizeof(double) * 3 * N, s));
@@ -725,6 +911,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     ++launches_;
   }
   if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
+  mark_end();
 }
 
 void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {

@@ -66,6 +66,18 @@ class Engine {
   // Raises if a kernel recorded an error (synchronises the stream).
   void check_device_error();
 
+  // Stage timer: when enabled, each stage of build_edges / efs is bracketed by CUDA events on
+  // the engine's stream.  Stages: 0 edge build, 1 Static/outer pass, 2 gate forward pass,
+  // 3 gate reverse pass, 4 force gather + frame reductions.
+  void set_timing(bool on);
+  // Synchronises, then adds the elapsed milliseconds and launch counts per stage since the last
+  // call into ms[8] / counts[8] and resets them.
+  void take_stage_times(double* ms, int* counts);
+
+  // Grow-only device staging buffer `slot` (0..7) of at least `bytes`, owned by the engine, for
+  // entry points that copy host arrays in and out.
+  void* io(int slot, size_t bytes) { io_[slot].ensure(bytes ? bytes : 1); return io_[slot].ptr; }
+
   // internal buffers exposed for the tests / parameter-gradient pass
   const int* d_row() const { return row_.as<int>(); }
   const int* d_nbr() const { return nbr_.as<int>(); }
@@ -87,7 +99,7 @@ class Engine {
   void* dev_model_ = nullptr;  // host copy of DevModel<Real>
 
   // geometry
-  int natoms_ = 0, nframes_ = 0, ncentres_ = 0;
+  int natoms_ = 0, nframes_ = 0, ncentres_ = 0, bins_frames_ = 0;
   long long nedges_ = 0;
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
@@ -95,10 +107,24 @@ class Engine {
   DevBuf bin_count_, bin_start_, bin_atoms_, bin_cursor_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
-  DevBuf ei_, hbar_atom_;
+  DevBuf ei_, hbar_atom_, bin_of_, frac_, off_;
+  int* host_total_ = nullptr;   // pinned
+  // stage timer (cudaEvent pairs per stage, enabled by set_timing)
+  bool timing_ = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks_;
+  std::vector<cudaEvent_t> event_pool_;
+  size_t event_next_ = 0;
+  double stage_ms_[8] = {0};
+  int stage_count_[8] = {0};
+  cudaEvent_t take_event();
+  void mark_begin(int stage);
+  void mark_end();
+  int open_stage_ = -1;
+  cudaEvent_t open_event_ = nullptr;
   // step buffers
   DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_;
   DevBuf scratch_;
+  DevBuf io_[8];
 };
 
 }  // namespace sus2g

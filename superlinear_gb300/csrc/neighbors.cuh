@@ -25,7 +25,14 @@ struct FramePlan {
   int use_bins;
   int nb[3];
   int bin0;         // first bin index of this frame in the global bin arrays
+  float cellf[9];   // FP32 copy of the cell for the candidate prefilter
+  double band;      // |r^2 error| bound of the FP32 prefilter; candidates within it get the FP64 test
 };
+
+// Per-atom wrapped fractional coordinates (FP32, in [0,1)) and the integer cell offsets
+// floor(frac) (FP64 arithmetic), written by the binning kernel for cell-list frames.
+struct AtomFrac { float x, y, z; int pad; };
+struct AtomOff { int x, y, z, pad; };
 
 __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, int n2) {
   return (static_cast<unsigned long long>(j) << 21) |
@@ -34,14 +41,19 @@ __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, in
          static_cast<unsigned long long>(n2 + 64);
 }
 
-// Enumerate the edges of centre i; Emit(j, n0, n1, n2, dx, dy, dz, r2) is called in a fixed order.
+// Enumerate edges of centre i; Emit(j, n0, n1, n2, dx, dy, dz, r2).  With cell lists, `part`
+// (0..26) selects one of the 27 neighbouring bins so that 27 threads share one centre; the image
+// scan of small frames is done entirely by part 0.  The per-centre order is fixed afterwards by
+// sorting on the (j, n) key, so the emission order does not matter.
 template <typename Emit>
-__device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, const double* pos, double rc2,
-                                                const int* bin_start, const int* bin_atoms, int* error, Emit&& emit) {
+__device__ __forceinline__ void enumerate_edges(int i, int part, const FramePlan& fp, const double* pos, double rc2,
+                                                const int* bin_start, const int* bin_atoms, const int* bin_of,
+                                                const AtomFrac* frac, const AtomOff* off, int* error, Emit&& emit) {
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   const double* c = fp.cell;
   const double* inv = fp.inv;
   if (!fp.use_bins) {
+    if (part != 0) return;
     for (int j = fp.a0; j < fp.a1; ++j) {
       const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
       double f[3];
@@ -67,43 +79,127 @@ __device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, cons
     }
     return;
   }
-  double si[3];
-  int oi[3], bi[3];
+  // Cell list.  Candidates are screened in FP32 on wrapped fractional coordinates; only those
+  // with r^2 below rc^2 + band (the FP32 rounding bound) get the exact FP64 test, so the edge
+  // set is decided in FP64 exactly as the image scan decides it.
+  const AtomFrac fi = frac[i];
+  const AtomOff oi = off[i];
+  // the centre's own bin, as assigned (in FP64) by the binning kernel
+  const int local = bin_of[i] - fp.bin0;
+  const int bi[3] = {local / (fp.nb[1] * fp.nb[2]), (local / fp.nb[2]) % fp.nb[1], local % fp.nb[2]};
+  const int d0 = part / 9 - 1, d1 = (part / 3) % 3 - 1, d2 = part % 3 - 1;
+  const int raw[3] = {bi[0] + d0, bi[1] + d1, bi[2] + d2};
+  int wb[3], W[3];
   for (int q = 0; q < 3; ++q) {
-    si[q] = xi * inv[q] + yi * inv[3 + q] + zi * inv[6 + q];
-    oi[q] = static_cast<int>(floor(si[q]));
-    double w = si[q] - oi[q];
-    bi[q] = min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1);
+    W[q] = raw[q] < 0 ? -1 : (raw[q] >= fp.nb[q] ? 1 : 0);
+    wb[q] = raw[q] - W[q] * fp.nb[q];
   }
-  for (int d0 = -1; d0 <= 1; ++d0)
-    for (int d1 = -1; d1 <= 1; ++d1)
-      for (int d2 = -1; d2 <= 1; ++d2) {
-        const int raw[3] = {bi[0] + d0, bi[1] + d1, bi[2] + d2};
-        int wb[3], W[3];
-        for (int q = 0; q < 3; ++q) {
-          W[q] = raw[q] < 0 ? -1 : (raw[q] >= fp.nb[q] ? 1 : 0);
-          wb[q] = raw[q] - W[q] * fp.nb[q];
-        }
-        const int bin = fp.bin0 + (wb[0] * fp.nb[1] + wb[1]) * fp.nb[2] + wb[2];
-        for (int p = bin_start[bin]; p < bin_start[bin + 1]; ++p) {
-          const int j = bin_atoms[p];
-          const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
-          int n[3];
-          for (int q = 0; q < 3; ++q) {
-            const double sj = xj * inv[q] + yj * inv[3 + q] + zj * inv[6 + q];
-            n[q] = W[q] + oi[q] - static_cast<int>(floor(sj));
-          }
-          if (i == j && n[0] == 0 && n[1] == 0 && n[2] == 0) continue;
-          const double vx = xj - xi + n[0] * c[0] + n[1] * c[3] + n[2] * c[6];
-          const double vy = yj - yi + n[0] * c[1] + n[1] * c[4] + n[2] * c[7];
-          const double vz = zj - zi + n[0] * c[2] + n[1] * c[5] + n[2] * c[8];
-          const double r2 = vx * vx + vy * vy + vz * vz;
-          if (r2 < rc2) {
-            if (n[0] < -64 || n[0] > 63 || n[1] < -64 || n[1] > 63 || n[2] < -64 || n[2] > 63) { record_error(error, kErrImageRange); continue; }
-            emit(j, n[0], n[1], n[2], vx, vy, vz, r2);
+  const float* cf = fp.cellf;
+  const float screen = static_cast<float>(rc2 + fp.band);
+  const int bin = fp.bin0 + (wb[0] * fp.nb[1] + wb[1]) * fp.nb[2] + wb[2];
+  for (int p = bin_start[bin]; p < bin_start[bin + 1]; ++p) {
+    const int j = bin_atoms[p];
+    const AtomFrac fj = frac[j];
+    const float sx = fj.x + static_cast<float>(W[0]) - fi.x, sy = fj.y + static_cast<float>(W[1]) - fi.y,
+                sz = fj.z + static_cast<float>(W[2]) - fi.z;
+    const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
+    const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
+    const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
+    if (fx * fx + fy * fy + fz * fz >= screen) continue;
+    const AtomOff oj = off[j];
+    const int n[3] = {W[0] + oi.x - oj.x, W[1] + oi.y - oj.y, W[2] + oi.z - oj.z};
+    if (i == j && n[0] == 0 && n[1] == 0 && n[2] == 0) continue;
+    const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
+    const double vx = xj - xi + n[0] * c[0] + n[1] * c[3] + n[2] * c[6];
+    const double vy = yj - yi + n[0] * c[1] + n[1] * c[4] + n[2] * c[7];
+    const double vz = zj - zi + n[0] * c[2] + n[1] * c[5] + n[2] * c[8];
+    const double r2 = vx * vx + vy * vy + vz * vz;
+    if (r2 < rc2) {
+      if (n[0] < -64 || n[0] > 63 || n[1] < -64 || n[1] > 63 || n[2] < -64 || n[2] > 63) { record_error(error, kErrImageRange); continue; }
+      emit(j, n[0], n[1], n[2], vx, vy, vz, r2);
+    }
+  }
+  (void)inv;
+}
+
+// Cell-list frames, one warp per centre i: the 27 neighbouring bins' atom ranges are laid end to
+// end (prefix sums over lanes), lanes take consecutive candidates of that flat list, and each
+// round's accepted edges are reported through Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r2)
+// so the caller can count or write them with one ballot per round.
+template <typename Round>
+__device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
+                                               const int* bin_start, const int* bin_atoms, const int* bin_of,
+                                               const AtomFrac* frac, const AtomOff* off, int* error, Round&& round) {
+  const int lane = threadIdx.x & 31;
+  const int local = bin_of[i] - fp.bin0;
+  const int bi0 = local / (fp.nb[1] * fp.nb[2]), bi1 = (local / fp.nb[2]) % fp.nb[1], bi2 = local % fp.nb[2];
+  int start = 0, len = 0, w0 = 0, w1 = 0, w2 = 0;
+  if (lane < 27) {
+    const int raw0 = bi0 + lane / 9 - 1, raw1 = bi1 + (lane / 3) % 3 - 1, raw2 = bi2 + lane % 3 - 1;
+    w0 = raw0 < 0 ? -1 : (raw0 >= fp.nb[0] ? 1 : 0);
+    w1 = raw1 < 0 ? -1 : (raw1 >= fp.nb[1] ? 1 : 0);
+    w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
+    const int bin = fp.bin0 + ((raw0 - w0 * fp.nb[0]) * fp.nb[1] + (raw1 - w1 * fp.nb[1])) * fp.nb[2] + (raw2 - w2 * fp.nb[2]);
+    start = bin_start[bin];
+    len = bin_start[bin + 1] - start;
+  }
+  // inclusive scan of len over lanes
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int excl = incl - len;
+  const AtomFrac fi = frac[i];
+  const AtomOff oi = off[i];
+  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const double* c = fp.cell;
+  const float* cf = fp.cellf;
+  const float screen = static_cast<float>(rc2 + fp.band);
+  for (int base = 0; base < total; base += 32) {
+    const int cand = base + lane;
+    // bin slot k of this candidate: the last lane whose exclusive offset is <= cand
+    int k = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int probe = k + step;
+      const int ex = __shfl_sync(0xffffffffu, excl, probe < 27 ? probe : 26);
+      if (probe < 27 && ex <= cand) k = probe;
+    }
+    const int kstart = __shfl_sync(0xffffffffu, start, k), kex = __shfl_sync(0xffffffffu, excl, k);
+    const int W0 = __shfl_sync(0xffffffffu, w0, k), W1 = __shfl_sync(0xffffffffu, w1, k), W2 = __shfl_sync(0xffffffffu, w2, k);
+    bool ok = false;
+    int j = 0, n0 = 0, n1 = 0, n2 = 0;
+    double vx = 0, vy = 0, vz = 0, r2 = 0;
+    if (cand < total) {
+      j = bin_atoms[kstart + cand - kex];
+      const AtomFrac fj = frac[j];
+      const float sx = fj.x + static_cast<float>(W0) - fi.x, sy = fj.y + static_cast<float>(W1) - fi.y,
+                  sz = fj.z + static_cast<float>(W2) - fi.z;
+      const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
+      const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
+      const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
+      if (fx * fx + fy * fy + fz * fz < screen) {
+        const AtomOff oj = off[j];
+        n0 = W0 + oi.x - oj.x; n1 = W1 + oi.y - oj.y; n2 = W2 + oi.z - oj.z;
+        if (!(i == j && n0 == 0 && n1 == 0 && n2 == 0)) {
+          vx = pos[3 * j] - xi + n0 * c[0] + n1 * c[3] + n2 * c[6];
+          vy = pos[3 * j + 1] - yi + n0 * c[1] + n1 * c[4] + n2 * c[7];
+          vz = pos[3 * j + 2] - zi + n0 * c[2] + n1 * c[5] + n2 * c[8];
+          r2 = vx * vx + vy * vy + vz * vz;
+          ok = r2 < rc2;
+          if (ok && (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63)) {
+            record_error(error, kErrImageRange);
+            ok = false;
           }
         }
       }
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, ok);
+    round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
+  }
 }
 
 }  // namespace sus2g

@@ -103,6 +103,18 @@ class Engine:
         check(load().sus2g_engine_edge_count(self._h, ctypes.byref(n)))
         return n.value
 
+    STAGES = ("edges", "outer", "gate_forward", "gate_reverse", "gather")
+
+    def set_timing(self, on: bool) -> None:
+        check(load().sus2g_engine_set_timing(self._h, 1 if on else 0))
+
+    def take_stage_times(self):
+        """{stage: (milliseconds, count)} accumulated since the last call (synchronises)."""
+        ms = (ctypes.c_double * 8)()
+        cnt = (ctypes.c_int * 8)()
+        check(load().sus2g_engine_take_stage_times(self._h, ms, cnt))
+        return {name: (ms[i], cnt[i]) for i, name in enumerate(self.STAGES)}
+
     # -- periodic frames ------------------------------------------------------------------------
     @staticmethod
     def pack_frames(frames):
