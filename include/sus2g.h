@@ -96,6 +96,27 @@ int sus2g_efs_edges_host(sus2g_engine engine, int nowned, int nall, const int* t
                          const int* ei, const int* ej, const double* d, double* energy, double* site_energy,
                          double* forces, double* virial);
 
+/* ---- allocation-free Static E / F / virial ------------------------------------------------------
+ * No counterpart in the reference: this entry point exists for callers that cannot allocate device
+ * memory during a step -- code recording into a CUDA stream capture, MD drivers whose device memory
+ * comes from a pre-sized arena, integrations that forbid driver allocations in their time loop.
+ * Every other entry point may grow engine-owned buffers with cudaMalloc; this one allocates
+ * nothing: its scratch is a fixed file-scope device array.
+ *   All array arguments are DEVICE pointers on the engine's device; the engine must hold a Static
+ *   model in FP32-bulk form.  natoms centre atoms (0..natoms-1) of nall >= natoms atoms;
+ *   types[nall]; edges in CSR by centre: row[natoms + 1] (row[0] = 0, row[natoms] = nedges),
+ *   nbr[nedges] (0..nall-1), vec[3 * nedges] = x_j - x_i (A).  Outputs (device, any may be NULL):
+ *   energy[1], forces[3 * nall] (overwritten), virial[6] (xx, yy, zz, xy, xz, yz),
+ *   site_energy[natoms].
+ *   Limits: natoms <= 16384 and nedges <= 524288; larger calls are rejected with an error.
+ *   The first call on a device looks up the scratch array's device address for that device
+ *   (cudaGetSymbolAddress); make that first call before any stream capture.  Calls share the
+ *   scratch array: calls that overlap on the GPU race and must be serialised by the caller.
+ *   The call synchronises the engine's stream to report input errors. */
+int sus2g_static_efs_noalloc(sus2g_engine engine, int natoms, int nall, const int* types, const int* row,
+                             const int* nbr, const double* vec, long long nedges, double* energy, double* forces,
+                             double* virial, double* site_energy);
+
 #ifdef __cplusplus
 }
 #endif

@@ -8,16 +8,7 @@
 #include <string>
 #include <vector>
 
-#include "engine.h"
-#include "model.h"
-
-struct sus2g_model_s {
-  sus2g::Model model;
-};
-struct sus2g_engine_s {
-  std::unique_ptr<sus2g::Engine> engine;
-  int launches = 0;
-};
+#include "capi_types.h"
 
 namespace {
 thread_local std::string g_error;
@@ -65,6 +56,8 @@ long long total_atoms(int nframes, const int* natoms) {
   return n;
 }
 }  // namespace
+
+void sus2g_set_last_error(const char* message) { g_error = message ? message : ""; }
 
 extern "C" {
 

@@ -914,6 +914,24 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   mark_end();
 }
 
+int Engine::static_pass_external(int natoms, const int* types, const int* row, const int* nbr, const void* d4, float* g,
+                                 double* site, double* vir, int* error) {
+  if (precision_ != kFP32 || model_.gated) throw Error(1, "external Static pass needs a Static model on an FP32 engine");
+  PassArgs<float> a{};
+  a.dm = *static_cast<DevModel<float>*>(dev_model_);
+  a.natoms = natoms;
+  a.types = types;
+  a.row = row;
+  a.nbr = nbr;
+  a.rev = nullptr;
+  a.d4 = static_cast<const EdgeF*>(d4);
+  a.g = g;
+  a.site_energy = site;
+  a.virial = vir;
+  a.error = error;
+  return launch_atom_pass<float>(model_.L, kModeStatic, a, sm_count_, stream_);
+}
+
 void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
   SUS2G_CUDA(cudaSetDevice(device_));
   if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site);

@@ -78,6 +78,13 @@ class Engine {
   // entry points that copy host arrays in and out.
   void* io(int slot, size_t bytes) { io_[slot].ensure(bytes ? bytes : 1); return io_[slot].ptr; }
 
+  // Static FP32 pass on caller / external buffers (used by the allocation-free entry point):
+  // natoms centres, CSR edges (row, nbr) with edge records d4 (EdgeF), outputs g[3E], site[natoms],
+  // vir[6 natoms]; launches on stream().  Returns the number of kernels launched.
+  int static_pass_external(int natoms, const int* types, const int* row, const int* nbr, const void* d4, float* g,
+                           double* site, double* vir, int* error);
+  int sm_count() const { return sm_count_; }
+
   // internal buffers exposed for the tests / parameter-gradient pass
   const int* d_row() const { return row_.as<int>(); }
   const int* d_nbr() const { return nbr_.as<int>(); }
