@@ -96,6 +96,18 @@ int sus2g_efs_edges_host(sus2g_engine engine, int nowned, int nall, const int* t
                          const int* ei, const int* ej, const double* d, double* energy, double* site_energy,
                          double* forces, double* virial);
 
+/* ---- parameter gradient (trainer contract) ------------------------------------------------------
+ * Replaces AnyLocalMLIP::AccumulateEFSCombinationGrad (src/basic_mlip.cpp:421-476) and
+ * MLMTPR::AccumulateEFSCombinationGrad (dev_src/mtpr.cpp:9188) for a batch of periodic frames:
+ *   grad += d/dtheta [ sum_i ene_w[i] E_i + sum_(edges i->j) w_ij . dE/dd_ij ],
+ *   w_ij = frc_w[i] - frc_w[j] + str_w(frame) d_ij  (str_w row-major, w_a = sum_b S_ab d_b),
+ * i.e. the energy / force / stress weights (dL/dE_i, dL/dF, dL/dS of a loss) pulled back onto the
+ * parameters in the Coeff() order.  Frames as in sus2g_calc_efs_host; ene_w[N], frc_w[3N],
+ * str_w[9 * nframes] and grad[param count] are host arrays (grad is accumulated into). */
+int sus2g_efs_combination_grad_host(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                                    const double* positions, const int* types, const double* ene_w,
+                                    const double* frc_w, const double* str_w, double* grad);
+
 /* ---- allocation-free Static E / F / virial ------------------------------------------------------
  * No counterpart in the reference: this entry point exists for callers that cannot allocate device
  * memory during a step -- code recording into a CUDA stream capture, MD drivers whose device memory

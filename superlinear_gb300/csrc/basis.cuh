@@ -187,6 +187,40 @@ __device__ __forceinline__ void cheb_raw_values(T r, T slope, T shift, int B, T*
     if (b < B) Tv[b] = T(2) * xi * Tv[b - 1] - Tv[b - 2];
 }
 
+// Warp variable and its derivatives for the parameter gradient: xi = tanh(s (r - sigma) / 2).
+template <typename T>
+struct WarpVar {
+  T xi, xr, xs, xg, xrs, xrg;  // xi, d/dr, d/ds, d/dsigma, d2/dr ds, d2/dr dsigma
+};
+
+template <typename T>
+__device__ __forceinline__ WarpVar<T> warp_var(T r, T slope, T shift) {
+  WarpVar<T> w;
+  w.xi = tanh(slope * (r - shift) * T(0.5));
+  const T e = T(1) - w.xi * w.xi;
+  w.xr = e * slope * T(0.5);
+  w.xs = e * (r - shift) * T(0.5);
+  w.xg = -e * slope * T(0.5);
+  w.xrs = e * T(0.5) - w.xi * w.xs * slope;
+  w.xrg = -w.xi * w.xg * slope;
+  return w;
+}
+
+// Chebyshev T_b(xi) with its first and second derivatives in xi, b < B <= kMaxB.
+template <typename T>
+__device__ __forceinline__ void cheb_full(T xi, int B, T* Tv, T* D, T* DD) {
+  Tv[0] = T(1); D[0] = T(0); DD[0] = T(0);
+  Tv[1] = xi; D[1] = T(1); DD[1] = T(0);
+#pragma unroll
+  for (int b = 2; b < kMaxB; ++b) {
+    if (b < B) {
+      Tv[b] = T(2) * xi * Tv[b - 1] - Tv[b - 2];
+      D[b] = T(2) * Tv[b - 1] + T(2) * xi * D[b - 1] - D[b - 2];
+      DD[b] = T(4) * D[b - 1] + T(2) * xi * DD[b - 1] - DD[b - 2];
+    }
+  }
+}
+
 // Cutoff envelope f_c and its r-derivative (CalcRadialCutoff, sus2_sl_radial_math.cpp:256-294).
 template <typename T>
 __device__ __forceinline__ void envelope(T r, T rc, int poly, int p, T& f, T& fd) {

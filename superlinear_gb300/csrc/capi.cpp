@@ -198,6 +198,38 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
   });
 }
 
+int sus2g_efs_combination_grad_host(sus2g_engine e, int nframes, const int* natoms, const double* cells,
+                                    const double* positions, const int* types, const double* ene_w,
+                                    const double* frc_w, const double* str_w, double* grad) {
+  return guarded([&] {
+    need(e && nframes >= 0 && (nframes == 0 || (natoms && cells)), "engine/frames");
+    const long long n = total_atoms(nframes, natoms);
+    need(n == 0 || (positions && types && ene_w && frc_w), "positions/types/weights");
+    need(grad && (nframes == 0 || str_w), "grad/stress weights");
+    auto& eng = *e->engine;
+    for (long long i = 0; i < n; ++i)
+      need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
+    const int P = eng.model().param_count();
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Slot pos(eng, 0, sizeof(double) * 3 * n), typ(eng, 1, sizeof(int) * n), ew(eng, 2, sizeof(double) * n),
+        fw(eng, 3, sizeof(double) * 3 * n), sw(eng, 4, sizeof(double) * 9 * nframes), g(eng, 5, sizeof(double) * P);
+    if (n) {
+      cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
+      cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
+      cuda(cudaMemcpyAsync(ew.p, ene_w, sizeof(double) * n, cudaMemcpyHostToDevice, s), "weights copy");
+      cuda(cudaMemcpyAsync(fw.p, frc_w, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "weights copy");
+    }
+    if (nframes) cuda(cudaMemcpyAsync(sw.p, str_w, sizeof(double) * 9 * nframes, cudaMemcpyHostToDevice, s), "weights copy");
+    cuda(cudaMemcpyAsync(g.p, grad, sizeof(double) * P, cudaMemcpyHostToDevice, s), "grad copy");
+    eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
+    if (n) eng.combination_grad(ew.as<double>(), fw.as<double>(), sw.as<double>(), g.as<double>());
+    eng.check_device_error();
+    cuda(cudaMemcpyAsync(grad, g.p, sizeof(double) * P, cudaMemcpyDeviceToHost, s), "grad copy");
+    cuda(cudaStreamSynchronize(s), "stream synchronize");
+  });
+}
+
 int sus2g_efs_edges_host(sus2g_engine e, int nowned, int nall, const int* types, int nedges, const int* ei,
                          const int* ej, const double* d, double* energy, double* site_energy, double* forces,
                          double* virial) {

@@ -63,6 +63,24 @@ struct PassTables {
   const Real* rprod_c;
 };
 
+// Parameter-vector offsets (the trainer's Coeff() order) and the gradient-only tables of one pass.
+struct PassGradLayout {
+  int coeff_off, coeff_stride;   // offset of R_mu's Chebyshev row mu: coeff_off + mu * coeff_stride
+  int scal_off;                  // offset of this pass's warp block
+  int wc_off, wc_mu_stride, wc_t_stride;  // factor (t, mu) at wc_off + t * wc_t_stride + mu * wc_mu_stride
+  int add_off;                   // Effect alpha block (t * F + mu), -1 if none
+  int rw_off;                    // rank weight block, -1 if none (weights fixed at 1)
+  int nw;                        // number of rank weights
+  const int* w_begin;            // [nw + 1] rows of each rank weight
+  const int* w_src;              // basic index of the row
+  const int* w_dst;              // contraction node of the row
+};
+
+struct GradLayout {
+  PassGradLayout outer, gate;
+  int shift_off, species_off, linear_off, gate_w_off, nparams;
+};
+
 template <typename Real>
 struct DevModel {
   int C, L, K, B, F, H, M, NB, S, Q, nblk, scaling_mode;
@@ -76,6 +94,7 @@ struct DevModel {
   const int* scalar_map;    // S
   const Real* gate_wmat;    // F x Q gate projection h = W g
   const int* gate_nodes;    // Q
+  GradLayout grad;          // parameter-gradient layout
 };
 
 __device__ __forceinline__ int warp_lane() { return threadIdx.x & (kWarp - 1); }

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -493,6 +494,8 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   stream_ = own_stream_;
   SUS2G_CUDA(upload_pass_constants<float>());
   SUS2G_CUDA(upload_pass_constants<double>());
+  SUS2G_CUDA(upload_grad_constants<float>());
+  SUS2G_CUDA(upload_grad_constants<double>());
   // scalar readout and gate nodes are written with plain stores; duplicates would race
   auto unique = [](std::vector<int> v) { std::sort(v.begin(), v.end()); return std::adjacent_find(v.begin(), v.end()) == v.end(); };
   if (!unique(model_.scalar_map)) throw Error(3, "SUS2 model: duplicate entries in alpha_moment_mapping");
@@ -537,6 +540,50 @@ void Engine::upload_tables() {
   }
   const int o_wmat = pk.add_real(wmat);
   const int o_nodes = pk.add_int(nodes);
+  // parameter-gradient layout: block offsets in the trainer's order and rank-weight row lists
+  std::map<std::string, int> off;
+  for (const auto& b : m.layout()) off[b.name] = b.offset;
+  auto block = [&](const char* n) { auto it = off.find(n); return it == off.end() ? -1 : it->second; };
+  auto weight_rows = [&](const std::vector<ContractionRow>& rows, int nw, int& o_begin, int& o_src, int& o_dst) {
+    std::vector<int> begin{0}, src, dst;
+    for (int w = 0; w < nw; ++w) {
+      for (const auto& r : rows)
+        if (r.widx == w) { src.push_back(r.src); dst.push_back(r.dst); }
+      begin.push_back(static_cast<int>(src.size()));
+    }
+    o_begin = pk.add_int(begin);
+    o_src = pk.add_int(src);
+    o_dst = pk.add_int(dst);
+  };
+  GradLayout gl{};
+  int ow_b = 0, ow_s = 0, ow_d = 0, gw_b = 0, gw_s = 0, gw_d = 0;
+  gl.shift_off = block("shift_coeffs");
+  gl.species_off = block("species_coeffs");
+  gl.linear_off = block("moment_coeffs");
+  gl.gate_w_off = block("two_layer_gate_weights");
+  gl.nparams = m.param_count();
+  gl.outer.coeff_off = block("radial_coeffs");
+  gl.outer.coeff_stride = m.B + m.C;
+  gl.outer.scal_off = block("scal_coeffs");
+  gl.outer.wc_off = block("radial_coeffs") + m.B;
+  gl.outer.wc_mu_stride = m.B + m.C;
+  gl.outer.wc_t_stride = 1;
+  gl.outer.add_off = block("two_layer_gate_additive_coeffs");
+  gl.outer.rw_off = block("outer_k_rank1_weights");
+  gl.outer.nw = static_cast<int>(m.outer_w.size());
+  weight_rows(m.outer_rows, gl.outer.nw, ow_b, ow_s, ow_d);
+  if (m.gated) {
+    gl.gate.coeff_off = m.gate_shared_radial ? block("two_layer_gate_radial_coeffs") : block("radial_coeffs");
+    gl.gate.coeff_stride = m.gate_shared_radial ? m.B : m.B + m.C;
+    gl.gate.scal_off = m.gate_decoupled ? block("two_layer_gate_scaling_coeffs") : block("scal_coeffs");
+    gl.gate.wc_off = block("two_layer_gate_type_coeffs");
+    gl.gate.wc_mu_stride = 1;
+    gl.gate.wc_t_stride = m.F;
+    gl.gate.add_off = -1;
+    gl.gate.rw_off = block("two_layer_gate_k_rank_weights");
+    gl.gate.nw = static_cast<int>(m.gate_w.size());
+    weight_rows(m.gate_rows, gl.gate.nw, gw_b, gw_s, gw_d);
+  }
   std::vector<double> dbl(m.species);
   dbl.insert(dbl.end(), m.shift.begin(), m.shift.end());
 
@@ -566,6 +613,9 @@ void Engine::upload_tables() {
   dm->scalar_map = I + o_map;
   dm->gate_wmat = R + o_wmat;
   dm->gate_nodes = I + o_nodes;
+  gl.outer.w_begin = I + ow_b; gl.outer.w_src = I + ow_s; gl.outer.w_dst = I + ow_d;
+  gl.gate.w_begin = I + gw_b; gl.gate.w_src = I + gw_s; gl.gate.w_dst = I + gw_d;
+  dm->grad = gl;
   delete static_cast<DevModel<Real>*>(dev_model_);
   dev_model_ = dm;
 }
@@ -912,6 +962,100 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   }
   if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
   mark_end();
+}
+
+namespace {
+// grad[p] += sum over gradient slices (fixed order).
+__global__ void k_slot_reduce(const double* slots, int nslots, int nparams, double* grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nparams) return;
+  double s = 0.0;
+  for (int w = 0; w < nslots; ++w) s += slots[static_cast<size_t>(w) * nparams + p];
+  grad[p] += s;
+}
+
+// Gate projection weights: dJ/dW[mu][q] = sum_atoms lambda_h[mu] g[node q] + mu_h[mu] gdot[node q].
+template <typename Real>
+__global__ void k_gate_weight_grad(int natoms, int F, int Q, int M, const int* nodes, const double* lh,
+                                   const Real* gmom, const Real* gmomd, double* grad) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= F * Q) return;
+  const int m = t / Q, q = t - m * Q, node = nodes[q];
+  double s = 0.0;
+  for (int a = 0; a < natoms; ++a)
+    s += lh[static_cast<size_t>(a) * 2 * F + m] * double(gmom[static_cast<size_t>(a) * M + node]) +
+         lh[static_cast<size_t>(a) * 2 * F + F + m] * double(gmomd[static_cast<size_t>(a) * M + node]);
+  grad[t] += s;
+}
+}  // namespace
+
+template <typename Real>
+void Engine::run_grad(const double* ew, const double* fw, const double* sw, double* grad) {
+  const Model& m = model_;
+  if (user_edges_) throw Error(1, "the parameter gradient runs on periodic frames (build_edges)");
+  if (m.body_combo) throw Error(1, "the parameter gradient of mu-body-linear-combo gates is not implemented");
+  cudaStream_t s = stream_;
+  const int N = natoms_, P = m.param_count();
+  const size_t E = std::max<long long>(1, nedges_);
+  const DevModel<Real>& dm = *static_cast<DevModel<Real>*>(dev_model_);
+  GradArgs<Real> a{};
+  a.dm = dm;
+  a.natoms = ncentres_;
+  a.types = d_types_;
+  a.row = row_.as<int>();
+  a.nbr = nbr_.as<int>();
+  a.rev = rev_.as<int>();
+  a.d4 = static_cast<const typename Vec4<Real>::type*>(d4_.ptr);
+  a.frame_of = frame_of_.as<int>();
+  a.ew = ew;
+  a.fw = fw;
+  a.sw = sw;
+  a.error = error_.as<int>();
+  const GradLaunch co = grad_pass_config<Real>(m.L, kGradOuter, dm, ncentres_, sm_count_);
+  GradLaunch cf = co, cr = co;
+  if (m.gated) {
+    cf = grad_pass_config<Real>(m.L, kGradGateForward, dm, ncentres_, sm_count_);
+    cr = grad_pass_config<Real>(m.L, kGradGateReverse, dm, ncentres_, sm_count_);
+  }
+  const int nslots = std::max({co.grid * co.warps, cf.grid * cf.warps, cr.grid * cr.warps});
+  slots_.ensure(sizeof(double) * static_cast<size_t>(nslots) * P);
+  SUS2G_CUDA(cudaMemsetAsync(slots_.ptr, 0, sizeof(double) * static_cast<size_t>(nslots) * P, s));
+  a.slots = slots_.as<double>();
+  if (m.gated) {
+    const size_t NF = static_cast<size_t>(std::max(1, N)) * m.F, NM = static_cast<size_t>(std::max(1, N)) * m.M;
+    hsig_.ensure(sizeof(Real) * NF);
+    hsigd_.ensure(sizeof(Real) * NF);
+    gmom_.ensure(sizeof(Real) * NM);
+    gmomd_.ensure(sizeof(Real) * NM);
+    lhm_.ensure(sizeof(Real) * E * 2 * m.F);
+    lh_atom_.ensure(sizeof(double) * 2 * NF);
+    a.hsig = hsig_.as<Real>();
+    a.hsigd = hsigd_.as<Real>();
+    a.gmom = gmom_.as<Real>();
+    a.gmomd = gmomd_.as<Real>();
+    a.lhm = lhm_.as<Real>();
+    a.lh_atom = lh_atom_.as<double>();
+    launches_ += launch_grad_pass<Real>(m.L, kGradGateForward, a, cf, s);
+    launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co, s);
+    launches_ += launch_grad_pass<Real>(m.L, kGradGateReverse, a, cr, s);
+    const int gw_off = dm.grad.gate_w_off;
+    if (N && gw_off >= 0) {
+      k_gate_weight_grad<Real><<<(m.F * m.Q + 255) / 256, 256, 0, s>>>(ncentres_, m.F, m.Q, m.M, dm.gate_nodes,
+                                                                       lh_atom_.as<double>(), gmom_.as<Real>(),
+                                                                       gmomd_.as<Real>(), grad + gw_off);
+      ++launches_;
+    }
+  } else {
+    launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co, s);
+  }
+  k_slot_reduce<<<(P + 255) / 256, 256, 0, s>>>(slots_.as<double>(), nslots, P, grad);
+  ++launches_;
+}
+
+void Engine::combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (precision_ == kFP32) run_grad<float>(d_ew, d_fw, d_sw, d_grad);
+  else run_grad<double>(d_ew, d_fw, d_sw, d_grad);
 }
 
 int Engine::static_pass_external(int natoms, const int* types, const int* row, const int* nbr, const void* d4, float* g,

@@ -57,6 +57,11 @@ class Engine {
   // [natoms]; any output may be null.
   void efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
 
+  // Parameter gradient of  sum_i ew_i E_i + sum_e (fw_i - fw_j + sw_frame d_e) . dE/dd_e  for the
+  // frames of the last build_edges (AccumulateEFSCombinationGrad).  Device arrays (double):
+  // ew [N], fw [N][3], sw [nframes][9] (row-major); the result is ADDED into grad [nparams].
+  void combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad);
+
   int natoms() const { return natoms_; }
   int nframes() const { return nframes_; }
   long long nedges() const { return nedges_; }
@@ -93,6 +98,8 @@ class Engine {
  private:
   template <typename Real> void upload_tables();
   template <typename Real> void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  template <typename Real> void run_grad(const double* ew, const double* fw, const double* sw, double* grad);
+  DevBuf slots_, hsigd_, gmomd_, lhm_, lh_atom_;
   void finalize_edges();
 
   Model model_;

@@ -1,0 +1,455 @@
+// Parameter gradient of the SUS2-SH energy model on the GPU (the trainer's
+// AccumulateEFSCombinationGrad contract, src/basic_mlip.cpp:421-476, dev_src/mtpr.cpp:9188):
+//
+//   J(theta) = sum_i eW_i E_i + sum_e w_e . dE/dd_e,     w_e = fW_i - fW_j + S_frame d_e
+//
+// i.e. the energy weights plus the force / stress weights pulled back to edge vectors.  The
+// second term is the directional derivative of the total energy when every edge vector moves
+// along w_e, so J is evaluated with forward tangents (dual numbers) through the whole model and
+// the parameter gradient follows from one reverse sweep over values and tangents:
+//
+//   forward   A = sum_e u Y,  Adot = sum_e (udot Y + u Ydot),  u = x0 x3 R,
+//             udot = x0 (x3dot R + x3 R' rdot),  rdot = u_e . w_e,  Ydot = grad Y . w_e
+//   graph     v[out] += c v_a v_b,  vdot[out] += c (vdot_a v_b + v_a vdot_b)
+//   readout   J_i = eW_i E_i + Edot_i  ->  lambda = dJ/dv, mu = dJ/dvdot seeds
+//   reverse   lambda_a += c (lambda_out v_b + mu_out vdot_b),  mu_a += c mu_out v_b  (and b)
+//   edges     per (k, l): S = sum_m lambda Y, T = sum_m mu Y, U = sum_m mu Ydot,
+//             dJ/dR = x0 (x3 (S + U) + x3dot T),  dJ/dR' = x0 x3 rdot T, then the Chebyshev
+//             coefficients, the warp (slope, shift) through dxi/ds, dxi/dsigma, and the species /
+//             gate factors.
+// The Effect gate chain runs the same steps for the gate pass, seeded with
+// dJ/dh_j and dJ/dhdot_j gathered per atom (stored at the reverse edge, like the force path).
+//
+// Reductions are deterministic: per-edge contributions are summed over the 32 lanes with fixed
+// shuffle trees and added by one lane to a private FP64 gradient slice of the warp; slices are
+// summed in a fixed order by k_slot_reduce.
+#pragma once
+#include "efs_kernels.cuh"
+
+namespace sus2g {
+
+enum GradMode : int { kGradOuter = 0, kGradGateForward = 1, kGradGateReverse = 2 };
+
+template <typename Real>
+struct GradArgs {
+  DevModel<Real> dm;
+  int natoms;
+  const int* types;
+  const int* row;
+  const int* nbr;
+  const int* rev;
+  const typename Vec4<Real>::type* d4;
+  const int* frame_of;
+  const double* ew;        // [N] energy weights
+  const double* fw;        // [N][3] force weights
+  const double* sw;        // [nframes][9] stress weights (row-major)
+  Real* hsig;              // [N][F] gate signal h
+  Real* hsigd;             // [N][F] tangent of h
+  Real* gmom;              // [N][M] gate values
+  Real* gmomd;             // [N][M] gate tangents
+  Real* lhm;               // [E][2F] dJ/dh, dJ/dhdot contributions stored at the reverse edge
+  double* lh_atom;         // [N][2F] gathered per atom (gate reverse)
+  double* slots;           // [warps in grid][nparams]
+  int* error;
+};
+
+template <typename Real>
+__host__ __device__ inline int grad_warp_size(int F, int H, int M, int K) {
+  return kWarp * (2 * F + 2 * H + 1) + 4 * M + 2 * K * H + 2 * F + 4;
+}
+
+template <typename Real>
+__device__ __forceinline__ void slot_add(double* slot, int idx, Real v, int lane) {
+  const Real s = warp_sum(v);
+  if (lane == 0) slot[idx] += double(s);
+}
+
+template <typename Real>
+__device__ __forceinline__ void contract_forward_dual(const PassTables<Real>& t, Real* v, Real* vd, int lane) {
+  for (int q = lane; q < t.ndst; q += kWarp) {
+    Real s = Real(0), sd = Real(0);
+    for (int p = t.dst_begin[q]; p < t.dst_begin[q + 1]; ++p) {
+      s += t.dst_w[p] * v[t.dst_src[p]];
+      sd += t.dst_w[p] * vd[t.dst_src[p]];
+    }
+    v[t.dst_node[q]] += s;
+    vd[t.dst_node[q]] += sd;
+  }
+  __syncwarp();
+}
+
+template <typename Real>
+__device__ __forceinline__ void graph_forward_dual(const PassTables<Real>& t, Real* v, Real* vd, int lane) {
+  for (int lv = 0; lv < t.levels; ++lv) {
+    for (int q = t.level_begin[lv] + lane; q < t.level_begin[lv + 1]; q += kWarp) {
+      Real s = Real(0), sd = Real(0);
+      for (int p = t.out_begin[q]; p < t.out_begin[q + 1]; ++p) {
+        const int x = t.fprod_a[p], y = t.fprod_b[p];
+        const Real c = t.fprod_c[p];
+        s += c * v[x] * v[y];
+        sd += c * (vd[x] * v[y] + v[x] * vd[y]);
+      }
+      v[t.out_nodes[q]] += s;
+      vd[t.out_nodes[q]] += sd;
+    }
+    __syncwarp();
+  }
+}
+
+template <typename Real>
+__device__ __forceinline__ void graph_reverse_dual(const PassTables<Real>& t, const Real* v, const Real* vd, Real* lam,
+                                                   Real* mu, int lane) {
+  for (int lv = t.levels - 1; lv >= 0; --lv) {
+    for (int q = t.rlevel_begin[lv] + lane; q < t.rlevel_begin[lv + 1]; q += kWarp) {
+      Real sl = Real(0), sm = Real(0);
+      for (int p = t.in_begin[q]; p < t.in_begin[q + 1]; ++p) {
+        const int o = t.rprod_out[p], x = t.rprod_other[p];
+        const Real c = t.rprod_c[p];
+        sl += c * (lam[o] * v[x] + mu[o] * vd[x]);
+        sm += c * mu[o] * v[x];
+      }
+      lam[t.in_nodes[q]] += sl;
+      mu[t.in_nodes[q]] += sm;
+    }
+    __syncwarp();
+  }
+}
+
+template <typename Real>
+__device__ __forceinline__ void contract_reverse_dual(const PassTables<Real>& t, const PassGradLayout& gl, int NB,
+                                                      const Real* v, const Real* vd, Real* lam, Real* mu, double* slot,
+                                                      int lane) {
+  if (t.ndst == 0) return;
+  // rank-weight gradients first (they read lam/mu of contraction nodes, which do not change below)
+  if (gl.rw_off >= 0)
+    for (int w = lane; w < gl.nw; w += kWarp) {
+      double s = 0.0;
+      for (int p = gl.w_begin[w]; p < gl.w_begin[w + 1]; ++p) {
+        const int src = gl.w_src[p], dst = gl.w_dst[p];
+        s += double(lam[dst]) * double(v[src]) + double(mu[dst]) * double(vd[src]);
+      }
+      slot[gl.rw_off + w] += s;
+    }
+  for (int b = lane; b < NB; b += kWarp) {
+    Real sl = Real(0), sm = Real(0);
+    for (int p = t.src_begin[b]; p < t.src_begin[b + 1]; ++p) {
+      sl += t.src_w[p] * lam[t.src_dst[p]];
+      sm += t.src_w[p] * mu[t.src_dst[p]];
+    }
+    lam[b] += sl;
+    mu[b] += sm;
+  }
+  __syncwarp();
+}
+
+template <int L, typename Real, int MODE, bool KAHAN>
+__global__ void grad_pass_kernel(GradArgs<Real> a) {
+  constexpr int Lp = L + 1, H = Lp * Lp;
+  constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
+  using V4 = typename Vec4<Real>::type;
+  const DevModel<Real>& dm = a.dm;
+  const bool gate_pass = MODE != kGradOuter;
+  const PassTables<Real>& pt = gate_pass ? dm.gate : dm.outer;
+  const PassGradLayout& gl = gate_pass ? dm.grad.gate : dm.grad.outer;
+  const int C = dm.C, F = dm.F, B = dm.B, K = dm.K, M = dm.M, NB = dm.NB, NP = dm.grad.nparams;
+  const int C2 = C * C;
+  const bool effect_outer = MODE == kGradOuter && dm.gated;
+  const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* sm = reinterpret_cast<Real*>(smem_raw);
+  Real* s_coeff = sm;
+  Real* s_scal = s_coeff + F * B;
+  Real* s_w0 = s_scal + 2 * dm.nblk * C2;
+  Real* s_w1 = s_w0 + C * F;
+  Real* s_wa = s_w1 + C * F;
+  Real* wbase = s_wa + C * F + grad_warp_size<Real>(F, H, M, K) * warp;
+  const int sw = 2 * F + 2 * H + 1;
+  Real* stage = wbase;
+  Real* v = stage + kWarp * sw;
+  Real* vd = v + M;
+  Real* lam = vd + M;
+  Real* mu = lam + M;
+  Real* abl = mu + M;
+  Real* abm = abl + K * H;
+  Real* hb = abm + K * H;  // [2F]
+
+  for (int q = threadIdx.x; q < F * B; q += blockDim.x) s_coeff[q] = pt.coeff[q];
+  for (int q = threadIdx.x; q < 2 * dm.nblk * C2; q += blockDim.x) s_scal[q] = pt.scal[q];
+  for (int q = threadIdx.x; q < C * F; q += blockDim.x) {
+    s_w0[q] = pt.wcenter[q];
+    s_w1[q] = pt.wsource[q];
+    s_wa[q] = pt.wadd ? pt.wadd[q] : Real(0);
+  }
+  __syncthreads();
+  double* slot = a.slots + static_cast<size_t>(blockIdx.x * warps + warp) * NP;
+
+  int it_u[kMaxItems], it_y[kMaxItems];
+#pragma unroll
+  for (int s = 0; s < kMaxItems; ++s) {
+    const int t = lane + kWarp * s;
+    if (t < K * H) {
+      const int kk = t / H, lm = t - kk * H;
+      int l = 0;
+      while ((l + 1) * (l + 1) <= lm) ++l;
+      it_u[s] = kk * Lp + l;
+      it_y[s] = 2 * F + lm;
+    } else {
+      it_u[s] = -1;
+      it_y[s] = 0;
+    }
+  }
+
+  for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
+    const int ti = a.types[atom];
+    const int e0 = a.row[atom], e1 = a.row[atom + 1];
+    const double* Sw = a.sw + 9 * a.frame_of[atom];
+    const Real S00 = Real(Sw[0]), S01 = Real(Sw[1]), S02 = Real(Sw[2]), S10 = Real(Sw[3]), S11 = Real(Sw[4]),
+               S12 = Real(Sw[5]), S20 = Real(Sw[6]), S21 = Real(Sw[7]), S22 = Real(Sw[8]);
+    const double fix = a.fw[3 * atom], fiy = a.fw[3 * atom + 1], fiz = a.fw[3 * atom + 2];
+
+    // geometry, tangent direction and harmonics (values + tangents) of edge e
+    auto edge_geometry = [&](int e, int& j, int& tj, Real& r, Real& ux, Real& uy, Real& uz, Real& rdot, Real* Y,
+                             Real* Yd, bool& ang) {
+      const V4 dv = a.d4[e];
+      j = a.nbr[e];
+      tj = a.types[j];
+      r = dv.w;
+      const Real ir = Real(1) / r;
+      ux = dv.x * ir; uy = dv.y * ir; uz = dv.z * ir;
+      const Real wx = Real(fix - a.fw[3 * j]) + S00 * dv.x + S01 * dv.y + S02 * dv.z;
+      const Real wy = Real(fiy - a.fw[3 * j + 1]) + S10 * dv.x + S11 * dv.y + S12 * dv.z;
+      const Real wz = Real(fiz - a.fw[3 * j + 2]) + S20 * dv.x + S21 * dv.y + S22 * dv.z;
+      rdot = ux * wx + uy * wy + uz * wz;
+      sph_values<L, Real>(ux, uy, uz, Y);
+      sph_tangent<L, Real>(ux, uy, uz, (wx - ux * rdot) * ir, (wy - uy * rdot) * ir, (wz - uz * rdot) * ir, Yd);
+      ang = !(r >= dm.rang);
+      if (!ang)
+#pragma unroll
+        for (int h = 1; h < H; ++h) { Y[h] = Real(0); Yd[h] = Real(0); }
+    };
+
+    if (MODE != kGradGateReverse) {
+      // ---------------- forward with tangents ----------------
+      Real acc[kMaxItems], cmp[kMaxItems], accd[kMaxItems], cmpd[kMaxItems];
+#pragma unroll
+      for (int s = 0; s < kMaxItems; ++s) { acc[s] = cmp[s] = accd[s] = cmpd[s] = Real(0); }
+      for (int base = e0; base < e1; base += kWarp) {
+        const int e = base + lane;
+        Real* rw = stage + lane * sw;
+        for (int q = 0; q < sw; ++q) rw[q] = Real(0);
+        if (e < e1) {
+          int j, tj;
+          Real r, ux, uy, uz, rdot, Y[H], Yd[H];
+          bool ang;
+          edge_geometry(e, j, tj, r, ux, uy, uz, rdot, Y, Yd, ang);
+#pragma unroll
+          for (int h = 0; h < H; ++h) { rw[2 * F + h] = Y[h]; rw[2 * F + H + h] = Yd[h]; }
+          const Real* hj = effect_outer ? a.hsig + static_cast<size_t>(j) * F : nullptr;
+          const Real* hdj = effect_outer ? a.hsigd + static_cast<size_t>(j) * F : nullptr;
+          radial_loop<L, Real, true>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int, int, int m_, Real R, Real Rd) {
+            const Real x0 = s_w0[ti * F + m_];
+            Real x3 = s_w1[tj * F + m_], x3d = Real(0);
+            if (effect_outer) {
+              x3 += s_wa[tj * F + m_] * hj[m_];
+              x3d = s_wa[tj * F + m_] * hdj[m_];
+            }
+            rw[m_] = x0 * x3 * R;
+            rw[F + m_] = x0 * (x3d * R + x3 * Rd * rdot);
+          });
+        }
+        __syncwarp();
+        const int nb = min(kWarp, e1 - base);
+        for (int q = 0; q < nb; ++q) {
+          const Real* sr = stage + q * sw;
+#pragma unroll
+          for (int s = 0; s < kMaxItems; ++s)
+            if (it_u[s] >= 0) {
+              const Real uu = sr[it_u[s]], ud = sr[F + it_u[s]], yy = sr[it_y[s]], yd = sr[it_y[s] + H];
+              kadd<Real, KAHAN>(acc[s], cmp[s], uu * yy);
+              kadd<Real, KAHAN>(accd[s], cmpd[s], ud * yy + uu * yd);
+            }
+        }
+        __syncwarp();
+      }
+      for (int q = lane; q < M; q += kWarp) { v[q] = Real(0); vd[q] = Real(0); }
+      __syncwarp();
+#pragma unroll
+      for (int s = 0; s < kMaxItems; ++s) {
+        const int t = lane + kWarp * s;
+        if (t < K * H) {
+          const int b = dm.basic_of[t];
+          if (b >= 0) { v[b] = acc[s]; vd[b] = accd[s]; }
+        }
+      }
+      __syncwarp();
+      contract_forward_dual<Real>(pt, v, vd, lane);
+      graph_forward_dual<Real>(pt, v, vd, lane);
+      if (MODE == kGradGateForward) {
+        for (int q = lane; q < M; q += kWarp) {
+          a.gmom[static_cast<size_t>(atom) * M + q] = v[q];
+          a.gmomd[static_cast<size_t>(atom) * M + q] = vd[q];
+        }
+        for (int m_ = lane; m_ < F; m_ += kWarp) {
+          Real h = Real(0), hd = Real(0);
+          for (int q = 0; q < dm.Q; ++q) {
+            h += dm.gate_wmat[m_ * dm.Q + q] * v[dm.gate_nodes[q]];
+            hd += dm.gate_wmat[m_ * dm.Q + q] * vd[dm.gate_nodes[q]];
+          }
+          a.hsig[static_cast<size_t>(atom) * F + m_] = h;
+          a.hsigd[static_cast<size_t>(atom) * F + m_] = hd;
+        }
+        __syncwarp();
+        continue;
+      }
+      // ---------------- readout gradient and seeds ----------------
+      const double ewi = a.ew[atom];
+      const double coef = dm.species_readout ? 1.0 : dm.species[ti];
+      const int off = dm.species_readout ? ti * dm.S : 0;
+      for (int q = lane; q < M; q += kWarp) { lam[q] = Real(0); mu[q] = Real(0); }
+      __syncwarp();
+      double sp = 0.0;
+      for (int q = lane; q < dm.S; q += kWarp) {
+        const int node = dm.scalar_map[q];
+        const double lin = double(dm.linear[off + q]);
+        const double g = ewi * double(v[node]) + double(vd[node]);
+        slot[dm.grad.linear_off + off + q] += coef * g;
+        if (!dm.species_readout) sp += lin * g;
+        lam[node] = Real(ewi * coef * lin);
+        mu[node] = Real(coef * lin);
+      }
+      sp = warp_sum(sp);
+      if (lane == 0) {
+        slot[dm.grad.shift_off + ti] += ewi;
+        slot[dm.grad.species_off + ti] += ewi + sp;
+      }
+      __syncwarp();
+    } else {
+      // ---------------- gate reverse seeds from dJ/dh, dJ/dhdot ----------------
+      for (int m_ = lane; m_ < 2 * F; m_ += kWarp) {
+        Real s = Real(0);
+        for (int e = e0; e < e1; ++e) s += a.lhm[static_cast<size_t>(e) * 2 * F + m_];
+        hb[m_] = s;
+        a.lh_atom[static_cast<size_t>(atom) * 2 * F + m_] = double(s);
+      }
+      for (int q = lane; q < M; q += kWarp) {
+        v[q] = a.gmom[static_cast<size_t>(atom) * M + q];
+        vd[q] = a.gmomd[static_cast<size_t>(atom) * M + q];
+        lam[q] = Real(0);
+        mu[q] = Real(0);
+      }
+      __syncwarp();
+      for (int q = lane; q < dm.Q; q += kWarp) {
+        Real sl = Real(0), sm_ = Real(0);
+        for (int m_ = 0; m_ < F; ++m_) {
+          sl += hb[m_] * dm.gate_wmat[m_ * dm.Q + q];
+          sm_ += hb[F + m_] * dm.gate_wmat[m_ * dm.Q + q];
+        }
+        lam[dm.gate_nodes[q]] += sl;
+        mu[dm.gate_nodes[q]] += sm_;
+      }
+      __syncwarp();
+    }
+
+    // ---------------- reverse over values and tangents ----------------
+    graph_reverse_dual<Real>(pt, v, vd, lam, mu, lane);
+    contract_reverse_dual<Real>(pt, gl, NB, v, vd, lam, mu, slot, lane);
+    for (int t = lane; t < K * H; t += kWarp) {
+      const int b = dm.basic_of[t];
+      abl[t] = b >= 0 ? lam[b] : Real(0);
+      abm[t] = b >= 0 ? mu[b] : Real(0);
+    }
+    __syncwarp();
+
+    // ---------------- per-edge parameter contributions ----------------
+    for (int base = e0; base < e1; base += kWarp) {
+      const int e = base + lane;
+      const bool valid = e < e1;
+      int j = 0, tj = 0;
+      Real r = Real(1), ux = Real(0), uy = Real(0), uz = Real(1), rdot = Real(0), Y[H], Yd[H];
+      bool ang = true;
+      if (valid) edge_geometry(e, j, tj, r, ux, uy, uz, rdot, Y, Yd, ang);
+      else
+#pragma unroll
+        for (int h = 0; h < H; ++h) { Y[h] = Real(0); Yd[h] = Real(0); }
+      Real f0, fd0, f1, fd1;
+      envelope<Real>(r, dm.rmax, dm.poly, dm.cutoff_p, f0, fd0);
+      if (dm.split) envelope<Real>(r, dm.rang, dm.poly, dm.cutoff_p, f1, fd1);
+      else { f1 = f0; fd1 = fd0; }
+      f0 *= dm.scaling; fd0 *= dm.scaling; f1 *= dm.scaling; fd1 *= dm.scaling;
+      const Real* hj = (effect_outer && valid) ? a.hsig + static_cast<size_t>(j) * F : nullptr;
+      const Real* hdj = (effect_outer && valid) ? a.hsigd + static_cast<size_t>(j) * F : nullptr;
+      for (int k = 0; k < K; ++k) {
+        Real Tv[kMaxB], D[kMaxB], DD[kMaxB];
+        WarpVar<Real> wv;
+        int sb_prev = -1;
+#pragma unroll
+        for (int l = 0; l < Lp; ++l) {
+          const int sb = scaling_block(dm.scaling_mode, k, l, Lp);
+          if (sb != sb_prev) {
+            wv = warp_var<Real>(r, s_scal[2 * sb * C2 + ti * C + tj], s_scal[(2 * sb + 1) * C2 + ti * C + tj]);
+            cheb_full<Real>(wv.xi, B, Tv, D, DD);
+            sb_prev = sb;
+          }
+          const int m_ = k * Lp + l;
+          const bool on = valid && (l == 0 || ang);
+          const Real* c = s_coeff + m_ * B;
+          Real cT = Real(0), cD = Real(0), cDD = Real(0);
+#pragma unroll
+          for (int b = 0; b < kMaxB; ++b)
+            if (b < B) { cT += c[b] * Tv[b]; cD += c[b] * D[b]; cDD += c[b] * DD[b]; }
+          const Real f = l == 0 ? f0 : f1, fd = l == 0 ? fd0 : fd1;
+          const Real R = f * cT, Rd = fd * cT + f * cD * wv.xr;
+          Real Sv = Real(0), Tt = Real(0), Uv = Real(0);
+#pragma unroll
+          for (int h = l * l; h < (l + 1) * (l + 1); ++h) {
+            Sv += abl[k * H + h] * Y[h];
+            Tt += abm[k * H + h] * Y[h];
+            Uv += abm[k * H + h] * Yd[h];
+          }
+          const Real x0 = s_w0[ti * F + m_];
+          Real x3 = s_w1[tj * F + m_], x3d = Real(0), al = Real(0), hv = Real(0), hdv = Real(0);
+          if (effect_outer && valid) {
+            al = s_wa[tj * F + m_];
+            hv = hj[m_];
+            hdv = hdj[m_];
+            x3 += al * hv;
+            x3d = al * hdv;
+          }
+          const Real Qv = R * (Sv + Uv) + Rd * rdot * Tt;
+          Real dR = on ? x0 * (x3 * (Sv + Uv) + x3d * Tt) : Real(0);
+          Real dRd = on ? x0 * x3 * rdot * Tt : Real(0);
+          const Real dx0 = on ? x3 * Qv + x3d * R * Tt : Real(0);
+          const Real dxj = on ? x0 * Qv : Real(0);
+          // Chebyshev coefficients of R_mu
+          for (int b = 0; b < B; ++b)
+            slot_add<Real>(slot, gl.coeff_off + m_ * gl.coeff_stride + b,
+                           dR * f * Tv[b] + dRd * (fd * Tv[b] + f * D[b] * wv.xr), lane);
+          // warp (slope, shift) of block sb and pair (t_i, t_j)
+          const Real ds = wv.xs * (dR * f + dRd * fd) * cD + dRd * f * (wv.xs * wv.xr * cDD + wv.xrs * cD);
+          const Real dg = wv.xg * (dR * f + dRd * fd) * cD + dRd * f * (wv.xg * wv.xr * cDD + wv.xrg * cD);
+          for (int t = 0; t < C; ++t) {
+            slot_add<Real>(slot, gl.scal_off + 2 * sb * C2 + ti * C + t, tj == t ? ds : Real(0), lane);
+            slot_add<Real>(slot, gl.scal_off + (2 * sb + 1) * C2 + ti * C + t, tj == t ? dg : Real(0), lane);
+          }
+          // species factors of the centre and the neighbour
+          slot_add<Real>(slot, gl.wc_off + ti * gl.wc_t_stride + m_ * gl.wc_mu_stride, dx0, lane);
+          for (int t = 0; t < C; ++t)
+            slot_add<Real>(slot, gl.wc_off + t * gl.wc_t_stride + m_ * gl.wc_mu_stride, tj == t ? dxj : Real(0), lane);
+          if (effect_outer) {
+            const Real dal = on ? x0 * (Qv * hv + R * Tt * hdv) : Real(0);
+            for (int t = 0; t < C; ++t) slot_add<Real>(slot, gl.add_off + t * F + m_, tj == t ? dal : Real(0), lane);
+            if (valid) {
+              Real* dst = a.lhm + static_cast<size_t>(a.rev[e]) * 2 * F;
+              dst[m_] = on ? x0 * al * Qv : Real(0);
+              dst[F + m_] = on ? x0 * al * R * Tt : Real(0);
+            }
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace sus2g

@@ -3,8 +3,21 @@
 #include <cuda_runtime.h>
 
 #include "efs_kernels.cuh"
+#include "grad_kernels.cuh"
 
 namespace sus2g {
+
+struct GradLaunch {
+  int grid = 0, block = 0, warps = 0;
+  size_t smem = 0;
+};
+
+// Launch shape of grad_pass_kernel<L, Real, mode> (grid sized from occupancy x SM count).
+template <typename Real>
+GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count);
+// Launches it with that shape (a.slots must hold cfg.grid * cfg.warps slices).
+template <typename Real>
+int launch_grad_pass(int L, int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t stream);
 
 // Launches atom_pass_kernel<L, Real, mode, Kahan = (Real is float)> sized as a multiple of the SM
 // count.  Returns the number of kernels launched (1) or throws on a configuration error.
@@ -14,5 +27,7 @@ int launch_atom_pass(int L, int mode, const PassArgs<Real>& args, int sm_count, 
 // Per-translation-unit constant-table upload (spherical-harmonic normalisation).
 template <typename Real>
 cudaError_t upload_pass_constants();
+template <typename Real>
+cudaError_t upload_grad_constants();
 
 }  // namespace sus2g

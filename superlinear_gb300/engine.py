@@ -148,6 +148,21 @@ class Engine:
         check(load().sus2g_calc_efs_device(self._h, natoms.size, _i(natoms), _d(cells), vp(pos_ptr), vp(types_ptr),
                                            vp(energy_ptr), vp(forces_ptr), vp(virial_ptr), vp(site_ptr)))
 
+    def combination_grad(self, frames, ene_w, frc_w, str_w, grad=None):
+        """d/dtheta of sum_i ene_w_i E_i + sum_e (frc_w_i - frc_w_j + str_w d_e) . dE/dd_e (host arrays).
+
+        ``ene_w`` [N], ``frc_w`` [N, 3], ``str_w`` [nframes, 3, 3]; returns ``grad`` (accumulated into
+        when given) in the parameter order of ``Model.params()``."""
+        natoms, cells, pos, types = self.pack_frames(frames)
+        nf = natoms.size
+        ew = np.ascontiguousarray(ene_w, dtype=np.float64).reshape(-1)
+        fw = np.ascontiguousarray(frc_w, dtype=np.float64).reshape(-1, 3)
+        sw = np.ascontiguousarray(str_w, dtype=np.float64).reshape(nf, 9)
+        g = np.zeros(self.model.nparams) if grad is None else np.ascontiguousarray(grad, dtype=np.float64)
+        check(load().sus2g_efs_combination_grad_host(self._h, nf, _i(natoms), _d(cells), _d(pos), _i(types), _d(ew),
+                                                     _d(fw), _d(sw), _d(g)))
+        return g
+
     # -- caller edge list (pair_style sus2/embedded) --------------------------------------------
     def efs_edges(self, nowned: int, types, ei, ej, d):
         types = np.ascontiguousarray(types, dtype=np.int32)
