@@ -156,3 +156,41 @@ class OracleModel:
 def virial6_to_matrix(v):
     """(xx, yy, zz, xy, xz, yz) -> symmetric 3x3 (the reference harness's virial layout)."""
     return np.array([[v[0], v[3], v[4]], [v[3], v[1], v[5]], [v[4], v[5], v[2]]])
+
+
+def loss_grad(model: "OracleModel", frames, wE: float, wF: float, wS: float, weighting: str = "vibrations",
+              norm_by_forces: int = 0):
+    """Energy / force / stress MSE objective summed over labelled frames and its parameter gradient,
+    restating NonLinearRegression::AddLoss / AddLossGrad (dev_src/non_linear_regression.cpp:768-1068)
+    with the std terms, penalties and regularisers off; the gradient goes through ``grad``."""
+    d = 0.1
+    loss = 0.0
+    grad = np.zeros(model.nparams)
+    for fr in frames:
+        n = fr.natoms
+        e, f, v, _, _ = model.efs(fr.cell, fr.positions, fr.types)
+        s = virial6_to_matrix(v)
+        avef = float(np.mean(np.sum(fr.forces ** 2, axis=1))) if fr.forces is not None else 0.0
+        scale_fn = d / (d + norm_by_forces * avef)
+        fw = np.zeros((n, 3))
+        if wF != 0 and fr.forces is not None:
+            wgt = wF / n if weighting == "structures" else wF
+            delta = f - fr.forces
+            loss += wgt * scale_fn * float(np.sum(delta ** 2))
+            fw = wgt * scale_fn * 2.0 * delta
+        we, ws = wE, wS
+        if weighting == "structures":
+            we, ws = wE / n, wS / n
+        elif weighting == "molecules":
+            we, ws = wE * n, wS * n
+        sw = np.zeros((3, 3))
+        if ws != 0 and fr.stress is not None:
+            ds = s - fr.stress
+            loss += ws * float(np.sum(ds ** 2)) / n
+            sw = -2.0 * ws * ds / n
+        ew = 0.0
+        if we != 0 and fr.energy is not None:
+            loss += we * (e - fr.energy) ** 2 * scale_fn / n
+            ew = 2.0 * we * (e - fr.energy) * scale_fn / n
+        grad += model.grad(fr.cell, fr.positions, fr.types, np.full(n, ew), fw, sw)
+    return loss, grad

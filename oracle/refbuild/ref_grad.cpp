@@ -17,6 +17,7 @@
 //   3x3 stress weight; the gradient is accumulated from zero for each configuration.
 #include "mtpr.h"
 #include "configuration.h"
+#include "non_linear_regression.h"
 #include <cstdio>
 #include <string>
 #include <fstream>
@@ -43,6 +44,34 @@ int main(int argc, char** argv) {
     for (int i = 0; i < mtpr.CoeffCount(); ++i) mtpr.Coeff()[i] = v[i];
     mtpr.DistributeCoeffs();
     mtpr.Save(argv[3]);
+    return 0;
+  }
+  if (std::string(argv[1]) == "--loss") {
+    // ref-grad --loss MODEL CFG wE wF wS [weighting]: NonLinearRegression::CalcObjectiveFunctionGrad
+    // (dev_src/non_linear_regression.cpp:1112) over the labelled CFG with the energy / force /
+    // stress MSE terms only (std terms, penalties and regularisers set to zero); prints the
+    // summed loss and gradient (the trainer divides both by the configuration count afterwards).
+    if (argc < 7) { std::fprintf(stderr, "usage: ref-grad --loss MODEL CFG wE wF wS [weighting]\n"); return 2; }
+    MLMTPR mtpr(argv[2]);
+    struct Objective : NonLinearRegression {
+      using NonLinearRegression::NonLinearRegression;
+      double loss() const { return loss_; }
+      const std::vector<double>& grad() const { return loss_grad_; }
+    };
+    Objective obj(&mtpr, std::stod(argv[4]), std::stod(argv[5]), std::stod(argv[6]), 0.0, 0.0);
+    obj.std_scaling = 0.0;
+    obj.stdd_scaling = 0.0;
+    obj.radial_smooth_regularization = 0.0;
+    obj.fixed_atomic_energy_weight = 0.0;
+    if (argc > 7) obj.weighting = argv[7];
+    std::ifstream in(argv[3]);
+    std::vector<Configuration> train;
+    Configuration c;
+    while (c.Load(in)) train.push_back(c);
+    obj.CalcObjectiveFunctionGrad(train);
+    std::printf("{\"loss\": %.17g, \"grad\": ", obj.loss());
+    vec(obj.grad().data(), (int)obj.grad().size());
+    std::printf(", \"configs\": %zu}\n", train.size());
     return 0;
   }
   MLMTPR mtpr(argv[1]);

@@ -622,6 +622,8 @@ void Engine::upload_tables() {
 
 void Engine::upload_model() {
   SUS2G_CUDA(cudaSetDevice(device_));
+  // work already queued on the engine's stream may still read the tables being replaced
+  if (stream_) SUS2G_CUDA(cudaStreamSynchronize(stream_));
   if (precision_ == kFP32) upload_tables<float>();
   else upload_tables<double>();
 }

@@ -40,6 +40,10 @@ class Engine {
 
   // Re-upload parameters after Model::set_params.
   void upload_model();
+  // Replace the engine's parameter vector (trainer order) and re-upload the device tables.
+  void set_params(const double* params) { model_.set_params(params); upload_model(); }
+  int nframes_of_plan() const { return nframes_; }
+  const int* d_frame_of() const { return frame_of_.as<int>(); }
 
   // --- geometry -----------------------------------------------------------------------------
   // Periodic frames: cells (row lattice vectors, 9 doubles each) live on the host, positions

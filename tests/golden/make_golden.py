@@ -94,6 +94,12 @@ def frames_for(name):
     raise KeyError(name)
 
 
+def LOSS_CASES():
+    """(model, frames to label, (wE, wF, wS)); loss weights of the reference's example profile."""
+    return [("effect_l3k4r2o2", training_frames(6, 8, 64, 3.0, 4.2, 0.1, seed=211, species=2), (1.0, 0.01, 0.001)),
+            ("static_l2k3o2_c2", training_frames(4, 8, 48, 3.0, 4.2, 0.1, seed=212, species=2), (1.0, 0.01, 0.001))]
+
+
 def weights_for(frames, seed):
     """Seeded loss-derivative weights (per-atom energy weight, per-atom force weight, 3x3 stress)."""
     rng = np.random.default_rng(seed)
@@ -194,6 +200,35 @@ def main():
                                            for ew, fw, sw in wts],
                                "trainer_efs": efs, "grad": grads}, fh)
                 print(name, label, "frames", len(frames), "atoms", [f.natoms for f in frames])
+        # 5. labelled training sets: teacher labels (another seeded parameter vector, evaluated by the
+        #    reference embedded engine), student loss + gradient from the reference trainer's
+        #    NonLinearRegression::CalcObjectiveFunctionGrad (energy / force / stress MSE terms)
+        os.makedirs(os.path.join(HERE, "loss"), exist_ok=True)
+        for name, frames, weights in LOSS_CASES():
+            kind, spec, (seed, rscale, oscale) = MODELS[name]
+            model = os.path.join(HERE, "models", f"{name}.sus2")
+            teacher = os.path.join(tmp, f"{name}_teacher.sus2")
+            fields = read_sus2(model)
+            vector_to_fields(fields, random_vector(fields, seed + 500, rscale, oscale))
+            write_sus2(teacher, fields)
+            for fr in frames:
+                one = os.path.join(tmp, "one.cfg")
+                write_cfg(one, [fr])
+                out = run([emb, teacher, one, "1", "direct"])
+                rec = json.loads(next(l for l in out.splitlines() if l.startswith("NATIVE_EFS_JSON")).split(" ", 1)[1])
+                fr.energy = rec["energy"]
+                fr.forces = np.asarray(rec["forces"])
+                fr.stress = np.asarray(rec["virial"])
+            cfg = os.path.join(HERE, "frames", f"{name}__labelled.cfg")
+            write_cfg(cfg, frames)
+            for weighting in ("vibrations", "structures"):
+                res = json.loads(run([refgrad, "--loss", model, cfg, *(str(w) for w in weights), weighting]))
+                with open(os.path.join(HERE, "loss", f"{name}__{weighting}.json"), "w") as fh:
+                    json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
+                               "weighting": weighting,
+                               "source": "reference NonLinearRegression::CalcObjectiveFunctionGrad (summed over configs)",
+                               "loss": res["loss"], "grad": res["grad"], "configs": res["configs"]}, fh)
+            print(name, "labelled frames", len(frames))
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 
