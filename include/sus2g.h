@@ -108,6 +108,37 @@ int sus2g_efs_combination_grad_host(sus2g_engine engine, int nframes, const int*
                                     const double* positions, const int* types, const double* ene_w,
                                     const double* frc_w, const double* str_w, double* grad);
 
+/* ---- training objective and BFGS --------------------------------------------------------------
+ * A trainer holds a fixed set of labelled frames resident on the engine's device (edges built
+ * once) and evaluates the energy / force / stress objective with its parameter gradient:
+ *   replaces NonLinearRegression::CalcObjectiveFunctionGrad (dev_src/non_linear_regression.cpp:1112)
+ *   over AddLoss / AddLossGrad (:768-880, :892-1068) with the std terms, relative force weights,
+ *   penalties and regularisers off, divided by the frame count K as MTPR_trainer::Train does
+ *   (dev_src/mtpr_trainer.cpp:4733-4745).
+ * Frames as in sus2g_calc_efs_host (host arrays, copied once).  Labels: energy[nframes],
+ * forces[3 * natoms], stress[9 * nframes] (row-major 3x3 in the virial convention of the
+ * reference's Configuration::stresses); has_labels[f] bit 0 energy, bit 1 forces, bit 2 stress.
+ * weighting: 0 "vibrations", 1 "structures", 2 "molecules" (NonLinearRegression::weighting).
+ * The trainer keeps a reference to the engine: free the trainer before the engine. */
+typedef struct sus2g_trainer_s* sus2g_trainer;
+int sus2g_trainer_create(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                         const double* positions, const int* types, const double* energy, const double* forces,
+                         const double* stress, const int* has_labels, double wE, double wF, double wS, int weighting,
+                         int norm_by_forces, sus2g_trainer* out);
+void sus2g_trainer_free(sus2g_trainer trainer);
+/* Loss (and, when grad != NULL, its gradient [param count], host) at params [param count, host,
+ * Coeff() order].  The engine's parameters are replaced by params. */
+int sus2g_trainer_loss_grad(sus2g_trainer trainer, const double* params, double* loss, double* grad);
+/* Replay the evaluation as one CUDA graph (enabled = 1, default) or launch it eagerly (0). */
+int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
+/* Dense BFGS from params (in/out) for at most max_iter accepted steps or until |grad| <= gtol:
+ * replaces the MTPR_trainer::Train BFGS loop (dev_src/mtpr_trainer.cpp:4985-4997) over
+ * BFGS::Iterate / UpdateInvHess (src/common/bfgs.cpp:251-329, 428-502); inverse Hessian,
+ * direction and update in FP64 on the device.  history[max_iter + 1] (may be NULL) receives the
+ * loss before the first and after each accepted step; *steps the accepted step count. */
+int sus2g_trainer_bfgs(sus2g_trainer trainer, double* params, int max_iter, double gtol, double* history,
+                       int* steps);
+
 /* ---- allocation-free Static E / F / virial ------------------------------------------------------
  * No counterpart in the reference: this entry point exists for callers that cannot allocate device
  * memory during a step -- code recording into a CUDA stream capture, MD drivers whose device memory

@@ -47,11 +47,13 @@ int main(int argc, char** argv) {
     return 0;
   }
   if (std::string(argv[1]) == "--loss") {
-    // ref-grad --loss MODEL CFG wE wF wS [weighting]: NonLinearRegression::CalcObjectiveFunctionGrad
-    // (dev_src/non_linear_regression.cpp:1112) over the labelled CFG with the energy / force /
-    // stress MSE terms only (std terms, penalties and regularisers set to zero); prints the
-    // summed loss and gradient (the trainer divides both by the configuration count afterwards).
-    if (argc < 7) { std::fprintf(stderr, "usage: ref-grad --loss MODEL CFG wE wF wS [weighting]\n"); return 2; }
+    // ref-grad --loss MODEL CFG wE wF wS [weighting [gate_x_l2]]:
+    // NonLinearRegression::CalcObjectiveFunctionGrad (dev_src/non_linear_regression.cpp:1112) over
+    // the labelled CFG with the energy / force / stress MSE terms only (std terms, penalties and
+    // regularisers set to zero; the Effect gate-x L2 term, default 1e-4 in the reference
+    // (non_linear_regression.h:128), is 0 unless given); prints the summed loss and gradient (the
+    // trainer divides both by the configuration count afterwards).
+    if (argc < 7) { std::fprintf(stderr, "usage: ref-grad --loss MODEL CFG wE wF wS [weighting [gate_x_l2]]\n"); return 2; }
     MLMTPR mtpr(argv[2]);
     struct Objective : NonLinearRegression {
       using NonLinearRegression::NonLinearRegression;
@@ -64,6 +66,7 @@ int main(int argc, char** argv) {
     obj.radial_smooth_regularization = 0.0;
     obj.fixed_atomic_energy_weight = 0.0;
     if (argc > 7) obj.weighting = argv[7];
+    obj.gate_x_l2_regularization = argc > 8 ? std::stod(argv[8]) : 0.0;
     std::ifstream in(argv[3]);
     std::vector<Configuration> train;
     Configuration c;

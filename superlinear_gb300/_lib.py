@@ -42,6 +42,13 @@ SIGNATURES = {
     "sus2g_efs_combination_grad_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
     "sus2g_static_efs_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                                 ctypes.c_longlong, _vp, _vp, _vp, _vp]),
+    "sus2g_trainer_create": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _ip,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                            ctypes.c_int, ctypes.POINTER(_vp)]),
+    "sus2g_trainer_free": (None, [_vp]),
+    "sus2g_trainer_loss_grad": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
+    "sus2g_trainer_set_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sus2g_trainer_bfgs": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_double, _dp, _ip]),
 }
 
 _lib = None

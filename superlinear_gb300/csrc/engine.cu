@@ -593,9 +593,13 @@ void Engine::upload_tables() {
   tab_int_.ensure(sizeof(int) * pk.ints.size());
   tab_real_.ensure(sizeof(Real) * reals.size());
   tab_dbl_.ensure(sizeof(double) * dbl.size());
-  SUS2G_CUDA(cudaMemcpy(tab_int_.ptr, pk.ints.data(), sizeof(int) * pk.ints.size(), cudaMemcpyHostToDevice));
-  SUS2G_CUDA(cudaMemcpy(tab_real_.ptr, reals.data(), sizeof(Real) * reals.size(), cudaMemcpyHostToDevice));
-  SUS2G_CUDA(cudaMemcpy(tab_dbl_.ptr, dbl.data(), sizeof(double) * dbl.size(), cudaMemcpyHostToDevice));
+  // stream-ordered copies: the engine stream is non-blocking, so a legacy-stream copy would not
+  // order against its next kernel; the host vectors die at return, hence the synchronisation
+  const cudaStream_t us = stream_ ? stream_ : own_stream_;
+  SUS2G_CUDA(cudaMemcpyAsync(tab_int_.ptr, pk.ints.data(), sizeof(int) * pk.ints.size(), cudaMemcpyHostToDevice, us));
+  SUS2G_CUDA(cudaMemcpyAsync(tab_real_.ptr, reals.data(), sizeof(Real) * reals.size(), cudaMemcpyHostToDevice, us));
+  SUS2G_CUDA(cudaMemcpyAsync(tab_dbl_.ptr, dbl.data(), sizeof(double) * dbl.size(), cudaMemcpyHostToDevice, us));
+  SUS2G_CUDA(cudaStreamSynchronize(us));
   const int* I = tab_int_.as<int>();
   const Real* R = tab_real_.as<Real>();
   auto* dm = new DevModel<Real>();
@@ -693,6 +697,7 @@ void Engine::take_stage_times(double* ms, int* counts) {
 void Engine::build_edges(int nframes, const int* frame_natoms, const double* cells, const double* d_pos,
                          const int* d_types) {
   SUS2G_CUDA(cudaSetDevice(device_));
+  ++edge_generation_;
   if (nframes < 0) throw Error(1, "negative frame count");
   const double rc = model_.max_dist, rc2 = rc * rc;
   std::vector<FramePlan>& plans = *plans_;
@@ -840,6 +845,7 @@ void Engine::finalize_edges() {
 
 void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j, const double* d_d) {
   SUS2G_CUDA(cudaSetDevice(device_));
+  ++edge_generation_;
   if (nowned < 0 || nall < nowned || nedges < 0) throw Error(1, "invalid atom layout");
   cudaStream_t s = stream_;
   ncentres_ = nowned;

@@ -42,8 +42,10 @@ class Engine {
   void upload_model();
   // Replace the engine's parameter vector (trainer order) and re-upload the device tables.
   void set_params(const double* params) { model_.set_params(params); upload_model(); }
-  int nframes_of_plan() const { return nframes_; }
-  const int* d_frame_of() const { return frame_of_.as<int>(); }
+  // Incremented by every build_edges / set_edges: a caller that captured work on this engine's
+  // buffers (a CUDA graph) must rebuild it when the generation it recorded has changed, since a
+  // rebuild may reallocate the edge and step buffers.
+  unsigned long long edge_generation() const { return edge_generation_; }
 
   // --- geometry -----------------------------------------------------------------------------
   // Periodic frames: cells (row lattice vectors, 9 doubles each) live on the host, positions
@@ -111,6 +113,7 @@ class Engine {
   cudaStream_t own_stream_ = nullptr, stream_ = nullptr;
   int sm_count_ = 0;
   int launches_ = 0;
+  unsigned long long edge_generation_ = 0;
 
   // model tables (both precisions are packed into one buffer each)
   DevBuf tab_int_, tab_real_, tab_dbl_;

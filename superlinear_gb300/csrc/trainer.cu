@@ -1,0 +1,451 @@
+// GPU training step for one engine: labelled frames resident on the device, the energy / force /
+// stress objective with its parameter gradient, and an FP64 BFGS on the device.
+//
+// Objective (NonLinearRegression::AddLoss / AddLossGrad, dev_src/non_linear_regression.cpp:768-1068,
+// energy / force / stress terms; std terms, penalties and regularisers off), summed over the K
+// frames and divided by K as the trainer does (dev_src/mtpr_trainer.cpp:4736-4745):
+//   d = 0.1, a = <|F0|^2>, s = d / (d + fn a)
+//   L_F = wF' s sum |F - F0|^2            dL/dF = 2 wF' s (F - F0)       wF' = wF (/N for "structures")
+//   L_S = wS' |S - S0|_F^2 / N            stress weight = -2 wS' (S - S0) / N
+//   L_E = wE' s (E - E0)^2 / N            dL/dE = 2 wE' s (E - E0) / N
+//   wE' = wE, wS' = wS ("vibrations"), / N ("structures"), * N ("molecules")
+// The derivative weights feed Engine::combination_grad (AccumulateEFSCombinationGrad contract).
+//
+// BFGS (src/common/bfgs.{h,cpp}): dense inverse-Hessian update in FP64 on the device, the
+// direction p = -H g on the device, the line search on host scalars with the reference's strong
+// Wolfe constants c1 = 0.1, c2 = 0.5 (bfgs.h:384-385).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sus2g.h"
+#include "capi_types.h"
+#include "device_common.cuh"
+
+namespace sus2g {
+
+#define TRAIN_CUDA(call)                                                                      \
+  do {                                                                                        \
+    cudaError_t err__ = (call);                                                               \
+    if (err__ != cudaSuccess)                                                                 \
+      throw Error(10, std::string("CUDA error: ") + cudaGetErrorString(err__) + " at " #call); \
+  } while (0)
+
+namespace {
+
+struct LossConfig {
+  double wE, wF, wS;
+  int weighting;  // 0 vibrations, 1 structures, 2 molecules
+  int norm_by_forces;
+};
+
+// One block per frame: loss terms and derivative weights.
+__global__ void k_loss(int nframes, const int* fbegin, const double* E, const double* F, const double* V,
+                       const double* E0, const double* F0, const double* S0, const int* has, LossConfig c,
+                       double* ew, double* fw, double* sw, double* loss_f) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  const int a0 = fbegin[f], a1 = fbegin[f + 1], n = a1 - a0;
+  __shared__ double red[2][256];
+  double avef = 0.0, fl = 0.0;
+  const bool hasE = has[f] & 1, hasF = has[f] & 2, hasS = has[f] & 4;
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x)
+    for (int q = 0; q < 3; ++q) avef += F0[3 * static_cast<size_t>(i) + q] * F0[3 * static_cast<size_t>(i) + q];
+  red[0][threadIdx.x] = avef;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[0][threadIdx.x] += red[0][threadIdx.x + s];
+    __syncthreads();
+  }
+  avef = n > 0 && hasF ? red[0][0] / n : 0.0;
+  const double d = 0.1, scale_fn = d / (d + c.norm_by_forces * avef);
+  double wF = c.wF, wE = c.wE, wS = c.wS;
+  if (c.weighting == 1 && n > 0) { wF /= n; wE /= n; wS /= n; }
+  else if (c.weighting == 2) { wE *= n; wS *= n; }
+  const bool useF = c.wF != 0.0 && hasF;
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x)
+    for (int q = 0; q < 3; ++q) {
+      const size_t k = 3 * static_cast<size_t>(i) + q;
+      const double delta = F[k] - F0[k];
+      if (useF) fl += wF * scale_fn * delta * delta;
+      fw[k] = useF ? wF * scale_fn * 2.0 * delta : 0.0;
+    }
+  __syncthreads();
+  red[1][threadIdx.x] = fl;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[1][threadIdx.x] += red[1][threadIdx.x + s];
+    __syncthreads();
+  }
+  double dE = 0.0;
+  if (threadIdx.x == 0) {
+    double L = red[1][0];
+    // virial (xx, yy, zz, xy, xz, yz) -> symmetric 3x3
+    const double* v = V + 6 * f;
+    const double S[9] = {v[0], v[3], v[4], v[3], v[1], v[5], v[4], v[5], v[2]};
+    for (int q = 0; q < 9; ++q) sw[9 * f + q] = 0.0;
+    if (wS != 0.0 && hasS && n > 0) {
+      for (int q = 0; q < 9; ++q) {
+        const double ds = S[q] - S0[9 * f + q];
+        L += wS * ds * ds / n;
+        sw[9 * f + q] = -2.0 * wS * ds / n;
+      }
+    }
+    if (wE != 0.0 && hasE && n > 0) {
+      const double de = E[f] - E0[f];
+      L += wE * de * de * scale_fn / n;
+      dE = 2.0 * wE * de * scale_fn / n;
+    }
+    loss_f[f] = L;
+    red[0][0] = dE;
+  }
+  __syncthreads();
+  dE = red[0][0];
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) ew[i] = dE;
+}
+
+// loss = sum_f loss_f / K (fixed order), grad /= K
+__global__ void k_loss_finish(int nframes, const double* loss_f, double* loss, double* grad, int nparams) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const double inv = nframes > 0 ? 1.0 / nframes : 0.0;
+  if (t == 0) {
+    double s = 0.0;
+    for (int f = 0; f < nframes; ++f) s += loss_f[f];
+    *loss = s * inv;
+  }
+  if (t < nparams) grad[t] *= inv;
+}
+
+// y = A x for a symmetric n x n matrix (row-major), one warp per row.
+__global__ void k_symv(int n, const double* A, const double* x, double alpha, double* y) {
+  const int row = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  double s = 0.0;
+  const double* a = A + static_cast<size_t>(row) * n;
+  for (int j = lane; j < n; j += kWarp) s += a[j] * x[j];
+  s = warp_sum(s);
+  if (lane == 0) y[row] = alpha * s;
+}
+
+// Fixed-order dot products: out[0] = x . y (one block).
+__global__ void k_dot(int n, const double* x, const double* y, double* out) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += x[i] * y[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// H <- H - rho (Hy s^T + s Hy^T) + (rho^2 y^T H y + rho) s s^T
+__global__ void k_bfgs_update(int n, double* H, const double* s, const double* Hy, double rho, double yHy) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * n) return;
+  const int i = static_cast<int>(t / n), j = static_cast<int>(t - static_cast<long long>(i) * n);
+  H[t] += -rho * (Hy[i] * s[j] + s[i] * Hy[j]) + (rho * rho * yHy + rho) * s[i] * s[j];
+}
+
+__global__ void k_scaled_identity(int n, double* H, double diag) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * n) return;
+  const int i = static_cast<int>(t / n), j = static_cast<int>(t - static_cast<long long>(i) * n);
+  H[t] = i == j ? diag : 0.0;
+}
+
+__global__ void k_axpy_to(int n, const double* x, double a, const double* p, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = x[i] + a * p[i];
+}
+
+__global__ void k_sub(int n, const double* a, const double* b, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] - b[i];
+}
+
+}  // namespace
+
+class Trainer {
+ public:
+  Trainer(Engine& eng, int nframes, const int* natoms, const double* cells, const double* pos, const int* types,
+          const double* E0, const double* F0, const double* S0, const int* has, LossConfig cfg)
+      : eng_(eng), nframes_(nframes), cfg_(cfg) {
+    cudaStream_t s = eng_.stream();
+    long long n = 0;
+    fbegin_host_.push_back(0);
+    for (int f = 0; f < nframes; ++f) { n += natoms[f]; fbegin_host_.push_back(static_cast<int>(n)); }
+    natoms_ = static_cast<int>(n);
+    nparams_ = eng_.model().param_count();
+    natoms_list_.assign(natoms, natoms + nframes);
+    cells_.assign(cells, cells + 9 * nframes);
+    pos_.ensure(sizeof(double) * 3 * std::max(1, natoms_));
+    types_.ensure(sizeof(int) * std::max(1, natoms_));
+    E0_.ensure(sizeof(double) * std::max(1, nframes));
+    F0_.ensure(sizeof(double) * 3 * std::max(1, natoms_));
+    S0_.ensure(sizeof(double) * 9 * std::max(1, nframes));
+    has_.ensure(sizeof(int) * std::max(1, nframes));
+    fbegin_.ensure(sizeof(int) * (nframes + 1));
+    TRAIN_CUDA(cudaMemcpyAsync(pos_.ptr, pos, sizeof(double) * 3 * natoms_, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(types_.ptr, types, sizeof(int) * natoms_, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(E0_.ptr, E0, sizeof(double) * nframes, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(F0_.ptr, F0, sizeof(double) * 3 * natoms_, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(S0_.ptr, S0, sizeof(double) * 9 * nframes, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(has_.ptr, has, sizeof(int) * nframes, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(fbegin_.ptr, fbegin_host_.data(), sizeof(int) * (nframes + 1), cudaMemcpyHostToDevice, s));
+    // predictions and loss derivatives
+    E_.ensure(sizeof(double) * std::max(1, nframes));
+    F_.ensure(sizeof(double) * 3 * std::max(1, natoms_));
+    V_.ensure(sizeof(double) * 6 * std::max(1, nframes));
+    ew_.ensure(sizeof(double) * std::max(1, natoms_));
+    fw_.ensure(sizeof(double) * 3 * std::max(1, natoms_));
+    sw_.ensure(sizeof(double) * 9 * std::max(1, nframes));
+    lossf_.ensure(sizeof(double) * std::max(1, nframes));
+    loss_.ensure(sizeof(double) * 8);
+    grad_.ensure(sizeof(double) * nparams_);
+    TRAIN_CUDA(cudaMallocHost(&host_scalars_, sizeof(double) * 8));
+    bind_edges();
+  }
+
+  // The edge set of the fixed frames is built once, and again only when the engine was used for
+  // other geometry in between (which also invalidates a captured graph).
+  void bind_edges() {
+    if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
+    if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+    eng_.build_edges(nframes_, natoms_list_.data(), cells_.data(), pos_.as<double>(), types_.as<int>());
+    eng_.check_device_error();
+    generation_ = eng_.edge_generation();
+  }
+
+  ~Trainer() {
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (host_scalars_) cudaFreeHost(host_scalars_);
+  }
+
+  void set_graph(bool on) { use_graph_ = on; }
+  int nparams() const { return nparams_; }
+
+  // Enqueues E/F/virial, loss, gradient on the engine stream (device results in loss_/grad_).
+  void enqueue_eval() {
+    cudaStream_t s = eng_.stream();
+    eng_.efs(E_.as<double>(), F_.as<double>(), V_.as<double>(), nullptr);
+    if (nframes_)
+      k_loss<<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), E_.as<double>(), F_.as<double>(), V_.as<double>(),
+                                      E0_.as<double>(), F0_.as<double>(), S0_.as<double>(), has_.as<int>(), cfg_,
+                                      ew_.as<double>(), fw_.as<double>(), sw_.as<double>(), lossf_.as<double>());
+    TRAIN_CUDA(cudaMemsetAsync(grad_.ptr, 0, sizeof(double) * nparams_, s));
+    if (natoms_) eng_.combination_grad(ew_.as<double>(), fw_.as<double>(), sw_.as<double>(), grad_.as<double>());
+    k_loss_finish<<<(nparams_ + 255) / 256, 256, 0, s>>>(nframes_, lossf_.as<double>(), loss_.as<double>(),
+                                                         grad_.as<double>(), nparams_);
+  }
+
+  // Loss and gradient at the parameters already in the engine; results stay on the device.
+  void eval_device() {
+    if (eng_.edge_generation() != generation_) bind_edges();
+    cudaStream_t s = eng_.stream();
+    if (!use_graph_) {
+      enqueue_eval();
+      return;
+    }
+    if (!graph_exec_) {
+      enqueue_eval();  // first evaluation runs eagerly (sizes buffers, configures kernels)
+      TRAIN_CUDA(cudaStreamSynchronize(s));
+      TRAIN_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+      enqueue_eval();
+      TRAIN_CUDA(cudaStreamEndCapture(s, &graph_));
+      TRAIN_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+      ++graph_builds_;
+      return;
+    }
+    TRAIN_CUDA(cudaGraphLaunch(graph_exec_, s));
+  }
+
+  double loss_grad(const double* params, double* grad_host) {
+    eng_.set_params(params);
+    eval_device();
+    cudaStream_t s = eng_.stream();
+    TRAIN_CUDA(cudaMemcpyAsync(host_scalars_, loss_.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (grad_host) TRAIN_CUDA(cudaMemcpyAsync(grad_host, grad_.ptr, sizeof(double) * nparams_, cudaMemcpyDeviceToHost, s));
+    TRAIN_CUDA(cudaStreamSynchronize(s));
+    eng_.check_device_error();
+    return host_scalars_[0];
+  }
+
+  // Dense BFGS on the device (BFGS::Iterate / UpdateInvHess, src/common/bfgs.cpp:251-329, 428-502):
+  // H starts at the identity (BFGS::Restart, bfgs.cpp:529-534); each iteration takes p = -H g, a line
+  // search x + a p from a = 1 until the strong Wolfe conditions f <= f0 + c1 a p.g0 and
+  // |p.g| <= c2 |p.g0| hold (c1 = 0.1, c2 = 0.5, bfgs.h:384-385), then the rank-2 update of H with
+  // s = a p, y = g - g0, skipped when s.y <= 64 eps.  The trial points bracket by doubling and
+  // bisection (the reference interpolates inside its bracket; accepted points satisfy the same
+  // conditions).  params (host) in/out; history[max_iter + 1] receives the loss after each
+  // accepted step (history[0] = initial).  Returns the number of accepted steps.
+  int bfgs(double* params, int max_iter, double gtol, double* history) {
+    const int n = nparams_;
+    cudaStream_t s = eng_.stream();
+    DevBuf H, x, g, p, xn, gn, sv, yv, Hy, sc;
+    H.ensure(sizeof(double) * static_cast<size_t>(n) * n);
+    for (DevBuf* b : {&x, &g, &p, &xn, &gn, &sv, &yv, &Hy}) b->ensure(sizeof(double) * n);
+    sc.ensure(sizeof(double) * 8);
+    const unsigned nn_blocks = static_cast<unsigned>((static_cast<long long>(n) * n + 255) / 256);
+    const unsigned n_blocks = static_cast<unsigned>((n + 255) / 256);
+    const unsigned row_blocks = static_cast<unsigned>((static_cast<long long>(n) * kWarp + 255) / 256);
+    std::vector<double> xh(params, params + n);
+    auto dot = [&](const double* a, const double* b) {
+      k_dot<<<1, 256, 0, s>>>(n, a, b, sc.as<double>());
+      TRAIN_CUDA(cudaMemcpyAsync(host_scalars_ + 1, sc.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
+      TRAIN_CUDA(cudaStreamSynchronize(s));
+      return host_scalars_[1];
+    };
+    double f = loss_grad(xh.data(), nullptr);
+    TRAIN_CUDA(cudaMemcpyAsync(x.ptr, xh.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(g.ptr, grad_.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    k_scaled_identity<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), 1.0);
+    if (history) history[0] = f;
+    int accepted = 0;
+    const double c1 = 0.1, c2 = 0.5, floor = 64.0 * 2.220446049250313e-16;
+    for (int it = 0; it < max_iter; ++it) {
+      if (!(std::sqrt(dot(g.as<double>(), g.as<double>())) > gtol)) break;
+      k_symv<<<row_blocks, 256, 0, s>>>(n, H.as<double>(), g.as<double>(), -1.0, p.as<double>());
+      const double gp = dot(g.as<double>(), p.as<double>());
+      if (!(gp < 0)) throw Error(5, "BFGS: search direction is not a descent direction");
+      double alpha = 1.0, lo = 0.0, hi = -1.0, fn = f;
+      bool ok = false;
+      for (int ls = 0; ls < 31; ++ls) {
+        k_axpy_to<<<n_blocks, 256, 0, s>>>(n, x.as<double>(), alpha, p.as<double>(), xn.as<double>());
+        TRAIN_CUDA(cudaMemcpyAsync(xh.data(), xn.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+        TRAIN_CUDA(cudaStreamSynchronize(s));
+        fn = loss_grad(xh.data(), nullptr);
+        TRAIN_CUDA(cudaMemcpyAsync(gn.ptr, grad_.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+        if (!std::isfinite(fn) || fn > f + c1 * alpha * gp) {
+          hi = alpha;
+        } else {
+          const double gpn = dot(gn.as<double>(), p.as<double>());
+          if (std::abs(gpn) <= c2 * std::abs(gp)) { ok = true; break; }
+          if (gpn < 0) lo = alpha;  // still descending steeply: longer step
+          else hi = alpha;          // past the minimum along p
+        }
+        alpha = hi < 0 ? 2.0 * alpha : 0.5 * (lo + hi);
+      }
+      if (!ok) break;  // line search exhausted: keep the last accepted point
+      k_sub<<<n_blocks, 256, 0, s>>>(n, xn.as<double>(), x.as<double>(), sv.as<double>());
+      k_sub<<<n_blocks, 256, 0, s>>>(n, gn.as<double>(), g.as<double>(), yv.as<double>());
+      const double ys = dot(yv.as<double>(), sv.as<double>());
+      if (std::isfinite(ys) && ys > floor) {
+        k_symv<<<row_blocks, 256, 0, s>>>(n, H.as<double>(), yv.as<double>(), 1.0, Hy.as<double>());
+        const double yHy = dot(yv.as<double>(), Hy.as<double>());
+        if (std::isfinite(yHy))
+          k_bfgs_update<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), sv.as<double>(), Hy.as<double>(), 1.0 / ys, yHy);
+      }
+      TRAIN_CUDA(cudaMemcpyAsync(x.ptr, xn.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      TRAIN_CUDA(cudaMemcpyAsync(g.ptr, gn.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      f = fn;
+      ++accepted;
+      if (history) history[accepted] = f;
+    }
+    TRAIN_CUDA(cudaMemcpyAsync(params, x.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    TRAIN_CUDA(cudaStreamSynchronize(s));
+    eng_.set_params(params);
+    return accepted;
+  }
+
+  int graph_builds() const { return graph_builds_; }
+
+ private:
+  Engine& eng_;
+  int nframes_ = 0, natoms_ = 0, nparams_ = 0;
+  LossConfig cfg_;
+  std::vector<int> fbegin_host_, natoms_list_;
+  std::vector<double> cells_;
+  DevBuf pos_, types_, E0_, F0_, S0_, has_, fbegin_;
+  DevBuf E_, F_, V_, ew_, fw_, sw_, lossf_, loss_, grad_;
+  double* host_scalars_ = nullptr;
+  bool use_graph_ = true;
+  cudaGraph_t graph_ = nullptr;
+  cudaGraphExec_t graph_exec_ = nullptr;
+  int graph_builds_ = 0;
+  unsigned long long generation_ = 0;
+};
+
+}  // namespace sus2g
+
+struct sus2g_trainer_s {
+  std::unique_ptr<sus2g::Trainer> trainer;
+};
+
+namespace {
+template <typename F>
+int train_guarded(F&& f) {
+  try {
+    f();
+    sus2g_set_last_error("");
+    return 0;
+  } catch (const sus2g::Error& e) {
+    sus2g_set_last_error(e.what());
+    return e.code > 0 ? e.code : 1;
+  } catch (const std::exception& e) {
+    sus2g_set_last_error(e.what());
+    return 1;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int sus2g_trainer_create(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                         const double* positions, const int* types, const double* energy, const double* forces,
+                         const double* stress, const int* has_labels, double wE, double wF, double wS, int weighting,
+                         int norm_by_forces, sus2g_trainer* out) {
+  return train_guarded([&] {
+    if (!engine || !out || nframes < 0 || (nframes && (!natoms || !cells || !energy || !stress || !has_labels)))
+      throw sus2g::Error(1, "invalid argument: trainer inputs");
+    long long n = 0;
+    for (int f = 0; f < nframes; ++f) {
+      if (natoms[f] < 0) throw sus2g::Error(1, "invalid argument: natoms");
+      n += natoms[f];
+    }
+    if (n && (!positions || !types || !forces)) throw sus2g::Error(1, "invalid argument: positions/types/forces");
+    for (long long i = 0; i < n; ++i)
+      if (types[i] < 0 || types[i] >= engine->engine->model().C) throw sus2g::Error(1, "atom species index out of range");
+    if (weighting < 0 || weighting > 2) throw sus2g::Error(1, "weighting must be 0 (vibrations), 1 (structures) or 2 (molecules)");
+    sus2g::LossConfig cfg{wE, wF, wS, weighting, norm_by_forces};
+    auto t = std::make_unique<sus2g_trainer_s>();
+    t->trainer = std::make_unique<sus2g::Trainer>(*engine->engine, nframes, natoms, cells, positions, types, energy,
+                                                  forces, stress, has_labels, cfg);
+    *out = t.release();
+  });
+}
+
+void sus2g_trainer_free(sus2g_trainer t) { delete t; }
+
+int sus2g_trainer_set_graph(sus2g_trainer t, int enabled) {
+  return train_guarded([&] {
+    if (!t) throw sus2g::Error(1, "invalid argument: trainer");
+    t->trainer->set_graph(enabled != 0);
+  });
+}
+
+int sus2g_trainer_loss_grad(sus2g_trainer t, const double* params, double* loss, double* grad) {
+  return train_guarded([&] {
+    if (!t || !params || !loss) throw sus2g::Error(1, "invalid argument: trainer/params/loss");
+    *loss = t->trainer->loss_grad(params, grad);
+  });
+}
+
+int sus2g_trainer_bfgs(sus2g_trainer t, double* params, int max_iter, double gtol, double* history, int* steps) {
+  return train_guarded([&] {
+    if (!t || !params || max_iter < 0) throw sus2g::Error(1, "invalid argument: trainer/params/max_iter");
+    const int k = t->trainer->bfgs(params, max_iter, gtol, history);
+    if (steps) *steps = k;
+  });
+}
+
+}  // extern "C"

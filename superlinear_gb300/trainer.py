@@ -1,0 +1,96 @@
+"""Training objective over labelled frames resident on the GPU, its gradient, and BFGS.
+
+Mirrors the reference trainer's objective / optimiser surface for this path:
+  * ``Trainer.loss_grad(params)``  ~ NonLinearRegression::CalcObjectiveFunctionGrad
+                                     (dev_src/non_linear_regression.cpp:1112) with the energy / force /
+                                     stress terms of AddLoss / AddLossGrad (:768-1068), divided by the
+                                     frame count as MTPR_trainer::Train does (dev_src/mtpr_trainer.cpp:4737-4745)
+  * ``Trainer.bfgs(params, ...)``  ~ the dense BFGS loop of MTPR_trainer::Train over BFGS::Iterate
+                                     (src/common/bfgs.cpp:251-329)
+``weighting`` takes the reference's names: "vibrations", "structures", "molecules".
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import check, load
+from .engine import Engine
+
+__all__ = ["Trainer", "WEIGHTINGS"]
+
+WEIGHTINGS = {"vibrations": 0, "structures": 1, "molecules": 2}
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+class Trainer:
+    """Labelled frames (``energy``, ``forces``, ``stress`` attributes, any may be None) bound to an engine."""
+
+    def __init__(self, engine: Engine, frames, wE: float = 1.0, wF: float = 0.01, wS: float = 0.001,
+                 weighting: str = "vibrations", norm_by_forces: int = 0):
+        if weighting not in WEIGHTINGS:
+            raise ValueError(f"weighting must be one of {sorted(WEIGHTINGS)}")
+        self.engine = engine
+        natoms, cells, pos, types = Engine.pack_frames(frames)
+        nf, n = natoms.size, int(natoms.sum())
+        energy = np.zeros(nf)
+        forces = np.zeros((n, 3))
+        stress = np.zeros((nf, 9))
+        has = np.zeros(nf, dtype=np.int32)
+        a = 0
+        for k, fr in enumerate(frames):
+            if fr.energy is not None:
+                energy[k] = fr.energy
+                has[k] |= 1
+            if fr.forces is not None:
+                forces[a:a + fr.natoms] = fr.forces
+                has[k] |= 2
+            if fr.stress is not None:
+                stress[k] = np.asarray(fr.stress, dtype=np.float64).reshape(9)
+                has[k] |= 4
+            a += fr.natoms
+        self.nframes = nf
+        self.natoms = n
+        h = ctypes.c_void_p()
+        check(load().sus2g_trainer_create(engine._h, nf, natoms.ctypes.data_as(_ip), _d(cells), _d(pos),
+                                          types.ctypes.data_as(_ip), _d(energy), _d(forces), _d(stress),
+                                          has.ctypes.data_as(_ip), float(wE), float(wF), float(wS),
+                                          WEIGHTINGS[weighting], int(norm_by_forces), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            load().sus2g_trainer_free(h)
+            self._h = None
+
+    @property
+    def nparams(self) -> int:
+        return self.engine.model.nparams
+
+    def set_graph(self, enabled: bool) -> None:
+        check(load().sus2g_trainer_set_graph(self._h, 1 if enabled else 0))
+
+    def loss_grad(self, params, want_grad: bool = True):
+        """(loss, grad) at ``params`` (Coeff() order); grad is None when ``want_grad`` is False."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        if p.size != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
+        loss = ctypes.c_double()
+        g = np.zeros(self.nparams) if want_grad else None
+        check(load().sus2g_trainer_loss_grad(self._h, _d(p), ctypes.byref(loss), _d(g)))
+        return loss.value, g
+
+    def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
+        """Runs BFGS from ``params``; returns (params, loss history)."""
+        p = np.array(params, dtype=np.float64)
+        hist = np.zeros(max_iter + 1)
+        steps = ctypes.c_int()
+        check(load().sus2g_trainer_bfgs(self._h, _d(p), int(max_iter), float(gtol), _d(hist), ctypes.byref(steps)))
+        return p, hist[:steps.value + 1]

@@ -1,0 +1,162 @@
+"""GPU training objective, its gradient, BFGS and the torch autograd binding, through the C ABI.
+
+Bars: FP64 plain within 1e-10 relative of the reference trainer's objective and gradient
+(tests/golden/loss, NonLinearRegression::CalcObjectiveFunctionGrad summed over configurations; the
+trainer reports both divided by the configuration count) and of the oracle's restatement on
+weightings / options the goldens do not cover; FP32 bulk within 1e-5 relative (loss) and 1e-4
+relative norm (gradient) of FP64.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_json
+from superlinear_gb300.synth import read_cfg, training_frames
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+
+
+def rel_norm(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def sg(engine_lib):
+    import superlinear_gb300
+    return superlinear_gb300
+
+
+def loss_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "loss", "*.json")))
+
+
+@pytest.mark.parametrize("path", loss_cases(), ids=os.path.basename)
+def test_objective_matches_reference_trainer(sg, golden, path):
+    data = load_json(path)
+    model = sg.Model(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    k = data["configs"]
+    ref_loss, ref_grad = data["loss"] / k, np.asarray(data["grad"]) / k
+    p = model.params()
+    out = {}
+    for prec in (sg.FP64, sg.FP32):
+        eng = sg.Engine(model, 0, prec)
+        tr = sg.Trainer(eng, frames, *data["weights"], weighting=data["weighting"])
+        out[prec] = tr.loss_grad(p)
+        del tr
+    loss, grad = out[sg.FP64]
+    assert abs(loss - ref_loss) <= FP64_TOL * abs(ref_loss)
+    assert rel_norm(grad, ref_grad) <= FP64_TOL
+    loss32, grad32 = out[sg.FP32]
+    assert abs(loss32 - loss) <= 1e-5 * abs(loss)
+    assert rel_norm(grad32, grad) <= 1e-4
+
+
+@pytest.mark.parametrize("weighting,nbf", [("molecules", 0), ("structures", 1), ("vibrations", 1)])
+def test_objective_matches_oracle_other_weightings(sg, oracle_lib, golden, weighting, nbf):
+    """Weightings and force normalisation the goldens do not exercise, on a ragged batch where some
+    frames lack energy, force or stress labels."""
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    frames = read_cfg(os.path.join(golden, "frames", "effect_l3k4r2o2__labelled.cfg"))
+    frames[1].energy = None
+    frames[2].forces = None
+    frames[3].stress = None
+    om = oracle_lib.OracleModel(path)
+    ref_loss, ref_grad = oracle_lib.loss_grad(om, frames, 1.0, 0.01, 0.001, weighting=weighting,
+                                              norm_by_forces=nbf)
+    model = sg.Model(path)
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, 1.0, 0.01, 0.001, weighting=weighting, norm_by_forces=nbf)
+    loss, grad = tr.loss_grad(model.params())
+    assert abs(loss - ref_loss / len(frames)) <= FP64_TOL * abs(ref_loss / len(frames))
+    assert rel_norm(grad, ref_grad / len(frames)) <= FP64_TOL
+
+
+def test_graph_replay_equals_eager_and_tracks_parameters(sg, golden):
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    p0 = model.params()
+    p1 = p0 * (1.0 + 1e-3 * np.cos(np.arange(p0.size)))
+    res = {}
+    for graph in (False, True):
+        tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames)
+        tr.set_graph(graph)
+        # the replayed graph must read the parameter tables re-uploaded between evaluations
+        res[graph] = [tr.loss_grad(p) for p in (p0, p1, p0, p1)]
+    for (le, ge), (lg, gg) in zip(res[False], res[True]):
+        assert le == lg and np.array_equal(ge, gg)
+    assert res[True][0][0] == res[True][2][0] and res[True][0][0] != res[True][1][0]
+
+
+def test_bfgs_decreases_loss(sg, golden):
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames)
+    p0 = model.params()
+    p, hist = tr.bfgs(p0, max_iter=8)
+    assert hist.size >= 3
+    assert np.all(np.diff(hist) <= 0.0)
+    assert hist[-1] < 0.9 * hist[0]
+    loss, _ = tr.loss_grad(p)
+    assert abs(loss - hist[-1]) <= 1e-12 * abs(hist[-1])
+
+
+def test_trainer_rejects_invalid_inputs(sg, golden):
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    eng = sg.Engine(model, 0, sg.FP64)
+    with pytest.raises(ValueError):
+        sg.Trainer(eng, frames, weighting="atoms")
+    bad = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    bad[0].types = bad[0].types.copy()
+    bad[0].types[0] = 7
+    with pytest.raises(sg.Sus2Error):
+        sg.Trainer(eng, bad)
+    tr = sg.Trainer(eng, frames)
+    with pytest.raises(ValueError):
+        tr.loss_grad(np.zeros(3))
+
+
+def test_autograd_function_matches_finite_differences(sg, golden):
+    torch = pytest.importorskip("torch")
+    from superlinear_gb300.autograd import efs
+    model = sg.Model(os.path.join(golden, "models", "effect_l3k4r2o2.sus2"))
+    eng = sg.Engine(model, 0, sg.FP64)
+    frames = training_frames(3, 8, 40, 3.0, 4.2, 0.1, seed=77, species=2)
+    rng = np.random.default_rng(3)
+    n = sum(f.natoms for f in frames)
+    a = torch.tensor(rng.normal(size=len(frames)), dtype=torch.float64)
+    b = torch.tensor(rng.normal(size=(n, 3)), dtype=torch.float64)
+    c = torch.tensor(rng.normal(size=(len(frames), 6)), dtype=torch.float64)
+
+    def objective(p):
+        e, f, v = efs(p, eng, frames)
+        return (a * e).sum() + (b * f).sum() + (c * v).sum()
+
+    p0 = torch.tensor(model.params(), dtype=torch.float64, requires_grad=True)
+    objective(p0).backward()
+    g = p0.grad.numpy().copy()
+    d = rng.normal(size=p0.numel())
+    h = 1e-6
+    with torch.no_grad():
+        fp = objective(p0 + h * torch.from_numpy(d)).item()
+        fm = objective(p0 - h * torch.from_numpy(d)).item()
+    fd = (fp - fm) / (2 * h)
+    assert abs(fd - g @ d) <= 1e-6 * max(1.0, abs(fd))
+
+
+def test_trainer_survives_other_use_of_its_engine(sg, golden):
+    """Evaluating other geometry on the trainer's engine rebuilds the trainer's edges (and graph)."""
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    eng = sg.Engine(model, 0, sg.FP64)
+    tr = sg.Trainer(eng, frames)
+    p = model.params()
+    first = tr.loss_grad(p)
+    tr.loss_grad(p)  # graph replay
+    eng.calc_efs(training_frames(3, 60, 200, 3.0, 4.2, 0.1, seed=5, species=2))
+    again = tr.loss_grad(p)
+    assert first[0] == again[0] and np.array_equal(first[1], again[1])

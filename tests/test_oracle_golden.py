@@ -77,3 +77,21 @@ def test_oracle_planted_error_is_detected(oracle_lib, golden):
     fr = read_cfg(os.path.join(golden, "frames", data["frames"]))[0]
     e, f, *_ = m.efs(fr.cell, fr.positions, fr.types)
     assert rel_err(f, data["records"][0]["forces"]) > 1e-9
+
+
+def loss_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "loss", "*.json")))
+
+
+@pytest.mark.parametrize("path", loss_cases(), ids=os.path.basename)
+def test_training_objective_goldens(oracle_lib, golden, path):
+    """Energy / force / stress objective and its gradient against the reference trainer's
+    NonLinearRegression::CalcObjectiveFunctionGrad (summed over configurations)."""
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    assert len(frames) == data["configs"]
+    loss, grad = oracle_lib.loss_grad(m, frames, *data["weights"], weighting=data["weighting"])
+    ref = np.asarray(data["grad"])
+    assert abs(loss - data["loss"]) <= 1e-12 * abs(data["loss"])
+    assert np.linalg.norm(grad - ref) <= 1e-12 * np.linalg.norm(ref)
