@@ -8,6 +8,9 @@ directed edge list from positions on the GPU, then energy, forces and virial (FP
 FP64 reductions; the FP64 plain path is timed alongside).  The inputs are smaller than L2, so L2 is flushed
 (a 256 MiB write) between timed steps, outside the step's events.
 
+The training loss + gradient throughput (frames/s, FP32 bulk vs FP64 plain) over a batch of 256
+uneven Effect L3/K4/R2/O2 frames is reported alongside under "train_effect_l3k4r2o2_256".
+
 --impl reference times the CPU reference path on the host cores instead: the FP64 CPU
 restatement of the reference algorithm (the reference's own sources do not travel to the GPU
 machine), all host threads, E/F/virial per step on the same frame.
@@ -36,6 +39,8 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 METRIC = "atom-steps/s E/F/virial; train loss+grad frames/s; FP32-bulk vs FP64, 1 GB300"
 MODEL = os.path.join(ROOT, "tests", "golden", "models", "static_l3k4o2.sus2")
 EFFECT_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l4k8r2o3.sus2")
+TRAIN_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l3k4r2o2.sus2")
+TRAIN_WEIGHTS = (1.0, 0.01, 0.0)  # energy + force MSE
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "dram_traffic.txt")
 
@@ -136,6 +141,69 @@ def read_traffic(key):
 
 
 # ------------------------------------------------------------------------------------------------
+def training_set(sg, nframes=256, seed=31):
+    """256 uneven periodic frames (8-216 atoms, fcc/bcc/diamond, a in [3.0, 4.2] A, sigma 0.1 A,
+    types Bernoulli(0.5)) labelled by a seeded random-init teacher of the same Effect L3/K4/R2/O2
+    topology (FP64 GPU evaluation, outside any timed region)."""
+    from superlinear_gb300.sus2_format import read_sus2
+    from superlinear_gb300.synth import random_vector, training_frames
+    frames = training_frames(nframes, 8, 216, 3.0, 4.2, 0.1, seed=seed, species=2)
+    teacher = sg.Model(TRAIN_MODEL)
+    teacher.set_params(random_vector(read_sus2(TRAIN_MODEL), seed + 500, 5.0, 8.0))
+    e, f, v, _ = sg.Engine(teacher, 0, sg.FP64).calc_efs(frames)
+    a = 0
+    for k, fr in enumerate(frames):
+        fr.energy = float(e[k])
+        fr.forces = f[a:a + fr.natoms].copy()
+        xx, yy, zz, xy, xz, yz = v[k]
+        fr.stress = np.array([[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]])
+        a += fr.natoms
+    return frames
+
+
+def bench_training(sg, torch, steps, warmup):
+    """Training loss + gradient frames/s over the 256-frame Effect batch, FP32 bulk and FP64 plain:
+    one step = one Trainer.loss_grad (parameter upload, the captured loss+gradient CUDA graph,
+    loss and gradient read back to the host), as a BFGS iteration calls it."""
+    frames = training_set(sg)
+    model = sg.Model(TRAIN_MODEL)
+    p = model.params()
+    out = {"workload": "effect_l3k4r2o2_train256", "frames": len(frames), "atoms": int(sum(f.natoms for f in frames)),
+           "weights": {"energy": TRAIN_WEIGHTS[0], "force": TRAIN_WEIGHTS[1], "stress": TRAIN_WEIGHTS[2]}}
+    losses = {}
+    for prec, key, nsteps in ((sg.FP32, "fp32", steps), (sg.FP64, "fp64", max(3, steps // 4))):
+        eng = sg.Engine(model, 0, prec)
+        tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS)
+        for _ in range(warmup):
+            tr.loss_grad(p)
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            loss, g = tr.loss_grad(p)
+            t.append(time.perf_counter() - t0)
+        ms = 1e3 * float(np.mean(t))
+        losses[key] = (loss, g)
+        out[key] = {"ms_per_step": ms, "frames_per_s": len(frames) / (ms / 1e3), "edges": eng.edge_count()}
+        del tr, eng
+    out["fp32_over_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
+    (l32, g32), (l64, g64) = losses["fp32"], losses["fp64"]
+    out["fp32_error"] = {"loss_rel": abs(l32 - l64) / abs(l64),
+                         "grad_rel_norm": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))}
+    return frames, out
+
+
+def cpu_train_sample(frames, min_seconds=8.0):
+    """Oracle port loss + gradient frames/s over the first frames of the batch (one thread)."""
+    import oracle as orc
+    m = orc.OracleModel(TRAIN_MODEL)
+    done, t0 = 0, time.perf_counter()
+    while done == 0 or (done < len(frames) and time.perf_counter() - t0 < min_seconds):
+        orc.loss_grad(m, frames[done:done + 1], *TRAIN_WEIGHTS)
+        done += 1
+    return done, time.perf_counter() - t0
+
+
 def cpu_sample(frame, threads, min_seconds=8.0, max_evals=50):
     """Time the oracle port on the frame: E/F/virial compute per evaluation (edge build reported
     separately), repeated until min_seconds of CPU work."""
@@ -183,6 +251,23 @@ def run_reference(args):
         "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_profile_train(args):
+    """FP32 trainer steps only (for ncu launch lists of the training workload)."""
+    import torch
+
+    import superlinear_gb300 as sg
+    frames = training_set(sg)
+    model = sg.Model(TRAIN_MODEL)
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP32), frames, *TRAIN_WEIGHTS)
+    tr.set_graph(not args.no_graph)
+    p = model.params()
+    for _ in range(args.warmup + args.steps):
+        loss, _ = tr.loss_grad(p)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_train": True, "frames": len(frames), "loss": loss}), flush=True)
     return 0
 
 
@@ -330,6 +415,15 @@ def run_ours(args):
             del e4
         extra["fp32_over_fp64"] = extra["fp64"]["ms_per_step"] / extra["fp32"]["ms_per_step"]
 
+    # training loss + gradient over the 256-frame Effect L3/K4/R2/O2 batch
+    train = None
+    if not args.skip_train:
+        tframes, train = bench_training(sg, torch, max(3, args.steps // 2), args.warmup)
+        nd, tcpu = cpu_train_sample(tframes)
+        train["cpu_baseline"] = {"value": nd / tcpu, "unit": "frames/s", "cores": 1, "kind": "port",
+                                 "sample": f"loss + gradient of the first {nd} frames of the batch by the FP64 "
+                                           "CPU restatement (one thread)"}
+
     line = {
         "metric": METRIC, "value": n * world / (ms32 / 1e3), "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
@@ -360,6 +454,7 @@ def run_ours(args):
         "clocks": clocks,
         "gpu_launches": launches,
         "effect_l4k8r2o3_110592": extra or None,
+        "train_effect_l3k4r2o2_256": train,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -374,14 +469,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-effect", action="store_true", help="skip the 110,592-atom Effect measurement")
+    ap.add_argument("--skip-train", action="store_true", help="skip the 256-frame training loss+gradient measurement")
     ap.add_argument("--profile-only", action="store_true",
                     help="only the FP32 timed steps (for ncu captures); prints a short JSON line")
     ap.add_argument("--cells", type=int, default=8, help="diamond cells per edge (8 -> the 4,096-atom workload)")
+    ap.add_argument("--profile-train", action="store_true",
+                    help="only FP32 training loss+gradient steps over the 256-frame batch (for ncu launch lists)")
+    ap.add_argument("--no-graph", action="store_true", help="with --profile-train: eager launches instead of the graph")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_train:
+        return run_profile_train(args)
     return run_ours(args)
 
 

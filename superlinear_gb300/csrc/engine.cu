@@ -982,18 +982,57 @@ __global__ void k_slot_reduce(const double* slots, int nslots, int nparams, doub
   grad[p] += s;
 }
 
-// Gate projection weights: dJ/dW[mu][q] = sum_atoms lambda_h[mu] g[node q] + mu_h[mu] gdot[node q].
+// Gate projection weights: dJ/dW[mu][q] = sum_atoms lambda_h[mu] g[node q] + mu_h[mu] gdot[node q],
+// a (2F x N) . (N x Q) product reduced over atoms.  Block b takes the atom chunks b, b + grid, ...,
+// stages each chunk's lambda / mu rows and gate-node values in shared memory, and adds its partial
+// sums into its own slot row (reduced later in fixed order with the other parameter slots), so the
+// result is deterministic.  Outputs are taken kGwTile at a time (one per thread and repeat).
+constexpr int kGwChunk = 32;
+constexpr int kGwThreads = 256;
+constexpr int kGwPer = 4;  // outputs per thread per tile
 template <typename Real>
-__global__ void k_gate_weight_grad(int natoms, int F, int Q, int M, const int* nodes, const double* lh,
-                                   const Real* gmom, const Real* gmomd, double* grad) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= F * Q) return;
-  const int m = t / Q, q = t - m * Q, node = nodes[q];
-  double s = 0.0;
-  for (int a = 0; a < natoms; ++a)
-    s += lh[static_cast<size_t>(a) * 2 * F + m] * double(gmom[static_cast<size_t>(a) * M + node]) +
-         lh[static_cast<size_t>(a) * 2 * F + F + m] * double(gmomd[static_cast<size_t>(a) * M + node]);
-  grad[t] += s;
+__global__ void __launch_bounds__(kGwThreads) k_gate_weight_grad(int natoms, int F, int Q, int M, const int* nodes,
+                                                                 const double* lh, const Real* gmom,
+                                                                 const Real* gmomd, double* slots, int nparams,
+                                                                 int gw_off) {
+  extern __shared__ double gw_sh[];
+  double* sl = gw_sh;                          // [kGwChunk][2F]
+  double* sg = gw_sh + kGwChunk * 2 * F;       // [kGwChunk][2Q]
+  const int FQ = F * Q;
+  double* out = slots + static_cast<size_t>(blockIdx.x) * nparams + gw_off;
+  for (int tile = 0; tile < FQ; tile += kGwThreads * kGwPer) {
+    double acc[kGwPer];
+#pragma unroll
+    for (int k = 0; k < kGwPer; ++k) acc[k] = 0.0;
+    for (int base = blockIdx.x * kGwChunk; base < natoms; base += gridDim.x * kGwChunk) {
+      const int n = min(kGwChunk, natoms - base);
+      __syncthreads();
+      for (int t = threadIdx.x; t < n * 2 * F; t += blockDim.x) sl[t] = lh[static_cast<size_t>(base) * 2 * F + t];
+      for (int t = threadIdx.x; t < n * Q; t += blockDim.x) {
+        const int a = t / Q, q = t - a * Q;
+        const size_t o = static_cast<size_t>(base + a) * M + nodes[q];
+        sg[a * 2 * Q + q] = double(gmom[o]);
+        sg[a * 2 * Q + Q + q] = double(gmomd[o]);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kGwPer; ++k) {
+        const int t = tile + k * kGwThreads + threadIdx.x;
+        if (t < FQ) {
+          const int m = t / Q, q = t - m * Q;
+          double v = 0.0;
+          for (int a = 0; a < n; ++a)
+            v += sl[a * 2 * F + m] * sg[a * 2 * Q + q] + sl[a * 2 * F + F + m] * sg[a * 2 * Q + Q + q];
+          acc[k] += v;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kGwPer; ++k) {
+      const int t = tile + k * kGwThreads + threadIdx.x;
+      if (t < FQ) out[t] += acc[k];
+    }
+  }
 }
 }  // namespace
 
@@ -1048,9 +1087,15 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
     launches_ += launch_grad_pass<Real>(m.L, kGradGateReverse, a, cr, s);
     const int gw_off = dm.grad.gate_w_off;
     if (N && gw_off >= 0) {
-      k_gate_weight_grad<Real><<<(m.F * m.Q + 255) / 256, 256, 0, s>>>(ncentres_, m.F, m.Q, m.M, dm.gate_nodes,
-                                                                       lh_atom_.as<double>(), gmom_.as<Real>(),
-                                                                       gmomd_.as<Real>(), grad + gw_off);
+      const int blocks = std::max(1, std::min(nslots, (ncentres_ + kGwChunk - 1) / kGwChunk));
+      const size_t smem = sizeof(double) * kGwChunk * 2 * (m.F + m.Q);
+      if (smem > 200 * 1024) throw Error(3, "gate weight gradient: radial functions + gate scalars above 400");
+      if (smem > 48 * 1024)
+        SUS2G_CUDA(cudaFuncSetAttribute(k_gate_weight_grad<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        static_cast<int>(smem)));
+      k_gate_weight_grad<Real><<<blocks, kGwThreads, smem, s>>>(ncentres_, m.F, m.Q, m.M, dm.gate_nodes,
+                                                                lh_atom_.as<double>(), gmom_.as<Real>(),
+                                                                gmomd_.as<Real>(), slots_.as<double>(), P, gw_off);
       ++launches_;
     }
   } else {

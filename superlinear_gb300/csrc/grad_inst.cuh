@@ -42,18 +42,32 @@ template <>
 GradLaunch grad_pass_config<PASS_REAL>(int L, int mode, const DevModel<PASS_REAL>& dm, int natoms, int sm_count) {
   if (dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
   GradKernel kern = grad_kernel(L, mode);
-  const int H = (L + 1) * (L + 1);
+  const int H = (L + 1) * (L + 1), Lp = L + 1;
+  int device = 0, optin = 0;
+  cudaGetDevice(&device);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  const size_t table = pass_table_size<PASS_REAL>(dm.C, dm.F, dm.B, dm.nblk);
+  const size_t per_warp = grad_warp_size<PASS_REAL>(dm.F, H, dm.M, dm.K);
+  // the gate forward pass has no per-edge parameter loop
+  const int cols = mode == kGradGateForward
+                       ? 0
+                       : grad_acc_cols(Lp, dm.B, dm.C, dm.scaling_mode, mode == kGradOuter && dm.gated);
   GradLaunch cfg;
   cfg.warps = kGradWarps;
-  cfg.block = kGradWarps * kWarp;
-  cfg.smem = sizeof(PASS_REAL) * (pass_table_size<PASS_REAL>(dm.C, dm.F, dm.B, dm.nblk) +
-                                   kGradWarps * grad_warp_size<PASS_REAL>(dm.F, H, dm.M, dm.K));
+  cfg.acc_cols = cols;
+  auto bytes = [&](int warps, int c) {
+    return sizeof(PASS_REAL) * (table + warps * (per_warp + static_cast<size_t>(c) * kAccStride));
+  };
+  if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) cfg.warps = 1;
+  if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) { cfg.warps = kGradWarps; cfg.acc_cols = 0; }
+  cfg.block = cfg.warps * kWarp;
+  cfg.smem = bytes(cfg.warps, cfg.acc_cols);
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cfg.smem));
   if (err != cudaSuccess) throw std::runtime_error(std::string("gradient shared memory: ") + cudaGetErrorString(err));
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, cfg.block, cfg.smem);
   if (per_sm < 1) throw std::runtime_error("gradient kernel does not fit on an SM (shared memory " + std::to_string(cfg.smem) + " B)");
-  const int need = std::max(1, (natoms + kGradWarps - 1) / kGradWarps);
+  const int need = std::max(1, (natoms + cfg.warps - 1) / cfg.warps);
   cfg.grid = std::max(1, std::min(need, per_sm * sm_count));
   return cfg;
 }
@@ -62,7 +76,9 @@ template <>
 int launch_grad_pass<PASS_REAL>(int L, int mode, const GradArgs<PASS_REAL>& a, const GradLaunch& cfg, cudaStream_t s) {
   if (a.natoms == 0) return 0;
   GradKernel kern = grad_kernel(L, mode);
-  kern<<<cfg.grid, cfg.block, cfg.smem, s>>>(a);
+  GradArgs<PASS_REAL> args = a;
+  args.acc_cols = cfg.acc_cols;
+  kern<<<cfg.grid, cfg.block, cfg.smem, s>>>(args);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) throw std::runtime_error(std::string("gradient launch: ") + cudaGetErrorString(err));
   return 1;

@@ -20,9 +20,13 @@
 // The Effect gate chain runs the same steps for the gate pass, seeded with
 // dJ/dh_j and dJ/dhdot_j gathered per atom (stored at the reverse edge, like the force path).
 //
-// Reductions are deterministic: per-edge contributions are summed over the 32 lanes with fixed
-// shuffle trees and added by one lane to a private FP64 gradient slice of the warp; slices are
-// summed in a fixed order by k_slot_reduce.
+// Reductions are deterministic.  Per-edge contributions to the per-(k, l) parameters (Chebyshev
+// coefficients, species factors, warp slope / shift, gate additive factors) go to lane-private
+// shared-memory columns (stride 33: conflict-free for a fixed column across lanes and for a fixed
+// lane across columns); after each 32-edge batch and radial index k the warp sums every column over
+// its 32 lanes in a fixed order (one column per lane) and adds the result to its private FP64
+// gradient slice.  Slices are summed in a fixed order by k_slot_reduce.  When the columns do not
+// fit in shared memory (many species), the contributions are summed with shuffle trees instead.
 #pragma once
 #include "efs_kernels.cuh"
 
@@ -51,11 +55,24 @@ struct GradArgs {
   double* lh_atom;         // [N][2F] gathered per atom (gate reverse)
   double* slots;           // [warps in grid][nparams]
   int* error;
+  int acc_cols;            // lane-private accumulator columns per k (0: shuffle-tree reductions)
 };
+
+constexpr int kAccStride = kWarp + 1;
 
 template <typename Real>
 __host__ __device__ inline int grad_warp_size(int F, int H, int M, int K) {
   return kWarp * (2 * F + 2 * H + 1) + 4 * M + 2 * K * H + 2 * F + 4;
+}
+
+// Accumulator columns per radial index k: Chebyshev coefficients [l][b], species factors [t][l]
+// (centre and neighbour factors index the same table), warp slope / shift [sb][t][2] (one warp
+// block per k, or one per l for the L and LK maps), gate additive factors [t][l] (Effect outer).
+__host__ __device__ inline int grad_acc_nsb(int scaling_mode, int Lp) {
+  return (scaling_mode == 1 || scaling_mode == 3) ? Lp : 1;
+}
+__host__ __device__ inline int grad_acc_cols(int Lp, int B, int C, int scaling_mode, bool effect_outer) {
+  return Lp * B + C * Lp + 2 * grad_acc_nsb(scaling_mode, Lp) * C + (effect_outer ? C * Lp : 0);
 }
 
 template <typename Real>
@@ -163,7 +180,8 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
   Real* s_w0 = s_scal + 2 * dm.nblk * C2;
   Real* s_w1 = s_w0 + C * F;
   Real* s_wa = s_w1 + C * F;
-  Real* wbase = s_wa + C * F + grad_warp_size<Real>(F, H, M, K) * warp;
+  const int ncol = a.acc_cols;
+  Real* wbase = s_wa + C * F + (grad_warp_size<Real>(F, H, M, K) + ncol * kAccStride) * warp;
   const int sw = 2 * F + 2 * H + 1;
   Real* stage = wbase;
   Real* v = stage + kWarp * sw;
@@ -173,6 +191,9 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
   Real* abl = mu + M;
   Real* abm = abl + K * H;
   Real* hb = abm + K * H;  // [2F]
+  Real* accs = wbase + grad_warp_size<Real>(F, H, M, K);  // [ncol][kAccStride]
+  const int nsb = grad_acc_nsb(dm.scaling_mode, Lp);
+  const int c_wc = Lp * B, c_scal = c_wc + C * Lp, c_add = c_scal + 2 * nsb * C;
 
   for (int q = threadIdx.x; q < F * B; q += blockDim.x) s_coeff[q] = pt.coeff[q];
   for (int q = threadIdx.x; q < 2 * dm.nblk * C2; q += blockDim.x) s_scal[q] = pt.scal[q];
@@ -181,6 +202,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
     s_w1[q] = pt.wsource[q];
     s_wa[q] = pt.wadd ? pt.wadd[q] : Real(0);
   }
+  for (int q = lane; q < ncol * kAccStride; q += kWarp) accs[q] = Real(0);
   __syncthreads();
   double* slot = a.slots + static_cast<size_t>(blockIdx.x * warps + warp) * NP;
 
@@ -421,30 +443,70 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           Real dRd = on ? x0 * x3 * rdot * Tt : Real(0);
           const Real dx0 = on ? x3 * Qv + x3d * R * Tt : Real(0);
           const Real dxj = on ? x0 * Qv : Real(0);
-          // Chebyshev coefficients of R_mu
-          for (int b = 0; b < B; ++b)
-            slot_add<Real>(slot, gl.coeff_off + m_ * gl.coeff_stride + b,
-                           dR * f * Tv[b] + dRd * (fd * Tv[b] + f * D[b] * wv.xr), lane);
           // warp (slope, shift) of block sb and pair (t_i, t_j)
           const Real ds = wv.xs * (dR * f + dRd * fd) * cD + dRd * f * (wv.xs * wv.xr * cDD + wv.xrs * cD);
           const Real dg = wv.xg * (dR * f + dRd * fd) * cD + dRd * f * (wv.xg * wv.xr * cDD + wv.xrg * cD);
-          for (int t = 0; t < C; ++t) {
-            slot_add<Real>(slot, gl.scal_off + 2 * sb * C2 + ti * C + t, tj == t ? ds : Real(0), lane);
-            slot_add<Real>(slot, gl.scal_off + (2 * sb + 1) * C2 + ti * C + t, tj == t ? dg : Real(0), lane);
-          }
-          // species factors of the centre and the neighbour
-          slot_add<Real>(slot, gl.wc_off + ti * gl.wc_t_stride + m_ * gl.wc_mu_stride, dx0, lane);
-          for (int t = 0; t < C; ++t)
-            slot_add<Real>(slot, gl.wc_off + t * gl.wc_t_stride + m_ * gl.wc_mu_stride, tj == t ? dxj : Real(0), lane);
-          if (effect_outer) {
-            const Real dal = on ? x0 * (Qv * hv + R * Tt * hdv) : Real(0);
-            for (int t = 0; t < C; ++t) slot_add<Real>(slot, gl.add_off + t * F + m_, tj == t ? dal : Real(0), lane);
-            if (valid) {
-              Real* dst = a.lhm + static_cast<size_t>(a.rev[e]) * 2 * F;
-              dst[m_] = on ? x0 * al * Qv : Real(0);
-              dst[F + m_] = on ? x0 * al * R * Tt : Real(0);
+          const Real dal = (effect_outer && on) ? x0 * (Qv * hv + R * Tt * hdv) : Real(0);
+          if (ncol) {
+            Real* ac = accs + lane;
+#pragma unroll
+            for (int b = 0; b < kMaxB; ++b)
+              if (b < B) ac[(l * B + b) * kAccStride] += dR * f * Tv[b] + dRd * (fd * Tv[b] + f * D[b] * wv.xr);
+            ac[(c_wc + ti * Lp + l) * kAccStride] += dx0;
+            ac[(c_wc + tj * Lp + l) * kAccStride] += dxj;
+            const int sc = c_scal + 2 * ((nsb > 1 ? l : 0) * C + tj);
+            ac[sc * kAccStride] += ds;
+            ac[(sc + 1) * kAccStride] += dg;
+            if (effect_outer) ac[(c_add + tj * Lp + l) * kAccStride] += dal;
+          } else {
+            // Chebyshev coefficients of R_mu
+            for (int b = 0; b < B; ++b)
+              slot_add<Real>(slot, gl.coeff_off + m_ * gl.coeff_stride + b,
+                             dR * f * Tv[b] + dRd * (fd * Tv[b] + f * D[b] * wv.xr), lane);
+            for (int t = 0; t < C; ++t) {
+              slot_add<Real>(slot, gl.scal_off + 2 * sb * C2 + ti * C + t, tj == t ? ds : Real(0), lane);
+              slot_add<Real>(slot, gl.scal_off + (2 * sb + 1) * C2 + ti * C + t, tj == t ? dg : Real(0), lane);
             }
+            // species factors of the centre and the neighbour
+            slot_add<Real>(slot, gl.wc_off + ti * gl.wc_t_stride + m_ * gl.wc_mu_stride, dx0, lane);
+            for (int t = 0; t < C; ++t)
+              slot_add<Real>(slot, gl.wc_off + t * gl.wc_t_stride + m_ * gl.wc_mu_stride, tj == t ? dxj : Real(0), lane);
+            if (effect_outer)
+              for (int t = 0; t < C; ++t) slot_add<Real>(slot, gl.add_off + t * F + m_, tj == t ? dal : Real(0), lane);
           }
+          if (effect_outer && valid) {
+            Real* dst = a.lhm + static_cast<size_t>(a.rev[e]) * 2 * F;
+            dst[m_] = on ? x0 * al * Qv : Real(0);
+            dst[F + m_] = on ? x0 * al * R * Tt : Real(0);
+          }
+        }
+        if (ncol) {
+          // flush the columns of radial index k: column c summed over the 32 lanes in lane order
+          __syncwarp();
+          for (int c = lane; c < ncol; c += kWarp) {
+            Real* col = accs + c * kAccStride;
+            Real sum = Real(0);
+#pragma unroll 8
+            for (int q = 0; q < kWarp; ++q) { sum += col[q]; col[q] = Real(0); }
+            int p;
+            if (c < c_wc) {
+              const int l = c / B, b = c - l * B;
+              p = gl.coeff_off + (k * Lp + l) * gl.coeff_stride + b;
+            } else if (c < c_scal) {
+              const int t = (c - c_wc) / Lp, l = c - c_wc - t * Lp;
+              p = gl.wc_off + t * gl.wc_t_stride + (k * Lp + l) * gl.wc_mu_stride;
+            } else if (c < c_add) {
+              const int idx = c - c_scal, pair = idx >> 1, which = idx & 1;
+              const int sbi = pair / C, t = pair - sbi * C;
+              const int sb = scaling_block(dm.scaling_mode, k, sbi, Lp);
+              p = gl.scal_off + (2 * sb + which) * C2 + ti * C + t;
+            } else {
+              const int t = (c - c_add) / Lp, l = c - c_add - t * Lp;
+              p = gl.add_off + t * F + k * Lp + l;
+            }
+            slot[p] += double(sum);
+          }
+          __syncwarp();
         }
       }
     }

@@ -9,6 +9,7 @@ namespace sus2g {
 
 struct GradLaunch {
   int grid = 0, block = 0, warps = 0;
+  int acc_cols = 0;  // lane-private accumulator columns (0: shuffle-tree reductions)
   size_t smem = 0;
 };
 
