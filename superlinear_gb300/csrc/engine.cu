@@ -106,7 +106,7 @@ __global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const 
 }
 
 template <typename Real>
-__device__ __forceinline__ void write_edge(int e, int j, int a, int b, int c, double x, double y, double z, double r2,
+__device__ __forceinline__ void write_edge(long long e, int j, int a, int b, int c, double x, double y, double z, double r2,
                                            int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key) {
   nbr[e] = j;
   typename Vec4<Real>::type v;
@@ -133,60 +133,71 @@ __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const d
                   });
 }
 
-// Cell-list frames: one warp per centre over the flattened 27-bin candidate list.
-__global__ void k_edge_count_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
-                                  double rc2, const int* bin_start, const int* bin_atoms, const int* bin_of,
-                                  const AtomFrac* frac, const AtomOff* off, int* counts, int* error) {
-  const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
-  if (i >= natoms) return;
-  const FramePlan& fp = plans[frame_of[i]];
-  if (!fp.use_bins) return;
-  int n = 0;
-  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
-                 [&](unsigned mask, bool, int, int, int, int, double, double, double, double) { n += __popc(mask); });
-  if ((threadIdx.x & 31) == 0) counts[i] = n;
-}
-
+// Cell-list frames: one warp per centre over the flattened 27-bin candidate list, one pass.  The
+// centre's edges go to its padded slots pad0 + (i - a0) cap .. + cap of the staging buffers; the
+// count is recorded in full, and a count above cap raises *overflow (the host then grows the
+// capacity and repeats the pass).
+constexpr int kFillWarps = 8;
 template <typename Real>
-__global__ void k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
-                                 double rc2, const int* bin_start, const int* bin_atoms, const int* bin_of,
-                                 const AtomFrac* frac, const AtomOff* off, const int* row, int* nbr,
-                                 typename Vec4<Real>::type* d4, unsigned long long* key, int* error) {
+__global__ void __launch_bounds__(kFillWarps * kWarp)
+k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
+                 const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                 const AtomOff* off, int* counts, int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key,
+                 int* overflow, int* error) {
+  __shared__ int2 queue[kFillWarps][kEdgeQueue];
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
   if (!fp.use_bins) return;
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
-  int cursor = row[i];
-  const int end = row[i + 1];
-  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
+  const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
+  const int cap = fp.cap;
+  int cursor = 0;
+  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
                  [&](unsigned mask, bool ok, int j, int a, int b, int c, double x, double y, double z, double r2) {
                    if (ok) {
-                     const int e = cursor + __popc(mask & below);
-                     if (e < end) write_edge<Real>(e, j, a, b, c, x, y, z, r2, nbr, d4, key);
-                     else record_error(error, kErrEdgeCapacity);
+                     const int k = cursor + __popc(mask & below);
+                     if (k < cap) write_edge<Real>(pad + k, j, a, b, c, x, y, z, r2, nbr, d4, key);
                    }
                    cursor += __popc(mask);
                  });
+  if (lane == 0) {
+    counts[i] = cursor;
+    if (cursor > cap) atomicMax(overflow, cursor);
+  }
 }
 
-// Sort one centre's edges by key (warp per centre, rank sort; keys within a centre are unique).
+// Sort one centre's edges by key into CSR order (warp per centre, rank sort; keys within a centre
+// are unique).  Cell-list centres read their padded staging slots, the others their CSR range of
+// the staging buffers (plans may be null when no frame uses cell lists).
 template <typename Real>
-__global__ void k_edge_sort(const int* row, int natoms, const unsigned long long* key_in, const int* nbr_in,
-                            const typename Vec4<Real>::type* d4_in, unsigned long long* key_out, int* nbr_out,
-                            typename Vec4<Real>::type* d4_out) {
+__global__ void k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame_of,
+                            const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
+                            const unsigned long long* pkey, const int* pnbr, const typename Vec4<Real>::type* pd4,
+                            unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
-  const int e0 = row[warp], e1 = row[warp + 1];
-  for (int e = e0 + lane; e < e1; e += kWarp) {
-    const unsigned long long k = key_in[e];
+  const int e0 = row[warp], n = row[warp + 1] - e0;
+  long long in0 = e0;
+  const unsigned long long* K = key_in;
+  const int* NB = nbr_in;
+  const typename Vec4<Real>::type* D = d4_in;
+  if (plans) {
+    const FramePlan& fp = plans[frame_of[warp]];
+    if (fp.use_bins) {
+      in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
+      K = pkey; NB = pnbr; D = pd4;
+    }
+  }
+  for (int q = lane; q < n; q += kWarp) {
+    const unsigned long long k = K[in0 + q];
     int rank = 0;
-    for (int q = e0; q < e1; ++q) rank += key_in[q] < k;
+    for (int t = 0; t < n; ++t) rank += K[in0 + t] < k;
     key_out[e0 + rank] = k;
-    nbr_out[e0 + rank] = nbr_in[e];
-    d4_out[e0 + rank] = d4_in[e];
+    nbr_out[e0 + rank] = NB[in0 + q];
+    d4_out[e0 + rank] = D[in0 + q];
   }
 }
 
@@ -502,7 +513,7 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   if (model_.gated && !unique(model_.gate_nodes)) throw Error(3, "SUS2 model: duplicate gate scalar moments");
   if (model_.K > kMaxK) throw Error(3, "SUS2 model: sh_k_max above 8 is not supported by the GPU engine");
   plans_ = new std::vector<FramePlan>();
-  SUS2G_CUDA(cudaMallocHost(&host_total_, sizeof(int)));
+  SUS2G_CUDA(cudaMallocHost(&host_total_, 4 * sizeof(int)));
   error_.ensure(sizeof(int));
   SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
   upload_model();
@@ -703,6 +714,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   std::vector<FramePlan>& plans = *plans_;
   plans.assign(nframes, FramePlan{});
   int a = 0, bins = 0;
+  long long pad_total = 0;
   bins_frames_ = 0;
   for (int f = 0; f < nframes; ++f) {
     FramePlan& fp = plans[f];
@@ -732,6 +744,14 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       fp.band = 2.0 * rc * (4.0 * 6.0e-8 * rows) * 4.0 + 1e-6;
       for (int q = 0; q < 9; ++q) fp.cellf[q] = static_cast<float>(fp.cell[q]);
       bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
+      // padded staging capacity: cap_scale x the mean neighbour count of the frame's density + 64
+      const double c = fp.cell[0] * (fp.cell[4] * fp.cell[8] - fp.cell[5] * fp.cell[7]) -
+                       fp.cell[1] * (fp.cell[3] * fp.cell[8] - fp.cell[5] * fp.cell[6]) +
+                       fp.cell[2] * (fp.cell[3] * fp.cell[7] - fp.cell[4] * fp.cell[6]);
+      const double mean = frame_natoms[f] / std::abs(c) * (4.0 / 3.0) * 3.141592653589793 * rc * rc2;
+      fp.cap = static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0));
+      fp.pad0 = pad_total;
+      pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
     }
   }
   natoms_ = ncentres_ = a;
@@ -766,54 +786,82 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   }
   const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
   const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);
+  const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
+  const FramePlan* P = plan_.as<FramePlan>();
+  const int* FO = frame_of_.as<int>();
+  const int *BS = bin_start_.as<int>(), *BA = bin_atoms_.as<int>(), *BO = bin_of.as<int>();
+  const AtomFrac* FR = frac_.as<AtomFrac>();
+  const AtomOff* OF = off_.as<AtomOff>();
+  overflow_.ensure(sizeof(int));
+  // cell-list frames: one pass into padded staging slots (repeated with a larger capacity on overflow)
+  auto fill_bins = [&]() {
+    const size_t slots = static_cast<size_t>(std::max<long long>(1, pad_total));
+    pad_nbr_.ensure(sizeof(int) * slots);
+    pad_d4_.ensure(rsz * slots);
+    pad_key_.ensure(sizeof(unsigned long long) * slots);
+    SUS2G_CUDA(cudaMemsetAsync(overflow_.ptr, 0, sizeof(int), s));
+    if (precision_ == kFP32)
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
+                                                                         pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+                                                                         pad_key_.as<unsigned long long>(), overflow_.as<int>(), error_.as<int>());
+    else
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
+                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+                                                                          pad_key_.as<unsigned long long>(), overflow_.as<int>(), error_.as<int>());
+    ++launches_;
+  };
   if (a) {
     SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
-    if (bins) {
-      k_edge_count_bins<<<warp_blocks, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
-                                                    bin_start_.as<int>(), bin_atoms_.as<int>(), bin_of.as<int>(),
-                                                    frac_.as<AtomFrac>(), off_.as<AtomOff>(), counts_.as<int>(), error_.as<int>());
-      ++launches_;
-    }
+    if (bins) fill_bins();
     if (bins_frames_ < nframes) {
-      k_edge_count<<<thread_blocks, 128, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, rc2,
-                                                 bin_start_.as<int>(), bin_atoms_.as<int>(), bin_of.as<int>(), frac_.as<AtomFrac>(),
-                                                 off_.as<AtomOff>(), counts_.as<int>(), error_.as<int>());
+      k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(), error_.as<int>());
       ++launches_;
     }
   }
-  k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
-  ++launches_;
-  // the only host synchronisation of the build: the edge total sizes the edge arrays
-  SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
-  SUS2G_CUDA(cudaStreamSynchronize(s));
-  const long long total = *host_total_;
+  long long total = 0;
+  for (int attempt = 0;; ++attempt) {
+    k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
+    ++launches_;
+    // the one host synchronisation of the build: the edge total sizes the edge arrays, and the
+    // overflow flag says whether a centre had more edges than its padded capacity
+    SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 1, overflow_.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SUS2G_CUDA(cudaStreamSynchronize(s));
+    total = host_total_[0];
+    const int over = bins ? host_total_[1] : 0;
+    if (over <= 0) break;
+    if (attempt >= 8) throw Error(4, "edge build: padded capacity did not converge");
+    // grow every cell-list frame's capacity to at least the largest count seen, and re-run
+    cap_scale_ *= 2.0;
+    pad_total = 0;
+    for (int f = 0; f < nframes; ++f) {
+      FramePlan& fp = plans[f];
+      if (!fp.use_bins) continue;
+      fp.cap = std::max(2 * fp.cap, over);
+      fp.pad0 = pad_total;
+      pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
+    }
+    SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
+    fill_bins();
+    SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
+  }
   nedges_ = total;
   const size_t E = std::max<long long>(1, total);
-  const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
   nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);
   rev_.ensure(sizeof(int) * E);
   d4_.ensure(rsz * E); tmp_d4_.ensure(rsz * E);
   key_.ensure(sizeof(unsigned long long) * E); tmp_key_.ensure(sizeof(unsigned long long) * E);
-  if (a) {
-    const FramePlan* P = plan_.as<FramePlan>();
-    const int* F = frame_of_.as<int>();
-    const int *BS = bin_start_.as<int>(), *BA = bin_atoms_.as<int>(), *BO = bin_of.as<int>();
-    const AtomFrac* FR = frac_.as<AtomFrac>();
-    const AtomOff* OF = off_.as<AtomOff>();
+  if (a && bins_frames_ < nframes) {
     unsigned long long* KY = tmp_key_.as<unsigned long long>();
-    if (precision_ == kFP32) {
-      if (bins) k_edge_fill_bins<float><<<warp_blocks, 256, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
-                                                                    tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
-      if (bins_frames_ < nframes) k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
-                                                                                 tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
-    } else {
-      if (bins) k_edge_fill_bins<double><<<warp_blocks, 256, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
-                                                                     tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
-      if (bins_frames_ < nframes) k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, F, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
-                                                                                  tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
-    }
-    launches_ += (bins ? 1 : 0) + (bins_frames_ < nframes ? 1 : 0);
+    if (precision_ == kFP32)
+      k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                       tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
+    else
+      k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+                                                        tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
+    ++launches_;
   }
+  sort_from_pad_ = bins > 0;
   finalize_edges();
   mark_end();
 }
@@ -823,12 +871,17 @@ void Engine::finalize_edges() {
   const int a = ncentres_;
   if (a) {
     const int blocks = (a * kWarp + 255) / 256;
+    const FramePlan* P = sort_from_pad_ ? plan_.as<FramePlan>() : nullptr;
     if (precision_ == kFP32)
-      k_edge_sort<float><<<blocks, 256, 0, s>>>(row_.as<int>(), a, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
-                                                  tmp_d4_.as<EdgeF>(), key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeF>());
+      k_edge_sort<float><<<blocks, 256, 0, s>>>(row_.as<int>(), a, P, frame_of_.as<int>(), tmp_key_.as<unsigned long long>(),
+                                                tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(),
+                                                pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), key_.as<unsigned long long>(),
+                                                nbr_.as<int>(), d4_.as<EdgeF>());
     else
-      k_edge_sort<double><<<blocks, 256, 0, s>>>(row_.as<int>(), a, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
-                                                   tmp_d4_.as<EdgeD>(), key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
+      k_edge_sort<double><<<blocks, 256, 0, s>>>(row_.as<int>(), a, P, frame_of_.as<int>(), tmp_key_.as<unsigned long long>(),
+                                                 tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(),
+                                                 pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), key_.as<unsigned long long>(),
+                                                 nbr_.as<int>(), d4_.as<EdgeD>());
     ++launches_;
   }
   if (nedges_ && user_edges_) {
@@ -846,6 +899,7 @@ void Engine::finalize_edges() {
 void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j, const double* d_d) {
   SUS2G_CUDA(cudaSetDevice(device_));
   ++edge_generation_;
+  sort_from_pad_ = false;
   if (nowned < 0 || nall < nowned || nedges < 0) throw Error(1, "invalid atom layout");
   cudaStream_t s = stream_;
   ncentres_ = nowned;

@@ -129,7 +129,10 @@ class Engine {
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf ei_, hbar_atom_, bin_of_, frac_, off_;
-  int* host_total_ = nullptr;   // pinned
+  DevBuf pad_nbr_, pad_d4_, pad_key_, overflow_;  // padded single-pass staging of cell-list frames
+  double cap_scale_ = 2.0;      // padded capacity = cap_scale x mean neighbour count + 64 (grows on overflow)
+  bool sort_from_pad_ = false;
+  int* host_total_ = nullptr;   // pinned [4]
   // stage timer (cudaEvent pairs per stage, enabled by set_timing)
   bool timing_ = false;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> marks_;

@@ -25,6 +25,8 @@ struct FramePlan {
   int use_bins;
   int nb[3];
   int bin0;         // first bin index of this frame in the global bin arrays
+  int cap;          // cell-list frames: edge slots per centre in the padded staging buffers
+  long long pad0;   // cell-list frames: first padded slot of the frame (centre i: pad0 + (i - a0) cap)
   float cellf[9];   // FP32 copy of the cell for the candidate prefilter
   double band;      // |r^2 error| bound of the FP32 prefilter; candidates within it get the FP64 test
 };
@@ -123,14 +125,24 @@ __device__ __forceinline__ void enumerate_edges(int i, int part, const FramePlan
 }
 
 // Cell-list frames, one warp per centre i: the 27 neighbouring bins' atom ranges are laid end to
-// end (prefix sums over lanes), lanes take consecutive candidates of that flat list, and each
-// round's accepted edges are reported through Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r2)
-// so the caller can count or write them with one ballot per round.
+// end (prefix sums over lanes) and lanes take consecutive candidates of that flat list.  Candidates
+// that pass the FP32 prefilter are appended to a per-warp queue in shared memory (`queue`, 64
+// entries); whenever 32 are queued the warp runs the exact FP64 test on a full warp of them, so
+// the FP64 work (1/64 of the FP32 rate on this GPU) is spent on prefilter survivors only rather
+// than on mostly idle lanes.  Accepted edges of each FP64 round are reported through
+// Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r2), so the caller can count or write them
+// with one ballot per round.
+constexpr int kEdgeQueue = 64;
+__device__ __forceinline__ int pack_image(int n0, int n1, int n2) {
+  return ((n0 + 64) << 14) | ((n1 + 64) << 7) | (n2 + 64);
+}
 template <typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
                                                const int* bin_start, const int* bin_atoms, const int* bin_of,
-                                               const AtomFrac* frac, const AtomOff* off, int* error, Round&& round) {
+                                               const AtomFrac* frac, const AtomOff* off, int* error, int2* queue,
+                                               Round&& round) {
   const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   const int local = bin_of[i] - fp.bin0;
   const int bi0 = local / (fp.nb[1] * fp.nb[2]), bi1 = (local / fp.nb[2]) % fp.nb[1], bi2 = local % fp.nb[2];
   int start = 0, len = 0, w0 = 0, w1 = 0, w2 = 0;
@@ -158,6 +170,25 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
   const double* c = fp.cell;
   const float* cf = fp.cellf;
   const float screen = static_cast<float>(rc2 + fp.band);
+  int queued = 0;  // warp-uniform
+  // exact FP64 test of queue entries [0, n) (one per lane) and the round callback
+  auto drain = [&](int n) {
+    bool ok = false;
+    int j = 0, n0 = 0, n1 = 0, n2 = 0;
+    double vx = 0, vy = 0, vz = 0, r2 = 0;
+    if (lane < n) {
+      const int2 q = queue[lane];
+      j = q.x;
+      n0 = ((q.y >> 14) & 127) - 64; n1 = ((q.y >> 7) & 127) - 64; n2 = (q.y & 127) - 64;
+      vx = pos[3 * j] - xi + n0 * c[0] + n1 * c[3] + n2 * c[6];
+      vy = pos[3 * j + 1] - yi + n0 * c[1] + n1 * c[4] + n2 * c[7];
+      vz = pos[3 * j + 2] - zi + n0 * c[2] + n1 * c[5] + n2 * c[8];
+      r2 = vx * vx + vy * vy + vz * vz;
+      ok = r2 < rc2;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, ok);
+    round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
+  };
   for (int base = 0; base < total; base += 32) {
     const int cand = base + lane;
     // bin slot k of this candidate: the last lane whose exclusive offset is <= cand
@@ -170,9 +201,8 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     }
     const int kstart = __shfl_sync(0xffffffffu, start, k), kex = __shfl_sync(0xffffffffu, excl, k);
     const int W0 = __shfl_sync(0xffffffffu, w0, k), W1 = __shfl_sync(0xffffffffu, w1, k), W2 = __shfl_sync(0xffffffffu, w2, k);
-    bool ok = false;
-    int j = 0, n0 = 0, n1 = 0, n2 = 0;
-    double vx = 0, vy = 0, vz = 0, r2 = 0;
+    bool pre = false;
+    int j = 0, packed = 0;
     if (cand < total) {
       j = bin_atoms[kstart + cand - kex];
       const AtomFrac fj = frac[j];
@@ -183,23 +213,35 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
       const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
       if (fx * fx + fy * fy + fz * fz < screen) {
         const AtomOff oj = off[j];
-        n0 = W0 + oi.x - oj.x; n1 = W1 + oi.y - oj.y; n2 = W2 + oi.z - oj.z;
+        const int n0 = W0 + oi.x - oj.x, n1 = W1 + oi.y - oj.y, n2 = W2 + oi.z - oj.z;
         if (!(i == j && n0 == 0 && n1 == 0 && n2 == 0)) {
-          vx = pos[3 * j] - xi + n0 * c[0] + n1 * c[3] + n2 * c[6];
-          vy = pos[3 * j + 1] - yi + n0 * c[1] + n1 * c[4] + n2 * c[7];
-          vz = pos[3 * j + 2] - zi + n0 * c[2] + n1 * c[5] + n2 * c[8];
-          r2 = vx * vx + vy * vy + vz * vz;
-          ok = r2 < rc2;
-          if (ok && (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63)) {
+          if (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63) {
             record_error(error, kErrImageRange);
-            ok = false;
+          } else {
+            pre = true;
+            packed = pack_image(n0, n1, n2);
           }
         }
       }
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, ok);
-    round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
+    const unsigned m = __ballot_sync(0xffffffffu, pre);
+    if (pre) queue[queued + __popc(m & below)] = make_int2(j, packed);
+    queued += __popc(m);
+    __syncwarp();
+    if (queued >= 32) {
+      drain(32);
+      __syncwarp();
+      // move the remainder (< 32 entries) to the front
+      int2 rest = make_int2(0, 0);
+      if (lane < queued - 32) rest = queue[32 + lane];
+      __syncwarp();
+      if (lane < queued - 32) queue[lane] = rest;
+      queued -= 32;
+      __syncwarp();
+    }
   }
+  if (queued > 0) drain(queued);
+  __syncwarp();
 }
 
 }  // namespace sus2g
