@@ -71,8 +71,44 @@ def algorithmic_bytes(d, edges, atoms, real_bytes=4):
 
 
 # ------------------------------------------------------------------------------------------------
+class NvmlClocks:
+    """Read-only NVML queries through ctypes (SM clock, max SM clock, power, clock-event reasons)."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes
+        self.c = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        found = False
+        try:  # the CUDA device's UUID, robust to a remapped device order
+            import torch
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(index).uuid)
+            found = self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(self.h)) == 0
+        except Exception:
+            found = False
+        if not found and self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML device")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sample(self):
+        c = self.c
+        sm, mx, pw, rs = c.c_uint(), c.c_uint(), c.c_uint(), c.c_ulonglong()
+        self.lib.nvmlDeviceGetClockInfo(self.h, 1, c.byref(sm))       # NVML_CLOCK_SM
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, c.byref(mx))
+        self.lib.nvmlDeviceGetPowerUsage(self.h, c.byref(pw))
+        self.reasons_fn(self.h, c.byref(rs))
+        return sm.value, mx.value, pw.value / 1000.0, rs.value
+
+
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """SM clocks / clock-event reasons sampled during the timed region: NVML every ~2 ms (plus one
+    sample at start and stop), or nvidia-smi every 200 ms when NVML cannot be loaded."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -80,10 +116,31 @@ class ClockSampler:
 
     def __init__(self, device: int):
         self.device = device
-        self.rows = []
+        self.rows = []      # (sm_mhz, max_mhz, reasons set)
         self.proc = None
+        self.nvml = None
+        self.stop_flag = threading.Event()
+        try:
+            self.nvml = NvmlClocks(device)
+        except (OSError, AttributeError):
+            self.nvml = None
+
+    def _nvml_row(self):
+        sm, mx, _, bits = self.nvml.sample()
+        return sm, mx, {name for bit, name in NvmlClocks.REASONS.items() if bits & bit}
+
+    def _poll(self):
+        while not self.stop_flag.is_set():
+            self.rows.append(self._nvml_row())
+            time.sleep(0.002)
 
     def start(self):
+        self.stop_flag.clear()
+        if self.nvml is not None:
+            self.rows.append(self._nvml_row())
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -94,30 +151,34 @@ class ClockSampler:
             self.proc = None
 
     def _read(self):
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                self.rows.append(parts)
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                reasons = {n for n, v in zip(names, parts[5:9]) if v.lower() == "active"}
+                self.rows.append((float(parts[1]), float(parts[2]), reasons))
 
     def stop(self):
-        if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        self.thread.join(timeout=2)
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
-        for r in self.rows:
-            for name, val in zip(names, r[5:9]):
-                if val.strip().lower() == "active":
-                    reasons.add(name)
+        if self.nvml is not None:
+            self.stop_flag.set()
+            self.thread.join(timeout=2)
+            self.rows.append(self._nvml_row())
+            source = "nvml"
+        elif self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+            source = "nvidia-smi"
+        else:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock query unavailable"], "samples": 0}
+        sm = [r[0] for r in self.rows]
+        mx = [r[1] for r in self.rows]
+        reasons = set().union(*[r[2] for r in self.rows]) if self.rows else set()
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(self.rows)}
+                "reasons": sorted(reasons), "samples": len(self.rows), "source": source}
 
 
 def dist_info():

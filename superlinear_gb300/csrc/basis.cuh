@@ -161,15 +161,16 @@ __device__ __forceinline__ void sph_tangent(T ux, T uy, T uz, T tx, T ty, T tz, 
   }
 }
 
-// Raw Chebyshev values and r-derivatives (envelope 1, scaling 1) for B <= kMaxB.
-template <typename T>
+// Raw Chebyshev values and r-derivatives (envelope 1, scaling 1) for B <= NBM <= kMaxB (NBM is
+// the compile-time array bound; with B == NBM known at compile time the loops are exact).
+template <typename T, int NBM = kMaxB>
 __device__ __forceinline__ void cheb_raw(T r, T slope, T shift, int B, T* Tv, T* Td) {
   const T xi = tanh(slope * (r - shift) * T(0.5));
   const T xr = (T(1) - xi * xi) * slope * T(0.5);
   Tv[0] = T(1); Td[0] = T(0);
   Tv[1] = xi; Td[1] = xr;
 #pragma unroll
-  for (int b = 2; b < kMaxB; ++b) {
+  for (int b = 2; b < NBM; ++b) {
     if (b < B) {
       Tv[b] = T(2) * xi * Tv[b - 1] - Tv[b - 2];
       Td[b] = T(2) * (xr * Tv[b - 1] + xi * Td[b - 1]) - Td[b - 2];
@@ -177,13 +178,13 @@ __device__ __forceinline__ void cheb_raw(T r, T slope, T shift, int B, T* Tv, T*
   }
 }
 
-template <typename T>
+template <typename T, int NBM = kMaxB>
 __device__ __forceinline__ void cheb_raw_values(T r, T slope, T shift, int B, T* Tv) {
   const T xi = tanh(slope * (r - shift) * T(0.5));
   Tv[0] = T(1);
   Tv[1] = xi;
 #pragma unroll
-  for (int b = 2; b < kMaxB; ++b)
+  for (int b = 2; b < NBM; ++b)
     if (b < B) Tv[b] = T(2) * xi * Tv[b - 1] - Tv[b - 2];
 }
 
@@ -206,13 +207,13 @@ __device__ __forceinline__ WarpVar<T> warp_var(T r, T slope, T shift) {
   return w;
 }
 
-// Chebyshev T_b(xi) with its first and second derivatives in xi, b < B <= kMaxB.
-template <typename T>
+// Chebyshev T_b(xi) with its first and second derivatives in xi, b < B <= NBM <= kMaxB.
+template <typename T, int NBM = kMaxB>
 __device__ __forceinline__ void cheb_full(T xi, int B, T* Tv, T* D, T* DD) {
   Tv[0] = T(1); D[0] = T(0); DD[0] = T(0);
   Tv[1] = xi; D[1] = T(1); DD[1] = T(0);
 #pragma unroll
-  for (int b = 2; b < kMaxB; ++b) {
+  for (int b = 2; b < NBM; ++b) {
     if (b < B) {
       Tv[b] = T(2) * xi * Tv[b - 1] - Tv[b - 2];
       D[b] = T(2) * Tv[b - 1] + T(2) * xi * D[b - 1] - D[b - 2];

@@ -16,8 +16,9 @@
 // GPU mapping: one warp owns one centre atom at a time.  Lanes take edges (32 per batch); each
 // lane evaluates Y_lm and the radial functions of its edge in registers and stages u_mu =
 // x0 x3 R_mu and Y_h in shared memory; lanes then switch to owning (k, lm) moment items and
-// reduce over the staged edges in a fixed order with Kahan compensation (FP32 bulk) -- no
-// atomics, deterministic.  The product graph runs level by level over shared-memory node
+// reduce over the staged edges in a fixed order: a plain sum over each batch of <= 32 edges, then a
+// Kahan-compensated add of the batch partial into the atom's moment (FP32 bulk) -- no atomics,
+// deterministic.  The product graph runs level by level over shared-memory node
 // arrays; the reverse graph is a gather per consumed node (no write conflicts).  The adjoint
 // pass recomputes Y and R per edge instead of storing them and writes g_e per edge; forces are
 // gathered per atom through the reverse-edge permutation by a separate kernel.
@@ -74,11 +75,13 @@ __device__ __forceinline__ void kadd(Real& s, Real& c, Real x) {
 // The warp (slope, shift) depends on (scaling block, t_i, t_j); the Chebyshev part is shared by
 // every l of a block and only the envelope differs between l = 0 and l > 0 with two cutoffs.
 // ---------------------------------------------------------------------------------------------
-template <int L, typename Real, bool DERIV, typename Body>
+// BF > 0: the basis size is the compile-time constant BF (= dm.B); BF = 0: runtime B <= kMaxB.
+template <int L, typename Real, bool DERIV, int BF = 0, typename Body>
 __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real* s_coeff, const Real* s_scal,
                                             int pair, Real r, Body&& body) {
   constexpr int Lp = L + 1;
-  const int B = dm.B, C2 = dm.C * dm.C;
+  constexpr int NBM = BF ? BF : kMaxB;
+  const int B = BF ? BF : dm.B, C2 = dm.C * dm.C;
   Real f0, fd0, f1, fd1;
   envelope<Real>(r, dm.rmax, dm.poly, dm.cutoff_p, f0, fd0);
   if (dm.split) envelope<Real>(r, dm.rang, dm.poly, dm.cutoff_p, f1, fd1);
@@ -86,7 +89,7 @@ __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real
   f0 *= dm.scaling; fd0 *= dm.scaling; f1 *= dm.scaling; fd1 *= dm.scaling;
   const bool angular_on = !(r >= dm.rang);
   for (int k = 0; k < dm.K; ++k) {
-    Real Tv[kMaxB], Td[kMaxB];
+    Real Tv[NBM], Td[NBM];
     int sb_prev = -1;
 #pragma unroll
     for (int l = 0; l < Lp; ++l) {
@@ -94,15 +97,15 @@ __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real
       const int sb = scaling_block(dm.scaling_mode, k, l, Lp);
       if (sb != sb_prev) {
         const Real slope = s_scal[2 * sb * C2 + pair], shift = s_scal[(2 * sb + 1) * C2 + pair];
-        if (DERIV) cheb_raw<Real>(r, slope, shift, B, Tv, Td);
-        else cheb_raw_values<Real>(r, slope, shift, B, Tv);
+        if (DERIV) cheb_raw<Real, NBM>(r, slope, shift, B, Tv, Td);
+        else cheb_raw_values<Real, NBM>(r, slope, shift, B, Tv);
         sb_prev = sb;
       }
       const int mu = k * Lp + l;
       const Real* c = s_coeff + mu * B;
       Real a = Real(0), ad = Real(0);
 #pragma unroll
-      for (int b = 0; b < kMaxB; ++b) {
+      for (int b = 0; b < NBM; ++b) {
         if (b < B) {
           a += c[b] * Tv[b];
           if (DERIV) ad += c[b] * Td[b];
@@ -167,15 +170,17 @@ __device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const R
 // ---------------------------------------------------------------------------------------------
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
-template <int L, typename Real, int MODE, bool KAHAN>
-__global__ void atom_pass_kernel(PassArgs<Real> a) {
+constexpr int kPassWarps = 4;
+
+template <int L, typename Real, int MODE, bool KAHAN, int BF>
+__global__ void __launch_bounds__(kPassWarps * kWarp, 3) atom_pass_kernel(PassArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;
   const DevModel<Real>& dm = a.dm;
   const bool gate_pass = MODE == kModeGateForward || MODE == kModeGateReverse;
   const PassTables<Real>& pt = gate_pass ? dm.gate : dm.outer;
-  const int C = dm.C, F = dm.F, B = dm.B, K = dm.K, M = dm.M, NB = dm.NB;
+  const int C = dm.C, F = dm.F, B = BF ? BF : dm.B, K = dm.K, M = dm.M, NB = dm.NB;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -245,7 +250,7 @@ __global__ void atom_pass_kernel(PassArgs<Real> a) {
           for (int h = 0; h < H; ++h) row[F + h] = (h == 0 || ang) ? Y[h] : Real(0);
           const Real* hj = effect_outer ? a.hsig + (size_t)j * F : nullptr;
           for (int mu = 0; mu < F; ++mu) row[mu] = Real(0);
-          radial_loop<L, Real, false>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real) {
+          radial_loop<L, Real, false, BF>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real) {
             Real x3 = s_w1[tj * F + mu];
             if (effect_outer) x3 += s_wa[tj * F + mu] * hj[mu];
             row[mu] = s_w0[ti * F + mu] * x3 * R;
@@ -255,13 +260,20 @@ __global__ void atom_pass_kernel(PassArgs<Real> a) {
           for (int h = 0; h < H; ++h) row[F + h] = Real(0);
         }
         __syncwarp();
+        // plain sum over the batch's (<= 32) staged edges, then a compensated add of the batch
+        // partial into the atom's running moment
         const int nb = min(kWarp, e1 - base);
+        Real part[kMaxItems];
+#pragma unroll
+        for (int s = 0; s < kMaxItems; ++s) part[s] = Real(0);
         for (int q = 0; q < nb; ++q) {
           const Real* sr = stage + q * sw;
 #pragma unroll
           for (int s = 0; s < kMaxItems; ++s)
-            if (it_u[s] >= 0) kadd<Real, KAHAN>(acc[s], cmp[s], sr[it_u[s]] * sr[it_y[s]]);
+            if (it_u[s] >= 0) part[s] += sr[it_u[s]] * sr[it_y[s]];
         }
+#pragma unroll
+        for (int s = 0; s < kMaxItems; ++s) kadd<Real, KAHAN>(acc[s], cmp[s], part[s]);
         __syncwarp();
       }
       for (int q = lane; q < M; q += kWarp) v[q] = Real(0);
@@ -351,7 +363,7 @@ __global__ void atom_pass_kernel(PassArgs<Real> a) {
       for (int h = 0; h < H; ++h) { P[h] = Real(0); Qd[h] = Real(0); if (h > 0 && !ang) Y[h] = Real(0); }
       const Real* hj = effect_outer ? a.hsig + (size_t)j * F : nullptr;
       Real* hc = effect_outer ? a.hcontrib + (size_t)a.rev[e] * F : nullptr;
-      radial_loop<L, Real, true>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real Rd) {
+      radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real Rd) {
         const Real x0 = s_w0[ti * F + mu];
         Real x3 = s_w1[tj * F + mu];
         if (effect_outer) x3 += s_wa[tj * F + mu] * hj[mu];

@@ -1,0 +1,5 @@
+// FP32-bulk parameter-gradient passes, sh_l_max = 4.
+#include "grad_inst.cuh"
+namespace sus2g {
+SUS2G_INSTANTIATE_GRAD(float, 4)
+}  // namespace sus2g

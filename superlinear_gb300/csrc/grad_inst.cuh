@@ -1,4 +1,6 @@
-// Instantiation body for the parameter-gradient passes; included by grad_fp32.cu and grad_fp64.cu.
+// Launch templates of the parameter-gradient passes for one spherical-harmonic order L; explicit
+// instantiations in the grad_fp{32,64}_l*.cu units, run-time selection in pass_dispatch.cu.
+#pragma once
 #include <algorithm>
 #include <stdexcept>
 #include <string>
@@ -6,48 +8,41 @@
 #include "pass_launch.h"
 
 namespace sus2g {
+namespace grad_detail {
 
-template <>
-cudaError_t upload_grad_constants<PASS_REAL>() { return sph_norm_upload(); }
-
-namespace {
 constexpr int kGradWarps = 2;
-using GradKernel = void (*)(GradArgs<PASS_REAL>);
+template <typename Real>
+using GradKernel = void (*)(GradArgs<Real>);
 
-template <int L>
-GradKernel grad_kernel_mode(int mode) {
-  constexpr bool kKahan = sizeof(PASS_REAL) == 4;
+template <typename Real, int L, int BF>
+GradKernel<Real> kernel_for(int mode) {
+  constexpr bool kKahan = sizeof(Real) == 4;
   switch (mode) {
-    case kGradOuter: return grad_pass_kernel<L, PASS_REAL, kGradOuter, kKahan>;
-    case kGradGateForward: return grad_pass_kernel<L, PASS_REAL, kGradGateForward, kKahan>;
-    case kGradGateReverse: return grad_pass_kernel<L, PASS_REAL, kGradGateReverse, kKahan>;
+    case kGradOuter: return grad_pass_kernel<L, Real, kGradOuter, kKahan, BF>;
+    case kGradGateForward: return grad_pass_kernel<L, Real, kGradGateForward, kKahan, BF>;
+    case kGradGateReverse: return grad_pass_kernel<L, Real, kGradGateReverse, kKahan, BF>;
   }
   throw std::runtime_error("unknown gradient mode");
 }
 
-GradKernel grad_kernel(int L, int mode) {
-  switch (L) {
-    case 0: return grad_kernel_mode<0>(mode);
-    case 1: return grad_kernel_mode<1>(mode);
-    case 2: return grad_kernel_mode<2>(mode);
-    case 3: return grad_kernel_mode<3>(mode);
-    case 4: return grad_kernel_mode<4>(mode);
-    case 5: return grad_kernel_mode<5>(mode);
-  }
-  throw std::runtime_error("sh_l_max above 5 is not supported");
+template <typename Real, int L>
+GradKernel<Real> kernel_for(int mode, int B) {
+  return B == 8 ? kernel_for<Real, L, 8>(mode) : kernel_for<Real, L, 0>(mode);
 }
-}  // namespace
 
-template <>
-GradLaunch grad_pass_config<PASS_REAL>(int L, int mode, const DevModel<PASS_REAL>& dm, int natoms, int sm_count) {
+}  // namespace grad_detail
+
+template <typename Real, int L>
+GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, int sm_count) {
+  using namespace grad_detail;
   if (dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
-  GradKernel kern = grad_kernel(L, mode);
-  const int H = (L + 1) * (L + 1), Lp = L + 1;
+  GradKernel<Real> kern = kernel_for<Real, L>(mode, dm.B);
+  constexpr int H = (L + 1) * (L + 1), Lp = L + 1;
   int device = 0, optin = 0;
   cudaGetDevice(&device);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
-  const size_t table = pass_table_size<PASS_REAL>(dm.C, dm.F, dm.B, dm.nblk);
-  const size_t per_warp = grad_warp_size<PASS_REAL>(dm.F, H, dm.M, dm.K);
+  const size_t table = pass_table_size<Real>(dm.C, dm.F, dm.B, dm.nblk);
+  const size_t per_warp = grad_warp_size<Real>(dm.F, H, dm.M, dm.K);
   // the gate forward pass has no per-edge parameter loop
   const int cols = mode == kGradGateForward
                        ? 0
@@ -56,7 +51,7 @@ GradLaunch grad_pass_config<PASS_REAL>(int L, int mode, const DevModel<PASS_REAL
   cfg.warps = kGradWarps;
   cfg.acc_cols = cols;
   auto bytes = [&](int warps, int c) {
-    return sizeof(PASS_REAL) * (table + warps * (per_warp + static_cast<size_t>(c) * kAccStride));
+    return sizeof(Real) * (table + warps * (per_warp + static_cast<size_t>(c) * kAccStride));
   };
   if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) cfg.warps = 1;
   if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) { cfg.warps = kGradWarps; cfg.acc_cols = 0; }
@@ -72,11 +67,11 @@ GradLaunch grad_pass_config<PASS_REAL>(int L, int mode, const DevModel<PASS_REAL
   return cfg;
 }
 
-template <>
-int launch_grad_pass<PASS_REAL>(int L, int mode, const GradArgs<PASS_REAL>& a, const GradLaunch& cfg, cudaStream_t s) {
+template <typename Real, int L>
+int launch_grad_pass_l(int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t s) {
   if (a.natoms == 0) return 0;
-  GradKernel kern = grad_kernel(L, mode);
-  GradArgs<PASS_REAL> args = a;
+  grad_detail::GradKernel<Real> kern = grad_detail::kernel_for<Real, L>(mode, a.dm.B);
+  GradArgs<Real> args = a;
   args.acc_cols = cfg.acc_cols;
   kern<<<cfg.grid, cfg.block, cfg.smem, s>>>(args);
   cudaError_t err = cudaGetLastError();
@@ -84,4 +79,12 @@ int launch_grad_pass<PASS_REAL>(int L, int mode, const GradArgs<PASS_REAL>& a, c
   return 1;
 }
 
+template <typename Real, int L>
+cudaError_t upload_grad_constants_l() { return sph_norm_upload(); }
+
 }  // namespace sus2g
+
+#define SUS2G_INSTANTIATE_GRAD(REAL, L)                                                                  \
+  template GradLaunch grad_pass_config_l<REAL, L>(int, const DevModel<REAL>&, int, int);                 \
+  template int launch_grad_pass_l<REAL, L>(int, const GradArgs<REAL>&, const GradLaunch&, cudaStream_t); \
+  template cudaError_t upload_grad_constants_l<REAL, L>();

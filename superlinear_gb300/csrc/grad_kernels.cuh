@@ -159,16 +159,17 @@ __device__ __forceinline__ void contract_reverse_dual(const PassTables<Real>& t,
   __syncwarp();
 }
 
-template <int L, typename Real, int MODE, bool KAHAN>
+template <int L, typename Real, int MODE, bool KAHAN, int BF>
 __global__ void grad_pass_kernel(GradArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
+  constexpr int NBM = BF ? BF : kMaxB;
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;
   const DevModel<Real>& dm = a.dm;
   const bool gate_pass = MODE != kGradOuter;
   const PassTables<Real>& pt = gate_pass ? dm.gate : dm.outer;
   const PassGradLayout& gl = gate_pass ? dm.grad.gate : dm.grad.outer;
-  const int C = dm.C, F = dm.F, B = dm.B, K = dm.K, M = dm.M, NB = dm.NB, NP = dm.grad.nparams;
+  const int C = dm.C, F = dm.F, B = BF ? BF : dm.B, K = dm.K, M = dm.M, NB = dm.NB, NP = dm.grad.nparams;
   const int C2 = C * C;
   const bool effect_outer = MODE == kGradOuter && dm.gated;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
@@ -269,7 +270,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           for (int h = 0; h < H; ++h) { rw[2 * F + h] = Y[h]; rw[2 * F + H + h] = Yd[h]; }
           const Real* hj = effect_outer ? a.hsig + static_cast<size_t>(j) * F : nullptr;
           const Real* hdj = effect_outer ? a.hsigd + static_cast<size_t>(j) * F : nullptr;
-          radial_loop<L, Real, true>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int, int, int m_, Real R, Real Rd) {
+          radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int, int, int m_, Real R, Real Rd) {
             const Real x0 = s_w0[ti * F + m_];
             Real x3 = s_w1[tj * F + m_], x3d = Real(0);
             if (effect_outer) {
@@ -281,16 +282,25 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           });
         }
         __syncwarp();
+        // plain sums over the batch, compensated adds of the batch partials
         const int nb = min(kWarp, e1 - base);
+        Real part[kMaxItems], partd[kMaxItems];
+#pragma unroll
+        for (int s = 0; s < kMaxItems; ++s) { part[s] = Real(0); partd[s] = Real(0); }
         for (int q = 0; q < nb; ++q) {
           const Real* sr = stage + q * sw;
 #pragma unroll
           for (int s = 0; s < kMaxItems; ++s)
             if (it_u[s] >= 0) {
               const Real uu = sr[it_u[s]], ud = sr[F + it_u[s]], yy = sr[it_y[s]], yd = sr[it_y[s] + H];
-              kadd<Real, KAHAN>(acc[s], cmp[s], uu * yy);
-              kadd<Real, KAHAN>(accd[s], cmpd[s], ud * yy + uu * yd);
+              part[s] += uu * yy;
+              partd[s] += ud * yy + uu * yd;
             }
+        }
+#pragma unroll
+        for (int s = 0; s < kMaxItems; ++s) {
+          kadd<Real, KAHAN>(acc[s], cmp[s], part[s]);
+          kadd<Real, KAHAN>(accd[s], cmpd[s], partd[s]);
         }
         __syncwarp();
       }
@@ -402,7 +412,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
       const Real* hj = (effect_outer && valid) ? a.hsig + static_cast<size_t>(j) * F : nullptr;
       const Real* hdj = (effect_outer && valid) ? a.hsigd + static_cast<size_t>(j) * F : nullptr;
       for (int k = 0; k < K; ++k) {
-        Real Tv[kMaxB], D[kMaxB], DD[kMaxB];
+        Real Tv[NBM], D[NBM], DD[NBM];
         WarpVar<Real> wv;
         int sb_prev = -1;
 #pragma unroll
@@ -410,7 +420,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           const int sb = scaling_block(dm.scaling_mode, k, l, Lp);
           if (sb != sb_prev) {
             wv = warp_var<Real>(r, s_scal[2 * sb * C2 + ti * C + tj], s_scal[(2 * sb + 1) * C2 + ti * C + tj]);
-            cheb_full<Real>(wv.xi, B, Tv, D, DD);
+            cheb_full<Real, NBM>(wv.xi, B, Tv, D, DD);
             sb_prev = sb;
           }
           const int m_ = k * Lp + l;
@@ -418,7 +428,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           const Real* c = s_coeff + m_ * B;
           Real cT = Real(0), cD = Real(0), cDD = Real(0);
 #pragma unroll
-          for (int b = 0; b < kMaxB; ++b)
+          for (int b = 0; b < NBM; ++b)
             if (b < B) { cT += c[b] * Tv[b]; cD += c[b] * D[b]; cDD += c[b] * DD[b]; }
           const Real f = l == 0 ? f0 : f1, fd = l == 0 ? fd0 : fd1;
           const Real R = f * cT, Rd = fd * cT + f * cD * wv.xr;
@@ -450,7 +460,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
           if (ncol) {
             Real* ac = accs + lane;
 #pragma unroll
-            for (int b = 0; b < kMaxB; ++b)
+            for (int b = 0; b < NBM; ++b)
               if (b < B) ac[(l * B + b) * kAccStride] += dR * f * Tv[b] + dRd * (fd * Tv[b] + f * D[b] * wv.xr);
             ac[(c_wc + ti * Lp + l) * kAccStride] += dx0;
             ac[(c_wc + tj * Lp + l) * kAccStride] += dxj;

@@ -1,0 +1,81 @@
+// Run-time selection of the per-L pass and gradient units (instantiated in pass_fp*_l*.cu and
+// grad_fp*_l*.cu); this unit sees only their declarations.
+#include <stdexcept>
+#include <string>
+
+#include "pass_launch.h"
+
+namespace sus2g {
+
+template <typename Real>
+int launch_atom_pass(int L, int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+  if (a.dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
+  switch (L) {
+    case 0: return launch_atom_pass_l<Real, 0>(mode, a, sm_count, s);
+    case 1: return launch_atom_pass_l<Real, 1>(mode, a, sm_count, s);
+    case 2: return launch_atom_pass_l<Real, 2>(mode, a, sm_count, s);
+    case 3: return launch_atom_pass_l<Real, 3>(mode, a, sm_count, s);
+    case 4: return launch_atom_pass_l<Real, 4>(mode, a, sm_count, s);
+    case 5: return launch_atom_pass_l<Real, 5>(mode, a, sm_count, s);
+  }
+  throw std::runtime_error("sh_l_max above 5 is not supported");
+}
+
+template <typename Real>
+GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count) {
+  switch (L) {
+    case 0: return grad_pass_config_l<Real, 0>(mode, dm, natoms, sm_count);
+    case 1: return grad_pass_config_l<Real, 1>(mode, dm, natoms, sm_count);
+    case 2: return grad_pass_config_l<Real, 2>(mode, dm, natoms, sm_count);
+    case 3: return grad_pass_config_l<Real, 3>(mode, dm, natoms, sm_count);
+    case 4: return grad_pass_config_l<Real, 4>(mode, dm, natoms, sm_count);
+    case 5: return grad_pass_config_l<Real, 5>(mode, dm, natoms, sm_count);
+  }
+  throw std::runtime_error("sh_l_max above 5 is not supported");
+}
+
+template <typename Real>
+int launch_grad_pass(int L, int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t s) {
+  switch (L) {
+    case 0: return launch_grad_pass_l<Real, 0>(mode, a, cfg, s);
+    case 1: return launch_grad_pass_l<Real, 1>(mode, a, cfg, s);
+    case 2: return launch_grad_pass_l<Real, 2>(mode, a, cfg, s);
+    case 3: return launch_grad_pass_l<Real, 3>(mode, a, cfg, s);
+    case 4: return launch_grad_pass_l<Real, 4>(mode, a, cfg, s);
+    case 5: return launch_grad_pass_l<Real, 5>(mode, a, cfg, s);
+  }
+  throw std::runtime_error("sh_l_max above 5 is not supported");
+}
+
+template <typename Real>
+cudaError_t upload_pass_constants() {
+  cudaError_t errs[6] = {upload_pass_constants_l<Real, 0>(), upload_pass_constants_l<Real, 1>(),
+                         upload_pass_constants_l<Real, 2>(), upload_pass_constants_l<Real, 3>(),
+                         upload_pass_constants_l<Real, 4>(), upload_pass_constants_l<Real, 5>()};
+  for (cudaError_t e : errs)
+    if (e != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+template <typename Real>
+cudaError_t upload_grad_constants() {
+  cudaError_t errs[6] = {upload_grad_constants_l<Real, 0>(), upload_grad_constants_l<Real, 1>(),
+                         upload_grad_constants_l<Real, 2>(), upload_grad_constants_l<Real, 3>(),
+                         upload_grad_constants_l<Real, 4>(), upload_grad_constants_l<Real, 5>()};
+  for (cudaError_t e : errs)
+    if (e != cudaSuccess) return e;
+  return cudaSuccess;
+}
+
+template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t);
+template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t);
+template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int);
+template GradLaunch grad_pass_config<double>(int, int, const DevModel<double>&, int, int);
+template int launch_grad_pass<float>(int, int, const GradArgs<float>&, const GradLaunch&, cudaStream_t);
+template int launch_grad_pass<double>(int, int, const GradArgs<double>&, const GradLaunch&, cudaStream_t);
+template cudaError_t upload_pass_constants<float>();
+template cudaError_t upload_pass_constants<double>();
+template cudaError_t upload_grad_constants<float>();
+template cudaError_t upload_grad_constants<double>();
+
+}  // namespace sus2g

@@ -1,0 +1,5 @@
+// FP32-bulk per-atom passes, sh_l_max = 3.
+#include "pass_inst.cuh"
+namespace sus2g {
+SUS2G_INSTANTIATE_PASS(float, 3)
+}  // namespace sus2g

@@ -1,22 +1,26 @@
-// Instantiation body for launch_atom_pass<Real>; included by pass_fp32.cu and pass_fp64.cu.
+// Launch templates of the per-atom passes for one spherical-harmonic order L.  The explicit
+// instantiations live in the small pass_fp{32,64}_l*.cu units (one group of L each) so that the
+// units compile in parallel; pass_dispatch.cu selects the unit by L at run time.  Each unit owns
+// its copy of the spherical-harmonic normalisation table and uploads it through
+// upload_pass_constants_l.
+#pragma once
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
 #include "pass_launch.h"
 
 namespace sus2g {
+namespace pass_detail {
 
-namespace {
-constexpr int kPassWarps = 4;
-
-template <int L, int MODE>
-int launch_one(const PassArgs<PASS_REAL>& a, int sm_count, cudaStream_t stream) {
-  constexpr bool kKahan = sizeof(PASS_REAL) == 4;
-  auto kern = atom_pass_kernel<L, PASS_REAL, MODE, kKahan>;
+template <typename Real, int L, int MODE, int BF>
+int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream) {
+  constexpr bool kKahan = sizeof(Real) == 4;
+  auto kern = atom_pass_kernel<L, Real, MODE, kKahan, BF>;
   const auto& dm = a.dm;
   const int H = (L + 1) * (L + 1);
-  const size_t smem = sizeof(PASS_REAL) *
-      (pass_table_size<PASS_REAL>(dm.C, dm.F, dm.B, dm.nblk) + kPassWarps * pass_warp_size<PASS_REAL>(dm.F, H, dm.M, dm.K));
+  const size_t smem = sizeof(Real) *
+      (pass_table_size<Real>(dm.C, dm.F, dm.B, dm.nblk) + kPassWarps * pass_warp_size<Real>(dm.F, H, dm.M, dm.K));
   static size_t configured = 0;
   if (smem > configured) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -35,33 +39,32 @@ int launch_one(const PassArgs<PASS_REAL>& a, int sm_count, cudaStream_t stream) 
   return 1;
 }
 
-template <int L>
-int launch_mode(int mode, const PassArgs<PASS_REAL>& a, int sm_count, cudaStream_t s) {
+template <typename Real, int L, int BF>
+int launch_mode(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
   switch (mode) {
-    case kModeStatic: return launch_one<L, kModeStatic>(a, sm_count, s);
-    case kModeGateForward: return launch_one<L, kModeGateForward>(a, sm_count, s);
-    case kModeOuter: return launch_one<L, kModeOuter>(a, sm_count, s);
-    case kModeGateReverse: return launch_one<L, kModeGateReverse>(a, sm_count, s);
+    case kModeStatic: return launch_one<Real, L, kModeStatic, BF>(a, sm_count, s);
+    case kModeGateForward: return launch_one<Real, L, kModeGateForward, BF>(a, sm_count, s);
+    case kModeOuter: return launch_one<Real, L, kModeOuter, BF>(a, sm_count, s);
+    case kModeGateReverse: return launch_one<Real, L, kModeGateReverse, BF>(a, sm_count, s);
   }
   throw std::runtime_error("unknown pass mode");
 }
-}  // namespace
 
-template <>
-int launch_atom_pass<PASS_REAL>(int L, int mode, const PassArgs<PASS_REAL>& a, int sm_count, cudaStream_t s) {
-  if (a.dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
-  switch (L) {
-    case 0: return launch_mode<0>(mode, a, sm_count, s);
-    case 1: return launch_mode<1>(mode, a, sm_count, s);
-    case 2: return launch_mode<2>(mode, a, sm_count, s);
-    case 3: return launch_mode<3>(mode, a, sm_count, s);
-    case 4: return launch_mode<4>(mode, a, sm_count, s);
-    case 5: return launch_mode<5>(mode, a, sm_count, s);
-  }
-  throw std::runtime_error("sh_l_max above 5 is not supported");
+}  // namespace pass_detail
+
+// B = 8 (the basis size the reference's model initialisation writes) runs the variant with the
+// basis size fixed at compile time; other sizes run the generic variant.
+template <typename Real, int L>
+int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+  if (a.dm.B == 8) return pass_detail::launch_mode<Real, L, 8>(mode, a, sm_count, s);
+  return pass_detail::launch_mode<Real, L, 0>(mode, a, sm_count, s);
 }
 
-template <>
-cudaError_t upload_pass_constants<PASS_REAL>() { return sph_norm_upload(); }
+template <typename Real, int L>
+cudaError_t upload_pass_constants_l() { return sph_norm_upload(); }
 
 }  // namespace sus2g
+
+#define SUS2G_INSTANTIATE_PASS(REAL, L)                                                               \
+  template int launch_atom_pass_l<REAL, L>(int, const PassArgs<REAL>&, int, cudaStream_t);            \
+  template cudaError_t upload_pass_constants_l<REAL, L>();

@@ -25,10 +25,22 @@ int launch_grad_pass(int L, int mode, const GradArgs<Real>& a, const GradLaunch&
 template <typename Real>
 int launch_atom_pass(int L, int mode, const PassArgs<Real>& args, int sm_count, cudaStream_t stream);
 
-// Per-translation-unit constant-table upload (spherical-harmonic normalisation).
+// Per-translation-unit constant-table upload (spherical-harmonic normalisation) of every unit.
 template <typename Real>
 cudaError_t upload_pass_constants();
 template <typename Real>
 cudaError_t upload_grad_constants();
+
+// Per-L entry points, explicitly instantiated in the pass_fp*_l* / grad_fp*_l* units.
+template <typename Real, int L>
+int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s);
+template <typename Real, int L>
+cudaError_t upload_pass_constants_l();
+template <typename Real, int L>
+GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, int sm_count);
+template <typename Real, int L>
+int launch_grad_pass_l(int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t s);
+template <typename Real, int L>
+cudaError_t upload_grad_constants_l();
 
 }  // namespace sus2g
