@@ -106,6 +106,33 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Compensated FP32 accumulation (Knuth two-sum; the running error is kept in lo): sums of FP32
+// terms with close to FP64 accuracy without FP64 arithmetic, which runs at 1/64 of the FP32 rate
+// on this GPU.  No multiplications are involved, so FMA contraction cannot alter the error terms.
+__device__ __forceinline__ void csum_add(float& hi, float& lo, float x) {
+  const float s = hi + x;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (x - bb);
+  hi = s;
+}
+// x * y added exactly (product split by an FMA: p + e == x * y).
+__device__ __forceinline__ void csum_add_prod(float& hi, float& lo, float x, float y) {
+  const float p = x * y;
+  const float e = fmaf(x, y, -p);
+  csum_add(hi, lo, p);
+  lo += e;
+}
+// Warp total of compensated partials (fixed butterfly order), returned in FP64 on every lane.
+__device__ __forceinline__ double warp_csum(float hi, float lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    csum_add(hi, lo, oh);
+    lo += ol;
+  }
+  return double(hi) + double(lo);
+}
+
 // Warp index of the scaling block for radial function (k, l) (sus2_sl_kernel.cpp:198).
 __device__ __forceinline__ int scaling_block(int mode, int k, int l, int Lp) {
   return mode == 2 ? k : (mode == 1 ? l : (mode == 0 ? 0 : k * Lp + l));

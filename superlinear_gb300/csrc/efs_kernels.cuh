@@ -228,7 +228,9 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, 3) atom_pass_kernel(PassAr
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
     const int ti = a.types[atom];
     const int e0 = a.row[atom], e1 = a.row[atom + 1];
+    // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form
     double vir[6] = {0, 0, 0, 0, 0, 0};
+    float vhi[6] = {0, 0, 0, 0, 0, 0}, vlo[6] = {0, 0, 0, 0, 0, 0};
 
     if (MODE != kModeGateReverse) {
       // ---------------- forward moments ----------------
@@ -397,12 +399,24 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, 3) atom_pass_kernel(PassAr
       } else {
         ge[0] = Gx; ge[1] = Gy; ge[2] = Gz;
       }
-      const double dx = dv.x, dy = dv.y, dz = dv.z;
-      vir[0] -= dx * double(Gx); vir[1] -= dy * double(Gy); vir[2] -= dz * double(Gz);
-      vir[3] -= dx * double(Gy); vir[4] -= dx * double(Gz); vir[5] -= dy * double(Gz);
+      if (sizeof(Real) == 4) {
+        const float dx = float(dv.x), dy = float(dv.y), dz = float(dv.z);
+        csum_add_prod(vhi[0], vlo[0], -dx, float(Gx)); csum_add_prod(vhi[1], vlo[1], -dy, float(Gy));
+        csum_add_prod(vhi[2], vlo[2], -dz, float(Gz)); csum_add_prod(vhi[3], vlo[3], -dx, float(Gy));
+        csum_add_prod(vhi[4], vlo[4], -dx, float(Gz)); csum_add_prod(vhi[5], vlo[5], -dy, float(Gz));
+      } else {
+        const double dx = dv.x, dy = dv.y, dz = dv.z;
+        vir[0] -= dx * double(Gx); vir[1] -= dy * double(Gy); vir[2] -= dz * double(Gz);
+        vir[3] -= dx * double(Gy); vir[4] -= dx * double(Gz); vir[5] -= dy * double(Gz);
+      }
     }
+    if (sizeof(Real) == 4) {
 #pragma unroll
-    for (int c = 0; c < 6; ++c) vir[c] = warp_sum(vir[c]);
+      for (int c = 0; c < 6; ++c) vir[c] = warp_csum(vhi[c], vlo[c]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 6; ++c) vir[c] = warp_sum(vir[c]);
+    }
     if (lane == 0) {
       double* vo = a.virial + (size_t)atom * 6;
       if (MODE == kModeGateReverse)

@@ -227,18 +227,27 @@ __global__ void k_reverse(const int* row, const int* nbr, const unsigned long lo
   rev[e] = found < 0 ? static_cast<int>(e) : found;
 }
 
-// F_i = sum over i's edges of (g_e - g_rev(e)), FP64 accumulation, warp per atom.
+// F_i = sum over i's edges of (g_e - g_rev(e)), warp per atom: FP64 accumulation for FP64 edge
+// gradients, compensated FP32 (two-sum, FP64 result) for FP32 ones.
 template <typename Real>
 __global__ void k_force_gather(const int* row, const int* rev, const Real* g, int natoms, double* force) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
   double f[3] = {0, 0, 0};
+  float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
   for (int e = row[warp] + lane; e < row[warp + 1]; e += kWarp) {
     const int r = rev[e];
-    for (int c = 0; c < 3; ++c) f[c] += double(g[3 * (size_t)e + c]) - double(g[3 * (size_t)r + c]);
+    for (int c = 0; c < 3; ++c) {
+      if (sizeof(Real) == 4) {
+        csum_add(hi[c], lo[c], float(g[3 * (size_t)e + c]));
+        csum_add(hi[c], lo[c], -float(g[3 * (size_t)r + c]));
+      } else {
+        f[c] += double(g[3 * (size_t)e + c]) - double(g[3 * (size_t)r + c]);
+      }
+    }
   }
-  for (int c = 0; c < 3; ++c) f[c] = warp_sum(f[c]);
+  for (int c = 0; c < 3; ++c) f[c] = sizeof(Real) == 4 ? warp_csum(hi[c], lo[c]) : warp_sum(f[c]);
   if (lane == 0)
     for (int c = 0; c < 3; ++c) force[3 * (size_t)warp + c] = f[c];
 }
@@ -277,28 +286,38 @@ __global__ void k_iota(int* v, long long n) {
   if (e < n) v[e] = static_cast<int>(e);
 }
 
-// Per-frame energy and virial: one block per frame, fixed-order tree reduction.
-__global__ void k_frame_reduce(const FramePlan* plans, int nframes, const double* site, const double* vir_atom,
-                               double* energy, double* virial) {
-  const int f = blockIdx.x;
+// Per-frame energy and virial in two deterministic steps: block (f, s) reduces the atoms
+// a0 + s * 256 + t, a0 + (S + s) * 256 + t, ... of frame f with a fixed-order tree into
+// partial[f][s][7]; k_frame_finish then adds the S slices of each frame in slice order.
+__global__ void k_frame_partial(const FramePlan* plans, int nframes, int S, const double* site,
+                                const double* vir_atom, double* partial) {
+  const int f = blockIdx.x, sl = blockIdx.y;
   if (f >= nframes) return;
   __shared__ double sh[7][256];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) {
+  for (int i = plans[f].a0 + sl * 256 + threadIdx.x; i < plans[f].a1; i += S * 256) {
     acc[0] += site[i];
     for (int c = 0; c < 6; ++c) acc[1 + c] += vir_atom[6 * (size_t)i + c];
   }
   for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + s];
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
     __syncthreads();
   }
-  if (threadIdx.x == 0) {
-    if (energy) energy[f] = sh[0][0];
-    if (virial)
-      for (int c = 0; c < 6; ++c) virial[6 * f + c] = sh[1 + c][0];
+  if (threadIdx.x < 7) partial[(static_cast<size_t>(f) * S + sl) * 7 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void k_frame_finish(int nframes, int S, const double* partial, double* energy, double* virial) {
+  const int f = blockIdx.x * blockDim.y + threadIdx.y, c = threadIdx.x;
+  if (f >= nframes || c >= 7) return;
+  double v = 0.0;
+  for (int sl = 0; sl < S; ++sl) v += partial[(static_cast<size_t>(f) * S + sl) * 7 + c];
+  if (c == 0) {
+    if (energy) energy[f] = v;
+  } else if (virial) {
+    virial[6 * f + c - 1] = v;
   }
 }
 
@@ -1019,8 +1038,14 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     }
   }
   if (nframes_) {
-    k_frame_reduce<<<nframes_, 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, site_.as<double>(), vir_atom_.as<double>(), d_energy, d_virial);
-    ++launches_;
+    int largest = 0;
+    for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
+    const int S = std::max(1, std::min(64, (largest + 1023) / 1024));
+    frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
+    k_frame_partial<<<dim3(nframes_, S), 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, S, site_.as<double>(),
+                                                      vir_atom_.as<double>(), frame_partial_.as<double>());
+    k_frame_finish<<<(nframes_ + 7) / 8, dim3(8, 8), 0, s>>>(nframes_, S, frame_partial_.as<double>(), d_energy, d_virial);
+    launches_ += 2;
   }
   if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
   mark_end();

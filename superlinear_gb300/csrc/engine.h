@@ -146,7 +146,7 @@ class Engine {
   int open_stage_ = -1;
   cudaEvent_t open_event_ = nullptr;
   // step buffers
-  DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_;
+  DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_, frame_partial_;
   DevBuf scratch_;
   DevBuf io_[8];
 };
