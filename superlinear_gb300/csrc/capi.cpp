@@ -161,9 +161,16 @@ int sus2g_calc_efs_device(sus2g_engine e, int nframes, const int* natoms, const 
     const long long n = total_atoms(nframes, natoms);
     need(n == 0 || (positions && types), "positions/types");
     auto& eng = *e->engine;
-    eng.build_edges(nframes, natoms, cells, positions, types);
-    eng.efs(energy, forces, virial, site_energy);
-    eng.check_device_error();
+    for (int attempt = 0;; ++attempt) {
+      try {
+        eng.build_edges(nframes, natoms, cells, positions, types);
+        eng.efs(energy, forces, virial, site_energy);
+        eng.check_device_error();
+        break;
+      } catch (const sus2g::EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: repeat the step
+      }
+    }
   });
 }
 
@@ -186,10 +193,17 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
       cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
       cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
     }
-    eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
-    eng.efs(energy ? out_e.as<double>() : nullptr, forces ? out_f.as<double>() : nullptr,
-            virial ? out_v.as<double>() : nullptr, site_energy ? out_s.as<double>() : nullptr);
-    eng.check_device_error();
+    for (int attempt = 0;; ++attempt) {
+      try {
+        eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
+        eng.efs(energy ? out_e.as<double>() : nullptr, forces ? out_f.as<double>() : nullptr,
+                virial ? out_v.as<double>() : nullptr, site_energy ? out_s.as<double>() : nullptr);
+        eng.check_device_error();
+        break;
+      } catch (const sus2g::EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: repeat the step
+      }
+    }
     if (energy && nframes) cuda(cudaMemcpyAsync(energy, out_e.p, sizeof(double) * nframes, cudaMemcpyDeviceToHost, s), "energy copy");
     if (forces && n) cuda(cudaMemcpyAsync(forces, out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "force copy");
     if (virial && nframes) cuda(cudaMemcpyAsync(virial, out_v.p, sizeof(double) * 6 * nframes, cudaMemcpyDeviceToHost, s), "virial copy");
@@ -221,10 +235,17 @@ int sus2g_efs_combination_grad_host(sus2g_engine e, int nframes, const int* nato
       cuda(cudaMemcpyAsync(fw.p, frc_w, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "weights copy");
     }
     if (nframes) cuda(cudaMemcpyAsync(sw.p, str_w, sizeof(double) * 9 * nframes, cudaMemcpyHostToDevice, s), "weights copy");
-    cuda(cudaMemcpyAsync(g.p, grad, sizeof(double) * P, cudaMemcpyHostToDevice, s), "grad copy");
-    eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
-    if (n) eng.combination_grad(ew.as<double>(), fw.as<double>(), sw.as<double>(), g.as<double>());
-    eng.check_device_error();
+    for (int attempt = 0;; ++attempt) {
+      try {
+        cuda(cudaMemcpyAsync(g.p, grad, sizeof(double) * P, cudaMemcpyHostToDevice, s), "grad copy");
+        eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
+        if (n) eng.combination_grad(ew.as<double>(), fw.as<double>(), sw.as<double>(), g.as<double>());
+        eng.check_device_error();
+        break;
+      } catch (const sus2g::EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: repeat the step
+      }
+    }
     cuda(cudaMemcpyAsync(grad, g.p, sizeof(double) * P, cudaMemcpyDeviceToHost, s), "grad copy");
     cuda(cudaStreamSynchronize(s), "stream synchronize");
   });

@@ -134,9 +134,9 @@ __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const d
 }
 
 // Cell-list frames: one warp per centre over the flattened 27-bin candidate list, one pass.  The
-// centre's edges go to its padded slots pad0 + (i - a0) cap .. + cap of the staging buffers; the
-// count is recorded in full, and a count above cap raises *overflow (the host then grows the
-// capacity and repeats the pass).
+// centre's edges go to its padded slots pad0 + (i - a0) cap .. + cap of the staging buffers; a
+// count above cap is clamped to cap and raises *overflow to the full count, which the host reads
+// with the step's error check (it then grows the capacity and repeats the step).
 constexpr int kFillWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
@@ -163,7 +163,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
                    cursor += __popc(mask);
                  });
   if (lane == 0) {
-    counts[i] = cursor;
+    counts[i] = min(cursor, cap);
     if (cursor > cap) atomicMax(overflow, cursor);
   }
 }
@@ -202,9 +202,10 @@ __global__ void k_edge_sort(const int* row, int natoms, const FramePlan* plans, 
 }
 
 __global__ void k_reverse(const int* row, const int* nbr, const unsigned long long* key, long long nedges, int* rev,
-                          const int* centre_of_edge_unused, int natoms, int* error) {
+                          int natoms, int* error) {
   const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= nedges) return;
+  // nedges bounds the launch; the exact total is row[natoms] on the device
+  if (e >= nedges || e >= row[natoms]) return;
   // centre of e: binary search in row
   int lo = 0, hi = natoms;
   while (hi - lo > 1) {
@@ -533,8 +534,8 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   if (model_.K > kMaxK) throw Error(3, "SUS2 model: sh_k_max above 8 is not supported by the GPU engine");
   plans_ = new std::vector<FramePlan>();
   SUS2G_CUDA(cudaMallocHost(&host_total_, 4 * sizeof(int)));
-  error_.ensure(sizeof(int));
-  SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
+  error_.ensure(2 * sizeof(int));  // [0] error code, [1] cell-list capacity overflow (largest count)
+  SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 2 * sizeof(int), stream_));
   upload_model();
 }
 
@@ -662,10 +663,26 @@ void Engine::upload_model() {
   else upload_tables<double>();
 }
 
+long long Engine::nedges() {
+  if (!nedges_exact_) {
+    SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 2, row_.as<int>() + ncentres_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    SUS2G_CUDA(cudaStreamSynchronize(stream_));
+    exact_edges_ = host_total_[2];
+    nedges_exact_ = true;
+  }
+  return exact_edges_;
+}
+
 void Engine::check_device_error() {
-  int h = 0;
-  SUS2G_CUDA(cudaMemcpyAsync(&h, error_.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 2, error_.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
   SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  const int h = host_total_[2], over = host_total_[3];
+  if (over > 0) {
+    SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 2 * sizeof(int), stream_));
+    cap_scale_ *= 2.0;
+    min_cap_ = std::max(min_cap_, over);
+    throw EdgeOverflow();
+  }
   if (h) {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
     static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
@@ -768,7 +785,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                        fp.cell[1] * (fp.cell[3] * fp.cell[8] - fp.cell[5] * fp.cell[6]) +
                        fp.cell[2] * (fp.cell[3] * fp.cell[7] - fp.cell[4] * fp.cell[6]);
       const double mean = frame_natoms[f] / std::abs(c) * (4.0 / 3.0) * 3.141592653589793 * rc * rc2;
-      fp.cap = static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0));
+      fp.cap = std::max(min_cap_, static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0)));
       fp.pad0 = pad_total;
       pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
     }
@@ -811,22 +828,22 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const int *BS = bin_start_.as<int>(), *BA = bin_atoms_.as<int>(), *BO = bin_of.as<int>();
   const AtomFrac* FR = frac_.as<AtomFrac>();
   const AtomOff* OF = off_.as<AtomOff>();
-  overflow_.ensure(sizeof(int));
+  int* overflow = error_.as<int>() + 1;
   // cell-list frames: one pass into padded staging slots (repeated with a larger capacity on overflow)
   auto fill_bins = [&]() {
     const size_t slots = static_cast<size_t>(std::max<long long>(1, pad_total));
     pad_nbr_.ensure(sizeof(int) * slots);
     pad_d4_.ensure(rsz * slots);
     pad_key_.ensure(sizeof(unsigned long long) * slots);
-    SUS2G_CUDA(cudaMemsetAsync(overflow_.ptr, 0, sizeof(int), s));
+    SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
       k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
-                                                                         pad_key_.as<unsigned long long>(), overflow_.as<int>(), error_.as<int>());
+                                                                         pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
       k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
-                                                                          pad_key_.as<unsigned long long>(), overflow_.as<int>(), error_.as<int>());
+                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;
   };
   if (a) {
@@ -838,33 +855,51 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     }
   }
   long long total = 0;
-  for (int attempt = 0;; ++attempt) {
+  if (bins_frames_ == nframes) {
+    // cell lists only: no host synchronisation.  The edge arrays are sized by the padded
+    // capacity; the exact total stays on the device (row[a]) and an overflow is reported by the
+    // step's check_device_error.
     k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
     ++launches_;
-    // the one host synchronisation of the build: the edge total sizes the edge arrays, and the
-    // overflow flag says whether a centre had more edges than its padded capacity
-    SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 1, overflow_.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    SUS2G_CUDA(cudaStreamSynchronize(s));
-    total = host_total_[0];
-    const int over = bins ? host_total_[1] : 0;
-    if (over <= 0) break;
-    if (attempt >= 8) throw Error(4, "edge build: padded capacity did not converge");
-    // grow every cell-list frame's capacity to at least the largest count seen, and re-run
-    cap_scale_ *= 2.0;
-    pad_total = 0;
-    for (int f = 0; f < nframes; ++f) {
-      FramePlan& fp = plans[f];
-      if (!fp.use_bins) continue;
-      fp.cap = std::max(2 * fp.cap, over);
-      fp.pad0 = pad_total;
-      pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
+    total = pad_total;
+    nedges_exact_ = false;
+  } else {
+    for (int attempt = 0;; ++attempt) {
+      k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
+      ++launches_;
+      // the edge total sizes the edge arrays (image-scan frames have no capacity bound), and the
+      // overflow word says whether a cell-list centre had more edges than its padded capacity
+      SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
+      SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 1, overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
+      SUS2G_CUDA(cudaStreamSynchronize(s));
+      total = host_total_[0];
+      const int over = bins ? host_total_[1] : 0;
+      if (over <= 0) break;
+      if (attempt >= 8) throw Error(4, "edge build: padded capacity did not converge");
+      // grow every cell-list frame's capacity to at least the largest count seen, and re-run
+      cap_scale_ *= 2.0;
+      min_cap_ = std::max(min_cap_, over);
+      pad_total = 0;
+      for (int f = 0; f < nframes; ++f) {
+        FramePlan& fp = plans[f];
+        if (!fp.use_bins) continue;
+        fp.cap = std::max(2 * fp.cap, over);
+        fp.pad0 = pad_total;
+        pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
+      }
+      SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
+      fill_bins();
+      if (bins_frames_ < nframes) {
+        k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(), error_.as<int>());
+        ++launches_;
+      }
+      SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
     }
-    SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
-    fill_bins();
-    SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
+    nedges_exact_ = true;
   }
+  if (total > 2147483647LL) throw Error(4, "edge build: more than 2^31 - 1 edge slots");
   nedges_ = total;
+  if (nedges_exact_) exact_edges_ = total;
   const size_t E = std::max<long long>(1, total);
   nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);
   rev_.ensure(sizeof(int) * E);
@@ -910,7 +945,7 @@ void Engine::finalize_edges() {
     launches_ += 2;
   } else if (nedges_) {
     k_reverse<<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(row_.as<int>(), nbr_.as<int>(), key_.as<unsigned long long>(),
-                                                                           nedges_, rev_.as<int>(), nullptr, a, error_.as<int>());
+                                                                           nedges_, rev_.as<int>(), a, error_.as<int>());
     ++launches_;
   }
 }
@@ -941,7 +976,8 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
   }
   long long total = 0;
   exclusive_scan_host_sync(counts_.as<int>(), nowned, row_.as<int>(), s, &total);
-  nedges_ = total;
+  nedges_ = exact_edges_ = total;
+  nedges_exact_ = true;
   const size_t E = std::max<long long>(1, total);
   const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
   nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);

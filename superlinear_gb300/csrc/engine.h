@@ -70,7 +70,9 @@ class Engine {
 
   int natoms() const { return natoms_; }
   int nframes() const { return nframes_; }
-  long long nedges() const { return nedges_; }
+  // Directed edges of the last build (for cell-list-only batches read back from the device on
+  // first request: the build itself does not synchronise).
+  long long nedges();
   // number of kernels launched by the last build_edges + efs (for launch accounting)
   int last_launches() const { return launches_; }
   void reset_launch_count() { launches_ = 0; }
@@ -121,7 +123,10 @@ class Engine {
 
   // geometry
   int natoms_ = 0, nframes_ = 0, ncentres_ = 0, bins_frames_ = 0;
-  long long nedges_ = 0;
+  long long nedges_ = 0;          // edge slots: exact count, or the padded capacity of a deferred build
+  long long exact_edges_ = 0;
+  bool nedges_exact_ = true;
+  int min_cap_ = 0;              // lower bound of the padded capacity after an overflow
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
   DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
@@ -129,7 +134,7 @@ class Engine {
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf ei_, hbar_atom_, bin_of_, frac_, off_;
-  DevBuf pad_nbr_, pad_d4_, pad_key_, overflow_;  // padded single-pass staging of cell-list frames
+  DevBuf pad_nbr_, pad_d4_, pad_key_;  // padded single-pass staging of cell-list frames
   double cap_scale_ = 2.0;      // padded capacity = cap_scale x mean neighbour count + 64 (grows on overflow)
   bool sort_from_pad_ = false;
   int* host_total_ = nullptr;   // pinned [4]

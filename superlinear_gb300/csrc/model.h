@@ -19,6 +19,12 @@ struct Error : std::runtime_error {
   Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// A cell-list centre had more edges than its padded capacity; the engine has already grown the
+// capacity, and the step that raised it is to be repeated.
+struct EdgeOverflow : Error {
+  EdgeOverflow() : Error(9, "edge build: padded neighbour capacity exceeded (capacity grown; repeat the step)") {}
+};
+
 struct Product { int a, b, out; double c; };
 
 // One per-atom graph evaluation schedule (forward levels and the reverse gather lists).

@@ -220,8 +220,15 @@ class Trainer {
   void bind_edges() {
     if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
     if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
-    eng_.build_edges(nframes_, natoms_list_.data(), cells_.data(), pos_.as<double>(), types_.as<int>());
-    eng_.check_device_error();
+    for (int attempt = 0;; ++attempt) {
+      try {
+        eng_.build_edges(nframes_, natoms_list_.data(), cells_.data(), pos_.as<double>(), types_.as<int>());
+        eng_.check_device_error();
+        break;
+      } catch (const EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: build again
+      }
+    }
     generation_ = eng_.edge_generation();
   }
 

@@ -1,6 +1,6 @@
 """GPU E / F / virial parity through the C ABI (FP64 plain and FP32 bulk).
 
-Bars (BASELINE the benchmark spec): FP64 plain within 1e-10 relative (tol * (1 + max|a|,|b|)) of the
+Bars: FP64 plain within 1e-10 relative (tol * (1 + max|a|,|b|)) of the
 reference's values; FP32 bulk within 1e-5 eV/A on forces and 1e-6 eV/atom on energy of the FP64
 oracle; exact edge sets; deterministic results.
 """
@@ -106,6 +106,40 @@ def test_large_static_box_cell_list_matches_oracle(lib, oracle_lib, golden):
     assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
     e32, f32, v32, s32 = g32.calc_efs([fr])
     check_fp32(e32[0], f32, eo, fo, fr.natoms)
+
+
+def test_cell_list_capacity_overflow_is_retried(lib, oracle_lib, golden):
+    """A dense cluster in a mostly empty box: ~170 neighbours per atom on average (~300 inside)
+    against a padded capacity estimated from the box's mean density (~93), so the first build
+    overflows; the step is repeated with a grown capacity and matches the oracle, through both
+    entry points."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    rng = np.random.default_rng(8)
+    grid = np.stack(np.meshgrid(*[np.arange(9)] * 3, indexing="ij"), -1).reshape(-1, 3) * 1.2
+    pos = grid + 2.0 + rng.normal(0, 0.03, grid.shape)
+    fr = Frame(np.eye(3) * 30.0, pos, np.zeros(len(pos), dtype=np.int32))
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+    assert ne > 150 * fr.natoms  # mean density x 4/3 pi rc^3 is 14, capacity 2 x 14 + 64
+    e, f, v, s = g64.calc_efs([fr])
+    assert g64.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
+    # device entry point on a fresh engine (overflow found by the step's final check)
+    import torch
+    g64b = lib.Engine(m, 0, lib.FP64)
+    dev = torch.device("cuda", 0)
+    p = torch.tensor(fr.positions, device=dev)
+    t = torch.tensor(fr.types, device=dev)
+    E = torch.zeros(1, dtype=torch.float64, device=dev)
+    F = torch.zeros(fr.natoms, 3, dtype=torch.float64, device=dev)
+    V = torch.zeros(1, 6, dtype=torch.float64, device=dev)
+    g64b.calc_efs_device(np.array([fr.natoms], np.int32), fr.cell.reshape(1, 9), p.data_ptr(), t.data_ptr(),
+                         E.data_ptr(), F.data_ptr(), V.data_ptr(), 0)
+    torch.cuda.synchronize()
+    assert g64b.edge_count() == ne
+    assert rel_err(float(E[0]), eo) < FP64_TOL and rel_err(F.cpu().numpy(), fo) < FP64_TOL
+    assert rel_err(V.cpu().numpy()[0], vo) < FP64_TOL
 
 
 def test_triclinic_cell(lib, oracle_lib, golden):
