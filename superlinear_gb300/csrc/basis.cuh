@@ -26,12 +26,16 @@
 
 namespace sus2g {
 
-// N_lm (times sqrt 2 for m > 0), index l*l + l + m for m >= 0.  Each translation unit that
-// includes this header owns a copy and fills it once per device through sph_norm_upload().
+// N_lm (times sqrt 2 for m > 0), index l*l + l + m for m >= 0, in FP64 and rounded to FP32 (the
+// FP32 form reads its own table: converting the FP64 entries at run time would occupy the FP64
+// pipe, 1/64 of the FP32 rate on this GPU).  Each translation unit that includes this header owns
+// a copy and fills it once per device through sph_norm_upload().
 static __constant__ double c_sph_norm[64];
+static __constant__ float c_sph_norm_f[64];
 
 static inline cudaError_t sph_norm_upload() {
   double n[64] = {0};
+  float nf[64] = {0};
   const double pi = 3.14159265358979323846;
   for (int l = 0; l <= 6; ++l)
     for (int m = 0; m <= l; ++m) {
@@ -39,17 +43,46 @@ static inline cudaError_t sph_norm_upload() {
       for (int a = l - m + 1; a <= l + m; ++a) ratio /= a;
       n[l * l + l + m] = std::sqrt((2 * l + 1) * ratio / (4 * pi)) * (m ? std::sqrt(2.0) : 1.0);
     }
-  return cudaMemcpyToSymbol(c_sph_norm, n, sizeof(n));
+  for (int q = 0; q < 64; ++q) nf[q] = static_cast<float>(n[q]);
+  cudaError_t err = cudaMemcpyToSymbol(c_sph_norm, n, sizeof(n));
+  if (err != cudaSuccess) return err;
+  return cudaMemcpyToSymbol(c_sph_norm_f, nf, sizeof(nf));
 }
 
 template <int L> struct Sph { static constexpr int Lp = L + 1, H = Lp * Lp; };
 
 __host__ __device__ constexpr int sh_index(int l, int m) { return l * l + l + m; }
-__host__ __device__ constexpr double dfact_odd(int m) {  // (2m-1)!!
-  return m <= 0 ? 1.0 : (2.0 * m - 1.0) * dfact_odd(m - 1);
+
+// (2m-1)!! and 1/n as literals of type T: with the unrolled (l, m) loops the argument is a
+// compile-time value and these fold to immediates (a constexpr double recursion would be
+// evaluated at run time in FP64).
+template <typename T>
+__device__ __forceinline__ T sph_dfact(int m) {
+  switch (m) {
+    case 0: case 1: return T(1);
+    case 2: return T(3);
+    case 3: return T(15);
+    case 4: return T(105);
+    case 5: return T(945);
+    case 6: return T(10395);
+    default: return T(135135);
+  }
+}
+template <typename T>
+__device__ __forceinline__ T sph_inv(int n) {
+  switch (n) {
+    case 1: return T(1);
+    case 2: return T(0.5);
+    case 3: return T(0.33333333333333333333);
+    case 4: return T(0.25);
+    case 5: return T(0.2);
+    case 6: return T(0.16666666666666666667);
+    default: return T(0.14285714285714285714);
+  }
 }
 
 template <typename T> __device__ __forceinline__ T norm_lm(int idx) { return T(c_sph_norm[idx]); }
+template <> __device__ __forceinline__ float norm_lm<float>(int idx) { return c_sph_norm_f[idx]; }
 
 // Values Y[h] for h < (L+1)^2 at unit vector (ux, uy, uz).
 template <int L, typename T>
@@ -63,13 +96,13 @@ __device__ __forceinline__ void sph_values(T ux, T uy, T uz, T* Y) {
   }
 #pragma unroll
   for (int m = 0; m <= L; ++m) {
-    T p2 = T(0), p1 = T(0), p0 = T(dfact_odd(m));
+    T p2 = T(0), p1 = T(0), p0 = sph_dfact<T>(m);
 #pragma unroll
     for (int l = m; l <= L; ++l) {
       T p;
       if (l == m) p = p0;
       else if (l == m + 1) p = T(2 * m + 1) * uz * p0;
-      else p = (T(2 * l - 1) * uz * p1 - T(l + m - 1) * p2) * T(1.0 / double(l - m));
+      else p = (T(2 * l - 1) * uz * p1 - T(l + m - 1) * p2) * sph_inv<T>(l - m);
       if (l == m) { p1 = p; }
       else { p2 = p1; p1 = p; }
       const T n = norm_lm<T>(sh_index(l, m)) * p;
@@ -95,7 +128,7 @@ __device__ __forceinline__ void sph_grad_dot(T ux, T uy, T uz, const T* P, T& gx
   }
 #pragma unroll
   for (int m = 0; m <= L; ++m) {
-    const T pmm = T(dfact_odd(m));
+    const T pmm = sph_dfact<T>(m);
     T p1 = T(0), p2 = T(0), d1 = T(0), d2 = T(0);
 #pragma unroll
     for (int l = m; l <= L; ++l) {
@@ -103,7 +136,7 @@ __device__ __forceinline__ void sph_grad_dot(T ux, T uy, T uz, const T* P, T& gx
       if (l == m) { p = pmm; d = T(0); }
       else if (l == m + 1) { p = T(2 * m + 1) * uz * pmm; d = T(2 * m + 1) * pmm; }
       else {
-        const T inv = T(1.0 / double(l - m));
+        const T inv = sph_inv<T>(l - m);
         p = (T(2 * l - 1) * uz * p1 - T(l + m - 1) * p2) * inv;
         d = (T(2 * l - 1) * (p1 + uz * d1) - T(l + m - 1) * d2) * inv;
       }
@@ -136,7 +169,7 @@ __device__ __forceinline__ void sph_tangent(T ux, T uy, T uz, T tx, T ty, T tz, 
   }
 #pragma unroll
   for (int m = 0; m <= L; ++m) {
-    const T pmm = T(dfact_odd(m));
+    const T pmm = sph_dfact<T>(m);
     T p1 = T(0), p2 = T(0), d1 = T(0), d2 = T(0);
 #pragma unroll
     for (int l = m; l <= L; ++l) {
@@ -144,7 +177,7 @@ __device__ __forceinline__ void sph_tangent(T ux, T uy, T uz, T tx, T ty, T tz, 
       if (l == m) { p = pmm; d = T(0); }
       else if (l == m + 1) { p = T(2 * m + 1) * uz * pmm; d = T(2 * m + 1) * pmm; }
       else {
-        const T inv = T(1.0 / double(l - m));
+        const T inv = sph_inv<T>(l - m);
         p = (T(2 * l - 1) * uz * p1 - T(l + m - 1) * p2) * inv;
         d = (T(2 * l - 1) * (p1 + uz * d1) - T(l + m - 1) * d2) * inv;
       }

@@ -170,12 +170,17 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
 
 // Sort one centre's edges by key into CSR order (warp per centre, rank sort; keys within a centre
 // are unique).  Cell-list centres read their padded staging slots, the others their CSR range of
-// the staging buffers (plans may be null when no frame uses cell lists).
+// the staging buffers (plans may be null when no frame uses cell lists).  Keys of centres with at
+// most `stage` edges are staged in shared memory (the rank loop then reads broadcast shared
+// memory); longer lists rank from global memory.
+constexpr int kSortWarps = 8;
 template <typename Real>
-__global__ void k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame_of,
-                            const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
-                            const unsigned long long* pkey, const int* pnbr, const typename Vec4<Real>::type* pd4,
-                            unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
+__global__ void __launch_bounds__(kSortWarps * kWarp)
+k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame_of, int stage,
+            const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
+            const unsigned long long* pkey, const int* pnbr, const typename Vec4<Real>::type* pd4,
+            unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
+  extern __shared__ unsigned long long sort_keys[];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
@@ -191,41 +196,45 @@ __global__ void k_edge_sort(const int* row, int natoms, const FramePlan* plans, 
       K = pkey; NB = pnbr; D = pd4;
     }
   }
+  const unsigned long long* src = K + in0;
+  if (n <= stage) {
+    unsigned long long* sk = sort_keys + (threadIdx.x / kWarp) * stage;
+    for (int q = lane; q < n; q += kWarp) sk[q] = src[q];
+    __syncwarp();
+    src = sk;
+  }
   for (int q = lane; q < n; q += kWarp) {
-    const unsigned long long k = K[in0 + q];
+    const unsigned long long k = src[q];
     int rank = 0;
-    for (int t = 0; t < n; ++t) rank += K[in0 + t] < k;
+    for (int t = 0; t < n; ++t) rank += src[t] < k;
     key_out[e0 + rank] = k;
     nbr_out[e0 + rank] = NB[in0 + q];
     d4_out[e0 + rank] = D[in0 + q];
   }
 }
 
-__global__ void k_reverse(const int* row, const int* nbr, const unsigned long long* key, long long nedges, int* rev,
-                          int natoms, int* error) {
-  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  // nedges bounds the launch; the exact total is row[natoms] on the device
-  if (e >= nedges || e >= row[natoms]) return;
-  // centre of e: binary search in row
-  int lo = 0, hi = natoms;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (row[mid] <= e) lo = mid; else hi = mid;
+// Reverse edge of every edge (warp per centre i): for e = (i -> j, n) the edge (j -> i, -n) is
+// found by binary search in j's sorted keys.
+__global__ void k_reverse(const int* row, const unsigned long long* key, int natoms, int* rev, int* error) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x & 31;
+  if (i >= natoms) return;
+  for (int e = row[i] + lane; e < row[i + 1]; e += kWarp) {
+    const unsigned long long k = key[e];
+    const int j = static_cast<int>(k >> 21);
+    const int n0 = static_cast<int>((k >> 14) & 127) - 64, n1 = static_cast<int>((k >> 7) & 127) - 64,
+              n2 = static_cast<int>(k & 127) - 64;
+    const unsigned long long want = edge_key(i, -n0, -n1, -n2);
+    int lo = row[j], hi = row[j + 1] - 1, found = -1;
+    while (lo <= hi) {
+      const int mid = (lo + hi) >> 1;
+      const unsigned long long km = key[mid];
+      if (km == want) { found = mid; break; }
+      if (km < want) lo = mid + 1; else hi = mid - 1;
+    }
+    if (found < 0) record_error(error, kErrReverseEdge);
+    rev[e] = found < 0 ? e : found;
   }
-  const int i = lo, j = nbr[e];
-  const unsigned long long k = key[e];
-  const int n0 = static_cast<int>((k >> 14) & 127) - 64, n1 = static_cast<int>((k >> 7) & 127) - 64,
-            n2 = static_cast<int>(k & 127) - 64;
-  const unsigned long long want = edge_key(i, -n0, -n1, -n2);
-  int a = row[j], b = row[j + 1] - 1, found = -1;
-  while (a <= b) {
-    const int mid = (a + b) >> 1;
-    const unsigned long long km = key[mid];
-    if (km == want) { found = mid; break; }
-    if (km < want) a = mid + 1; else b = mid - 1;
-  }
-  if (found < 0) record_error(error, kErrReverseEdge);
-  rev[e] = found < 0 ? static_cast<int>(e) : found;
 }
 
 // F_i = sum over i's edges of (g_e - g_rev(e)), warp per atom: FP64 accumulation for FP64 edge
@@ -924,18 +933,24 @@ void Engine::finalize_edges() {
   cudaStream_t s = stream_;
   const int a = ncentres_;
   if (a) {
-    const int blocks = (a * kWarp + 255) / 256;
+    const int blocks = (a + kSortWarps - 1) / kSortWarps;
     const FramePlan* P = sort_from_pad_ ? plan_.as<FramePlan>() : nullptr;
+    // shared-memory key staging up to the largest padded capacity (at most 512 keys per warp)
+    int stage = 0;
+    if (sort_from_pad_)
+      for (const FramePlan& fp : *plans_) stage = std::max(stage, fp.use_bins ? fp.cap : 0);
+    stage = std::min(stage, 512);
+    const size_t smem = sizeof(unsigned long long) * kSortWarps * stage;
     if (precision_ == kFP32)
-      k_edge_sort<float><<<blocks, 256, 0, s>>>(row_.as<int>(), a, P, frame_of_.as<int>(), tmp_key_.as<unsigned long long>(),
-                                                tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(),
-                                                pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), key_.as<unsigned long long>(),
-                                                nbr_.as<int>(), d4_.as<EdgeF>());
+      k_edge_sort<float><<<blocks, kSortWarps * kWarp, smem, s>>>(
+          row_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+          tmp_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+          key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeF>());
     else
-      k_edge_sort<double><<<blocks, 256, 0, s>>>(row_.as<int>(), a, P, frame_of_.as<int>(), tmp_key_.as<unsigned long long>(),
-                                                 tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(),
-                                                 pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), key_.as<unsigned long long>(),
-                                                 nbr_.as<int>(), d4_.as<EdgeD>());
+      k_edge_sort<double><<<blocks, kSortWarps * kWarp, smem, s>>>(
+          row_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+          tmp_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+          key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
     ++launches_;
   }
   if (nedges_ && user_edges_) {
@@ -943,9 +958,9 @@ void Engine::finalize_edges() {
     ei_.ensure(sizeof(int) * nedges_);
     k_centre_of_edge<<<a, 128, 0, s>>>(row_.as<int>(), a, ei_.as<int>());
     launches_ += 2;
-  } else if (nedges_) {
-    k_reverse<<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(row_.as<int>(), nbr_.as<int>(), key_.as<unsigned long long>(),
-                                                                           nedges_, rev_.as<int>(), a, error_.as<int>());
+  } else if (nedges_ && a) {
+    k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, s>>>(
+        row_.as<int>(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
     ++launches_;
   }
 }
