@@ -171,9 +171,11 @@ __device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const R
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
 constexpr int kPassWarps = 4;
+// Minimum resident blocks per SM: 4 (<= 128 registers) where the FP32 kernels fit without
+// spilling (L <= 3), 3 otherwise (measured: the FP64 kernels and L >= 4 run faster at 3).
 
 template <int L, typename Real, int MODE, bool KAHAN, int BF>
-__global__ void __launch_bounds__(kPassWarps * kWarp, 3) atom_pass_kernel(PassArgs<Real> a) {
+__global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) == 4) ? 4 : 3) atom_pass_kernel(PassArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;
