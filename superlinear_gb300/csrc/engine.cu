@@ -1103,12 +1103,30 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
 }
 
 namespace {
-// grad[p] += sum over gradient slices (fixed order).
-__global__ void k_slot_reduce(const double* slots, int nslots, int nparams, double* grad) {
+// grad[p] += sum over gradient slices, in two fixed-order levels: block (x, c) sums slices
+// c, c + G, c + 2G, ... (G = gridDim.y) of parameters 32 x .. 32 x + 31 in 8 interleaved lanes
+// per parameter, combined in shared memory in lane order, into part[c][p]; k_slot_finish adds
+// the G partials in order.
+constexpr int kSlotGroups = 32;
+__global__ void k_slot_partial(const double* slots, int nslots, int nparams, double* part) {
+  __shared__ double sh[8][33];
+  const int p = blockIdx.x * 32 + threadIdx.x, g = threadIdx.y, c = blockIdx.y, G = gridDim.y;
+  double s = 0.0;
+  if (p < nparams)
+    for (int w = c + G * g; w < nslots; w += 8 * G) s += slots[static_cast<size_t>(w) * nparams + p];
+  sh[g][threadIdx.x] = s;
+  __syncthreads();
+  if (g == 0 && p < nparams) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += sh[q][threadIdx.x];
+    part[static_cast<size_t>(c) * nparams + p] = t;
+  }
+}
+__global__ void k_slot_finish(const double* part, int groups, int nparams, double* grad) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nparams) return;
   double s = 0.0;
-  for (int w = 0; w < nslots; ++w) s += slots[static_cast<size_t>(w) * nparams + p];
+  for (int c = 0; c < groups; ++c) s += part[static_cast<size_t>(c) * nparams + p];
   grad[p] += s;
 }
 
@@ -1231,8 +1249,11 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
   } else {
     launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co, s);
   }
-  k_slot_reduce<<<(P + 255) / 256, 256, 0, s>>>(slots_.as<double>(), nslots, P, grad);
-  ++launches_;
+  slot_part_.ensure(sizeof(double) * kSlotGroups * static_cast<size_t>(P));
+  k_slot_partial<<<dim3((P + 31) / 32, kSlotGroups), dim3(32, 8), 0, s>>>(slots_.as<double>(), nslots, P,
+                                                                         slot_part_.as<double>());
+  k_slot_finish<<<(P + 255) / 256, 256, 0, s>>>(slot_part_.as<double>(), kSlotGroups, P, grad);
+  launches_ += 2;
 }
 
 void Engine::combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad) {

@@ -107,7 +107,7 @@ class Engine {
   template <typename Real> void upload_tables();
   template <typename Real> void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
   template <typename Real> void run_grad(const double* ew, const double* fw, const double* sw, double* grad);
-  DevBuf slots_, hsigd_, gmomd_, lhm_, lh_atom_;
+  DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;
   void finalize_edges();
 
   Model model_;
