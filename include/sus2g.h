@@ -96,6 +96,32 @@ int sus2g_efs_edges_host(sus2g_engine engine, int nowned, int nall, const int* t
                          const int* ei, const int* ej, const double* d, double* energy, double* site_energy,
                          double* forces, double* virial);
 
+/* ---- staged evaluation with a caller halo exchange (multi-domain pair_style sus2/embedded) -------
+ * Replaces SUS2SL::Kernel::begin / pack_forward / unpack_forward / outer / pack_reverse /
+ * add_reverse / finish (sus2_sl_kernel.h:36-42, sus2_sl_kernel.cpp:381-562) as driven by
+ * PairSUS2Embedded::compute and its comm callbacks (pair_sus2_embedded.cpp:289-298, 327-374):
+ *   begin         caller edges of the owned centres (as in sus2g_efs_edges_host) + the Effect gate
+ *                 pass of the owned atoms;
+ *   forward comm  pack_forward(owned atoms by index) -> caller -> unpack_forward(ghost rows
+ *                 first .. first + n - 1): the gate signal h, comm_width doubles per atom;
+ *   outer         the outer (or Static) pass;
+ *   reverse comm  pack_reverse(ghost rows first ..) -> caller -> add_reverse(owned atoms by index):
+ *                 the gate-signal adjoint, comm_width doubles per atom;
+ *   finish        gate reverse pass; energy (owned site energies), site_energy[nowned],
+ *                 forces[3 * nall] (ghost contributions included, for the caller's force reverse
+ *                 communication), virial[6].
+ * comm_width is 0 for Static models (the exchanges are then empty).  All buffers are host memory;
+ * the calls are synchronous.  Results are deterministic (no floating-point atomics). */
+int sus2g_engine_comm_width(sus2g_engine engine, int* width);
+int sus2g_stage_begin(sus2g_engine engine, int nowned, int nall, const int* types, int nedges, const int* ei,
+                      const int* ej, const double* d);
+int sus2g_stage_pack_forward(sus2g_engine engine, int n, const int* atoms, double* buf);
+int sus2g_stage_unpack_forward(sus2g_engine engine, int n, int first, const double* buf);
+int sus2g_stage_outer(sus2g_engine engine);
+int sus2g_stage_pack_reverse(sus2g_engine engine, int n, int first, double* buf);
+int sus2g_stage_add_reverse(sus2g_engine engine, int n, const int* atoms, const double* buf);
+int sus2g_stage_finish(sus2g_engine engine, double* energy, double* site_energy, double* forces, double* virial);
+
 /* ---- parameter gradient (trainer contract) ------------------------------------------------------
  * Replaces AnyLocalMLIP::AccumulateEFSCombinationGrad (src/basic_mlip.cpp:421-476) and
  * MLMTPR::AccumulateEFSCombinationGrad (dev_src/mtpr.cpp:9188) for a batch of periodic frames:

@@ -42,6 +42,14 @@ SIGNATURES = {
     "sus2g_efs_combination_grad_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
     "sus2g_static_efs_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                                 ctypes.c_longlong, _vp, _vp, _vp, _vp]),
+    "sus2g_engine_comm_width": (ctypes.c_int, [_vp, _ip]),
+    "sus2g_stage_begin": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp]),
+    "sus2g_stage_pack_forward": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp]),
+    "sus2g_stage_unpack_forward": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    "sus2g_stage_outer": (ctypes.c_int, [_vp]),
+    "sus2g_stage_pack_reverse": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    "sus2g_stage_add_reverse": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp]),
+    "sus2g_stage_finish": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "sus2g_trainer_create": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _ip,
                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                             ctypes.c_int, ctypes.POINTER(_vp)]),

@@ -251,6 +251,131 @@ int sus2g_efs_combination_grad_host(sus2g_engine e, int nframes, const int* nato
   });
 }
 
+// Staged evaluation: device staging slots -- 0 types (held from begin to finish), 1..3 edge input
+// at begin and outputs at finish, 4 atom indices and 5 row buffers of the exchanges.
+namespace {
+void check_edges(sus2g::Engine& eng, int nowned, int nall, const int* types, int nedges, const int* ei, const int* ej,
+                 const double* d) {
+  need(nowned >= 0 && nall >= nowned && nedges >= 0, "engine/layout");
+  need(nall == 0 || types, "types");
+  need(nedges == 0 || (ei && ej && d), "edges");
+  for (int i = 0; i < nall; ++i) need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
+  for (long long q = 0; q < nedges; ++q) {
+    need(ei[q] >= 0 && ei[q] < nowned && ej[q] >= 0 && ej[q] < nall, "edge atom index out of range");
+    const double r2 = d[3 * q] * d[3 * q] + d[3 * q + 1] * d[3 * q + 1] + d[3 * q + 2] * d[3 * q + 2];
+    need(r2 > 0 && r2 < 1e300, "edge with zero or non-finite length");
+  }
+}
+
+void stage_rows_host(sus2g_engine e, int which, int op, int n, const int* atoms, int first, double* buf) {
+  need(e && n >= 0 && (n == 0 || buf), "engine/rows");
+  auto& eng = *e->engine;
+  const int W = eng.comm_width();
+  if (n == 0 || W == 0) return;
+  if (atoms)
+    for (int k = 0; k < n; ++k) need(atoms[k] >= 0 && atoms[k] < eng.natoms(), "exchange atom index out of range");
+  // add_reverse may name one owner several times (its periodic images are distinct ghosts): rows of
+  // the same atom are summed here in call order, so each atom is updated once on the device
+  std::vector<int> uniq;
+  std::vector<double> summed;
+  if (which == 1 && op == 1 && atoms) {
+    std::vector<int> slot_of(eng.natoms(), -1);
+    for (int k = 0; k < n; ++k) {
+      int& q = slot_of[atoms[k]];
+      if (q < 0) {
+        q = static_cast<int>(uniq.size());
+        uniq.push_back(atoms[k]);
+        summed.insert(summed.end(), buf + static_cast<size_t>(k) * W, buf + static_cast<size_t>(k + 1) * W);
+      } else {
+        for (int w = 0; w < W; ++w) summed[static_cast<size_t>(q) * W + w] += buf[static_cast<size_t>(k) * W + w];
+      }
+    }
+    n = static_cast<int>(uniq.size());
+    atoms = uniq.data();
+    buf = summed.data();
+  }
+  cudaStream_t s = eng.stream();
+  cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+  Slot idx(eng, 4, sizeof(int) * n), rows(eng, 5, sizeof(double) * static_cast<size_t>(n) * W);
+  if (atoms) cuda(cudaMemcpyAsync(idx.p, atoms, sizeof(int) * n, cudaMemcpyHostToDevice, s), "index copy");
+  if (op == 1) cuda(cudaMemcpyAsync(rows.p, buf, sizeof(double) * n * W, cudaMemcpyHostToDevice, s), "row copy");
+  eng.stage_rows(which, op, n, atoms ? idx.as<int>() : nullptr, first, rows.as<double>());
+  if (op == 0) cuda(cudaMemcpyAsync(buf, rows.p, sizeof(double) * n * W, cudaMemcpyDeviceToHost, s), "row copy");
+  eng.check_device_error();
+}
+}  // namespace
+
+int sus2g_engine_comm_width(sus2g_engine e, int* width) {
+  return guarded([&] { need(e && width, "engine/width"); *width = e->engine->comm_width(); });
+}
+
+int sus2g_stage_begin(sus2g_engine e, int nowned, int nall, const int* types, int nedges, const int* ei,
+                      const int* ej, const double* d) {
+  return guarded([&] {
+    need(e, "engine");
+    auto& eng = *e->engine;
+    check_edges(eng, nowned, nall, types, nedges, ei, ej, d);
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Slot typ(eng, 0, sizeof(int) * nall), di(eng, 1, sizeof(int) * nedges), dj(eng, 2, sizeof(int) * nedges),
+        dd(eng, 3, sizeof(double) * 3 * nedges);
+    if (nall) cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * nall, cudaMemcpyHostToDevice, s), "types copy");
+    if (nedges) {
+      cuda(cudaMemcpyAsync(di.p, ei, sizeof(int) * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+      cuda(cudaMemcpyAsync(dj.p, ej, sizeof(int) * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+      cuda(cudaMemcpyAsync(dd.p, d, sizeof(double) * 3 * nedges, cudaMemcpyHostToDevice, s), "edge copy");
+    }
+    eng.stage_begin(nowned, nall, typ.as<int>(), nedges, di.as<int>(), dj.as<int>(), dd.as<double>());
+    eng.check_device_error();
+  });
+}
+
+int sus2g_stage_pack_forward(sus2g_engine e, int n, const int* atoms, double* buf) {
+  return guarded([&] { need(n == 0 || atoms, "atoms"); stage_rows_host(e, 0, 0, n, atoms, 0, buf); });
+}
+
+int sus2g_stage_unpack_forward(sus2g_engine e, int n, int first, const double* buf) {
+  return guarded([&] { stage_rows_host(e, 0, 1, n, nullptr, first, const_cast<double*>(buf)); });
+}
+
+int sus2g_stage_outer(sus2g_engine e) {
+  return guarded([&] {
+    need(e, "engine");
+    e->engine->stage_outer();
+    e->engine->check_device_error();
+  });
+}
+
+int sus2g_stage_pack_reverse(sus2g_engine e, int n, int first, double* buf) {
+  return guarded([&] { stage_rows_host(e, 1, 0, n, nullptr, first, buf); });
+}
+
+int sus2g_stage_add_reverse(sus2g_engine e, int n, const int* atoms, const double* buf) {
+  return guarded([&] { need(n == 0 || atoms, "atoms"); stage_rows_host(e, 1, 1, n, atoms, 0, const_cast<double*>(buf)); });
+}
+
+int sus2g_stage_finish(sus2g_engine e, double* energy, double* site_energy, double* forces, double* virial) {
+  return guarded([&] {
+    need(e, "engine");
+    auto& eng = *e->engine;
+    const int nall = eng.natoms(), nowned = eng.ncentres();
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Slot ev(eng, 1, sizeof(double) * 7), out_f(eng, 2, sizeof(double) * 3 * std::max(1, nall)),
+        out_s(eng, 3, sizeof(double) * std::max(1, nowned));
+    eng.stage_finish(ev.as<double>(), forces ? out_f.as<double>() : nullptr, ev.as<double>() + 1,
+                     site_energy ? out_s.as<double>() : nullptr);
+    eng.check_device_error();
+    double h[7];
+    cuda(cudaMemcpyAsync(h, ev.p, sizeof(h), cudaMemcpyDeviceToHost, s), "energy copy");
+    if (forces && nall) cuda(cudaMemcpyAsync(forces, out_f.p, sizeof(double) * 3 * nall, cudaMemcpyDeviceToHost, s), "force copy");
+    if (site_energy && nowned) cuda(cudaMemcpyAsync(site_energy, out_s.p, sizeof(double) * nowned, cudaMemcpyDeviceToHost, s), "site copy");
+    cuda(cudaStreamSynchronize(s), "stream synchronize");
+    if (energy) *energy = h[0];
+    if (virial) std::memcpy(virial, h + 1, sizeof(double) * 6);
+  });
+}
+
 int sus2g_efs_edges_host(sus2g_engine e, int nowned, int nall, const int* types, int nedges, const int* ei,
                          const int* ej, const double* d, double* energy, double* site_energy, double* forces,
                          double* virial) {

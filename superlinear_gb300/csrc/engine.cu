@@ -262,33 +262,92 @@ __global__ void k_force_gather(const int* row, const int* rev, const Real* g, in
     for (int c = 0; c < 3; ++c) force[3 * (size_t)warp + c] = f[c];
 }
 
-// Caller-supplied edges: F_i += g_e, F_j -= g_e with FP64 atomics (forces zeroed beforehand).
-template <typename Real>
-__global__ void k_force_scatter(const int* ei, const int* nbr, const Real* g, long long n, double* force) {
+
+// Caller edges: incoming lists.  in(j) = the edges whose neighbour is j, sorted by edge index, so
+// that per-atom sums over them run in a fixed order (no floating-point atomics).
+__global__ void k_count_in(const int* nbr, long long n, int* counts) {
+  const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < n) atomicAdd(counts + nbr[e], 1);
+}
+__global__ void k_fill_in(const int* nbr, long long n, const int* in_row, int* cursor, int* in_tmp) {
   const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  const int i = ei[e], j = nbr[e];
-  for (int c = 0; c < 3; ++c) {
-    const double v = double(g[3 * e + c]);
-    atomicAdd(force + 3 * (size_t)i + c, v);
-    atomicAdd(force + 3 * (size_t)j + c, -v);
+  const int j = nbr[e];
+  in_tmp[in_row[j] + atomicAdd(cursor + j, 1)] = static_cast<int>(e);
+}
+// warp per atom: rank sort of the (unique) edge indices of in(j)
+__global__ void k_sort_in(const int* in_row, int nall, const int* in_tmp, int* in_edge) {
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x & 31;
+  if (j >= nall) return;
+  const int b = in_row[j], n = in_row[j + 1] - b;
+  for (int q = lane; q < n; q += kWarp) {
+    const int x = in_tmp[b + q];
+    int rank = 0;
+    for (int t = 0; t < n; ++t) rank += in_tmp[b + t] < x;
+    in_edge[b + rank] = x;
   }
 }
 
-// Caller-supplied edges: hbar_j[mu] += per-edge contribution (stored at the edge itself).
+// hbar[j][mu] = sum over in(j), in edge order, of the per-edge contributions hc[e][mu]
+// (compensated FP32 for FP32 contributions, FP64 result).
 template <typename Real>
-__global__ void k_hbar_scatter(const int* nbr, const Real* hc, long long n, int F, double* hbar) {
+__global__ void k_hbar_gather(const int* in_row, const int* in_edge, const Real* hc, int nall, int F, double* hbar) {
   const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= n * F) return;
-  const long long e = t / F;
-  const int mu = static_cast<int>(t - e * F);
-  atomicAdd(hbar + (size_t)nbr[e] * F + mu, double(hc[t]));
+  if (t >= static_cast<long long>(nall) * F) return;
+  const int j = static_cast<int>(t / F), mu = static_cast<int>(t - static_cast<long long>(j) * F);
+  double acc = 0.0;
+  float hi = 0.f, lo = 0.f;
+  for (int q = in_row[j]; q < in_row[j + 1]; ++q) {
+    const Real v = hc[static_cast<size_t>(in_edge[q]) * F + mu];
+    if (sizeof(Real) == 4) csum_add(hi, lo, float(v));
+    else acc += double(v);
+  }
+  hbar[t] = sizeof(Real) == 4 ? double(hi) + double(lo) : acc;
 }
 
-__global__ void k_centre_of_edge(const int* row, int ncentres, int* ei) {
-  const int i = blockIdx.x;
-  if (i >= ncentres) return;
-  for (int e = row[i] + threadIdx.x; e < row[i + 1]; e += blockDim.x) ei[e] = i;
+// Caller edges: F_i = sum_{e in out(i)} g_e - sum_{e in in(i)} g_e for every atom (ghosts have
+// no out-edges), warp per atom, fixed order.
+template <typename Real>
+__global__ void k_force_gather_user(const int* row, int nowned, const int* in_row, const int* in_edge, const Real* g,
+                                    int nall, double* force) {
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int lane = threadIdx.x & 31;
+  if (i >= nall) return;
+  double f[3] = {0, 0, 0};
+  float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
+  auto add = [&](int e, float sign) {
+    for (int c = 0; c < 3; ++c) {
+      if (sizeof(Real) == 4) csum_add(hi[c], lo[c], sign * float(g[3 * (size_t)e + c]));
+      else f[c] += double(sign) * double(g[3 * (size_t)e + c]);
+    }
+  };
+  if (i < nowned)
+    for (int e = row[i] + lane; e < row[i + 1]; e += kWarp) add(e, 1.f);
+  for (int q = in_row[i] + lane; q < in_row[i + 1]; q += kWarp) add(in_edge[q], -1.f);
+  for (int c = 0; c < 3; ++c) f[c] = sizeof(Real) == 4 ? warp_csum(hi[c], lo[c]) : warp_sum(f[c]);
+  if (lane == 0)
+    for (int c = 0; c < 3; ++c) force[3 * (size_t)i + c] = f[c];
+}
+
+// Row pack / unpack of per-atom vectors for the caller's halo exchange: buf[k][w] = v[atom_k][w]
+// (atoms[k], or first + k when atoms is null); mode 0 copies buf into v, mode 1 adds it.
+template <typename T>
+__global__ void k_rows_pack(const T* v, int width, int n, const int* atoms, int first, double* buf) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * width) return;
+  const int k = static_cast<int>(t / width), w = static_cast<int>(t - static_cast<long long>(k) * width);
+  const int atom = atoms ? atoms[k] : first + k;
+  buf[t] = double(v[static_cast<size_t>(atom) * width + w]);
+}
+template <typename T>
+__global__ void k_rows_unpack(T* v, int width, int n, const int* atoms, int first, const double* buf, int add) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * width) return;
+  const int k = static_cast<int>(t / width), w = static_cast<int>(t - static_cast<long long>(k) * width);
+  const int atom = atoms ? atoms[k] : first + k;
+  T& dst = v[static_cast<size_t>(atom) * width + w];
+  dst = add ? T(double(dst) + buf[t]) : T(buf[t]);
 }
 
 __global__ void k_iota(int* v, long long n) {
@@ -953,11 +1012,28 @@ void Engine::finalize_edges() {
           key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
     ++launches_;
   }
-  if (nedges_ && user_edges_) {
-    k_iota<<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(rev_.as<int>(), nedges_);
-    ei_.ensure(sizeof(int) * nedges_);
-    k_centre_of_edge<<<a, 128, 0, s>>>(row_.as<int>(), a, ei_.as<int>());
-    launches_ += 2;
+  if (user_edges_) {
+    const int nall = natoms_;
+    in_row_.ensure(sizeof(int) * (nall + 1));
+    in_edge_.ensure(sizeof(int) * std::max<long long>(1, nedges_));
+    counts_.ensure(sizeof(int) * (nall + 1));
+    SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (nall + 1), s));
+    if (nedges_) {
+      const unsigned eb = static_cast<unsigned>((nedges_ + 255) / 256);
+      k_iota<<<eb, 256, 0, s>>>(rev_.as<int>(), nedges_);
+      k_count_in<<<eb, 256, 0, s>>>(nbr_.as<int>(), nedges_, counts_.as<int>());
+      launches_ += 2;
+    }
+    k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), nall, in_row_.as<int>(), error_.as<int>());
+    ++launches_;
+    if (nedges_) {
+      const unsigned eb = static_cast<unsigned>((nedges_ + 255) / 256);
+      SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (nall + 1), s));
+      k_fill_in<<<eb, 256, 0, s>>>(nbr_.as<int>(), nedges_, in_row_.as<int>(), counts_.as<int>(), tmp_nbr_.as<int>());
+      k_sort_in<<<static_cast<unsigned>((static_cast<long long>(nall) * kWarp + 255) / 256), 256, 0, s>>>(
+          in_row_.as<int>(), nall, tmp_nbr_.as<int>(), in_edge_.as<int>());
+      launches_ += 2;
+    }
   } else if (nedges_ && a) {
     k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, s>>>(
         row_.as<int>(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
@@ -1021,7 +1097,7 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
 }
 
 template <typename Real>
-void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
+void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages) {
   const Model& m = model_;
   cudaStream_t s = stream_;
   const int N = natoms_;
@@ -1029,8 +1105,6 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   g_.ensure(sizeof(Real) * 3 * E);
   site_.ensure(sizeof(double) * std::max(1, N));
   vir_atom_.ensure(sizeof(double) * 6 * std::max(1, N));
-  SUS2G_CUDA(cudaMemsetAsync(site_.ptr, 0, sizeof(double) * std::max(1, N), s));
-  SUS2G_CUDA(cudaMemsetAsync(vir_atom_.ptr, 0, sizeof(double) * 6 * std::max(1, N), s));
   PassArgs<Real> a{};
   a.dm = *static_cast<DevModel<Real>*>(dev_model_);
   a.natoms = ncentres_;
@@ -1043,63 +1117,71 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   a.site_energy = site_.as<double>();
   a.virial = vir_atom_.as<double>();
   a.error = error_.as<int>();
-  if (!m.gated) {
-    mark_begin(1);
-    launches_ += launch_atom_pass<Real>(m.L, kModeStatic, a, sm_count_, s);
-    mark_end();
-  } else {
+  if (m.gated) {
     hsig_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F);
     hcontrib_.ensure(sizeof(Real) * E * m.F);
     gmom_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.M);
     a.hsig = hsig_.as<Real>();
     a.hcontrib = hcontrib_.as<Real>();
     a.gmom = gmom_.as<Real>();
-    if (ncentres_ != natoms_) throw Error(1, "Effect models on a ghost layout need the forward gate exchange (not in this call)");
-    mark_begin(2);
-    launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
-    mark_end();
-    mark_begin(1);
-    launches_ += launch_atom_pass<Real>(m.L, kModeOuter, a, sm_count_, s);
-    mark_end();
-    if (user_edges_) {
-      hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
-      SUS2G_CUDA(cudaMemsetAsync(hbar_atom_.ptr, 0, sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F, s));
-      if (nedges_) {
-        const long long n = nedges_ * m.F;
-        k_hbar_scatter<Real><<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(nbr_.as<int>(), hcontrib_.as<Real>(), nedges_, m.F, hbar_atom_.as<double>());
-        ++launches_;
-      }
-      a.hbar_atom = hbar_atom_.as<double>();
-    }
-    mark_begin(3);
-    launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
-    mark_end();
   }
-  mark_begin(4);
-  if (d_forces && N) {
-    if (user_edges_) {
-      SUS2G_CUDA(cudaMemsetAsync(d_forces, 0, sizeof(double) * 3 * N, s));
-      if (nedges_) {
-        k_force_scatter<Real><<<static_cast<unsigned>((nedges_ + 255) / 256), 256, 0, s>>>(ei_.as<int>(), nbr_.as<int>(), g_.as<Real>(), nedges_, d_forces);
+  // stage 1: gate forward (Effect) -- gate signals of the centre atoms
+  if (stages & kStageGate) {
+    SUS2G_CUDA(cudaMemsetAsync(site_.ptr, 0, sizeof(double) * std::max(1, N), s));
+    SUS2G_CUDA(cudaMemsetAsync(vir_atom_.ptr, 0, sizeof(double) * 6 * std::max(1, N), s));
+    if (m.gated) {
+      // ghost rows (caller edges) are filled by the caller's forward exchange
+      SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
+      mark_begin(2);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
+      mark_end();
+    }
+  }
+  // stage 2: Static pass, or Effect outer pass and the gate-signal adjoint per atom
+  if (stages & kStageOuter) {
+    mark_begin(1);
+    launches_ += launch_atom_pass<Real>(m.L, m.gated ? kModeOuter : kModeStatic, a, sm_count_, s);
+    mark_end();
+    if (m.gated && user_edges_) {
+      hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
+      const long long n = static_cast<long long>(N) * m.F;
+      if (n) {
+        k_hbar_gather<Real><<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(
+            in_row_.as<int>(), in_edge_.as<int>(), hcontrib_.as<Real>(), N, m.F, hbar_atom_.as<double>());
         ++launches_;
       }
-    } else {
-      k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), rev_.as<int>(), g_.as<Real>(), ncentres_, d_forces);
+    }
+  }
+  // stage 3: Effect gate reverse, forces, per-frame energy and virial
+  if (stages & kStageFinish) {
+    if (m.gated) {
+      if (user_edges_) a.hbar_atom = hbar_atom_.as<double>();
+      mark_begin(3);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
+      mark_end();
+    }
+    mark_begin(4);
+    if (d_forces && N) {
+      if (user_edges_)
+        k_force_gather_user<Real><<<static_cast<unsigned>((static_cast<long long>(N) * kWarp + 255) / 256), 256, 0, s>>>(
+            row_.as<int>(), ncentres_, in_row_.as<int>(), in_edge_.as<int>(), g_.as<Real>(), N, d_forces);
+      else
+        k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), rev_.as<int>(), g_.as<Real>(), ncentres_, d_forces);
       ++launches_;
     }
+    if (nframes_) {
+      int largest = 0;
+      for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
+      const int S = std::max(1, std::min(64, (largest + 1023) / 1024));
+      frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
+      k_frame_partial<<<dim3(nframes_, S), 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, S, site_.as<double>(),
+                                                        vir_atom_.as<double>(), frame_partial_.as<double>());
+      k_frame_finish<<<(nframes_ + 7) / 8, dim3(8, 8), 0, s>>>(nframes_, S, frame_partial_.as<double>(), d_energy, d_virial);
+      launches_ += 2;
+    }
+    if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
+    mark_end();
   }
-  if (nframes_) {
-    int largest = 0;
-    for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
-    const int S = std::max(1, std::min(64, (largest + 1023) / 1024));
-    frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
-    k_frame_partial<<<dim3(nframes_, S), 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, S, site_.as<double>(),
-                                                      vir_atom_.as<double>(), frame_partial_.as<double>());
-    k_frame_finish<<<(nframes_ + 7) / 8, dim3(8, 8), 0, s>>>(nframes_, S, frame_partial_.as<double>(), d_energy, d_virial);
-    launches_ += 2;
-  }
-  if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
-  mark_end();
 }
 
 namespace {
@@ -1282,8 +1364,60 @@ int Engine::static_pass_external(int natoms, const int* types, const int* row, c
 
 void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
   SUS2G_CUDA(cudaSetDevice(device_));
-  if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site);
-  else run_efs<double>(d_energy, d_forces, d_virial, d_site);
+  if (model_.gated && user_edges_ && ncentres_ != natoms_)
+    throw Error(1, "Effect models on a ghost layout need the caller's gate-signal exchange: use the staged calls");
+  if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site, kStageAll);
+  else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
+}
+
+void Engine::stage_begin(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j,
+                         const double* d_d) {
+  set_edges(nowned, nall, d_types, nedges, d_i, d_j, d_d);
+  if (precision_ == kFP32) run_efs<float>(nullptr, nullptr, nullptr, nullptr, kStageGate);
+  else run_efs<double>(nullptr, nullptr, nullptr, nullptr, kStageGate);
+  staged_ = 1;
+}
+
+void Engine::stage_outer() {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (staged_ != 1) throw Error(1, "staged evaluation: outer() needs begin() first");
+  if (precision_ == kFP32) run_efs<float>(nullptr, nullptr, nullptr, nullptr, kStageOuter);
+  else run_efs<double>(nullptr, nullptr, nullptr, nullptr, kStageOuter);
+  staged_ = 2;
+}
+
+void Engine::stage_finish(double* d_energy, double* d_forces, double* d_virial, double* d_site) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (staged_ != 2) throw Error(1, "staged evaluation: finish() needs outer() first");
+  if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site, kStageFinish);
+  else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageFinish);
+  staged_ = 0;
+}
+
+void Engine::stage_rows(int which, int op, int n, const int* d_atoms, int first, double* d_buf) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (!model_.gated || n <= 0) return;
+  const int W = model_.F;
+  // forward exchange (h) between begin and outer; reverse exchange (hbar) between outer and finish
+  if (which == 0 && staged_ != 1) throw Error(1, "staged evaluation: the gate-signal exchange runs between begin() and outer()");
+  if (which == 1 && staged_ != 2) throw Error(1, "staged evaluation: the adjoint exchange runs between outer() and finish()");
+  if (!d_atoms && (first < 0 || first + n > natoms_)) throw Error(1, "staged evaluation: atom range outside the layout");
+  const long long t = static_cast<long long>(n) * W;
+  const unsigned blocks = static_cast<unsigned>((t + 255) / 256);
+  cudaStream_t s = stream_;
+  if (which == 0) {
+    if (op == 0) {
+      if (precision_ == kFP32) k_rows_pack<float><<<blocks, 256, 0, s>>>(hsig_.as<float>(), W, n, d_atoms, first, d_buf);
+      else k_rows_pack<double><<<blocks, 256, 0, s>>>(hsig_.as<double>(), W, n, d_atoms, first, d_buf);
+    } else {
+      if (precision_ == kFP32) k_rows_unpack<float><<<blocks, 256, 0, s>>>(hsig_.as<float>(), W, n, d_atoms, first, d_buf, 0);
+      else k_rows_unpack<double><<<blocks, 256, 0, s>>>(hsig_.as<double>(), W, n, d_atoms, first, d_buf, 0);
+    }
+  } else {
+    if (op == 0) k_rows_pack<double><<<blocks, 256, 0, s>>>(hbar_atom_.as<double>(), W, n, d_atoms, first, d_buf);
+    else k_rows_unpack<double><<<blocks, 256, 0, s>>>(hbar_atom_.as<double>(), W, n, d_atoms, first, d_buf, 1);
+  }
+  ++launches_;
 }
 
 }  // namespace sus2g

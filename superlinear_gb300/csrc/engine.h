@@ -63,12 +63,30 @@ class Engine {
   // [natoms]; any output may be null.
   void efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
 
+  // --- staged evaluation on caller edges (SUS2SL::Kernel begin / pack_forward / unpack_forward /
+  // outer / pack_reverse / add_reverse / finish, sus2_sl_kernel.h:36-42) ---------------------
+  // Width of the per-atom halo vectors (the Effect gate signal h and its adjoint): F, or 0.
+  int comm_width() const { return model_.gated ? model_.F : 0; }
+  // Edges + gate forward pass of the owned centres.
+  void stage_begin(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j,
+                   const double* d_d);
+  // Outer (or Static) pass; for Effect models also the per-atom gate-signal adjoint of every atom.
+  void stage_outer();
+  // Gate reverse pass, forces (all atoms, ghosts included), site energies, energy, virial.
+  void stage_finish(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  // Halo rows (device arrays): which 0 = gate signal h (between begin and outer), 1 = its adjoint
+  // (between outer and finish); op 0 packs rows into d_buf, op 1 writes (h) / adds (adjoint) them.
+  // Rows are d_atoms[k] (distinct atoms), or first + k when d_atoms is null; d_buf is
+  // [n][comm_width()] FP64.
+  void stage_rows(int which, int op, int n, const int* d_atoms, int first, double* d_buf);
+
   // Parameter gradient of  sum_i ew_i E_i + sum_e (fw_i - fw_j + sw_frame d_e) . dE/dd_e  for the
   // frames of the last build_edges (AccumulateEFSCombinationGrad).  Device arrays (double):
   // ew [N], fw [N][3], sw [nframes][9] (row-major); the result is ADDED into grad [nparams].
   void combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad);
 
   int natoms() const { return natoms_; }
+  int ncentres() const { return ncentres_; }
   int nframes() const { return nframes_; }
   // Directed edges of the last build (for cell-list-only batches read back from the device on
   // first request: the build itself does not synchronise).
@@ -105,7 +123,10 @@ class Engine {
 
  private:
   template <typename Real> void upload_tables();
-  template <typename Real> void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  enum : int { kStageGate = 1, kStageOuter = 2, kStageFinish = 4, kStageAll = 7 };
+  template <typename Real>
+  void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages);
+  int staged_ = 0;  // staged evaluation: 1 after begin, 2 after outer
   template <typename Real> void run_grad(const double* ew, const double* fw, const double* sw, double* grad);
   DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;
   void finalize_edges();
@@ -133,7 +154,7 @@ class Engine {
   DevBuf bin_count_, bin_start_, bin_atoms_, bin_cursor_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
-  DevBuf ei_, hbar_atom_, bin_of_, frac_, off_;
+  DevBuf hbar_atom_, bin_of_, frac_, off_, in_row_, in_edge_;  // in_*: caller edges grouped by neighbour
   DevBuf pad_nbr_, pad_d4_, pad_key_;  // padded single-pass staging of cell-list frames
   double cap_scale_ = 2.0;      // padded capacity = cap_scale x mean neighbour count + 64 (grows on overflow)
   bool sort_from_pad_ = false;

@@ -5,6 +5,9 @@ Mirrors the reference's call surface for this path:
   * ``Engine.calc_efs(frames)``        ~ MLMTPR::CalcEFS over a batch of periodic frames (calc-efs)
   * ``Engine.efs_edges(...)``          ~ SUS2SL::Kernel begin/outer/finish as called by
                                          PairSUS2Embedded::compute (sus2/embedded)
+  * ``Engine.stage_*`` / ``pack_*``    ~ the same with the pair style's halo exchange between the
+                                         stages (pack_forward / unpack_forward / pack_reverse /
+                                         add_reverse, pair_sus2_embedded.cpp:327-374)
 Errors raise ``Sus2Error`` with the library's message, as the reference raises on invalid input.
 """
 from __future__ import annotations
@@ -176,4 +179,51 @@ class Engine:
         v = np.zeros(6)
         check(load().sus2g_efs_edges_host(self._h, int(nowned), nall, _i(types), ei.size, _i(ei), _i(ej), _d(d),
                                           _d(e), _d(s), _d(f), _d(v)))
+        return float(e[0]), s, f, v
+
+    # -- staged evaluation with a caller halo exchange (multi-domain sus2/embedded) ---------------
+    def comm_width(self) -> int:
+        """Doubles per atom in each halo exchange (the Effect gate signal width F; 0 for Static)."""
+        w = ctypes.c_int()
+        check(load().sus2g_engine_comm_width(self._h, ctypes.byref(w)))
+        return w.value
+
+    def stage_begin(self, nowned: int, types, ei, ej, d) -> None:
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        ei = np.ascontiguousarray(ei, dtype=np.int32)
+        ej = np.ascontiguousarray(ej, dtype=np.int32)
+        d = np.ascontiguousarray(d, dtype=np.float64).reshape(-1, 3)
+        check(load().sus2g_stage_begin(self._h, int(nowned), types.size, _i(types), ei.size, _i(ei), _i(ej), _d(d)))
+
+    def pack_forward(self, atoms) -> np.ndarray:
+        atoms = np.ascontiguousarray(atoms, dtype=np.int32)
+        buf = np.zeros((atoms.size, self.comm_width()))
+        check(load().sus2g_stage_pack_forward(self._h, atoms.size, _i(atoms), _d(buf)))
+        return buf
+
+    def unpack_forward(self, first: int, buf) -> None:
+        buf = np.ascontiguousarray(buf, dtype=np.float64)
+        n = buf.shape[0] if buf.ndim == 2 else 0
+        check(load().sus2g_stage_unpack_forward(self._h, n, int(first), _d(buf)))
+
+    def stage_outer(self) -> None:
+        check(load().sus2g_stage_outer(self._h))
+
+    def pack_reverse(self, first: int, n: int) -> np.ndarray:
+        buf = np.zeros((int(n), self.comm_width()))
+        check(load().sus2g_stage_pack_reverse(self._h, int(n), int(first), _d(buf)))
+        return buf
+
+    def add_reverse(self, atoms, buf) -> None:
+        atoms = np.ascontiguousarray(atoms, dtype=np.int32)
+        buf = np.ascontiguousarray(buf, dtype=np.float64)
+        check(load().sus2g_stage_add_reverse(self._h, atoms.size, _i(atoms), _d(buf)))
+
+    def stage_finish(self, nowned: int, nall: int):
+        """(energy, site_energy[nowned], forces[nall, 3], virial[6])."""
+        e = np.zeros(1)
+        s = np.zeros(nowned)
+        f = np.zeros((nall, 3))
+        v = np.zeros(6)
+        check(load().sus2g_stage_finish(self._h, _d(e), _d(s), _d(f), _d(v)))
         return float(e[0]), s, f, v
