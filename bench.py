@@ -234,7 +234,7 @@ def bench_training(sg, torch, steps, warmup):
     losses = {}
     for prec, key, nsteps in ((sg.FP32, "fp32", steps), (sg.FP64, "fp64", max(3, steps // 4))):
         eng = sg.Engine(model, 0, prec)
-        tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS)
+        tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
         for _ in range(warmup):
             tr.loss_grad(p)
         torch.cuda.synchronize()
@@ -322,7 +322,7 @@ def run_profile_train(args):
     import superlinear_gb300 as sg
     frames = training_set(sg)
     model = sg.Model(TRAIN_MODEL)
-    tr = sg.Trainer(sg.Engine(model, 0, sg.FP32), frames, *TRAIN_WEIGHTS)
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP32), frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
     tr.set_graph(not args.no_graph)
     p = model.params()
     for _ in range(args.warmup + args.steps):

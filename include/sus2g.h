@@ -138,19 +138,23 @@ int sus2g_efs_combination_grad_host(sus2g_engine engine, int nframes, const int*
  * A trainer holds a fixed set of labelled frames resident on the engine's device (edges built
  * once) and evaluates the energy / force / stress objective with its parameter gradient:
  *   replaces NonLinearRegression::CalcObjectiveFunctionGrad (dev_src/non_linear_regression.cpp:1112)
- *   over AddLoss / AddLossGrad (:768-880, :892-1068) with the std terms, relative force weights,
- *   penalties and regularisers off, divided by the frame count K as MTPR_trainer::Train does
+ *   over AddLoss / AddLossGrad (:768-880, :892-1068) with the energy / force / stress terms and
+ *   the Effect gate-x term (std terms, relative force weights, other penalties and regularisers
+ *   off), divided by the frame count K as MTPR_trainer::Train does
  *   (dev_src/mtpr_trainer.cpp:4733-4745).
  * Frames as in sus2g_calc_efs_host (host arrays, copied once).  Labels: energy[nframes],
  * forces[3 * natoms], stress[9 * nframes] (row-major 3x3 in the virial convention of the
  * reference's Configuration::stresses); has_labels[f] bit 0 energy, bit 1 forces, bit 2 stress.
  * weighting: 0 "vibrations", 1 "structures", 2 "molecules" (NonLinearRegression::weighting).
+ * gate_x_l2: coefficient of the Effect gate-x L2 term (NonLinearRegression::AddGateXRegularization,
+ * non_linear_regression.cpp:293-320, MLMTPR::AddTwoLayerGateX2Penalty, mtpr_sh.cpp:5869; the
+ * reference's default is 1e-4, non_linear_regression.h:128); ignored for Static models.
  * The trainer keeps a reference to the engine: free the trainer before the engine. */
 typedef struct sus2g_trainer_s* sus2g_trainer;
 int sus2g_trainer_create(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
                          const double* positions, const int* types, const double* energy, const double* forces,
                          const double* stress, const int* has_labels, double wE, double wF, double wS, int weighting,
-                         int norm_by_forces, sus2g_trainer* out);
+                         int norm_by_forces, double gate_x_l2, sus2g_trainer* out);
 void sus2g_trainer_free(sus2g_trainer trainer);
 /* Loss (and, when grad != NULL, its gradient [param count], host) at params [param count, host,
  * Coeff() order].  The engine's parameters are replaced by params. */

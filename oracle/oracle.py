@@ -51,6 +51,8 @@ def lib():
                                     _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
                                ctypes.c_int]
+        L.orc_grad_gatex.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
+                                     _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -138,8 +140,9 @@ class OracleModel:
             raise RuntimeError(err.value.decode())
         return float(e[0]), f, v, s
 
-    def grad(self, cell, pos, types, ew, fw, sw) -> np.ndarray:
-        """d/dtheta of sum_i ew_i E_i + sum_e (fw_i - fw_j + sw d_e) . dE/dd_e (one frame)."""
+    def grad(self, cell, pos, types, ew, fw, sw, gate_x: float = 0.0) -> np.ndarray:
+        """d/dtheta of sum_i ew_i E_i + sum_e (fw_i - fw_j + sw d_e) . dE/dd_e (one frame); with
+        gate_x > 0 also of the Effect gate-x L2 term, whose value is left in ``self.last_penalty``."""
         cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
         types = np.ascontiguousarray(types, dtype=np.int32)
@@ -148,6 +151,13 @@ class OracleModel:
         sw = np.ascontiguousarray(sw, dtype=np.float64).reshape(9)
         g = np.zeros(self.nparams)
         err = ctypes.create_string_buffer(512)
+        if gate_x > 0.0:
+            pen = np.zeros(1)
+            if lib().orc_grad_gatex(self._h, types.size, _d(cell), _d(pos), _i(types), _d(ew), _d(fw), _d(sw),
+                                    float(gate_x), _d(g), _d(pen), err, 512):
+                raise RuntimeError(err.value.decode())
+            self.last_penalty = float(pen[0])
+            return g
         if lib().orc_grad(self._h, types.size, _d(cell), _d(pos), _i(types), _d(ew), _d(fw), _d(sw), _d(g), err, 512):
             raise RuntimeError(err.value.decode())
         return g
@@ -159,10 +169,11 @@ def virial6_to_matrix(v):
 
 
 def loss_grad(model: "OracleModel", frames, wE: float, wF: float, wS: float, weighting: str = "vibrations",
-              norm_by_forces: int = 0):
+              norm_by_forces: int = 0, gate_x_l2: float = 0.0):
     """Energy / force / stress MSE objective summed over labelled frames and its parameter gradient,
     restating NonLinearRegression::AddLoss / AddLossGrad (dev_src/non_linear_regression.cpp:768-1068)
-    with the std terms, penalties and regularisers off; the gradient goes through ``grad``."""
+    with the std terms, penalties and regularisers off, plus, when gate_x_l2 > 0, the Effect gate-x
+    L2 term (AddGateXRegularization, :293-320); the gradient goes through ``grad``."""
     d = 0.1
     loss = 0.0
     grad = np.zeros(model.nparams)
@@ -192,5 +203,7 @@ def loss_grad(model: "OracleModel", frames, wE: float, wF: float, wS: float, wei
         if we != 0 and fr.energy is not None:
             loss += we * (e - fr.energy) ** 2 * scale_fn / n
             ew = 2.0 * we * (e - fr.energy) * scale_fn / n
-        grad += model.grad(fr.cell, fr.positions, fr.types, np.full(n, ew), fw, sw)
+        grad += model.grad(fr.cell, fr.positions, fr.types, np.full(n, ew), fw, sw, gate_x=gate_x_l2)
+        if gate_x_l2 > 0.0:
+            loss += model.last_penalty
     return loss, grad

@@ -694,7 +694,14 @@ void radial_param_grad(const Model& m, const Pass& p, const EdgeEval& ev, int ti
   }
 }
 
-void gradient(const Ctx& cx, const double* ew, const double* fw, const double* sw, double* grad) {
+// gate_x > 0 adds the Effect gate-x L2 term of the reference objective for this configuration
+// (MLMTPR::AddTwoLayerGateX2Penalty, dev_src/mtpr_sh.cpp:5869-6047, default coefficient 1e-4 in
+// NonLinearRegression, non_linear_regression.h:128): P = sum over edges (i -> j) of
+// norm(t_j) sum_mu (alpha(t_j, mu) h_j[mu])^2, norm(t) = gate_x / (active types x F x edges whose
+// neighbour type is t); *penalty receives P and grad receives dP/dtheta (direct alpha part, and
+// dP/dh_j through the gate chain like the outer pass's gate-signal adjoint).
+void gradient(const Ctx& cx, const double* ew, const double* fw, const double* sw, double* grad, double gate_x = 0.0,
+              double* penalty = nullptr) {
   const Model& m = *cx.m;
   const int F = m.F, M = m.M, N = cx.n, Lp = m.L + 1;
   const Pass po = outer_pass(m), pg = gate_pass(m);
@@ -823,6 +830,24 @@ void gradient(const Ctx& cx, const double* ew, const double* fw, const double* s
     }
   }
   if (!m.gated) return;
+  if (gate_x > 0.0) {
+    vector<long long> count(m.C, 0);
+    for (size_t e = 0; e < E; ++e) ++count[cx.types[cx.edges[e].j]];
+    int active = 0;
+    for (long long c : count) active += c > 0;
+    double P = 0.0;
+    for (size_t e = 0; e < E; ++e) {
+      const int j = cx.edges[e].j, t = cx.types[j];
+      const double norm = gate_x / (double(active) * F * double(count[t]));
+      for (int mu = 0; mu < F; ++mu) {
+        const double al = m.gate_add[t * F + mu], hj = h[static_cast<size_t>(j) * F + mu], x = al * hj;
+        P += norm * x * x;
+        grad[m.o_gadd + t * F + mu] += 2.0 * norm * x * hj;
+        lh[static_cast<size_t>(j) * F + mu] += 2.0 * norm * x * al;
+      }
+    }
+    if (penalty) *penalty = P;
+  }
   // gate reverse with tangents
   for (int i = 0; i < N; ++i) {
     EdgeEval ev;
@@ -996,6 +1021,21 @@ int orc_grad(void* mp, int n, const double* cell, const double* pos, const int* 
     const Model& m = *static_cast<Model*>(mp);
     Ctx cx = make_ctx(m, n, cell, pos, types);
     gradient(cx, ew, fw, sw, grad);
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, errlen, e.what());
+    return -1;
+  }
+}
+
+int orc_grad_gatex(void* mp, int n, const double* cell, const double* pos, const int* types, const double* ew,
+                   const double* fw, const double* sw, double gate_x, double* grad, double* penalty, char* err,
+                   int errlen) {
+  try {
+    const Model& m = *static_cast<Model*>(mp);
+    Ctx cx = make_ctx(m, n, cell, pos, types);
+    *penalty = 0.0;
+    gradient(cx, ew, fw, sw, grad, gate_x, penalty);
     return 0;
   } catch (const std::exception& e) {
     set_err(err, errlen, e.what());

@@ -33,6 +33,11 @@ int orc_efs_edges(void* model, int nowned, int nall, const int* types, int nedge
  * edges of one periodic frame.  Returns 0 or -1. */
 int orc_grad(void* model, int n, const double* cell, const double* pos, const int* types, const double* ew,
              const double* fw, const double* sw, double* grad, char* err, int errlen);
+/* orc_grad plus the Effect gate-x L2 term of the reference objective with coefficient gate_x:
+ * *penalty = the term's value for this configuration, grad += its parameter gradient as well. */
+int orc_grad_gatex(void* model, int n, const double* cell, const double* pos, const int* types, const double* ew,
+                   const double* fw, const double* sw, double gate_x, double* grad, double* penalty, char* err,
+                   int errlen);
 #ifdef __cplusplus
 }
 #endif

@@ -52,7 +52,7 @@ SIGNATURES = {
     "sus2g_stage_finish": (ctypes.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "sus2g_trainer_create": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _ip,
                                             ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
-                                            ctypes.c_int, ctypes.POINTER(_vp)]),
+                                            ctypes.c_int, ctypes.c_double, ctypes.POINTER(_vp)]),
     "sus2g_trainer_free": (None, [_vp]),
     "sus2g_trainer_loss_grad": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "sus2g_trainer_set_graph": (ctypes.c_int, [_vp, ctypes.c_int]),

@@ -1267,7 +1267,8 @@ __global__ void __launch_bounds__(kGwThreads) k_gate_weight_grad(int natoms, int
 }  // namespace
 
 template <typename Real>
-void Engine::run_grad(const double* ew, const double* fw, const double* sw, double* grad) {
+void Engine::run_grad(const double* ew, const double* fw, const double* sw, double* grad,
+                      const double* extra_h) {
   const Model& m = model_;
   if (user_edges_) throw Error(1, "the parameter gradient runs on periodic frames (build_edges)");
   if (m.body_combo) throw Error(1, "the parameter gradient of mu-body-linear-combo gates is not implemented");
@@ -1287,6 +1288,7 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
   a.ew = ew;
   a.fw = fw;
   a.sw = sw;
+  a.extra_h = extra_h;
   a.error = error_.as<int>();
   const GradLaunch co = grad_pass_config<Real>(m.L, kGradOuter, dm, ncentres_, sm_count_);
   GradLaunch cf = co, cr = co;
@@ -1338,10 +1340,23 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
   launches_ += 2;
 }
 
-void Engine::combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad) {
+void Engine::combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad,
+                              const double* d_extra_h) {
   SUS2G_CUDA(cudaSetDevice(device_));
-  if (precision_ == kFP32) run_grad<float>(d_ew, d_fw, d_sw, d_grad);
-  else run_grad<double>(d_ew, d_fw, d_sw, d_grad);
+  if (precision_ == kFP32) run_grad<float>(d_ew, d_fw, d_sw, d_grad, d_extra_h);
+  else run_grad<double>(d_ew, d_fw, d_sw, d_grad, d_extra_h);
+}
+
+const void* Engine::d_gate_additive() const {
+  if (!model_.gated) return nullptr;
+  if (precision_ == kFP32) return static_cast<const DevModel<float>*>(dev_model_)->outer.wadd;
+  return static_cast<const DevModel<double>*>(dev_model_)->outer.wadd;
+}
+
+int Engine::gate_additive_offset() const {
+  if (!model_.gated) return -1;
+  if (precision_ == kFP32) return static_cast<const DevModel<float>*>(dev_model_)->grad.outer.add_off;
+  return static_cast<const DevModel<double>*>(dev_model_)->grad.outer.add_off;
 }
 
 int Engine::static_pass_external(int natoms, const int* types, const int* row, const int* nbr, const void* d4, float* g,

@@ -83,7 +83,16 @@ class Engine {
   // Parameter gradient of  sum_i ew_i E_i + sum_e (fw_i - fw_j + sw_frame d_e) . dE/dd_e  for the
   // frames of the last build_edges (AccumulateEFSCombinationGrad).  Device arrays (double):
   // ew [N], fw [N][3], sw [nframes][9] (row-major); the result is ADDED into grad [nparams].
-  void combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad);
+  // d_extra_h [N][F] (Effect, optional): further dJ/dh per atom of objective terms that depend on
+  // the gate signal h, pulled back through the gate chain with the rest.
+  void combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad,
+                        const double* d_extra_h = nullptr);
+  // Device views used by objective terms of the gate signal (Effect): h [N][F] of the last
+  // evaluation (compute precision), the gate additive factors alpha [C][F] (compute precision) and
+  // their offset in the parameter vector.
+  const void* d_gate_signal() const { return hsig_.ptr; }
+  const void* d_gate_additive() const;
+  int gate_additive_offset() const;
 
   int natoms() const { return natoms_; }
   int ncentres() const { return ncentres_; }
@@ -127,7 +136,8 @@ class Engine {
   template <typename Real>
   void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages);
   int staged_ = 0;  // staged evaluation: 1 after begin, 2 after outer
-  template <typename Real> void run_grad(const double* ew, const double* fw, const double* sw, double* grad);
+  template <typename Real>
+  void run_grad(const double* ew, const double* fw, const double* sw, double* grad, const double* extra_h);
   DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;
   void finalize_edges();
 

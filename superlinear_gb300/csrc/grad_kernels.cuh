@@ -53,6 +53,7 @@ struct GradArgs {
   Real* gmomd;             // [N][M] gate tangents
   Real* lhm;               // [E][2F] dJ/dh, dJ/dhdot contributions stored at the reverse edge
   double* lh_atom;         // [N][2F] gathered per atom (gate reverse)
+  const double* extra_h;   // [N][F] additional dJ/dh per atom (objective terms of h), or null
   double* slots;           // [warps in grid][nparams]
   int* error;
   int acc_cols;            // lane-private accumulator columns per k (0: shuffle-tree reductions)
@@ -361,8 +362,10 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
       for (int m_ = lane; m_ < 2 * F; m_ += kWarp) {
         Real s = Real(0);
         for (int e = e0; e < e1; ++e) s += a.lhm[static_cast<size_t>(e) * 2 * F + m_];
-        hb[m_] = s;
-        a.lh_atom[static_cast<size_t>(atom) * 2 * F + m_] = double(s);
+        double sd = double(s);
+        if (a.extra_h && m_ < F) sd += a.extra_h[static_cast<size_t>(atom) * F + m_];
+        hb[m_] = Real(sd);
+        a.lh_atom[static_cast<size_t>(atom) * 2 * F + m_] = sd;
       }
       for (int q = lane; q < M; q += kWarp) {
         v[q] = a.gmom[static_cast<size_t>(atom) * M + q];

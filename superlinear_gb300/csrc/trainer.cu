@@ -2,7 +2,8 @@
 // stress objective with its parameter gradient, and an FP64 BFGS on the device.
 //
 // Objective (NonLinearRegression::AddLoss / AddLossGrad, dev_src/non_linear_regression.cpp:768-1068,
-// energy / force / stress terms; std terms, penalties and regularisers off), summed over the K
+// energy / force / stress terms and the Effect gate-x L2 term; std terms, other penalties and
+// regularisers off), summed over the K
 // frames and divided by K as the trainer does (dev_src/mtpr_trainer.cpp:4736-4745):
 //   d = 0.1, a = <|F0|^2>, s = d / (d + fn a)
 //   L_F = wF' s sum |F - F0|^2            dL/dF = 2 wF' s (F - F0)       wF' = wF (/N for "structures")
@@ -42,6 +43,7 @@ struct LossConfig {
   double wE, wF, wS;
   int weighting;  // 0 vibrations, 1 structures, 2 molecules
   int norm_by_forces;
+  double gate_x_l2;  // Effect gate-x L2 coefficient (0: off)
 };
 
 // One block per frame: loss terms and derivative weights.
@@ -107,6 +109,71 @@ __global__ void k_loss(int nframes, const int* fbegin, const double* E, const do
   __syncthreads();
   dE = red[0][0];
   for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) ew[i] = dE;
+}
+
+// Effect gate-x L2 term of one frame (block per frame; MLMTPR::AddTwoLayerGateX2Penalty,
+// dev_src/mtpr_sh.cpp:5869-6047):  P_f = sum over edges (i -> j) of norm(t_j) sum_mu (alpha(t_j, mu)
+// h_j[mu])^2 with norm(t) = coeff / (active types x F x edges whose neighbour type is t).  Edges
+// are symmetric, so the edges with neighbour j number deg(j) = row[j + 1] - row[j].  Adds P_f to
+// loss_f[f]; writes dP/dh_j to extra_h[j] (the gate-chain seed) and the frame's dP/dalpha to
+// agrad[f][t F + mu]; fixed-order sums throughout.
+template <typename Real>
+__global__ void k_gatex_frame(int nframes, const int* fbegin, const int* row, const int* types, const Real* h,
+                              const Real* alpha, int C, int F, double coeff, double* extra_h, double* loss_f,
+                              double* agrad) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  const int a0 = fbegin[f], a1 = fbegin[f + 1];
+  __shared__ unsigned long long count[64];
+  __shared__ double red[256];
+  for (int t = threadIdx.x; t < C; t += blockDim.x) count[t] = 0;
+  __syncthreads();
+  for (int j = a0 + threadIdx.x; j < a1; j += blockDim.x)
+    atomicAdd(&count[types[j]], static_cast<unsigned long long>(row[j + 1] - row[j]));
+  __syncthreads();
+  int active = 0;
+  for (int t = 0; t < C; ++t) active += count[t] > 0;
+  auto weight = [&](int j) {  // deg(j) norm(t_j)
+    const int t = types[j], deg = row[j + 1] - row[j];
+    return deg > 0 ? coeff * deg / (double(active) * F * double(count[t])) : 0.0;
+  };
+  double pen = 0.0;
+  for (int j = a0 + threadIdx.x; j < a1; j += blockDim.x) {
+    const double w = weight(j);
+    const int t = types[j];
+    for (int mu = 0; mu < F; ++mu) {
+      const double al = double(alpha[t * F + mu]), x = al * double(h[static_cast<size_t>(j) * F + mu]);
+      pen += w * x * x;
+      extra_h[static_cast<size_t>(j) * F + mu] = 2.0 * w * x * al;
+    }
+  }
+  red[threadIdx.x] = pen;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) loss_f[f] += red[0];
+  for (int q = threadIdx.x; q < C * F; q += blockDim.x) {
+    const int t = q / F, mu = q - t * F;
+    const double al = double(alpha[q]);
+    double g = 0.0;
+    for (int j = a0; j < a1; ++j)
+      if (types[j] == t) {
+        const double hj = double(h[static_cast<size_t>(j) * F + mu]);
+        g += 2.0 * weight(j) * al * hj * hj;
+      }
+    agrad[static_cast<size_t>(f) * C * F + q] = g;
+  }
+}
+
+// grad[q] += sum over frames of agrad[f][q] (frame order)
+__global__ void k_gatex_alpha(int nframes, int n, const double* agrad, double* grad) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  double s = 0.0;
+  for (int f = 0; f < nframes; ++f) s += agrad[static_cast<size_t>(f) * n + q];
+  grad[q] += s;
 }
 
 // loss = sum_f loss_f / K (fixed order), grad /= K
@@ -211,6 +278,13 @@ class Trainer {
     lossf_.ensure(sizeof(double) * std::max(1, nframes));
     loss_.ensure(sizeof(double) * 8);
     grad_.ensure(sizeof(double) * nparams_);
+    const Model& m = eng_.model();
+    gatex_ = cfg_.gate_x_l2 > 0.0 && m.gated && natoms_ > 0;
+    if (gatex_) {
+      if (m.C > 64) throw Error(1, "gate-x term: more than 64 species");
+      extra_h_.ensure(sizeof(double) * static_cast<size_t>(natoms_) * m.F);
+      agrad_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, nframes)) * m.C * m.F);
+    }
     TRAIN_CUDA(cudaMallocHost(&host_scalars_, sizeof(double) * 8));
     bind_edges();
   }
@@ -249,8 +323,28 @@ class Trainer {
       k_loss<<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), E_.as<double>(), F_.as<double>(), V_.as<double>(),
                                       E0_.as<double>(), F0_.as<double>(), S0_.as<double>(), has_.as<int>(), cfg_,
                                       ew_.as<double>(), fw_.as<double>(), sw_.as<double>(), lossf_.as<double>());
+    const Model& m = eng_.model();
+    if (gatex_) {
+      if (eng_.precision() == kFP32)
+        k_gatex_frame<float><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), types_.as<int>(),
+                                                      static_cast<const float*>(eng_.d_gate_signal()),
+                                                      static_cast<const float*>(eng_.d_gate_additive()), m.C, m.F,
+                                                      cfg_.gate_x_l2, extra_h_.as<double>(), lossf_.as<double>(),
+                                                      agrad_.as<double>());
+      else
+        k_gatex_frame<double><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), types_.as<int>(),
+                                                       static_cast<const double*>(eng_.d_gate_signal()),
+                                                       static_cast<const double*>(eng_.d_gate_additive()), m.C, m.F,
+                                                       cfg_.gate_x_l2, extra_h_.as<double>(), lossf_.as<double>(),
+                                                       agrad_.as<double>());
+    }
     TRAIN_CUDA(cudaMemsetAsync(grad_.ptr, 0, sizeof(double) * nparams_, s));
-    if (natoms_) eng_.combination_grad(ew_.as<double>(), fw_.as<double>(), sw_.as<double>(), grad_.as<double>());
+    if (natoms_)
+      eng_.combination_grad(ew_.as<double>(), fw_.as<double>(), sw_.as<double>(), grad_.as<double>(),
+                            gatex_ ? extra_h_.as<double>() : nullptr);
+    if (gatex_)
+      k_gatex_alpha<<<(m.C * m.F + 255) / 256, 256, 0, s>>>(nframes_, m.C * m.F, agrad_.as<double>(),
+                                                           grad_.as<double>() + eng_.gate_additive_offset());
     k_loss_finish<<<(nparams_ + 255) / 256, 256, 0, s>>>(nframes_, lossf_.as<double>(), loss_.as<double>(),
                                                          grad_.as<double>(), nparams_);
   }
@@ -374,6 +468,8 @@ class Trainer {
   std::vector<double> cells_;
   DevBuf pos_, types_, E0_, F0_, S0_, has_, fbegin_;
   DevBuf E_, F_, V_, ew_, fw_, sw_, lossf_, loss_, grad_;
+  bool gatex_ = false;
+  DevBuf extra_h_, agrad_;  // gate-x term: dP/dh per atom, dP/dalpha per frame
   double* host_scalars_ = nullptr;
   bool use_graph_ = true;
   cudaGraph_t graph_ = nullptr;
@@ -410,7 +506,7 @@ extern "C" {
 int sus2g_trainer_create(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
                          const double* positions, const int* types, const double* energy, const double* forces,
                          const double* stress, const int* has_labels, double wE, double wF, double wS, int weighting,
-                         int norm_by_forces, sus2g_trainer* out) {
+                         int norm_by_forces, double gate_x_l2, sus2g_trainer* out) {
   return train_guarded([&] {
     if (!engine || !out || nframes < 0 || (nframes && (!natoms || !cells || !energy || !stress || !has_labels)))
       throw sus2g::Error(1, "invalid argument: trainer inputs");
@@ -423,7 +519,8 @@ int sus2g_trainer_create(sus2g_engine engine, int nframes, const int* natoms, co
     for (long long i = 0; i < n; ++i)
       if (types[i] < 0 || types[i] >= engine->engine->model().C) throw sus2g::Error(1, "atom species index out of range");
     if (weighting < 0 || weighting > 2) throw sus2g::Error(1, "weighting must be 0 (vibrations), 1 (structures) or 2 (molecules)");
-    sus2g::LossConfig cfg{wE, wF, wS, weighting, norm_by_forces};
+    if (!(gate_x_l2 >= 0.0) || !std::isfinite(gate_x_l2)) throw sus2g::Error(1, "gate_x_l2 must be finite and >= 0");
+    sus2g::LossConfig cfg{wE, wF, wS, weighting, norm_by_forces, gate_x_l2};
     auto t = std::make_unique<sus2g_trainer_s>();
     t->trainer = std::make_unique<sus2g::Trainer>(*engine->engine, nframes, natoms, cells, positions, types, energy,
                                                   forces, stress, has_labels, cfg);

@@ -7,7 +7,9 @@ Mirrors the reference trainer's objective / optimiser surface for this path:
                                      frame count as MTPR_trainer::Train does (dev_src/mtpr_trainer.cpp:4737-4745)
   * ``Trainer.bfgs(params, ...)``  ~ the dense BFGS loop of MTPR_trainer::Train over BFGS::Iterate
                                      (src/common/bfgs.cpp:251-329)
-``weighting`` takes the reference's names: "vibrations", "structures", "molecules".
+``weighting`` takes the reference's names: "vibrations", "structures", "molecules".  ``gate_x_l2``
+is the coefficient of the Effect gate-x L2 term of the reference objective (its default 1e-4,
+dev_src/non_linear_regression.h:128; ignored for Static models).
 """
 from __future__ import annotations
 
@@ -33,7 +35,7 @@ class Trainer:
     """Labelled frames (``energy``, ``forces``, ``stress`` attributes, any may be None) bound to an engine."""
 
     def __init__(self, engine: Engine, frames, wE: float = 1.0, wF: float = 0.01, wS: float = 0.001,
-                 weighting: str = "vibrations", norm_by_forces: int = 0):
+                 weighting: str = "vibrations", norm_by_forces: int = 0, gate_x_l2: float = 1e-4):
         if weighting not in WEIGHTINGS:
             raise ValueError(f"weighting must be one of {sorted(WEIGHTINGS)}")
         self.engine = engine
@@ -61,7 +63,8 @@ class Trainer:
         check(load().sus2g_trainer_create(engine._h, nf, natoms.ctypes.data_as(_ip), _d(cells), _d(pos),
                                           types.ctypes.data_as(_ip), _d(energy), _d(forces), _d(stress),
                                           has.ctypes.data_as(_ip), float(wE), float(wF), float(wS),
-                                          WEIGHTINGS[weighting], int(norm_by_forces), ctypes.byref(h)))
+                                          WEIGHTINGS[weighting], int(norm_by_forces), float(gate_x_l2),
+                                          ctypes.byref(h)))
         self._h = h
 
     def __del__(self):

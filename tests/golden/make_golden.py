@@ -202,8 +202,8 @@ def main():
                 print(name, label, "frames", len(frames), "atoms", [f.natoms for f in frames])
         # 5. labelled training sets: teacher labels (another seeded parameter vector, evaluated by the
         #    reference embedded engine), student loss + gradient from the reference trainer's
-        #    NonLinearRegression::CalcObjectiveFunctionGrad (energy / force / stress MSE terms; the
-        #    Effect gate-x L2 regulariser is switched off)
+        #    NonLinearRegression::CalcObjectiveFunctionGrad (energy / force / stress MSE terms; for
+        #    Effect models also with the gate-x L2 regulariser at its default 1e-4)
         os.makedirs(os.path.join(HERE, "loss"), exist_ok=True)
         for name, frames, weights in LOSS_CASES():
             kind, spec, (seed, rscale, oscale) = MODELS[name]
@@ -222,11 +222,15 @@ def main():
                 fr.stress = np.asarray(rec["virial"])
             cfg = os.path.join(HERE, "frames", f"{name}__labelled.cfg")
             write_cfg(cfg, frames)
-            for weighting in ("vibrations", "structures"):
-                res = json.loads(run([refgrad, "--loss", model, cfg, *(str(w) for w in weights), weighting, "0"]))
-                with open(os.path.join(HERE, "loss", f"{name}__{weighting}.json"), "w") as fh:
+            # the MSE terms alone, and (Effect) with the reference's default gate-x L2 coefficient
+            cases = [(w, 0.0, "") for w in ("vibrations", "structures")]
+            if kind == "coordination-effect":
+                cases += [(w, 1e-4, "__gatex") for w in ("vibrations", "structures")]
+            for weighting, gx, tag in cases:
+                res = json.loads(run([refgrad, "--loss", model, cfg, *(str(w) for w in weights), weighting, repr(gx)]))
+                with open(os.path.join(HERE, "loss", f"{name}__{weighting}{tag}.json"), "w") as fh:
                     json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
-                               "weighting": weighting, "gate_x_l2": 0.0,
+                               "weighting": weighting, "gate_x_l2": gx,
                                "source": "reference NonLinearRegression::CalcObjectiveFunctionGrad (summed over configs)",
                                "loss": res["loss"], "grad": res["grad"], "configs": res["configs"]}, fh)
             print(name, "labelled frames", len(frames))

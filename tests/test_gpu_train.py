@@ -1,8 +1,8 @@
 """GPU training objective, its gradient, BFGS and the torch autograd binding, through the C ABI.
 
 Bars: FP64 plain within 1e-10 relative of the reference trainer's objective and gradient
-(tests/golden/loss, NonLinearRegression::CalcObjectiveFunctionGrad summed over configurations; the
-trainer reports both divided by the configuration count) and of the oracle's restatement on
+(tests/golden/loss, NonLinearRegression::CalcObjectiveFunctionGrad summed over configurations, with
+and without the Effect gate-x L2 term; the trainer reports both divided by the configuration count) and of the oracle's restatement on
 weightings / options the goldens do not cover; FP32 bulk within 1e-5 relative (loss) and 1e-4
 relative norm (gradient) of FP64.
 """
@@ -45,7 +45,7 @@ def test_objective_matches_reference_trainer(sg, golden, path):
     out = {}
     for prec in (sg.FP64, sg.FP32):
         eng = sg.Engine(model, 0, prec)
-        tr = sg.Trainer(eng, frames, *data["weights"], weighting=data["weighting"])
+        tr = sg.Trainer(eng, frames, *data["weights"], weighting=data["weighting"], gate_x_l2=data["gate_x_l2"])
         out[prec] = tr.loss_grad(p)
         del tr
     loss, grad = out[sg.FP64]
@@ -56,10 +56,11 @@ def test_objective_matches_reference_trainer(sg, golden, path):
     assert rel_norm(grad32, grad) <= 1e-4
 
 
-@pytest.mark.parametrize("weighting,nbf", [("molecules", 0), ("structures", 1), ("vibrations", 1)])
-def test_objective_matches_oracle_other_weightings(sg, oracle_lib, golden, weighting, nbf):
-    """Weightings and force normalisation the goldens do not exercise, on a ragged batch where some
-    frames lack energy, force or stress labels."""
+@pytest.mark.parametrize("weighting,nbf,gx", [("molecules", 0, 0.0), ("structures", 1, 0.0), ("vibrations", 1, 1e-4),
+                                              ("molecules", 0, 3e-2)])
+def test_objective_matches_oracle_other_weightings(sg, oracle_lib, golden, weighting, nbf, gx):
+    """Weightings, force normalisation and gate-x coefficients the goldens do not exercise, on a
+    ragged batch where some frames lack energy, force or stress labels."""
     path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
     frames = read_cfg(os.path.join(golden, "frames", "effect_l3k4r2o2__labelled.cfg"))
     frames[1].energy = None
@@ -67,9 +68,10 @@ def test_objective_matches_oracle_other_weightings(sg, oracle_lib, golden, weigh
     frames[3].stress = None
     om = oracle_lib.OracleModel(path)
     ref_loss, ref_grad = oracle_lib.loss_grad(om, frames, 1.0, 0.01, 0.001, weighting=weighting,
-                                              norm_by_forces=nbf)
+                                              norm_by_forces=nbf, gate_x_l2=gx)
     model = sg.Model(path)
-    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, 1.0, 0.01, 0.001, weighting=weighting, norm_by_forces=nbf)
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, 1.0, 0.01, 0.001, weighting=weighting, norm_by_forces=nbf,
+                    gate_x_l2=gx)
     loss, grad = tr.loss_grad(model.params())
     assert abs(loss - ref_loss / len(frames)) <= FP64_TOL * abs(ref_loss / len(frames))
     assert rel_norm(grad, ref_grad / len(frames)) <= FP64_TOL

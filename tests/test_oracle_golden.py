@@ -85,13 +85,15 @@ def loss_cases():
 
 @pytest.mark.parametrize("path", loss_cases(), ids=os.path.basename)
 def test_training_objective_goldens(oracle_lib, golden, path):
-    """Energy / force / stress objective and its gradient against the reference trainer's
+    """Energy / force / stress objective (and, in the __gatex files, the Effect gate-x L2 term at the
+    reference's default coefficient) and its gradient against the reference trainer's
     NonLinearRegression::CalcObjectiveFunctionGrad (summed over configurations)."""
     data = load_json(path)
     m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
     frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
     assert len(frames) == data["configs"]
-    loss, grad = oracle_lib.loss_grad(m, frames, *data["weights"], weighting=data["weighting"])
+    loss, grad = oracle_lib.loss_grad(m, frames, *data["weights"], weighting=data["weighting"],
+                                      gate_x_l2=data.get("gate_x_l2", 0.0))
     ref = np.asarray(data["grad"])
     assert abs(loss - data["loss"]) <= 1e-12 * abs(data["loss"])
     assert np.linalg.norm(grad - ref) <= 1e-12 * np.linalg.norm(ref)
