@@ -159,6 +159,11 @@ void sus2g_trainer_free(sus2g_trainer trainer);
 /* Loss (and, when grad != NULL, its gradient [param count], host) at params [param count, host,
  * Coeff() order].  The engine's parameters are replaced by params. */
 int sus2g_trainer_loss_grad(sus2g_trainer trainer, const double* params, double* loss, double* grad);
+/* The trainer's error metrics at params (E/F/virial only): out6 = energy MAE and RMSE (meV/atom),
+ * force MAE and RMSE (meV/A), stress MAE and RMSE (eV), as NonLinearRegression collects and reports
+ * them (dev_src/non_linear_regression.cpp:781-804, 1150-1184) -- the training-set error report of
+ * the reference's calc-errors / train logs.  The engine's parameters are replaced by params. */
+int sus2g_trainer_metrics(sus2g_trainer trainer, const double* params, double* out6);
 /* Replay the evaluation as one CUDA graph (enabled = 1, default) or launch it eagerly (0). */
 int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
 /* Dense BFGS from params (in/out) for at most max_iter accepted steps or until |grad| <= gtol:

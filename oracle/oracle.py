@@ -207,3 +207,39 @@ def loss_grad(model: "OracleModel", frames, wE: float, wF: float, wS: float, wei
         if gate_x_l2 > 0.0:
             loss += model.last_penalty
     return loss, grad
+
+
+METRIC_NAMES = ("energy_mae_mev_per_atom", "energy_rmse_mev_per_atom", "force_mae_mev_per_a", "force_rmse_mev_per_a",
+                "stress_mae_ev", "stress_rmse_ev")
+
+
+def error_metrics(model: "OracleModel", frames):
+    """The trainer's error metrics over labelled frames, restating the sums NonLinearRegression::AddLoss
+    collects (dev_src/non_linear_regression.cpp:781-804) and their reports (:1150-1184): energy
+    sum|dE| / sum N and sqrt(sum dE^2/N / sum N) in meV/atom, force component MAE / RMSE in meV/A,
+    stress MAE / RMSE over the six components xx, yy, zz, yz, xz, xy in eV."""
+    ea = es = fa = fs = sa = ss = 0.0
+    en = fn = sn = 0
+    for fr in frames:
+        n = fr.natoms
+        e, f, v, _, _ = model.efs(fr.cell, fr.positions, fr.types)
+        if fr.energy is not None:
+            d = fr.energy - e
+            ea += abs(d)
+            es += d * d / n
+            en += n
+        if fr.forces is not None:
+            df = f - fr.forces
+            fa += float(np.sum(np.abs(df)))
+            fs += float(np.sum(df * df))
+            fn += 3 * n
+        if fr.stress is not None:
+            ds = virial6_to_matrix(v) - fr.stress
+            comps = [ds[0, 0], ds[1, 1], ds[2, 2], ds[1, 2], ds[0, 2], ds[0, 1]]
+            sa += sum(abs(c) for c in comps)
+            ss += sum(c * c for c in comps)
+            sn += 6
+    vals = (1000.0 * ea / en if en else 0.0, 1000.0 * np.sqrt(es / en) if en else 0.0,
+            1000.0 * fa / fn if fn else 0.0, 1000.0 * np.sqrt(fs / fn) if fn else 0.0,
+            sa / sn if sn else 0.0, np.sqrt(ss / sn) if sn else 0.0)
+    return dict(zip(METRIC_NAMES, (float(x) for x in vals)))

@@ -48,7 +48,8 @@ int main(int argc, char** argv) {
   }
   if (std::string(argv[1]) == "--loss") {
     // ref-grad --loss MODEL CFG wE wF wS [weighting [gate_x_l2]]:
-    // NonLinearRegression::CalcObjectiveFunctionGrad (dev_src/non_linear_regression.cpp:1112) over
+    // NonLinearRegression::CalcObjectiveFunctionGrad (dev_src/non_linear_regression.cpp:1112), and
+    // the error metrics it collects (energy / force / stress MAE and RMSE, :1150-1184), over
     // the labelled CFG with the energy / force / stress MSE terms only (std terms, penalties and
     // regularisers set to zero; the Effect gate-x L2 term, default 1e-4 in the reference
     // (non_linear_regression.h:128), is 0 unless given); prints the summed loss and gradient (the
@@ -74,6 +75,11 @@ int main(int argc, char** argv) {
     obj.CalcObjectiveFunctionGrad(train);
     std::printf("{\"loss\": %.17g, \"grad\": ", obj.loss());
     vec(obj.grad().data(), (int)obj.grad().size());
+    // the trainer's error metrics collected over the same pass (NonLinearRegression::EnergyMAE_meVPerAtom ...)
+    const double metrics[6] = {obj.EnergyMAE_meVPerAtom(), obj.EnergyRMSE_meVPerAtom(), obj.ForceMAE_meVPerA(),
+                               obj.ForceRMSE_meVPerA(), obj.StressMAE_eV(), obj.StressRMSE_eV()};
+    std::printf(", \"metrics\": ");
+    vec(metrics, 6);
     std::printf(", \"configs\": %zu}\n", train.size());
     return 0;
   }

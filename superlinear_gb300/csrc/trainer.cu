@@ -176,6 +176,58 @@ __global__ void k_gatex_alpha(int nframes, int n, const double* agrad, double* g
   grad[q] += s;
 }
 
+// Error-metric partial sums of one frame (block per frame), as NonLinearRegression::AddLoss collects
+// them (dev_src/non_linear_regression.cpp:781-804): out[f][0..8] = |dE|, dE^2 / N, N (energy
+// labelled), sum |dF|, sum dF^2, 3N (forces), sum |dS|, sum dS^2, 6 (stress; components xx, yy,
+// zz, yz, xz, xy).
+__global__ void k_metrics(int nframes, const int* fbegin, const double* E, const double* F, const double* V,
+                          const double* E0, const double* F0, const double* S0, const int* has, double* out) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  const int a0 = fbegin[f], a1 = fbegin[f + 1], n = a1 - a0;
+  __shared__ double red[2][256];
+  double fa = 0.0, fs = 0.0;
+  if (has[f] & 2)
+    for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x)
+      for (int q = 0; q < 3; ++q) {
+        const double d = F[3 * static_cast<size_t>(i) + q] - F0[3 * static_cast<size_t>(i) + q];
+        fa += fabs(d);
+        fs += d * d;
+      }
+  red[0][threadIdx.x] = fa;
+  red[1][threadIdx.x] = fs;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + st];
+      red[1][threadIdx.x] += red[1][threadIdx.x + st];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double* o = out + 9 * static_cast<size_t>(f);
+    for (int q = 0; q < 9; ++q) o[q] = 0.0;
+    if ((has[f] & 1) && n > 0) {
+      const double d = E0[f] - E[f];
+      o[0] = fabs(d);
+      o[1] = d * d / n;
+      o[2] = n;
+    }
+    if (has[f] & 2) {
+      o[3] = red[0][0];
+      o[4] = red[1][0];
+      o[5] = 3.0 * n;
+    }
+    if (has[f] & 4) {
+      const double* v = V + 6 * f;  // (xx, yy, zz, xy, xz, yz)
+      const double* s0 = S0 + 9 * f;
+      const double d[6] = {v[0] - s0[0], v[1] - s0[4], v[2] - s0[8], v[5] - s0[5], v[4] - s0[2], v[3] - s0[1]};
+      for (int q = 0; q < 6; ++q) { o[6] += fabs(d[q]); o[7] += d[q] * d[q]; }
+      o[8] = 6.0;
+    }
+  }
+}
+
 // loss = sum_f loss_f / K (fixed order), grad /= K
 __global__ void k_loss_finish(int nframes, const double* loss_f, double* loss, double* grad, int nparams) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -458,6 +510,35 @@ class Trainer {
     return accepted;
   }
 
+  // The trainer's error metrics at params (E/F/virial only, no gradient): out6 = energy MAE and
+  // RMSE (meV/atom), force MAE and RMSE (meV/A), stress MAE and RMSE (eV); 0 where nothing is
+  // labelled.  The per-frame partial sums are added on the host in frame order.
+  void metrics(const double* params, double* out6) {
+    eng_.set_params(params);
+    if (eng_.edge_generation() != generation_) bind_edges();
+    cudaStream_t s = eng_.stream();
+    eng_.efs(E_.as<double>(), F_.as<double>(), V_.as<double>(), nullptr);
+    metric_part_.ensure(sizeof(double) * 9 * std::max(1, nframes_));
+    if (nframes_)
+      k_metrics<<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), E_.as<double>(), F_.as<double>(), V_.as<double>(),
+                                         E0_.as<double>(), F0_.as<double>(), S0_.as<double>(), has_.as<int>(),
+                                         metric_part_.as<double>());
+    std::vector<double> part(9 * static_cast<size_t>(nframes_));
+    if (nframes_)
+      TRAIN_CUDA(cudaMemcpyAsync(part.data(), metric_part_.ptr, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, s));
+    TRAIN_CUDA(cudaStreamSynchronize(s));
+    eng_.check_device_error();
+    double t[9] = {0};
+    for (int f = 0; f < nframes_; ++f)
+      for (int q = 0; q < 9; ++q) t[q] += part[9 * static_cast<size_t>(f) + q];
+    out6[0] = t[2] > 0 ? 1000.0 * t[0] / t[2] : 0.0;
+    out6[1] = t[2] > 0 ? 1000.0 * std::sqrt(t[1] / t[2]) : 0.0;
+    out6[2] = t[5] > 0 ? 1000.0 * t[3] / t[5] : 0.0;
+    out6[3] = t[5] > 0 ? 1000.0 * std::sqrt(t[4] / t[5]) : 0.0;
+    out6[4] = t[8] > 0 ? t[6] / t[8] : 0.0;
+    out6[5] = t[8] > 0 ? std::sqrt(t[7] / t[8]) : 0.0;
+  }
+
   int graph_builds() const { return graph_builds_; }
 
  private:
@@ -470,6 +551,7 @@ class Trainer {
   DevBuf E_, F_, V_, ew_, fw_, sw_, lossf_, loss_, grad_;
   bool gatex_ = false;
   DevBuf extra_h_, agrad_;  // gate-x term: dP/dh per atom, dP/dalpha per frame
+  DevBuf metric_part_;
   double* host_scalars_ = nullptr;
   bool use_graph_ = true;
   cudaGraph_t graph_ = nullptr;
@@ -541,6 +623,13 @@ int sus2g_trainer_loss_grad(sus2g_trainer t, const double* params, double* loss,
   return train_guarded([&] {
     if (!t || !params || !loss) throw sus2g::Error(1, "invalid argument: trainer/params/loss");
     *loss = t->trainer->loss_grad(params, grad);
+  });
+}
+
+int sus2g_trainer_metrics(sus2g_trainer t, const double* params, double* out6) {
+  return train_guarded([&] {
+    if (!t || !params || !out6) throw sus2g::Error(1, "invalid argument: trainer/params/out");
+    t->trainer->metrics(params, out6);
   });
 }
 

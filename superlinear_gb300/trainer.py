@@ -90,6 +90,18 @@ class Trainer:
         check(load().sus2g_trainer_loss_grad(self._h, _d(p), ctypes.byref(loss), _d(g)))
         return loss.value, g
 
+    METRICS = ("energy_mae_mev_per_atom", "energy_rmse_mev_per_atom", "force_mae_mev_per_a", "force_rmse_mev_per_a",
+               "stress_mae_ev", "stress_rmse_ev")
+
+    def metrics(self, params):
+        """The reference trainer's error metrics over the labelled frames at ``params``."""
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        if p.size != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
+        out = np.zeros(6)
+        check(load().sus2g_trainer_metrics(self._h, _d(p), _d(out)))
+        return dict(zip(self.METRICS, (float(x) for x in out)))
+
     def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
         """Runs BFGS from ``params``; returns (params, loss history)."""
         p = np.array(params, dtype=np.float64)

@@ -94,6 +94,10 @@ def frames_for(name):
     raise KeyError(name)
 
 
+# (model, radial_cutoff_p): polynomial-envelope variants (sus2_sl_radial_math.cpp:256-294)
+POLY_VARIANTS = (("static_l2k3o2_c2", 5), ("effect_l3k4r2o2", 3))
+
+
 def LOSS_CASES():
     """(model, frames to label, (wE, wF, wS)); loss weights of the reference's example profile."""
     return [("effect_l3k4r2o2", training_frames(6, 8, 64, 3.0, 4.2, 0.1, seed=211, species=2), (1.0, 0.01, 0.001)),
@@ -111,6 +115,48 @@ def weights_for(frames, seed):
         sw = rng.normal(0, 0.2, (3, 3))
         out.append((ew, fw, sw))
     return out
+
+
+def golden_efs_and_grad(name, model, frame_sets, seed, tmp, emb, refgrad):
+    """E/F/virial goldens (reference embedded engine, one frame at a time) and parameter-gradient
+    goldens (reference trainer, seeded weights) of one model over its labelled frame sets."""
+    for label, frames in frame_sets:
+        cfg = os.path.join(HERE, "frames", f"{name}__{label}.cfg")
+        write_cfg(cfg, frames)
+        # 3. embedded engine E/F/virial, one frame at a time
+        records = []
+        for k, fr in enumerate(frames):
+            one = os.path.join(tmp, "one.cfg")
+            write_cfg(one, [fr])
+            out = run([emb, model, one, "1", "direct"])
+            line = next(l for l in out.splitlines() if l.startswith("NATIVE_EFS_JSON"))
+            rec = json.loads(line.split(" ", 1)[1])
+            rec["config"] = k
+            records.append(rec)
+        with open(os.path.join(HERE, "efs", f"{name}__{label}.json"), "w") as fh:
+            json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
+                       "source": "reference embedded engine (embedded_efs.cpp, domains=1, direct)",
+                       "records": records}, fh)
+        # 4. trainer gradient for seeded weights
+        wts = weights_for(frames, seed + 1000)
+        wfile = os.path.join(tmp, "w.txt")
+        with open(wfile, "w") as fh:
+            for ew, fw, sw in wts:
+                fh.write(f"{len(ew)}\n")
+                for i in range(len(ew)):
+                    fh.write("%.17g %.17g %.17g %.17g\n" % (ew[i], *fw[i]))
+                for row in sw:
+                    fh.write("%.17g %.17g %.17g\n" % tuple(row))
+        lines = [json.loads(l) for l in run([refgrad, model, cfg, wfile]).splitlines()]
+        efs = [l for l in lines if "energy" in l]
+        grads = [l["grad"] for l in lines if "grad" in l]
+        with open(os.path.join(HERE, "grad", f"{name}__{label}.json"), "w") as fh:
+            json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
+                       "source": "reference trainer MLMTPR::CalcEFS + AccumulateEFSCombinationGrad",
+                       "weights": [{"energy": ew.tolist(), "force": fw.tolist(), "stress": sw.tolist()}
+                                   for ew, fw, sw in wts],
+                       "trainer_efs": efs, "grad": grads}, fh)
+        print(name, label, "frames", len(frames), "atoms", [f.natoms for f in frames])
 
 
 def main():
@@ -163,43 +209,23 @@ def main():
             assert np.array_equal(fields_to_vector(read_sus2(model)), vec)
             manifest[f"models/{name}.sus2"] = hashlib.sha256(open(model, "rb").read()).hexdigest()
 
-            for label, frames in frames_for(name):
-                cfg = os.path.join(HERE, "frames", f"{name}__{label}.cfg")
-                write_cfg(cfg, frames)
-                # 3. embedded engine E/F/virial, one frame at a time
-                records = []
-                for k, fr in enumerate(frames):
-                    one = os.path.join(tmp, "one.cfg")
-                    write_cfg(one, [fr])
-                    out = run([emb, model, one, "1", "direct"])
-                    line = next(l for l in out.splitlines() if l.startswith("NATIVE_EFS_JSON"))
-                    rec = json.loads(line.split(" ", 1)[1])
-                    rec["config"] = k
-                    records.append(rec)
-                with open(os.path.join(HERE, "efs", f"{name}__{label}.json"), "w") as fh:
-                    json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
-                               "source": "reference embedded engine (embedded_efs.cpp, domains=1, direct)",
-                               "records": records}, fh)
-                # 4. trainer gradient for seeded weights
-                wts = weights_for(frames, seed + 1000)
-                wfile = os.path.join(tmp, "w.txt")
-                with open(wfile, "w") as fh:
-                    for ew, fw, sw in wts:
-                        fh.write(f"{len(ew)}\n")
-                        for i in range(len(ew)):
-                            fh.write("%.17g %.17g %.17g %.17g\n" % (ew[i], *fw[i]))
-                        for row in sw:
-                            fh.write("%.17g %.17g %.17g\n" % tuple(row))
-                lines = [json.loads(l) for l in run([refgrad, model, cfg, wfile]).splitlines()]
-                efs = [l for l in lines if "energy" in l]
-                grads = [l["grad"] for l in lines if "grad" in l]
-                with open(os.path.join(HERE, "grad", f"{name}__{label}.json"), "w") as fh:
-                    json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
-                               "source": "reference trainer MLMTPR::CalcEFS + AccumulateEFSCombinationGrad",
-                               "weights": [{"energy": ew.tolist(), "force": fw.tolist(), "stress": sw.tolist()}
-                                           for ew, fw, sw in wts],
-                               "trainer_efs": efs, "grad": grads}, fh)
-                print(name, label, "frames", len(frames), "atoms", [f.natoms for f in frames])
+            golden_efs_and_grad(name, model, frames_for(name), seed, tmp, emb, refgrad)
+        # 4b. polynomial radial cutoff (radial_cutoff_type = polynomial): variants of two models
+        for base, p in POLY_VARIANTS:
+            seed = MODELS[base][2][0]
+            src = os.path.join(HERE, "models", f"{base}.sus2")
+            name = f"{base}_poly{p}"
+            model = os.path.join(HERE, "models", f"{name}.sus2")
+            with open(src) as fh:
+                text = fh.read()
+            head, sep, rest = text.partition("radial_basis_size = ")
+            line, nl, tail = rest.partition("\n")
+            with open(model, "w") as fh:
+                fh.write(head + sep + line + nl + f"\tradial_cutoff_type = polynomial\n\tradial_cutoff_p = {p}\n" + tail)
+            back = json.loads(run([refgrad, model, "/dev/null"]).splitlines()[0])["coeffs"]
+            assert np.array_equal(np.asarray(back), fields_to_vector(read_sus2(src))), f"{name}: reference load"
+            manifest[f"models/{name}.sus2"] = hashlib.sha256(open(model, "rb").read()).hexdigest()
+            golden_efs_and_grad(name, model, [(l, f) for l, f in frames_for(base)], seed, tmp, emb, refgrad)
         # 5. labelled training sets: teacher labels (another seeded parameter vector, evaluated by the
         #    reference embedded engine), student loss + gradient from the reference trainer's
         #    NonLinearRegression::CalcObjectiveFunctionGrad (energy / force / stress MSE terms; for
@@ -232,7 +258,10 @@ def main():
                     json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
                                "weighting": weighting, "gate_x_l2": gx,
                                "source": "reference NonLinearRegression::CalcObjectiveFunctionGrad (summed over configs)",
-                               "loss": res["loss"], "grad": res["grad"], "configs": res["configs"]}, fh)
+                               "loss": res["loss"], "grad": res["grad"], "configs": res["configs"],
+                               "metrics": dict(zip(("energy_mae_mev_per_atom", "energy_rmse_mev_per_atom",
+                                                    "force_mae_mev_per_a", "force_rmse_mev_per_a", "stress_mae_ev",
+                                                    "stress_rmse_ev"), res["metrics"]))}, fh)
             print(name, "labelled frames", len(frames))
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)

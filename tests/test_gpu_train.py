@@ -50,6 +50,9 @@ def test_objective_matches_reference_trainer(sg, golden, path):
         del tr
     loss, grad = out[sg.FP64]
     assert abs(loss - ref_loss) <= FP64_TOL * abs(ref_loss)
+    metrics = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, *data["weights"]).metrics(p)
+    for name, value in data["metrics"].items():
+        assert abs(metrics[name] - value) <= FP64_TOL * abs(value), name
     assert rel_norm(grad, ref_grad) <= FP64_TOL
     loss32, grad32 = out[sg.FP32]
     assert abs(loss32 - loss) <= 1e-5 * abs(loss)

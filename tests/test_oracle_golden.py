@@ -97,3 +97,6 @@ def test_training_objective_goldens(oracle_lib, golden, path):
     ref = np.asarray(data["grad"])
     assert abs(loss - data["loss"]) <= 1e-12 * abs(data["loss"])
     assert np.linalg.norm(grad - ref) <= 1e-12 * np.linalg.norm(ref)
+    metrics = oracle_lib.error_metrics(m, frames)
+    for name, value in data["metrics"].items():
+        assert abs(metrics[name] - value) <= 1e-11 * max(abs(value), 1e-300), name
