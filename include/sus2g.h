@@ -48,6 +48,10 @@ int sus2g_model_cutoff(sus2g_model model, double* cutoff);
 int sus2g_model_param_count(sus2g_model model, int* count);
 int sus2g_model_get_params(sus2g_model model, double* out, int n);
 int sus2g_model_set_params(sus2g_model model, const double* in, int n);
+/* Write the model with its current parameter vector as a .sus2 file the reference loads
+ * (replaces MLMTPR::Save, dev_src/mtpr.cpp:6893): the loaded fields in file order, the trainable
+ * blocks replaced by the current values in %.17e (bit-exact on reload). */
+int sus2g_model_save(sus2g_model model, const char* path);
 
 /* ---- engine -----------------------------------------------------------------------------------
  * Replaces SUS2SL::Kernel(const Model&) (sus2_sl_kernel.cpp:45-106): binds a model to one CUDA

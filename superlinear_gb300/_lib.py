@@ -27,6 +27,7 @@ SIGNATURES = {
     "sus2g_model_param_count": (ctypes.c_int, [_vp, _ip]),
     "sus2g_model_get_params": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
     "sus2g_model_set_params": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+    "sus2g_model_save": (ctypes.c_int, [_vp, ctypes.c_char_p]),
     "sus2g_engine_create": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)]),
     "sus2g_engine_free": (None, [_vp]),
     "sus2g_engine_update_params": (ctypes.c_int, [_vp, _vp]),

@@ -109,6 +109,13 @@ int sus2g_model_set_params(sus2g_model h, const double* in, int n) {
   });
 }
 
+int sus2g_model_save(sus2g_model h, const char* path) {
+  return guarded([&] {
+    need(h && path, "model/path");
+    h->model.save(path);
+  });
+}
+
 int sus2g_engine_create(sus2g_model model, int device, int precision, sus2g_engine* out) {
   return guarded([&] {
     need(model && out, "model/out");

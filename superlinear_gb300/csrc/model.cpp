@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cctype>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <fstream>
 #include <limits>
@@ -102,7 +103,12 @@ void Model::load(const std::string& path) {
     if (!header) { require(line == "MTP", "missing MTP header"); header = true; continue; }
     const size_t eq = line.find('=');
     if (eq == std::string::npos) {
-      if (line == "radial_coeffs") { require(!radial && radial_text.empty(), "duplicate radial_coeffs"); radial = true; continue; }
+      if (line == "radial_coeffs") {
+        require(!radial && radial_text.empty(), "duplicate radial_coeffs");
+        radial = true;
+        field_order.push_back("radial_coeffs");
+        continue;
+      }
       require(radial, "unrecognized line: " + line);
       if (line == "0-0") continue;
       require(line[0] == '{', "invalid radial coefficient block");
@@ -122,6 +128,7 @@ void Model::load(const std::string& path) {
     }
     require(depth == 0, "unbalanced braces in " + key);
     fields[key] = value;
+    field_order.push_back(key);
   }
   require(header, "empty model");
   C = integer("species_count"); L = integer("sh_l_max"); K = integer("sh_k_max");
@@ -405,6 +412,69 @@ std::vector<Model::Block> Model::layout() const {
   add("species_coeffs", species.size());
   add("moment_coeffs", linear.size());
   return out;
+}
+
+void Model::save(const std::string& path) const {
+  std::map<std::string, std::string> out = fields;
+  std::vector<std::string> order = field_order;
+  auto place = [&](const std::string& key, const std::string& after) {
+    if (std::find(order.begin(), order.end(), key) != order.end()) return;
+    auto it = std::find(order.begin(), order.end(), after);
+    order.insert(it == order.end() ? order.end() : it + 1, key);
+  };
+  static const std::map<std::string, std::string> count_keys = {
+      {"two_layer_gate_radial_coeffs", "two_layer_gate_radial_coeff_count"},
+      {"two_layer_gate_additive_coeffs", "two_layer_gate_additive_coeff_count"},
+      {"two_layer_gate_type_coeffs", "two_layer_gate_type_coeff_count"},
+      {"two_layer_gate_weights", "two_layer_gate_weight_count"},
+      {"two_layer_gate_k_rank_weights", "two_layer_gate_k_rank_weight_count"},
+      {"outer_k_rank1_weights", "outer_k_rank1_weight_count"}};
+  char buf[64];
+  auto fmt = [&](const double* v, size_t n) {
+    std::string t = "{";
+    for (size_t q = 0; q < n; ++q) {
+      std::snprintf(buf, sizeof(buf), "%.17e", v[q]);
+      if (q) t += ", ";
+      t += buf;
+    }
+    return t + "}";
+  };
+  std::string prev = "scal_coeffs";
+  for (const Block& b : layout()) {
+    const std::vector<double>& v = *const_cast<Model*>(this)->block_ptr(b.name);
+    out[b.name] = fmt(v.data(), v.size());
+    place(b.name, prev);
+    auto ck = count_keys.find(b.name);
+    if (ck != count_keys.end()) {
+      out[ck->second] = std::to_string(v.size());
+      place(ck->second, b.name);
+    }
+    prev = b.name;
+  }
+  // the trainer's sequential reader wants the radial block after scal_coeffs (dev_src/mtpr.cpp:5100-5150)
+  auto r = std::find(order.begin(), order.end(), "radial_coeffs");
+  auto sc = std::find(order.begin(), order.end(), "scal_coeffs");
+  if (r != order.end() && sc != order.end() && r < sc) {
+    order.erase(r);
+    sc = std::find(order.begin(), order.end(), "scal_coeffs");
+    order.insert(sc + 1, "radial_coeffs");
+  }
+  static const std::set<std::string> radial_meta = {"scaling_inner", "min_dist", "max_dist", "angular_max_dist",
+                                                    "radial_basis_size", "radial_cutoff_type", "radial_cutoff_p",
+                                                    "radial_funcs_count"};
+  std::ofstream os(path.c_str());
+  if (!os) throw Error(2, "cannot write model " + path);
+  os << "MTP\n";
+  for (const std::string& key : order) {
+    if (key == "radial_coeffs") {
+      os << "\tradial_coeffs\n\t\t0-0\n";
+      const size_t w = static_cast<size_t>(B + C);
+      for (size_t row = 0; row * w < radial.size(); ++row) os << "\t\t\t" << fmt(radial.data() + row * w, w) << "\n";
+      continue;
+    }
+    os << (radial_meta.count(key) ? "\t" : "") << key << " = " << out.at(key) << "\n";
+  }
+  if (!os) throw Error(2, "cannot write model " + path);
 }
 
 std::vector<double>* Model::block_ptr(const std::string& n) {

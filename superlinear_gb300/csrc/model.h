@@ -48,6 +48,7 @@ struct ContractionRow { int src, dst, widx; };  // v[dst] += W[widx] * v[src]
 
 struct Model {
   std::map<std::string, std::string> fields;
+  std::vector<std::string> field_order;  // keys in file order ("radial_coeffs" at its block)
   // dimensions
   int C = 0, L = 0, K = 0, B = 0, F = 0, H = 0, M = 0, NB = 0, P = 0, S = 0;
   int nblk = 0, scaling_mode = 3;  // 0 pair, 1 L, 2 K, 3 LK
@@ -80,6 +81,10 @@ struct Model {
   GraphSchedule outer_graph, gate_graph;
 
   void load(const std::string& path);
+  // Writes the model as a .sus2 file with the current parameter vector (MLMTPR::Save,
+  // dev_src/mtpr.cpp:6893): the loaded fields in file order, the trainable blocks replaced by the
+  // current values (%.17e, which reads back bit-exactly), the radial block after scal_coeffs.
+  void save(const std::string& path) const;
   // flat trainable vector in the reference trainer's order (dev_src/mtpr.h, DistributeCoeffs)
   struct Block { std::string name; int offset, size; };
   std::vector<Block> layout() const;

@@ -73,6 +73,10 @@ class Model:
         v = np.ascontiguousarray(values, dtype=np.float64)
         check(load().sus2g_model_set_params(self._h, _d(v), v.size))
 
+    def save(self, path: str) -> None:
+        """Write the model with its current parameters as a ``.sus2`` file (MLMTPR::Save)."""
+        check(load().sus2g_model_save(self._h, str(path).encode()))
+
 
 class Engine:
     """A model bound to one CUDA device in FP64 (``FP64``) or FP32-bulk (``FP32``) form."""
