@@ -90,6 +90,13 @@ int sus2g_calc_efs_device(sus2g_engine engine, int nframes, const int* natoms, c
                           const double* positions, const int* types, double* energy, double* forces,
                           double* virial, double* site_energy);
 
+/* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
+ * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors
+ * (dev_src/mtpr.cpp:6554, the trainer's calc-descriptors command) for Static and Effect models.
+ * S = dims[8] of sus2g_model_dims.  Frames as in sus2g_calc_efs_host. */
+int sus2g_calc_descriptors_host(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                                const double* positions, const int* types, double* desc);
+
 /* ---- E / F / virial of a caller edge list (pair_style sus2/embedded compute contract) ----------
  * Replaces SUS2SL::Kernel::begin / outer / finish (sus2_sl_kernel.cpp:381-562) as called by
  * PairSUS2Embedded::compute (pair_sus2_embedded.cpp:250-314) with a single domain: nowned centre

@@ -51,6 +51,8 @@ def lib():
                                     _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
                                ctypes.c_int]
+        L.orc_descriptors.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, ctypes.c_char_p,
+                                      ctypes.c_int]
         L.orc_grad_gatex.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
                                      _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         _lib = L
@@ -139,6 +141,17 @@ class OracleModel:
         if rc:
             raise RuntimeError(err.value.decode())
         return float(e[0]), f, v, s
+
+    def descriptors(self, cell, pos, types, nscalars: int) -> np.ndarray:
+        """Per-atom scalar moments [n][nscalars] of one frame (MLMTPR::CalcDescriptors)."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        out = np.zeros((types.size, nscalars))
+        err = ctypes.create_string_buffer(512)
+        if lib().orc_descriptors(self._h, types.size, _d(cell), _d(pos), _i(types), _d(out), err, 512):
+            raise RuntimeError(err.value.decode())
+        return out
 
     def grad(self, cell, pos, types, ew, fw, sw, gate_x: float = 0.0) -> np.ndarray:
         """d/dtheta of sum_i ew_i E_i + sum_e (fw_i - fw_j + sw d_e) . dE/dd_e (one frame); with

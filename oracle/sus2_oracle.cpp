@@ -522,6 +522,7 @@ struct Result {
   double energy = 0;
   vector<double> site;
   vector<V3> g;      // per edge dE/dd
+  double* desc = nullptr;  // optional [ncentres][S]: the scalar moments v[alpha_moment_mapping[q]]
 };
 
 // E / F / virial of the edges in ctx (owned centres are 0..ncentres-1)
@@ -586,6 +587,7 @@ void evaluate(const Ctx& cx, int ncentres, Result& res, int threads) {
     for (int q = 0; q < m.S; ++q) {
       E += coef * m.linear[off + q] * v[m.smap[q]];
       lam[m.smap[q]] += coef * m.linear[off + q];
+      if (res.desc) res.desc[static_cast<size_t>(i) * m.S + q] = v[m.smap[q]];
     }
     res.site[i] = E;
     contract_graph_reverse(m, po, v, nullptr, lam, nullptr, nullptr);
@@ -1021,6 +1023,23 @@ int orc_grad(void* mp, int n, const double* cell, const double* pos, const int* 
     const Model& m = *static_cast<Model*>(mp);
     Ctx cx = make_ctx(m, n, cell, pos, types);
     gradient(cx, ew, fw, sw, grad);
+    return 0;
+  } catch (const std::exception& e) {
+    set_err(err, errlen, e.what());
+    return -1;
+  }
+}
+
+// Per-atom descriptors of one periodic frame: the S scalar moments after the product graph
+// (MLMTPR::CalcDescriptors, dev_src/mtpr.cpp:6554: basis_vals[1 + q] per atom), desc[n][S].
+int orc_descriptors(void* mp, int n, const double* cell, const double* pos, const int* types, double* desc, char* err,
+                    int errlen) {
+  try {
+    const Model& m = *static_cast<Model*>(mp);
+    Ctx cx = make_ctx(m, n, cell, pos, types);
+    Result res;
+    res.desc = desc;
+    evaluate(cx, n, res, 1);
     return 0;
   } catch (const std::exception& e) {
     set_err(err, errlen, e.what());

@@ -35,6 +35,9 @@ int orc_grad(void* model, int n, const double* cell, const double* pos, const in
              const double* fw, const double* sw, double* grad, char* err, int errlen);
 /* orc_grad plus the Effect gate-x L2 term of the reference objective with coefficient gate_x:
  * *penalty = the term's value for this configuration, grad += its parameter gradient as well. */
+/* Per-atom descriptors (the S scalar moments, MLMTPR::CalcDescriptors) of one frame, desc[n][S]. */
+int orc_descriptors(void* model, int n, const double* cell, const double* pos, const int* types, double* desc,
+                    char* err, int errlen);
 int orc_grad_gatex(void* model, int n, const double* cell, const double* pos, const int* types, const double* ew,
                    const double* fw, const double* sw, double gate_x, double* grad, double* penalty, char* err,
                    int errlen);

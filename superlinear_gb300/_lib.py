@@ -40,6 +40,7 @@ SIGNATURES = {
     "sus2g_calc_efs_device": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sus2g_efs_edges_host": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp, _dp,
                                             _dp, _dp, _dp]),
+    "sus2g_calc_descriptors_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp]),
     "sus2g_efs_combination_grad_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
     "sus2g_static_efs_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                                 ctypes.c_longlong, _vp, _vp, _vp, _vp]),

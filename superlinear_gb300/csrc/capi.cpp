@@ -219,6 +219,43 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
   });
 }
 
+int sus2g_calc_descriptors_host(sus2g_engine e, int nframes, const int* natoms, const double* cells,
+                                const double* positions, const int* types, double* desc) {
+  return guarded([&] {
+    need(e && nframes >= 0 && (nframes == 0 || (natoms && cells)), "engine/frames");
+    const long long n = total_atoms(nframes, natoms);
+    need(n == 0 || (positions && types && desc), "positions/types/desc");
+    auto& eng = *e->engine;
+    for (long long i = 0; i < n; ++i)
+      need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
+    const int S = eng.model().S;
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    Slot pos(eng, 0, sizeof(double) * 3 * n), typ(eng, 1, sizeof(int) * n), out(eng, 2, sizeof(double) * n * S);
+    if (n) {
+      cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
+      cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
+    }
+    struct Reset {  // the descriptor output is for this call only
+      sus2g::Engine& e;
+      ~Reset() { e.set_descriptor_output(nullptr); }
+    } reset{eng};
+    for (int attempt = 0;; ++attempt) {
+      try {
+        eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
+        eng.set_descriptor_output(out.as<double>());
+        eng.efs(nullptr, nullptr, nullptr, nullptr);
+        eng.check_device_error();
+        break;
+      } catch (const sus2g::EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: repeat the step
+      }
+    }
+    if (n && S) cuda(cudaMemcpyAsync(desc, out.p, sizeof(double) * n * S, cudaMemcpyDeviceToHost, s), "descriptor copy");
+    cuda(cudaStreamSynchronize(s), "stream synchronize");
+  });
+}
+
 int sus2g_efs_combination_grad_host(sus2g_engine e, int nframes, const int* natoms, const double* cells,
                                     const double* positions, const int* types, const double* ene_w,
                                     const double* frc_w, const double* str_w, double* grad) {

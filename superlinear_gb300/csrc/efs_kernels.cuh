@@ -45,6 +45,7 @@ struct PassArgs {
   const double* hbar_atom; // [natoms][F] gate-signal adjoint already summed per atom (caller edges), or null
   double* site_energy;     // [natoms]
   double* virial;          // [natoms][6] (xx, yy, zz, xy, xz, yz), minus d (x) g
+  double* desc;            // [natoms][S] scalar moments (descriptors), or null
   int* error;
 };
 
@@ -316,6 +317,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
         const double rho = coef * double(dm.linear[off + q]);
         es += rho * double(v[node]);
         adj[node] = Real(rho);
+        if (a.desc) a.desc[static_cast<size_t>(atom) * dm.S + q] = double(v[node]);
       }
       es = warp_sum(es);
       if (lane == 0) a.site_energy[atom] = dm.species[ti] + dm.shift[ti] + es;

@@ -1116,6 +1116,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   a.g = g_.as<Real>();
   a.site_energy = site_.as<double>();
   a.virial = vir_atom_.as<double>();
+  a.desc = desc_out_;
   a.error = error_.as<int>();
   if (m.gated) {
     hsig_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F);

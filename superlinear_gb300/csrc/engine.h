@@ -62,6 +62,9 @@ class Engine {
   // forces [natoms][3], per-frame virial [nframes][6] in (xx, yy, zz, xy, xz, yz), site energies
   // [natoms]; any output may be null.
   void efs(double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  // Per-atom descriptors of the next efs() call (device [natoms][S] FP64: the scalar moments the
+  // readout weighs, MLMTPR::CalcDescriptors); null turns the output off.
+  void set_descriptor_output(double* d_desc) { desc_out_ = d_desc; }
 
   // --- staged evaluation on caller edges (SUS2SL::Kernel begin / pack_forward / unpack_forward /
   // outer / pack_reverse / add_reverse / finish, sus2_sl_kernel.h:36-42) ---------------------
@@ -136,6 +139,7 @@ class Engine {
   template <typename Real>
   void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages);
   int staged_ = 0;  // staged evaluation: 1 after begin, 2 after outer
+  double* desc_out_ = nullptr;
   template <typename Real>
   void run_grad(const double* ew, const double* fw, const double* sw, double* grad, const double* extra_h);
   DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;

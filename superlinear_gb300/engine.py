@@ -146,6 +146,14 @@ class Engine:
                                          _d(v), _d(s)))
         return e, f, v, s
 
+    def calc_descriptors(self, frames) -> np.ndarray:
+        """Per-atom descriptors [N, S] (the scalar moments; MLMTPR::CalcDescriptors / calc-descriptors)."""
+        natoms, cells, pos, types = self.pack_frames(frames)
+        out = np.zeros((int(natoms.sum()), self.model.dims["S"]))
+        check(load().sus2g_calc_descriptors_host(self._h, natoms.size, _i(natoms), _d(cells), _d(pos), _i(types),
+                                                 _d(out)))
+        return out
+
     def calc_efs_device(self, natoms, cells, pos_ptr: int, types_ptr: int, energy_ptr: int = 0, forces_ptr: int = 0,
                         virial_ptr: int = 0, site_ptr: int = 0) -> None:
         """Device pointers (e.g. ``tensor.data_ptr()``) for positions/types/outputs; host natoms/cells."""

@@ -94,6 +94,9 @@ def frames_for(name):
     raise KeyError(name)
 
 
+# (model, frame set) of the descriptor goldens
+DESC_CASES = (("static_l3k4o2", "diamond64_s05"), ("static_l2k3o2_c2", "mixed"), ("effect_l3k4r2o2", "train4"))
+
 # (model, radial_cutoff_p): polynomial-envelope variants (sus2_sl_radial_math.cpp:256-294)
 POLY_VARIANTS = (("static_l2k3o2_c2", 5), ("effect_l3k4r2o2", 3))
 
@@ -226,6 +229,25 @@ def main():
             assert np.array_equal(np.asarray(back), fields_to_vector(read_sus2(src))), f"{name}: reference load"
             manifest[f"models/{name}.sus2"] = hashlib.sha256(open(model, "rb").read()).hexdigest()
             golden_efs_and_grad(name, model, [(l, f) for l, f in frames_for(base)], seed, tmp, emb, refgrad)
+        # 4c. per-atom descriptors (the S scalar moments) from the reference trainer's calc-descriptors
+        os.makedirs(os.path.join(HERE, "desc"), exist_ok=True)
+        for name, label in DESC_CASES:
+            model = os.path.join(HERE, "models", f"{name}.sus2")
+            cfg = os.path.join(HERE, "frames", f"{name}__{label}.cfg")
+            out = os.path.join(tmp, "desc.txt")
+            run([mlp, "calc-descriptors", model, cfg, out], cwd=tmp)
+            types, values = [], []
+            with open(out) as fh:
+                for line in fh:
+                    if line.startswith("#") or not line.strip():
+                        continue
+                    row = line.split()
+                    types.append(int(row[0]))
+                    values.append([float(x) for x in row[1:]])
+            with open(os.path.join(HERE, "desc", f"{name}__{label}.json"), "w") as fh:
+                json.dump({"model": f"{name}.sus2", "frames": f"{name}__{label}.cfg",
+                           "source": "reference trainer calc-descriptors (MLMTPR::CalcDescriptors), 16 digits",
+                           "types": types, "descriptors": values}, fh)
         # 5. labelled training sets: teacher labels (another seeded parameter vector, evaluated by the
         #    reference embedded engine), student loss + gradient from the reference trainer's
         #    NonLinearRegression::CalcObjectiveFunctionGrad (energy / force / stress MSE terms; for

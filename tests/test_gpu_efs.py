@@ -254,3 +254,18 @@ def test_invalid_inputs_raise(lib, golden):
         g64.calc_efs([singular])
     with pytest.raises(lib.Sus2Error):
         lib.Engine(m, 0, 7)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "desc", "*.json"))),
+                         ids=os.path.basename)
+def test_descriptors_match_reference(lib, golden, path):
+    """sus2g_calc_descriptors_host against the reference's calc-descriptors (16-digit print)."""
+    data = load_json(path)
+    m, g64, g32 = engines(lib, os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    ref = np.asarray(data["descriptors"])
+    d64 = g64.calc_descriptors(frames)
+    assert d64.shape == ref.shape
+    assert rel_err(d64, ref) < 1e-13
+    d32 = g32.calc_descriptors(frames)
+    assert rel_err(d32, ref) < 1e-5

@@ -100,3 +100,20 @@ def test_training_objective_goldens(oracle_lib, golden, path):
     metrics = oracle_lib.error_metrics(m, frames)
     for name, value in data["metrics"].items():
         assert abs(metrics[name] - value) <= 1e-11 * max(abs(value), 1e-300), name
+
+
+def desc_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "desc", "*.json")))
+
+
+@pytest.mark.parametrize("path", desc_cases(), ids=os.path.basename)
+def test_descriptor_goldens(oracle_lib, golden, path):
+    """Per-atom scalar moments against the reference trainer's calc-descriptors (printed with 16
+    significant digits)."""
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    ref = np.asarray(data["descriptors"])
+    ours = np.concatenate([m.descriptors(fr.cell, fr.positions, fr.types, ref.shape[1]) for fr in frames])
+    assert np.array_equal(np.concatenate([fr.types for fr in frames]), data["types"])
+    assert rel_err(ours, ref) < 1e-13
