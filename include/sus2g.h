@@ -175,6 +175,13 @@ int sus2g_trainer_loss_grad(sus2g_trainer trainer, const double* params, double*
  * them (dev_src/non_linear_regression.cpp:781-804, 1150-1184) -- the training-set error report of
  * the reference's calc-errors / train logs.  The engine's parameters are replaced by params. */
 int sus2g_trainer_metrics(sus2g_trainer trainer, const double* params, double* out6);
+/* Linear warm-up: replaces MTPR_trainer::TrainLinear (dev_src/mtpr_trainer.cpp:1455) with its
+ * AddToSLAE rows (:1130-1453) and SolveSLAE (:971) -- the radial Chebyshev rows normalised to unit
+ * norm (MLMTPR::Orthogonalize, dev_src/mtpr.cpp:14110), then the least-squares solve of the species
+ * constants and the scalar readout against the labels with the trainer's weights, applied as
+ * centre factor 1, shift = constant - 1, readout = solution.  params (host) in/out; the engine's
+ * parameters become the result. */
+int sus2g_trainer_train_linear(sus2g_trainer trainer, double* params);
 /* Replay the evaluation as one CUDA graph (enabled = 1, default) or launch it eagerly (0). */
 int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
 /* Dense BFGS from params (in/out) for at most max_iter accepted steps or until |grad| <= gtol:

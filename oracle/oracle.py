@@ -51,6 +51,7 @@ def lib():
                                     _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
                                ctypes.c_int]
+        L.orc_layout.argtypes = [ctypes.c_void_p, _ip]
         L.orc_descriptors.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, ctypes.c_char_p,
                                       ctypes.c_int]
         L.orc_grad_gatex.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, ctypes.c_double,
@@ -141,6 +142,13 @@ class OracleModel:
         if rc:
             raise RuntimeError(err.value.decode())
         return float(e[0]), f, v, s
+
+    def layout(self) -> dict:
+        out = np.zeros(12, dtype=np.int32)
+        lib().orc_layout(self._h, _i(out))
+        keys = ("C", "S", "B", "F", "species_readout", "o_shift", "o_radial", "o_species", "o_linear", "nparams",
+                "nblk", "K")
+        return dict(zip(keys, (int(x) for x in out)))
 
     def descriptors(self, cell, pos, types, nscalars: int) -> np.ndarray:
         """Per-atom scalar moments [n][nscalars] of one frame (MLMTPR::CalcDescriptors)."""
@@ -256,3 +264,88 @@ def error_metrics(model: "OracleModel", frames):
             1000.0 * fa / fn if fn else 0.0, 1000.0 * np.sqrt(fs / fn) if fn else 0.0,
             sa / sn if sn else 0.0, np.sqrt(ss / sn) if sn else 0.0)
     return dict(zip(METRIC_NAMES, (float(x) for x in vals)))
+
+
+def train_linear(model: "OracleModel", frames, wE: float, wF: float, wS: float, weighting: str = "vibrations",
+                 norm_by_forces: int = 0) -> np.ndarray:
+    """The linear warm-up solve, restating MTPR_trainer::TrainLinear (dev_src/mtpr_trainer.cpp:1455)
+    for Static and Effect models: the radial Chebyshev rows are normalised to unit L2 norm
+    (MLMTPR::Orthogonalize, dev_src/mtpr.cpp:14110), the normal equations of the energy / force /
+    stress rows (AddToSLAE, mtpr_trainer.cpp:1130-1453) in the species constants and the scalar
+    readout are built from one E/F/virial evaluation per readout column, a 1e-13 ridge is added and
+    the system is solved by Gaussian elimination (SolveSLAE, :971; SolveSLAEGaussian, :282), and the
+    solution is applied as centre factor 1, shift = constant - 1, readout = solution.  Returns the new
+    parameter vector (the model keeps it)."""
+    lay = model.layout()
+    C, S, B, F = lay["C"], lay["S"], lay["B"], lay["F"]
+    p = model.params()
+    for mu in range(F):                       # Orthogonalize
+        row = p[lay["o_radial"] + mu * (B + C): lay["o_radial"] + mu * (B + C) + B]
+        norm = np.sqrt(np.sum(row * row + 1e-30))
+        p[lay["o_radial"] + mu * (B + C): lay["o_radial"] + mu * (B + C) + B] = row / norm
+    heads = C if lay["species_readout"] else 1
+    ncol = C + heads * S
+    d = 0.1
+    # rows and weights per frame
+    cols = []
+    for q in range(heads * S):
+        pq = p.copy()
+        pq[lay["o_species"]: lay["o_species"] + C] = 1.0
+        pq[lay["o_shift"]: lay["o_shift"] + C] = -1.0
+        pq[lay["o_linear"]: lay["o_linear"] + heads * S] = 0.0
+        pq[lay["o_linear"] + q] = 1.0
+        model.set_params(pq)
+        cols.append([model.efs(fr.cell, fr.positions, fr.types) for fr in frames])
+    A = np.zeros((ncol, ncol))
+    b = np.zeros(ncol)
+    for k, fr in enumerate(frames):
+        n = fr.natoms
+        we, wf, ws = wE / n, wF, wS / n
+        if weighting == "structures":
+            we, ws, wf = we / n, ws / n, wf / n
+        elif weighting == "molecules":
+            we, ws = we * n, ws * n
+        avef = float(np.mean(np.sum(fr.forces ** 2, axis=1))) if fr.forces is not None else 0.0
+        scale = d / (d + norm_by_forces * avef)
+        rows, rhs, alpha = [], [], []
+        if fr.energy is not None:
+            e_row = np.zeros(ncol)
+            for t in range(C):
+                e_row[t] = float(np.sum(fr.types == t))
+            for q in range(heads * S):
+                e_row[C + q] = cols[q][k][0]
+            rows.append(e_row); rhs.append(fr.energy); alpha.append(we * scale)
+        if wF > 0 and fr.forces is not None:
+            for i in range(n):
+                for a in range(3):
+                    r = np.zeros(ncol)
+                    for q in range(heads * S):
+                        r[C + q] = cols[q][k][1][i, a]
+                    rows.append(r); rhs.append(fr.forces[i, a]); alpha.append(wf * scale)
+        if wS > 0 and fr.stress is not None:
+            for a in range(3):
+                for bb in range(3):
+                    r = np.zeros(ncol)
+                    for q in range(heads * S):
+                        r[C + q] = virial6_to_matrix(cols[q][k][2])[a, bb]
+                    rows.append(r); rhs.append(fr.stress[a, bb]); alpha.append(ws)
+        for r, y, al in zip(rows, rhs, alpha):
+            A += al * np.outer(r, r)
+            b += al * y * r
+    for i in range(ncol):
+        A[i, i] += 1e-13 * (1.0 + A[i, i])
+    # Gaussian elimination without pivoting, as SolveSLAEGaussian
+    M, x = A.copy(), b.copy()
+    for i in range(ncol - 1):
+        for j in range(i + 1, ncol):
+            ratio = M[j, i] / M[i, i]
+            M[j, i:] -= ratio * M[i, i:]
+            x[j] -= ratio * x[i]
+    x[ncol - 1] /= M[ncol - 1, ncol - 1]
+    for i in range(ncol - 2, -1, -1):
+        x[i] = (x[i] - M[i, i + 1:] @ x[i + 1:]) / M[i, i]
+    p[lay["o_species"]: lay["o_species"] + C] = 1.0
+    p[lay["o_shift"]: lay["o_shift"] + C] = x[:C] - 1.0
+    p[lay["o_linear"]: lay["o_linear"] + heads * S] = x[C:]
+    model.set_params(p)
+    return p

@@ -8,6 +8,9 @@
 //     {"cfg": c, "grad": [...]}                       AccumulateEFSCombinationGrad
 //                                                     (src/basic_mlip.cpp:421, dev_src/mtpr.cpp:9188)
 //
+// Usage: ref-grad --linear MODEL CFG wE wF wS [weighting]
+//   MTPR_trainer::TrainLinear on the labelled CFG; prints {"coeffs": [...]} after the solve.
+//
 // Usage: ref-grad --write MODEL OUT VALUES
 //   Loads MODEL, replaces its parameter vector by the whitespace-separated VALUES (same length
 //   and order as Coeff()), and saves it with MLMTPR::Save, so that the written .sus2 is in the
@@ -18,6 +21,7 @@
 #include "mtpr.h"
 #include "configuration.h"
 #include "non_linear_regression.h"
+#include "mtpr_trainer.h"
 #include <cstdio>
 #include <string>
 #include <fstream>
@@ -80,6 +84,24 @@ int main(int argc, char** argv) {
                                obj.ForceRMSE_meVPerA(), obj.StressMAE_eV(), obj.StressRMSE_eV()};
     std::printf(", \"metrics\": ");
     vec(metrics, 6);
+    std::printf(", \"configs\": %zu}\n", train.size());
+    return 0;
+  }
+  if (std::string(argv[1]) == "--linear") {
+    // ref-grad --linear MODEL CFG wE wF wS [weighting]: MTPR_trainer::TrainLinear
+    // (dev_src/mtpr_trainer.cpp:1455) on the labelled CFG -- the linear warm-up solve of the species
+    // constants and the scalar readout -- and prints the resulting parameter vector.
+    if (argc < 7) { std::fprintf(stderr, "usage: ref-grad --linear MODEL CFG wE wF wS [weighting]\n"); return 2; }
+    MLMTPR mtpr(argv[2]);
+    MTPR_trainer trainer(&mtpr, std::stod(argv[4]), std::stod(argv[5]), std::stod(argv[6]));
+    if (argc > 7) trainer.weighting = argv[7];
+    std::ifstream in(argv[3]);
+    std::vector<Configuration> train;
+    Configuration c;
+    while (c.Load(in)) train.push_back(c);
+    trainer.TrainLinear(0, train, nullptr, "golden");
+    std::printf("{\"coeffs\": ");
+    vec(mtpr.Coeff(), mtpr.CoeffCount());
     std::printf(", \"configs\": %zu}\n", train.size());
     return 0;
   }

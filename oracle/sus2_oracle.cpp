@@ -1047,6 +1047,16 @@ int orc_descriptors(void* mp, int n, const double* cell, const double* pos, cons
   }
 }
 
+// Dimensions and parameter offsets: out[12] = {C, S, B, F, species_readout, o_shift, o_radial,
+// o_species, o_linear, nparams, nblk, K}.
+int orc_layout(void* mp, int* out) {
+  const Model& m = *static_cast<Model*>(mp);
+  const int v[12] = {m.C, m.S, m.B, m.F, m.species_readout ? 1 : 0, m.o_shift, m.o_radial, m.o_species, m.o_linear,
+                     m.nparams, m.nblk, m.K};
+  for (int q = 0; q < 12; ++q) out[q] = v[q];
+  return 0;
+}
+
 int orc_grad_gatex(void* mp, int n, const double* cell, const double* pos, const int* types, const double* ew,
                    const double* fw, const double* sw, double gate_x, double* grad, double* penalty, char* err,
                    int errlen) {

@@ -35,6 +35,9 @@ int orc_grad(void* model, int n, const double* cell, const double* pos, const in
              const double* fw, const double* sw, double* grad, char* err, int errlen);
 /* orc_grad plus the Effect gate-x L2 term of the reference objective with coefficient gate_x:
  * *penalty = the term's value for this configuration, grad += its parameter gradient as well. */
+/* Dimensions and parameter offsets: out[12] = {C, S, B, F, species_readout, o_shift, o_radial,
+ * o_species, o_linear, nparams, nblk, K}. */
+int orc_layout(void* model, int* out);
 /* Per-atom descriptors (the S scalar moments, MLMTPR::CalcDescriptors) of one frame, desc[n][S]. */
 int orc_descriptors(void* model, int n, const double* cell, const double* pos, const int* types, double* desc,
                     char* err, int errlen);

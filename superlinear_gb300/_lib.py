@@ -59,6 +59,7 @@ SIGNATURES = {
     "sus2g_trainer_loss_grad": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "sus2g_trainer_set_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_trainer_metrics": (ctypes.c_int, [_vp, _dp, _dp]),
+    "sus2g_trainer_train_linear": (ctypes.c_int, [_vp, _dp]),
     "sus2g_trainer_bfgs": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_double, _dp, _ip]),
 }
 

@@ -228,6 +228,112 @@ __global__ void k_metrics(int nframes, const int* fbegin, const double* E, const
   }
 }
 
+// ---- linear warm-up (MTPR_trainer::TrainLinear, dev_src/mtpr_trainer.cpp:1455) ------------------
+// Row layout of the component matrix cm[rows][ncol]: energy rows [0, K), force rows
+// [K, K + 3N) in atom order, stress rows [K + 3N, K + 3N + 9K) (a, b row-major per frame).
+// Row weights and right-hand sides follow AddToSLAE (mtpr_trainer.cpp:1130-1453).
+__global__ void k_lin_rows(int nframes, const int* fbegin, const double* E0, const double* F0, const double* S0,
+                           const int* has, LossConfig c, int natoms, double* alpha, double* rhs) {
+  const int f = blockIdx.x;
+  if (f >= nframes) return;
+  const int a0 = fbegin[f], a1 = fbegin[f + 1], n = a1 - a0;
+  __shared__ double red[256];
+  double avef = 0.0;
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x)
+    for (int q = 0; q < 3; ++q) avef += F0[3 * static_cast<size_t>(i) + q] * F0[3 * static_cast<size_t>(i) + q];
+  red[threadIdx.x] = avef;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  avef = (has[f] & 2) && n > 0 ? red[0] / n : 0.0;
+  const double d = 0.1, scale = d / (d + c.norm_by_forces * avef);
+  double we = n > 0 ? c.wE / n : 0.0, wf = c.wF, ws = n > 0 ? c.wS / n : 0.0;
+  if (c.weighting == 1 && n > 0) { we /= n; ws /= n; wf /= n; }
+  else if (c.weighting == 2) { we *= n; ws *= n; }
+  const size_t fr0 = static_cast<size_t>(nframes), sr0 = fr0 + 3 * static_cast<size_t>(natoms);
+  if (threadIdx.x == 0) {
+    alpha[f] = (has[f] & 1) ? we * scale : 0.0;
+    rhs[f] = E0[f];
+    for (int q = 0; q < 9; ++q) {
+      alpha[sr0 + 9 * f + q] = (c.wS > 0 && (has[f] & 4)) ? ws : 0.0;
+      rhs[sr0 + 9 * f + q] = S0[9 * f + q];
+    }
+  }
+  for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x)
+    for (int q = 0; q < 3; ++q) {
+      const size_t r = fr0 + 3 * static_cast<size_t>(i) + q;
+      alpha[r] = (c.wF > 0 && (has[f] & 2)) ? wf * scale : 0.0;
+      rhs[r] = F0[3 * static_cast<size_t>(i) + q];
+    }
+}
+
+// species columns: the frame's count of type t in the energy row (force and stress rows 0)
+__global__ void k_lin_species(int nframes, const int* fbegin, const int* types, int C, int ncol, double* cm) {
+  const int f = blockIdx.x;
+  if (f >= nframes || threadIdx.x >= C) return;
+  int count = 0;
+  for (int i = fbegin[f]; i < fbegin[f + 1]; ++i) count += types[i] == static_cast<int>(threadIdx.x);
+  cm[static_cast<size_t>(f) * ncol + threadIdx.x] = count;
+}
+
+// column col from one evaluation: energies, forces, and the virial as a symmetric 3x3
+__global__ void k_lin_column(int nframes, int natoms, const double* E, const double* F, const double* V, int ncol,
+                             int col, double* cm) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long long rows = nframes + 3LL * natoms + 9LL * nframes;
+  if (t >= rows) return;
+  double v;
+  if (t < nframes) {
+    v = E[t];
+  } else if (t < nframes + 3LL * natoms) {
+    v = F[t - nframes];
+  } else {
+    const long long u = t - nframes - 3LL * natoms;
+    const int f = static_cast<int>(u / 9), ab = static_cast<int>(u - 9LL * f);
+    const double* w = V + 6 * static_cast<size_t>(f);  // (xx, yy, zz, xy, xz, yz)
+    const int map[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
+    v = w[map[ab]];
+  }
+  cm[static_cast<size_t>(t) * ncol + col] = v;
+}
+
+// A[j][k] = sum_r alpha_r cm[r][j] cm[r][k] (k >= j) and b[j] = sum_r alpha_r rhs_r cm[r][j]: one block
+// per output, rows strided over the threads, fixed-order tree (deterministic).  Block index
+// < npairs: pair (j, k) in row-major upper-triangle order; then the ncol entries of b.
+__global__ void k_lin_normal(long long rows, int ncol, const double* cm, const double* alpha, const double* rhs,
+                             double* A, double* b) {
+  __shared__ double red[256];
+  const int npairs = ncol * (ncol + 1) / 2;
+  const int o = blockIdx.x;
+  int j = 0, k = -1;
+  if (o < npairs) {
+    int rem = o;
+    while (rem >= ncol - j) { rem -= ncol - j; ++j; }
+    k = j + rem;
+  } else {
+    j = o - npairs;
+  }
+  double s = 0.0;
+  for (long long r = threadIdx.x; r < rows; r += blockDim.x) {
+    const double a = alpha[r];
+    if (a == 0.0) continue;
+    const double x = cm[static_cast<size_t>(r) * ncol + j];
+    s += k >= 0 ? a * x * cm[static_cast<size_t>(r) * ncol + k] : a * rhs[r] * x;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (k >= 0) A[static_cast<size_t>(j) * ncol + k] = red[0];
+    else b[j] = red[0];
+  }
+}
+
 // loss = sum_f loss_f / K (fixed order), grad /= K
 __global__ void k_loss_finish(int nframes, const double* loss_f, double* loss, double* grad, int nparams) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -539,6 +645,88 @@ class Trainer {
     out6[5] = t[8] > 0 ? std::sqrt(t[7] / t[8]) : 0.0;
   }
 
+  // Linear warm-up (MTPR_trainer::TrainLinear): normalise the radial Chebyshev rows
+  // (MLMTPR::Orthogonalize, dev_src/mtpr.cpp:14110), build the normal equations of the species
+  // constants and the scalar readout from one E/F/virial evaluation per readout column (the model
+  // with that readout weight 1, centre factors 1 and no constant), add the 1e-13 ridge, solve by
+  // Gaussian elimination (SolveSLAE / SolveSLAEGaussian, mtpr_trainer.cpp:971, 282) and apply:
+  // centre factor 1, shift = constant - 1, readout = solution.  params (host) in/out.
+  void train_linear(double* params) {
+    const Model& m = eng_.model();
+    const int C = m.C, S = m.S, B = m.B, F = m.F;
+    const int heads = m.species_readout ? C : 1, ncol = C + heads * S;
+    int o_shift = -1, o_radial = -1, o_species = -1, o_linear = -1;
+    for (const auto& blk : m.layout()) {
+      if (blk.name == "shift_coeffs") o_shift = blk.offset;
+      else if (blk.name == "radial_coeffs") o_radial = blk.offset;
+      else if (blk.name == "species_coeffs") o_species = blk.offset;
+      else if (blk.name == "moment_coeffs") o_linear = blk.offset;
+    }
+    std::vector<double> p(params, params + nparams_);
+    for (int mu = 0; mu < F; ++mu) {
+      double* row = p.data() + o_radial + static_cast<size_t>(mu) * (B + C);
+      double norm = 0.0;
+      for (int b = 0; b < B; ++b) norm += row[b] * row[b] + 1e-30;
+      norm = std::sqrt(norm);
+      for (int b = 0; b < B; ++b) row[b] /= norm;
+    }
+    if (eng_.edge_generation() != generation_) bind_edges();
+    cudaStream_t s = eng_.stream();
+    const long long rows = nframes_ + 3LL * natoms_ + 9LL * nframes_;
+    lin_cm_.ensure(sizeof(double) * static_cast<size_t>(std::max(1LL, rows)) * ncol);
+    lin_alpha_.ensure(sizeof(double) * std::max(1LL, rows));
+    lin_rhs_.ensure(sizeof(double) * std::max(1LL, rows));
+    lin_A_.ensure(sizeof(double) * ncol * ncol);
+    lin_b_.ensure(sizeof(double) * ncol);
+    TRAIN_CUDA(cudaMemsetAsync(lin_cm_.ptr, 0, sizeof(double) * static_cast<size_t>(std::max(1LL, rows)) * ncol, s));
+    TRAIN_CUDA(cudaMemsetAsync(lin_A_.ptr, 0, sizeof(double) * ncol * ncol, s));
+    if (nframes_) {
+      k_lin_rows<<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), E0_.as<double>(), F0_.as<double>(),
+                                          S0_.as<double>(), has_.as<int>(), cfg_, natoms_, lin_alpha_.as<double>(),
+                                          lin_rhs_.as<double>());
+      k_lin_species<<<nframes_, 64, 0, s>>>(nframes_, fbegin_.as<int>(), types_.as<int>(), C, ncol, lin_cm_.as<double>());
+    }
+    for (int q = 0; q < heads * S; ++q) {
+      std::vector<double> pq(p);
+      for (int t = 0; t < C; ++t) { pq[o_species + t] = 1.0; pq[o_shift + t] = -1.0; }
+      for (int r = 0; r < heads * S; ++r) pq[o_linear + r] = r == q ? 1.0 : 0.0;
+      eng_.set_params(pq.data());
+      eng_.efs(E_.as<double>(), F_.as<double>(), V_.as<double>(), nullptr);
+      if (rows)
+        k_lin_column<<<static_cast<unsigned>((rows + 255) / 256), 256, 0, s>>>(
+            nframes_, natoms_, E_.as<double>(), F_.as<double>(), V_.as<double>(), ncol, C + q, lin_cm_.as<double>());
+    }
+    const int outputs = ncol * (ncol + 1) / 2 + ncol;
+    k_lin_normal<<<outputs, 256, 0, s>>>(rows, ncol, lin_cm_.as<double>(), lin_alpha_.as<double>(),
+                                         lin_rhs_.as<double>(), lin_A_.as<double>(), lin_b_.as<double>());
+    std::vector<double> A(static_cast<size_t>(ncol) * ncol), x(ncol);
+    TRAIN_CUDA(cudaMemcpyAsync(A.data(), lin_A_.ptr, sizeof(double) * A.size(), cudaMemcpyDeviceToHost, s));
+    TRAIN_CUDA(cudaMemcpyAsync(x.data(), lin_b_.ptr, sizeof(double) * ncol, cudaMemcpyDeviceToHost, s));
+    TRAIN_CUDA(cudaStreamSynchronize(s));
+    eng_.check_device_error();
+    for (int i = 0; i < ncol; ++i) {
+      for (int j = i + 1; j < ncol; ++j) A[static_cast<size_t>(j) * ncol + i] = A[static_cast<size_t>(i) * ncol + j];
+      A[static_cast<size_t>(i) * ncol + i] += 1e-13 * (1.0 + A[static_cast<size_t>(i) * ncol + i]);
+    }
+    // Gaussian elimination without pivoting (the reference's solver; the ridged matrix is SPD)
+    for (int i = 0; i + 1 < ncol; ++i)
+      for (int j = i + 1; j < ncol; ++j) {
+        const double ratio = A[static_cast<size_t>(j) * ncol + i] / A[static_cast<size_t>(i) * ncol + i];
+        for (int c = i; c < ncol; ++c) A[static_cast<size_t>(j) * ncol + c] -= ratio * A[static_cast<size_t>(i) * ncol + c];
+        x[j] -= ratio * x[i];
+      }
+    for (int i = ncol - 1; i >= 0; --i) {
+      double t = x[i];
+      for (int j = i + 1; j < ncol; ++j) t -= A[static_cast<size_t>(i) * ncol + j] * x[j];
+      x[i] = t / A[static_cast<size_t>(i) * ncol + i];
+      if (!std::isfinite(x[i])) throw Error(5, "linear warm-up: singular normal equations");
+    }
+    for (int t = 0; t < C; ++t) { p[o_species + t] = 1.0; p[o_shift + t] = x[t] - 1.0; }
+    for (int q = 0; q < heads * S; ++q) p[o_linear + q] = x[C + q];
+    std::copy(p.begin(), p.end(), params);
+    eng_.set_params(params);
+  }
+
   int graph_builds() const { return graph_builds_; }
 
  private:
@@ -552,6 +740,7 @@ class Trainer {
   bool gatex_ = false;
   DevBuf extra_h_, agrad_;  // gate-x term: dP/dh per atom, dP/dalpha per frame
   DevBuf metric_part_;
+  DevBuf lin_cm_, lin_alpha_, lin_rhs_, lin_A_, lin_b_;  // linear warm-up
   double* host_scalars_ = nullptr;
   bool use_graph_ = true;
   cudaGraph_t graph_ = nullptr;
@@ -630,6 +819,13 @@ int sus2g_trainer_metrics(sus2g_trainer t, const double* params, double* out6) {
   return train_guarded([&] {
     if (!t || !params || !out6) throw sus2g::Error(1, "invalid argument: trainer/params/out");
     t->trainer->metrics(params, out6);
+  });
+}
+
+int sus2g_trainer_train_linear(sus2g_trainer t, double* params) {
+  return train_guarded([&] {
+    if (!t || !params) throw sus2g::Error(1, "invalid argument: trainer/params");
+    t->trainer->train_linear(params);
   });
 }
 

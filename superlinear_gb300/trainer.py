@@ -7,6 +7,9 @@ Mirrors the reference trainer's objective / optimiser surface for this path:
                                      frame count as MTPR_trainer::Train does (dev_src/mtpr_trainer.cpp:4737-4745)
   * ``Trainer.bfgs(params, ...)``  ~ the dense BFGS loop of MTPR_trainer::Train over BFGS::Iterate
                                      (src/common/bfgs.cpp:251-329)
+  * ``Trainer.train_linear(params)`` ~ MTPR_trainer::TrainLinear, the linear warm-up before BFGS
+                                     (dev_src/mtpr_trainer.cpp:1455)
+  * ``Trainer.metrics(params)``    ~ the trainer's energy / force / stress MAE and RMSE
 ``weighting`` takes the reference's names: "vibrations", "structures", "molecules".  ``gate_x_l2``
 is the coefficient of the Effect gate-x L2 term of the reference objective (its default 1e-4,
 dev_src/non_linear_regression.h:128; ignored for Static models).
@@ -101,6 +104,14 @@ class Trainer:
         out = np.zeros(6)
         check(load().sus2g_trainer_metrics(self._h, _d(p), _d(out)))
         return dict(zip(self.METRICS, (float(x) for x in out)))
+
+    def train_linear(self, params) -> np.ndarray:
+        """Linear warm-up (MTPR_trainer::TrainLinear): returns the parameters after the solve."""
+        p = np.array(params, dtype=np.float64)
+        if p.size != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
+        check(load().sus2g_trainer_train_linear(self._h, _d(p)))
+        return p
 
     def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
         """Runs BFGS from ``params``; returns (params, loss history)."""

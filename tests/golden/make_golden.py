@@ -285,6 +285,16 @@ def main():
                                                     "force_mae_mev_per_a", "force_rmse_mev_per_a", "stress_mae_ev",
                                                     "stress_rmse_ev"), res["metrics"]))}, fh)
             print(name, "labelled frames", len(frames))
+    # 6. linear warm-up: MTPR_trainer::TrainLinear on the labelled sets
+    os.makedirs(os.path.join(HERE, "linear"), exist_ok=True)
+    for name, _, weights in LOSS_CASES():
+        model = os.path.join(HERE, "models", f"{name}.sus2")
+        cfg = os.path.join(HERE, "frames", f"{name}__labelled.cfg")
+        res = json.loads(run([refgrad, "--linear", model, cfg, *(str(w) for w in weights)]))
+        with open(os.path.join(HERE, "linear", f"{name}__labelled.json"), "w") as fh:
+            json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
+                       "weighting": "vibrations", "source": "reference MTPR_trainer::TrainLinear",
+                       "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 

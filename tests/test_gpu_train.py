@@ -165,3 +165,26 @@ def test_trainer_survives_other_use_of_its_engine(sg, golden):
     eng.calc_efs(training_frames(3, 60, 200, 3.0, 4.2, 0.1, seed=5, species=2))
     again = tr.loss_grad(p)
     assert first[0] == again[0] and np.array_equal(first[1], again[1])
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*.json"))),
+                         ids=os.path.basename)
+def test_linear_warmup_matches_reference_trainer(sg, golden, path):
+    """Trainer.train_linear (GPU components, device normal equations) against the reference's
+    MTPR_trainer::TrainLinear; the FP32 bulk form lowers the objective likewise."""
+    data = load_json(path)
+    model = sg.Model(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    p0 = model.params()
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, *data["weights"], weighting=data["weighting"], gate_x_l2=0.0)
+    p = tr.train_linear(p0)
+    # the normal equations are ill-conditioned (condition numbers 3.3e11 Static, 1.5e8 Effect):
+    # last-bit differences of the FP64 components move the solution by ~1e-9 relative
+    assert np.max(np.abs(p - np.asarray(data["coeffs"])) / (1.0 + np.abs(data["coeffs"]))) < 1e-8
+    tr32 = sg.Trainer(sg.Engine(model, 0, sg.FP32), frames, *data["weights"], weighting=data["weighting"], gate_x_l2=0.0)
+    before, _ = tr32.loss_grad(p0, want_grad=False)
+    p32 = tr32.train_linear(p0)
+    after, _ = tr32.loss_grad(p32, want_grad=False)
+    assert after < before
+    ref_after, _ = tr.loss_grad(p, want_grad=False)
+    assert abs(after - ref_after) <= 1e-3 * abs(ref_after)

@@ -117,3 +117,17 @@ def test_descriptor_goldens(oracle_lib, golden, path):
     ours = np.concatenate([m.descriptors(fr.cell, fr.positions, fr.types, ref.shape[1]) for fr in frames])
     assert np.array_equal(np.concatenate([fr.types for fr in frames]), data["types"])
     assert rel_err(ours, ref) < 1e-13
+
+
+def linear_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*.json")))
+
+
+@pytest.mark.parametrize("path", linear_cases(), ids=os.path.basename)
+def test_linear_warmup_goldens(oracle_lib, golden, path):
+    """The linear warm-up solve against the reference's MTPR_trainer::TrainLinear."""
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    p = oracle_lib.train_linear(m, frames, *data["weights"], weighting=data["weighting"])
+    assert rel_err(p, data["coeffs"]) < 1e-9
