@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <map>
 #include <cstring>
 #include <numeric>
@@ -69,38 +70,30 @@ __global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const d
   atomicAdd(bin_count + bin, 1);
 }
 
-__global__ void k_bin_fill(const int* bin_of, int natoms, const int* bin_start, int* cursor, int* bin_atoms) {
+// Atoms grouped by bin, as one 32-byte record per slot (order inside a bin is arbitrary: each
+// centre's edges are sorted by (j, image) afterwards).
+__global__ void k_bin_fill(const int* bin_of, int natoms, const int* bin_start, int* cursor, const AtomFrac* frac,
+                           const AtomOff* off, BinAtom* bin_rec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   const int bin = bin_of[i];
   if (bin < 0) return;
-  bin_atoms[bin_start[bin] + atomicAdd(cursor + bin, 1)] = i;
+  const AtomFrac f = frac[i];
+  const AtomOff o = off[i];
+  bin_rec[bin_start[bin] + atomicAdd(cursor + bin, 1)] = BinAtom{f.x, f.y, f.z, i, o.x, o.y, o.z, 0};
 }
 
-// Atom order inside a bin is made deterministic (ascending index).
-__global__ void k_bin_sort(const int* bin_start, int nbins, int* bin_atoms) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= nbins) return;
-  int* a = bin_atoms + bin_start[b];
-  const int n = bin_start[b + 1] - bin_start[b];
-  for (int i = 1; i < n; ++i) {
-    const int x = a[i];
-    int j = i - 1;
-    while (j >= 0 && a[j] > x) { a[j + 1] = a[j]; --j; }
-    a[j + 1] = x;
-  }
-}
 
 // Image-scan frames: one thread per centre (cell-list frames are left to the warp kernels).
 __global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                             const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                             const int* bin_start, const int* bin_of, const AtomFrac* frac,
                              const AtomOff* off, int* counts, int* error) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
   if (fp.use_bins) return;
   int n = 0;
-  enumerate_edges(i, 0, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
+  enumerate_edges(i, fp, pos, rc2, error,
                   [&](int, int, int, int, double, double, double, double) { ++n; });
   counts[i] = n;
 }
@@ -117,7 +110,7 @@ __device__ __forceinline__ void write_edge(long long e, int j, int a, int b, int
 
 template <typename Real>
 __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                            const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                            const int* bin_start, const int* bin_of, const AtomFrac* frac,
                             const AtomOff* off, const int* row, int* nbr, typename Vec4<Real>::type* d4,
                             unsigned long long* key, int* error) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -126,7 +119,7 @@ __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const d
   if (fp.use_bins) return;
   int e = row[i];
   const int end = row[i + 1];
-  enumerate_edges(i, 0, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error,
+  enumerate_edges(i, fp, pos, rc2, error,
                   [&](int j, int a, int b, int c, double x, double y, double z, double r2) {
                     if (e >= end) { record_error(error, kErrEdgeCapacity); return; }
                     write_edge<Real>(e++, j, a, b, c, x, y, z, r2, nbr, d4, key);
@@ -141,7 +134,7 @@ constexpr int kFillWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                 const int* bin_start, const int* bin_atoms, const int* bin_of, const AtomFrac* frac,
+                 const int* bin_start, const BinAtom* bin_rec, const int* bin_of, const AtomFrac* frac,
                  const AtomOff* off, int* counts, int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key,
                  int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
@@ -154,7 +147,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
-  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_atoms, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
+  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_rec, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
                  [&](unsigned mask, bool ok, int j, int a, int b, int c, double x, double y, double z, double r2) {
                    if (ok) {
                      const int k = cursor + __popc(mask & below);
@@ -872,7 +865,6 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   bin_count_.ensure(sizeof(int) * (bins + 1));
   bin_start_.ensure(sizeof(int) * (bins + 1));
   bin_cursor_.ensure(sizeof(int) * (bins + 1));
-  bin_atoms_.ensure(sizeof(int) * std::max(1, a));
   DevBuf& bin_of = bin_of_;
   bin_of.ensure(sizeof(int) * std::max(1, a));
   if (nframes) { k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>()); ++launches_; }
@@ -885,7 +877,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                                                bin_count_.as<int>(), frac_.as<AtomFrac>(), off_.as<AtomOff>());
     k_exclusive_scan<<<1, 1024, 0, s>>>(bin_count_.as<int>(), bins, bin_start_.as<int>(), error_.as<int>());
     ++launches_;
-    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(), bin_atoms_.as<int>());
+    bin_rec_.ensure(sizeof(BinAtom) * std::max(1, a));
+    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(),
+                                              frac_.as<AtomFrac>(), off_.as<AtomOff>(), bin_rec_.as<BinAtom>());
     launches_ += 2;
   }
   const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
@@ -893,7 +887,8 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
   const FramePlan* P = plan_.as<FramePlan>();
   const int* FO = frame_of_.as<int>();
-  const int *BS = bin_start_.as<int>(), *BA = bin_atoms_.as<int>(), *BO = bin_of.as<int>();
+  const int *BS = bin_start_.as<int>(), *BO = bin_of.as<int>();
+  const BinAtom* BR = bin_rec_.as<BinAtom>();
   const AtomFrac* FR = frac_.as<AtomFrac>();
   const AtomOff* OF = off_.as<AtomOff>();
   int* overflow = error_.as<int>() + 1;
@@ -905,11 +900,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     pad_key_.ensure(sizeof(unsigned long long) * slots);
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BO, FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BO, FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
                                                                           pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;
@@ -918,7 +913,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
     if (bins) fill_bins();
     if (bins_frames_ < nframes) {
-      k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(), error_.as<int>());
+      k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, counts_.as<int>(), error_.as<int>());
       ++launches_;
     }
   }
@@ -958,7 +953,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
       fill_bins();
       if (bins_frames_ < nframes) {
-        k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, counts_.as<int>(), error_.as<int>());
+        k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, counts_.as<int>(), error_.as<int>());
         ++launches_;
       }
       SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
@@ -976,10 +971,10 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   if (a && bins_frames_ < nframes) {
     unsigned long long* KY = tmp_key_.as<unsigned long long>();
     if (precision_ == kFP32)
-      k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+      k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, row_.as<int>(),
                                                        tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
     else
-      k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BA, BO, FR, OF, row_.as<int>(),
+      k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, row_.as<int>(),
                                                         tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
     ++launches_;
   }
@@ -1173,7 +1168,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (nframes_) {
       int largest = 0;
       for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
-      const int S = std::max(1, std::min(64, (largest + 1023) / 1024));
+      const int S = std::max(1, std::min(64, (largest + 255) / 256));
       frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
       k_frame_partial<<<dim3(nframes_, S), 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, S, site_.as<double>(),
                                                         vir_atom_.as<double>(), frame_partial_.as<double>());

@@ -35,6 +35,9 @@ struct FramePlan {
 // floor(frac) (FP64 arithmetic), written by the binning kernel for cell-list frames.
 struct AtomFrac { float x, y, z; int pad; };
 struct AtomOff { int x, y, z, pad; };
+// One bin slot (atoms grouped by bin): fractional coordinates, the atom's index and its integer
+// cell offset, so that a candidate is one 32-byte load.
+struct __align__(16) BinAtom { float x, y, z; int j; int ox, oy, oz, pad; };
 
 __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, int n2) {
   return (static_cast<unsigned long long>(j) << 21) |
@@ -43,102 +46,57 @@ __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, in
          static_cast<unsigned long long>(n2 + 64);
 }
 
-// Enumerate edges of centre i; Emit(j, n0, n1, n2, dx, dy, dz, r2).  With cell lists, `part`
-// (0..26) selects one of the 27 neighbouring bins so that 27 threads share one centre; the image
-// scan of small frames is done entirely by part 0.  The per-centre order is fixed afterwards by
-// sorting on the (j, n) key, so the emission order does not matter.
+// Image scan of centre i (frames without cell lists): for each j of the frame the image range
+// ceil(-f - reach) .. floor(-f + reach) per axis, f = (x_j - x_i) . inv(cell); Emit(j, n0, n1, n2,
+// dx, dy, dz, r2) for every image inside the cutoff.  The per-centre order is fixed afterwards by
+// sorting on the (j, n) key.
 template <typename Emit>
-__device__ __forceinline__ void enumerate_edges(int i, int part, const FramePlan& fp, const double* pos, double rc2,
-                                                const int* bin_start, const int* bin_atoms, const int* bin_of,
-                                                const AtomFrac* frac, const AtomOff* off, int* error, Emit&& emit) {
+__device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, const double* pos, double rc2, int* error,
+                                                Emit&& emit) {
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   const double* c = fp.cell;
   const double* inv = fp.inv;
-  if (!fp.use_bins) {
-    if (part != 0) return;
-    for (int j = fp.a0; j < fp.a1; ++j) {
-      const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
-      double f[3];
-      int lo[3], hi[3];
-      for (int q = 0; q < 3; ++q) {
-        f[q] = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
-        lo[q] = static_cast<int>(ceil(-f[q] - fp.reach[q]));
-        hi[q] = static_cast<int>(floor(-f[q] + fp.reach[q]));
-      }
-      for (int a = lo[0]; a <= hi[0]; ++a)
-        for (int b = lo[1]; b <= hi[1]; ++b)
-          for (int cc = lo[2]; cc <= hi[2]; ++cc) {
-            if (i == j && a == 0 && b == 0 && cc == 0) continue;
-            const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
-            const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
-            const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
-            const double r2 = vx * vx + vy * vy + vz * vz;
-            if (r2 < rc2) {
-              if (a < -64 || a > 63 || b < -64 || b > 63 || cc < -64 || cc > 63) { record_error(error, kErrImageRange); continue; }
-              emit(j, a, b, cc, vx, vy, vz, r2);
-            }
+  for (int j = fp.a0; j < fp.a1; ++j) {
+    const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
+    double f[3];
+    int lo[3], hi[3];
+    for (int q = 0; q < 3; ++q) {
+      f[q] = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
+      lo[q] = static_cast<int>(ceil(-f[q] - fp.reach[q]));
+      hi[q] = static_cast<int>(floor(-f[q] + fp.reach[q]));
+    }
+    for (int a = lo[0]; a <= hi[0]; ++a)
+      for (int b = lo[1]; b <= hi[1]; ++b)
+        for (int cc = lo[2]; cc <= hi[2]; ++cc) {
+          if (i == j && a == 0 && b == 0 && cc == 0) continue;
+          const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
+          const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
+          const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
+          const double r2 = vx * vx + vy * vy + vz * vz;
+          if (r2 < rc2) {
+            if (a < -64 || a > 63 || b < -64 || b > 63 || cc < -64 || cc > 63) { record_error(error, kErrImageRange); continue; }
+            emit(j, a, b, cc, vx, vy, vz, r2);
           }
-    }
-    return;
+        }
   }
-  // Cell list.  Candidates are screened in FP32 on wrapped fractional coordinates; only those
-  // with r^2 below rc^2 + band (the FP32 rounding bound) get the exact FP64 test, so the edge
-  // set is decided in FP64 exactly as the image scan decides it.
-  const AtomFrac fi = frac[i];
-  const AtomOff oi = off[i];
-  // the centre's own bin, as assigned (in FP64) by the binning kernel
-  const int local = bin_of[i] - fp.bin0;
-  const int bi[3] = {local / (fp.nb[1] * fp.nb[2]), (local / fp.nb[2]) % fp.nb[1], local % fp.nb[2]};
-  const int d0 = part / 9 - 1, d1 = (part / 3) % 3 - 1, d2 = part % 3 - 1;
-  const int raw[3] = {bi[0] + d0, bi[1] + d1, bi[2] + d2};
-  int wb[3], W[3];
-  for (int q = 0; q < 3; ++q) {
-    W[q] = raw[q] < 0 ? -1 : (raw[q] >= fp.nb[q] ? 1 : 0);
-    wb[q] = raw[q] - W[q] * fp.nb[q];
-  }
-  const float* cf = fp.cellf;
-  const float screen = static_cast<float>(rc2 + fp.band);
-  const int bin = fp.bin0 + (wb[0] * fp.nb[1] + wb[1]) * fp.nb[2] + wb[2];
-  for (int p = bin_start[bin]; p < bin_start[bin + 1]; ++p) {
-    const int j = bin_atoms[p];
-    const AtomFrac fj = frac[j];
-    const float sx = fj.x + static_cast<float>(W[0]) - fi.x, sy = fj.y + static_cast<float>(W[1]) - fi.y,
-                sz = fj.z + static_cast<float>(W[2]) - fi.z;
-    const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
-    const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
-    const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
-    if (fx * fx + fy * fy + fz * fz >= screen) continue;
-    const AtomOff oj = off[j];
-    const int n[3] = {W[0] + oi.x - oj.x, W[1] + oi.y - oj.y, W[2] + oi.z - oj.z};
-    if (i == j && n[0] == 0 && n[1] == 0 && n[2] == 0) continue;
-    const double xj = pos[3 * j], yj = pos[3 * j + 1], zj = pos[3 * j + 2];
-    const double vx = xj - xi + n[0] * c[0] + n[1] * c[3] + n[2] * c[6];
-    const double vy = yj - yi + n[0] * c[1] + n[1] * c[4] + n[2] * c[7];
-    const double vz = zj - zi + n[0] * c[2] + n[1] * c[5] + n[2] * c[8];
-    const double r2 = vx * vx + vy * vy + vz * vz;
-    if (r2 < rc2) {
-      if (n[0] < -64 || n[0] > 63 || n[1] < -64 || n[1] > 63 || n[2] < -64 || n[2] > 63) { record_error(error, kErrImageRange); continue; }
-      emit(j, n[0], n[1], n[2], vx, vy, vz, r2);
-    }
-  }
-  (void)inv;
 }
 
 // Cell-list frames, one warp per centre i: the 27 neighbouring bins' atom ranges are laid end to
-// end (prefix sums over lanes) and lanes take consecutive candidates of that flat list.  Candidates
-// that pass the FP32 prefilter are appended to a per-warp queue in shared memory (`queue`, 64
+// end (prefix sums over lanes) and lanes take consecutive candidates of that flat list, two per
+// lane per iteration (independent loads in flight).  Candidates
+// that pass the FP32 prefilter are appended to a per-warp queue in shared memory (`queue`, 128
 // entries); whenever 32 are queued the warp runs the exact FP64 test on a full warp of them, so
 // the FP64 work (1/64 of the FP32 rate on this GPU) is spent on prefilter survivors only rather
 // than on mostly idle lanes.  Accepted edges of each FP64 round are reported through
 // Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r2), so the caller can count or write them
 // with one ballot per round.
-constexpr int kEdgeQueue = 64;
+constexpr int kEdgeQueue = 128;
 __device__ __forceinline__ int pack_image(int n0, int n1, int n2) {
   return ((n0 + 64) << 14) | ((n1 + 64) << 7) | (n2 + 64);
 }
 template <typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
-                                               const int* bin_start, const int* bin_atoms, const int* bin_of,
+                                               const int* bin_start, const BinAtom* bin_rec, const int* bin_of,
                                                const AtomFrac* frac, const AtomOff* off, int* error, int2* queue,
                                                Round&& round) {
   const int lane = threadIdx.x & 31;
@@ -189,8 +147,8 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     const unsigned mask = __ballot_sync(0xffffffffu, ok);
     round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
   };
-  for (int base = 0; base < total; base += 32) {
-    const int cand = base + lane;
+  // candidate cand of the flattened list: FP32 prefilter; returns the packed image (or -1)
+  auto screen_candidate = [&](int cand, int& j) -> int {
     // bin slot k of this candidate: the last lane whose exclusive offset is <= cand
     int k = 0;
 #pragma unroll
@@ -201,43 +159,50 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     }
     const int kstart = __shfl_sync(0xffffffffu, start, k), kex = __shfl_sync(0xffffffffu, excl, k);
     const int W0 = __shfl_sync(0xffffffffu, w0, k), W1 = __shfl_sync(0xffffffffu, w1, k), W2 = __shfl_sync(0xffffffffu, w2, k);
-    bool pre = false;
-    int j = 0, packed = 0;
-    if (cand < total) {
-      j = bin_atoms[kstart + cand - kex];
-      const AtomFrac fj = frac[j];
-      const float sx = fj.x + static_cast<float>(W0) - fi.x, sy = fj.y + static_cast<float>(W1) - fi.y,
-                  sz = fj.z + static_cast<float>(W2) - fi.z;
-      const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
-      const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
-      const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
-      if (fx * fx + fy * fy + fz * fz < screen) {
-        const AtomOff oj = off[j];
-        const int n0 = W0 + oi.x - oj.x, n1 = W1 + oi.y - oj.y, n2 = W2 + oi.z - oj.z;
-        if (!(i == j && n0 == 0 && n1 == 0 && n2 == 0)) {
-          if (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63) {
-            record_error(error, kErrImageRange);
-          } else {
-            pre = true;
-            packed = pack_image(n0, n1, n2);
-          }
-        }
-      }
+    if (cand >= total) return -1;
+    const BinAtom rec = bin_rec[kstart + cand - kex];
+    j = rec.j;
+    const float sx = rec.x + static_cast<float>(W0) - fi.x, sy = rec.y + static_cast<float>(W1) - fi.y,
+                sz = rec.z + static_cast<float>(W2) - fi.z;
+    const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
+    const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
+    const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
+    if (fx * fx + fy * fy + fz * fz >= screen) return -1;
+    const int n0 = W0 + oi.x - rec.ox, n1 = W1 + oi.y - rec.oy, n2 = W2 + oi.z - rec.oz;
+    if (i == j && n0 == 0 && n1 == 0 && n2 == 0) return -1;
+    if (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63) {
+      record_error(error, kErrImageRange);
+      return -1;
     }
+    return pack_image(n0, n1, n2);
+  };
+  auto push = [&](int packed, int j) {
+    const bool pre = packed >= 0;
     const unsigned m = __ballot_sync(0xffffffffu, pre);
     if (pre) queue[queued + __popc(m & below)] = make_int2(j, packed);
     queued += __popc(m);
+  };
+  // two independent candidates per lane per iteration (their loads overlap)
+  for (int base = 0; base < total; base += 64) {
+    int ja = 0, jb = 0;
+    const int pa = screen_candidate(base + lane, ja);
+    const int pb = screen_candidate(base + 32 + lane, jb);
+    push(pa, ja);
+    push(pb, jb);
     __syncwarp();
-    if (queued >= 32) {
+    while (queued >= 32) {
       drain(32);
       __syncwarp();
-      // move the remainder (< 32 entries) to the front
-      int2 rest = make_int2(0, 0);
-      if (lane < queued - 32) rest = queue[32 + lane];
-      __syncwarp();
-      if (lane < queued - 32) queue[lane] = rest;
+      // move the remainder (< 96 entries) to the front, 32 at a time in order
+      for (int q0 = 32; q0 < queued; q0 += 32) {
+        int2 rest = make_int2(0, 0);
+        const bool have = q0 + lane < queued;
+        if (have) rest = queue[q0 + lane];
+        __syncwarp();
+        if (have) queue[q0 - 32 + lane] = rest;
+        __syncwarp();
+      }
       queued -= 32;
-      __syncwarp();
     }
   }
   if (queued > 0) drain(queued);
