@@ -89,6 +89,13 @@ int sus2g_calc_efs_host(sus2g_engine engine, int nframes, const int* natoms, con
 int sus2g_calc_efs_device(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
                           const double* positions, const int* types, double* energy, double* forces,
                           double* virial, double* site_energy);
+/* Step graph of the two calls above: when two consecutive calls have the same layout (frame
+ * sizes, cells, buffer addresses, stream) and every frame uses cell lists, the second is captured
+ * as one CUDA graph (edge build + E/F/virial) and later ones replay it -- positions may change
+ * between calls, as in an MD run.  Another edge build on the engine, a parameter update, the
+ * stage timer or a neighbour-capacity overflow makes the next call eager again.
+ * enabled = 1 (default) or 0. */
+int sus2g_engine_set_step_graph(sus2g_engine engine, int enabled);
 
 /* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
  * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors

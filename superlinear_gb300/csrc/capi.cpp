@@ -156,6 +156,10 @@ int sus2g_engine_set_timing(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_timing(enabled != 0); });
 }
 
+int sus2g_engine_set_step_graph(sus2g_engine e, int enabled) {
+  return guarded([&] { need(e, "engine"); e->engine->set_step_graphs(enabled != 0); });
+}
+
 int sus2g_engine_take_stage_times(sus2g_engine e, double* ms, int* counts) {
   return guarded([&] { need(e, "engine"); e->engine->take_stage_times(ms, counts); });
 }
@@ -170,8 +174,7 @@ int sus2g_calc_efs_device(sus2g_engine e, int nframes, const int* natoms, const 
     auto& eng = *e->engine;
     for (int attempt = 0;; ++attempt) {
       try {
-        eng.build_edges(nframes, natoms, cells, positions, types);
-        eng.efs(energy, forces, virial, site_energy);
+        eng.step_frames(nframes, natoms, cells, positions, types, energy, forces, virial, site_energy);
         eng.check_device_error();
         break;
       } catch (const sus2g::EdgeOverflow&) {
@@ -202,9 +205,9 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
     }
     for (int attempt = 0;; ++attempt) {
       try {
-        eng.build_edges(nframes, natoms, cells, pos.as<double>(), typ.as<int>());
-        eng.efs(energy ? out_e.as<double>() : nullptr, forces ? out_f.as<double>() : nullptr,
-                virial ? out_v.as<double>() : nullptr, site_energy ? out_s.as<double>() : nullptr);
+        eng.step_frames(nframes, natoms, cells, pos.as<double>(), typ.as<int>(), energy ? out_e.as<double>() : nullptr,
+                        forces ? out_f.as<double>() : nullptr, virial ? out_v.as<double>() : nullptr,
+                        site_energy ? out_s.as<double>() : nullptr);
         eng.check_device_error();
         break;
       } catch (const sus2g::EdgeOverflow&) {

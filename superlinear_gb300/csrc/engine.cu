@@ -72,15 +72,22 @@ __global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const d
 
 // Atoms grouped by bin, as one 32-byte record per slot (order inside a bin is arbitrary: each
 // centre's edges are sorted by (j, image) afterwards).
-__global__ void k_bin_fill(const int* bin_of, int natoms, const int* bin_start, int* cursor, const AtomFrac* frac,
-                           const AtomOff* off, BinAtom* bin_rec) {
+__global__ void k_bin_fill(const FramePlan* plans, const int* frame_of, const double* pos, const int* bin_of,
+                           int natoms, const int* bin_start, int* cursor, const AtomFrac* frac, const AtomOff* off,
+                           BinAtom* bin_rec, BinPos* bin_pos) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   const int bin = bin_of[i];
   if (bin < 0) return;
   const AtomFrac f = frac[i];
   const AtomOff o = off[i];
-  bin_rec[bin_start[bin] + atomicAdd(cursor + bin, 1)] = BinAtom{f.x, f.y, f.z, i, o.x, o.y, o.z, 0};
+  const double* c = plans[frame_of[i]].cell;
+  const int slot = bin_start[bin] + atomicAdd(cursor + bin, 1);
+  bin_rec[slot] = BinAtom{f.x, f.y, f.z, i, o.x, o.y, o.z, 0};
+  const double a0 = o.x, a1 = o.y, a2 = o.z;
+  bin_pos[slot] = BinPos{pos[3 * i] - (a0 * c[0] + a1 * c[3] + a2 * c[6]),
+                         pos[3 * i + 1] - (a0 * c[1] + a1 * c[4] + a2 * c[7]),
+                         pos[3 * i + 2] - (a0 * c[2] + a1 * c[5] + a2 * c[8]), i, 0};
 }
 
 
@@ -103,7 +110,11 @@ __device__ __forceinline__ void write_edge(long long e, int j, int a, int b, int
                                            int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key) {
   nbr[e] = j;
   typename Vec4<Real>::type v;
-  v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
+  v.x = Real(x); v.y = Real(y); v.z = Real(z);
+  // FP32 records: the distance from the rounded r^2 (an FP32 square root; the FP64 one costs tens
+  // of FP64-pipe instructions)
+  if constexpr (sizeof(Real) == 4) v.w = sqrtf(static_cast<float>(r2));
+  else v.w = sqrt(r2);
   d4[e] = v;
   key[e] = edge_key(j, a, b, c);
 }
@@ -134,9 +145,9 @@ constexpr int kFillWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                 const int* bin_start, const BinAtom* bin_rec, const int* bin_of, const AtomFrac* frac,
-                 const AtomOff* off, int* counts, int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key,
-                 int* overflow, int* error) {
+                 const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos, const int* bin_of,
+                 const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr, typename Vec4<Real>::type* d4,
+                 unsigned long long* key, int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
@@ -147,7 +158,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
-  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_rec, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
+  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_rec, bin_pos, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
                  [&](unsigned mask, bool ok, int j, int a, int b, int c, double x, double y, double z, double r2) {
                    if (ok) {
                      const int k = cursor + __popc(mask & below);
@@ -406,7 +417,11 @@ __global__ void k_scatter_user_edges(const int* ei, const int* ej, const double*
   const int p = row[i] + atomicAdd(cursor + i, 1);
   nbr[p] = j;
   typename Vec4<Real>::type v;
-  v.x = Real(x); v.y = Real(y); v.z = Real(z); v.w = Real(sqrt(r2));
+  v.x = Real(x); v.y = Real(y); v.z = Real(z);
+  // FP32 records: the distance from the rounded r^2 (an FP32 square root; the FP64 one costs tens
+  // of FP64-pipe instructions)
+  if constexpr (sizeof(Real) == 4) v.w = sqrtf(static_cast<float>(r2));
+  else v.w = sqrt(r2);
   d4[p] = v;
   // Order key: neighbour, then the caller's edge index (unique, deterministic).
   key[p] = (static_cast<unsigned long long>(j) << 32) | static_cast<unsigned long long>(e & 0xffffffffLL);
@@ -601,6 +616,7 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
 }
 
 Engine::~Engine() {
+  reset_step_graph();
   delete plans_;
   if (host_total_) cudaFreeHost(host_total_);
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
@@ -720,6 +736,7 @@ void Engine::upload_model() {
   SUS2G_CUDA(cudaSetDevice(device_));
   // work already queued on the engine's stream may still read the tables being replaced
   if (stream_) SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  reset_step_graph();  // a captured step holds the old tables' values
   if (precision_ == kFP32) upload_tables<float>();
   else upload_tables<double>();
 }
@@ -742,6 +759,7 @@ void Engine::check_device_error() {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 2 * sizeof(int), stream_));
     cap_scale_ *= 2.0;
     min_cap_ = std::max(min_cap_, over);
+    reset_step_graph();
     throw EdgeOverflow();
   }
   if (h) {
@@ -858,7 +876,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   cudaStream_t s = stream_;
   mark_begin(0);
   plan_.ensure(sizeof(FramePlan) * std::max(1, nframes));
-  if (nframes) SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
+  // (a captured step leaves the plans out: they are on the device already, identical by the step key)
+  if (nframes && !capturing_)
+    SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
   frame_of_.ensure(sizeof(int) * std::max(1, a));
   counts_.ensure(sizeof(int) * (a + 1));
   row_.ensure(sizeof(int) * (a + 1));
@@ -878,8 +898,10 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     k_exclusive_scan<<<1, 1024, 0, s>>>(bin_count_.as<int>(), bins, bin_start_.as<int>(), error_.as<int>());
     ++launches_;
     bin_rec_.ensure(sizeof(BinAtom) * std::max(1, a));
-    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(bin_of.as<int>(), a, bin_start_.as<int>(), bin_cursor_.as<int>(),
-                                              frac_.as<AtomFrac>(), off_.as<AtomOff>(), bin_rec_.as<BinAtom>());
+    bin_pos_.ensure(sizeof(BinPos) * std::max(1, a));
+    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, bin_of.as<int>(), a,
+                                              bin_start_.as<int>(), bin_cursor_.as<int>(), frac_.as<AtomFrac>(),
+                                              off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>());
     launches_ += 2;
   }
   const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
@@ -889,6 +911,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const int* FO = frame_of_.as<int>();
   const int *BS = bin_start_.as<int>(), *BO = bin_of.as<int>();
   const BinAtom* BR = bin_rec_.as<BinAtom>();
+  const BinPos* BP = bin_pos_.as<BinPos>();
   const AtomFrac* FR = frac_.as<AtomFrac>();
   const AtomOff* OF = off_.as<AtomOff>();
   int* overflow = error_.as<int>() + 1;
@@ -900,11 +923,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     pad_key_.ensure(sizeof(unsigned long long) * slots);
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BO, FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BO, FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
                                                                           pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;
@@ -1379,6 +1402,90 @@ void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d
     throw Error(1, "Effect models on a ghost layout need the caller's gate-signal exchange: use the staged calls");
   if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site, kStageAll);
   else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
+}
+
+void Engine::reset_step_graph() {
+  if (step_exec_) cudaGraphExecDestroy(step_exec_);
+  if (step_graph_) cudaGraphDestroy(step_graph_);
+  step_exec_ = nullptr;
+  step_graph_ = nullptr;
+  step_key_.clear();
+}
+
+void Engine::step_frames(int nframes, const int* frame_natoms, const double* cells, const double* d_pos,
+                         const int* d_types, double* d_energy, double* d_forces, double* d_virial, double* d_site) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  // layout key: everything the captured launches depend on besides device memory contents
+  std::vector<double> key;
+  key.reserve(16 + 10 * static_cast<size_t>(std::max(0, nframes)));
+  auto ptr = [](const void* p) { return static_cast<double>(reinterpret_cast<uintptr_t>(p)); };
+  key.push_back(nframes);
+  for (int f = 0; f < nframes; ++f) {
+    key.push_back(frame_natoms[f]);
+    for (int q = 0; q < 9; ++q) key.push_back(cells[9 * f + q]);
+  }
+  for (const void* p : {static_cast<const void*>(d_pos), static_cast<const void*>(d_types),
+                        static_cast<const void*>(d_energy), static_cast<const void*>(d_forces),
+                        static_cast<const void*>(d_virial), static_cast<const void*>(d_site),
+                        static_cast<const void*>(stream_)})
+    key.push_back(ptr(p));
+  key.push_back(cap_scale_);
+  key.push_back(min_cap_);
+  // the same layout as the previous step, with no other edge build, staged call or parameter
+  // upload since (those may have regrown the buffers whose addresses a graph holds)
+  const bool same = step_graphs_ && !timing_ && key == step_key_ && edge_generation_ == step_gen_;
+  if (same && step_exec_) {
+    SUS2G_CUDA(cudaGraphLaunch(step_exec_, stream_));
+    launches_ += step_launches_;
+    step_gen_ = ++edge_generation_;  // the replay rebuilds the edge arrays
+    nedges_exact_ = false;
+    return;
+  }
+  // cell-list batches build their edges without host synchronisation: the second step of a
+  // layout is captured and launched, later ones replay (a one-off layout is never captured)
+  if (same && nframes > 0 && bins_frames_ == nframes) {
+    reset_step_graph();
+    const int before = launches_;
+    capturing_ = true;
+    cudaGraph_t graph = nullptr;
+    cudaError_t err = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeRelaxed);
+    if (err == cudaSuccess) {
+      try {
+        build_edges(nframes, frame_natoms, cells, d_pos, d_types);
+        efs(d_energy, d_forces, d_virial, d_site);
+      } catch (...) {
+        capturing_ = false;
+        cudaStreamEndCapture(stream_, &graph);
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        launches_ = before;
+        throw;
+      }
+      err = cudaStreamEndCapture(stream_, &graph);
+    }
+    capturing_ = false;
+    step_launches_ = launches_ - before;
+    launches_ = before;  // the capture ran nothing
+    if (err == cudaSuccess && graph && cudaGraphInstantiate(&step_exec_, graph, 0) == cudaSuccess) {
+      step_graph_ = graph;
+      SUS2G_CUDA(cudaGraphLaunch(step_exec_, stream_));
+      launches_ += step_launches_;
+      step_key_ = key;
+      step_gen_ = edge_generation_;
+      return;
+    }
+    // capture refused (e.g. a legacy-stream caller): run this step eagerly and stop capturing
+    cudaGetLastError();
+    if (graph) cudaGraphDestroy(graph);
+    step_exec_ = nullptr;
+    step_graphs_ = false;
+  } else {
+    reset_step_graph();
+  }
+  build_edges(nframes, frame_natoms, cells, d_pos, d_types);
+  efs(d_energy, d_forces, d_virial, d_site);
+  step_key_ = key;
+  step_gen_ = edge_generation_;
 }
 
 void Engine::stage_begin(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j,

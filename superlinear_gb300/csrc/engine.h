@@ -57,6 +57,16 @@ class Engine {
   void set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j,
                  const double* d_d);
 
+  // One E/F/virial step of periodic frames with device positions / types / outputs (build_edges +
+  // efs).  For cell-list batches the second consecutive step of a layout -- frame sizes, cells,
+  // buffer addresses, stream -- is captured as a CUDA graph and later ones replay it (positions
+  // may change: the replay reads them); a layout change, any other edge build, a parameter
+  // upload, the stage timer or a capacity overflow makes the next step eager again.
+  void step_frames(int nframes, const int* frame_natoms, const double* cells, const double* d_pos, const int* d_types,
+                   double* d_energy, double* d_forces, double* d_virial, double* d_site);
+  void set_step_graphs(bool on) { step_graphs_ = on; if (!on) reset_step_graph(); }
+  void reset_step_graph();
+
   // --- evaluation ---------------------------------------------------------------------------
   // E / F / virial for the current edges.  Outputs (device, double): per-frame energy [nframes],
   // forces [natoms][3], per-frame virial [nframes][6] in (xx, yy, zz, xy, xz, yz), site energies
@@ -140,6 +150,13 @@ class Engine {
   void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages);
   int staged_ = 0;  // staged evaluation: 1 after begin, 2 after outer
   double* desc_out_ = nullptr;
+  // step graph (step_frames)
+  bool step_graphs_ = true, capturing_ = false;
+  cudaGraph_t step_graph_ = nullptr;
+  cudaGraphExec_t step_exec_ = nullptr;
+  std::vector<double> step_key_;
+  int step_launches_ = 0;
+  unsigned long long step_gen_ = ~0ull;
   template <typename Real>
   void run_grad(const double* ew, const double* fw, const double* sw, double* grad, const double* extra_h);
   DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;
@@ -165,7 +182,7 @@ class Engine {
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
   DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
-  DevBuf bin_count_, bin_start_, bin_cursor_, bin_rec_;
+  DevBuf bin_count_, bin_start_, bin_cursor_, bin_rec_, bin_pos_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf hbar_atom_, bin_of_, frac_, off_, in_row_, in_edge_;  // in_*: caller edges grouped by neighbour

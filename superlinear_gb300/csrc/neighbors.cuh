@@ -38,6 +38,10 @@ struct AtomOff { int x, y, z, pad; };
 // One bin slot (atoms grouped by bin): fractional coordinates, the atom's index and its integer
 // cell offset, so that a candidate is one 32-byte load.
 struct __align__(16) BinAtom { float x, y, z; int j; int ox, oy, oz, pad; };
+// The same slot's exact position wrapped into the home cell, x - floor(frac) . cell (FP64), and the
+// atom's index: the exact test forms x_j + n.cell - x_i as wrapped x_j + ((w + off_i) . cell - x_i),
+// whose second term is one constant per (centre, neighbouring bin).
+struct __align__(16) BinPos { double x, y, z; int j, pad; };
 
 __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, int n2) {
   return (static_cast<unsigned long long>(j) << 21) |
@@ -96,9 +100,9 @@ __device__ __forceinline__ int pack_image(int n0, int n1, int n2) {
 }
 template <typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
-                                               const int* bin_start, const BinAtom* bin_rec, const int* bin_of,
-                                               const AtomFrac* frac, const AtomOff* off, int* error, int2* queue,
-                                               Round&& round) {
+                                               const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos,
+                                               const int* bin_of, const AtomFrac* frac, const AtomOff* off,
+                                               int* error, int2* queue, Round&& round) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const int local = bin_of[i] - fp.bin0;
@@ -124,31 +128,47 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
   const int excl = incl - len;
   const AtomFrac fi = frac[i];
   const AtomOff oi = off[i];
-  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
   const double* c = fp.cell;
   const float* cf = fp.cellf;
+  // lane k < 27: shift of bin slot k, (w_k + off_i) . cell - x_i
+  double sx = 0, sy = 0, sz = 0;
+  if (lane < 27) {
+    const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
+    sx = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
+    sy = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
+    sz = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
+  }
   const float screen = static_cast<float>(rc2 + fp.band);
   int queued = 0;  // warp-uniform
   // exact FP64 test of queue entries [0, n) (one per lane) and the round callback
+  // queue entry: (bin slot, packed image | neighbouring-bin index k << 21)
   auto drain = [&](int n) {
     bool ok = false;
-    int j = 0, n0 = 0, n1 = 0, n2 = 0;
+    int j = 0, n0 = 0, n1 = 0, n2 = 0, k = 0;
+    int2 q = make_int2(0, 0);
+    if (lane < n) {
+      q = queue[lane];
+      k = q.y >> 21;
+    }
+    const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
+                 kz = __shfl_sync(0xffffffffu, sz, k);
     double vx = 0, vy = 0, vz = 0, r2 = 0;
     if (lane < n) {
-      const int2 q = queue[lane];
-      j = q.x;
+      const BinPos bp = bin_pos[q.x];
+      j = bp.j;
       n0 = ((q.y >> 14) & 127) - 64; n1 = ((q.y >> 7) & 127) - 64; n2 = (q.y & 127) - 64;
-      vx = pos[3 * j] - xi + n0 * c[0] + n1 * c[3] + n2 * c[6];
-      vy = pos[3 * j + 1] - yi + n0 * c[1] + n1 * c[4] + n2 * c[7];
-      vz = pos[3 * j + 2] - zi + n0 * c[2] + n1 * c[5] + n2 * c[8];
+      vx = bp.x + kx;
+      vy = bp.y + ky;
+      vz = bp.z + kz;
       r2 = vx * vx + vy * vy + vz * vz;
       ok = r2 < rc2;
     }
     const unsigned mask = __ballot_sync(0xffffffffu, ok);
     round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
   };
-  // candidate cand of the flattened list: FP32 prefilter; returns the packed image (or -1)
-  auto screen_candidate = [&](int cand, int& j) -> int {
+  // candidate cand of the flattened list: FP32 prefilter; returns the packed image with the
+  // neighbouring-bin index (or -1) and the candidate's bin slot
+  auto screen_candidate = [&](int cand, int& slot) -> int {
     // bin slot k of this candidate: the last lane whose exclusive offset is <= cand
     int k = 0;
 #pragma unroll
@@ -160,8 +180,9 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     const int kstart = __shfl_sync(0xffffffffu, start, k), kex = __shfl_sync(0xffffffffu, excl, k);
     const int W0 = __shfl_sync(0xffffffffu, w0, k), W1 = __shfl_sync(0xffffffffu, w1, k), W2 = __shfl_sync(0xffffffffu, w2, k);
     if (cand >= total) return -1;
-    const BinAtom rec = bin_rec[kstart + cand - kex];
-    j = rec.j;
+    slot = kstart + cand - kex;
+    const BinAtom rec = bin_rec[slot];
+    const int j = rec.j;
     const float sx = rec.x + static_cast<float>(W0) - fi.x, sy = rec.y + static_cast<float>(W1) - fi.y,
                 sz = rec.z + static_cast<float>(W2) - fi.z;
     const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
@@ -174,12 +195,12 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
       record_error(error, kErrImageRange);
       return -1;
     }
-    return pack_image(n0, n1, n2);
+    return pack_image(n0, n1, n2) | (k << 21);
   };
-  auto push = [&](int packed, int j) {
+  auto push = [&](int packed, int slot) {
     const bool pre = packed >= 0;
     const unsigned m = __ballot_sync(0xffffffffu, pre);
-    if (pre) queue[queued + __popc(m & below)] = make_int2(j, packed);
+    if (pre) queue[queued + __popc(m & below)] = make_int2(slot, packed);
     queued += __popc(m);
   };
   // two independent candidates per lane per iteration (their loads overlap)

@@ -110,6 +110,10 @@ class Engine:
         check(load().sus2g_engine_edge_count(self._h, ctypes.byref(n)))
         return n.value
 
+    def set_step_graph(self, on: bool) -> None:
+        """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
+        check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))
+
     STAGES = ("edges", "outer", "gate_forward", "gate_reverse", "gather")
 
     def set_timing(self, on: bool) -> None:
