@@ -334,6 +334,33 @@ def run_profile_train(args):
     return 0
 
 
+def run_profile_effect(args):
+    """FP32 E/F/virial steps of the Effect L4/K8/R2/O3 model on a diamond of --cells cells per edge
+    (24 -> the 110,592-atom configuration; smaller boxes for ncu captures)."""
+    import torch
+
+    import superlinear_gb300 as sg
+    from superlinear_gb300.synth import diamond
+    fr = diamond(args.cells, a=3.567, sigma=0.1, seed=4, species=2, type_prob=0.5)
+    dev = torch.device("cuda", 0)
+    eng = sg.Engine(sg.Model(EFFECT_MODEL), 0, sg.FP32)
+    pos = torch.tensor(fr.positions, device=dev)
+    typ = torch.tensor(fr.types, device=dev)
+    out = torch.zeros(fr.natoms * 3 + 7, dtype=torch.float64, device=dev)
+    args_ = (np.array([fr.natoms], np.int32), fr.cell.reshape(1, 9).copy(), pos.data_ptr(), typ.data_ptr(),
+             out.data_ptr(), out.data_ptr() + 8, out.data_ptr() + 8 * (1 + 3 * fr.natoms), 0)
+    for _ in range(args.warmup + args.steps):
+        eng.calc_efs_device(*args_)
+    torch.cuda.synchronize()
+    eng.set_timing(True)
+    eng.take_stage_times()
+    eng.calc_efs_device(*args_)
+    stages = {k: v[0] for k, v in eng.take_stage_times().items() if v[1]}
+    print(json.dumps({"profile_effect": True, "atoms": fr.natoms, "edges": eng.edge_count(), "stages_ms": stages}),
+          flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -553,6 +580,8 @@ def main():
     ap.add_argument("--profile-train", action="store_true",
                     help="only FP32 training loss+gradient steps over the 256-frame batch (for ncu launch lists)")
     ap.add_argument("--no-graph", action="store_true", help="with --profile-train: eager launches instead of the graph")
+    ap.add_argument("--profile-effect", action="store_true",
+                    help="only FP32 Effect L4/K8/R2/O3 steps on a --cells diamond (for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -560,6 +589,8 @@ def main():
         return run_reference(args)
     if args.profile_train:
         return run_profile_train(args)
+    if args.profile_effect:
+        return run_profile_effect(args)
     return run_ours(args)
 
 

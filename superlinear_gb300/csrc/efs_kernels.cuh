@@ -23,6 +23,8 @@
 // pass recomputes Y and R per edge instead of storing them and writes g_e per edge; forces are
 // gathered per atom through the reverse-edge permutation by a separate kernel.
 #pragma once
+#include <type_traits>
+
 #include "basis.cuh"
 
 namespace sus2g {
@@ -53,9 +55,26 @@ template <typename Real>
 __host__ __device__ inline int pass_table_size(int C, int F, int B, int nblk) {
   return F * B + 2 * nblk * C * C + 3 * C * F;
 }
+__host__ __device__ constexpr int round4(int n) { return (n + 3) & ~3; }
+// Staged edge row of the forward reduction: u_mu at [0, F), Y_h at [stage_yoff, + H), padded so
+// that rows start on 16-byte boundaries and the row stride in 16-byte units is odd (128-bit row
+// stores of a warp then hit distinct bank groups).
+__host__ __device__ constexpr int stage_yoff(int F) { return round4(F); }
+__host__ __device__ constexpr int stage_stride(int F, int H) {
+  return ((round4(stage_yoff(F) + H) / 4) % 2) ? round4(stage_yoff(F) + H) : round4(stage_yoff(F) + H) + 4;
+}
+// E/F/virial pass tables: radial coefficients [F][B], warp (slope, shift) [2 nblk][C^2], and per
+// species pair (t_i, t_j) the products x0(t_i) x1(t_j) and x0(t_i) wadd(t_j) [C^2][F] each.
+__host__ __device__ inline int efs_table_size(int C, int F, int B, int nblk) {
+  return round4(F * B + 2 * nblk * C * C + 2 * C * C * F);
+}
+// Per-warp scratch: the staged edge rows, the node values v [M], the node adjoints [M] (in the
+// staging rows when they fit: those are free once the forward reduction is done), abar [K][H] and
+// hbar [F].
+__host__ __device__ constexpr bool adj_in_stage(int F, int H, int M) { return M <= kWarp * stage_stride(F, H); }
 template <typename Real>
 __host__ __device__ inline int pass_warp_size(int F, int H, int M, int K) {
-  return kWarp * (F + H + 1) + 2 * M + K * H + F + 4;
+  return round4(kWarp * stage_stride(F, H) + M + (adj_in_stage(F, H, M) ? 0 : M) + K * H + F + 4);
 }
 
 // Kahan-compensated accumulation for the FP32 bulk form; plain sums in FP64.
@@ -76,6 +95,73 @@ __device__ __forceinline__ void kadd(Real& s, Real& c, Real x) {
 // The warp (slope, shift) depends on (scaling block, t_i, t_j); the Chebyshev part is shared by
 // every l of a block and only the envelope differs between l = 0 and l > 0 with two cutoffs.
 // ---------------------------------------------------------------------------------------------
+// One row of radial coefficients (16-byte aligned when BF > 0: rows of BF = 8 values from an
+// aligned table) into registers, with 128-bit loads where the size allows.
+template <typename Real, int BF, int NBM>
+__device__ __forceinline__ void load_coeff_row(const Real* c, int B, Real (&cc)[NBM]) {
+  if constexpr (BF > 0 && sizeof(Real) == 4 && BF % 4 == 0) {
+    const float4* c4 = reinterpret_cast<const float4*>(c);
+#pragma unroll
+    for (int q = 0; q < BF / 4; ++q) {
+      const float4 v = c4[q];
+      cc[4 * q] = v.x; cc[4 * q + 1] = v.y; cc[4 * q + 2] = v.z; cc[4 * q + 3] = v.w;
+    }
+  } else if constexpr (BF > 0 && sizeof(Real) == 8 && BF % 2 == 0) {
+    const double2* c2 = reinterpret_cast<const double2*>(c);
+#pragma unroll
+    for (int q = 0; q < BF / 2; ++q) {
+      const double2 v = c2[q];
+      cc[2 * q] = v.x; cc[2 * q + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < NBM; ++b) cc[b] = b < B ? c[b] : Real(0);
+  }
+}
+
+// One edge's inputs: the record (d, r), the neighbour and its species.
+template <typename Real>
+struct EdgeIn {
+  typename Vec4<Real>::type d;
+  int j, tj;
+};
+template <typename Real>
+__device__ __forceinline__ EdgeIn<Real> load_edge(const typename Vec4<Real>::type* d4, const int* nbr,
+                                                  const int* types, int e) {
+  EdgeIn<Real> x;
+  x.d = d4[e];
+  x.j = nbr[e];
+  x.tj = types[x.j];
+  return x;
+}
+
+// n values between a global row and a shared-memory row, 128-bit accesses when n is a multiple
+// of 16 bytes' worth (both rows are then 16-byte aligned: row starts are multiples of n values).
+template <typename Real>
+__device__ __forceinline__ void copy_row(Real* dst, const Real* src, int n) {
+  constexpr int V = 16 / sizeof(Real);
+  if (n % V == 0) {
+    using W = typename std::conditional<sizeof(Real) == 4, float4, double2>::type;
+    for (int q = 0; q < n / V; ++q) reinterpret_cast<W*>(dst)[q] = reinterpret_cast<const W*>(src)[q];
+  } else {
+    for (int q = 0; q < n; ++q) dst[q] = src[q];
+  }
+}
+
+// N (a multiple of 4) values to a 16-byte aligned shared-memory row, 128-bit stores for FP32.
+template <typename Real, int N>
+__device__ __forceinline__ void store_row(Real* dst, const Real (&x)[N]) {
+  static_assert(N % 4 == 0, "row length");
+  if constexpr (sizeof(Real) == 4) {
+#pragma unroll
+    for (int q = 0; q < N / 4; ++q)
+      reinterpret_cast<float4*>(dst)[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < N / 2; ++q) reinterpret_cast<double2*>(dst)[q] = make_double2(x[2 * q], x[2 * q + 1]);
+  }
+}
+
 // BF > 0: the basis size is the compile-time constant BF (= dm.B); BF = 0: runtime B <= kMaxB.
 template <int L, typename Real, bool DERIV, int BF = 0, typename Body>
 __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real* s_coeff, const Real* s_scal,
@@ -104,14 +190,18 @@ __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real
       }
       const int mu = k * Lp + l;
       const Real* c = s_coeff + mu * B;
-      Real a = Real(0), ad = Real(0);
+      Real cc[NBM];
+      load_coeff_row<Real, BF, NBM>(c, B, cc);
+      // two interleaved partial sums per dot product (shorter dependency chains)
+      Real a0 = Real(0), a1 = Real(0), d0 = Real(0), d1 = Real(0);
 #pragma unroll
       for (int b = 0; b < NBM; ++b) {
         if (b < B) {
-          a += c[b] * Tv[b];
-          if (DERIV) ad += c[b] * Td[b];
+          if (b & 1) { a1 += cc[b] * Tv[b]; if (DERIV) d1 += cc[b] * Td[b]; }
+          else { a0 += cc[b] * Tv[b]; if (DERIV) d0 += cc[b] * Td[b]; }
         }
       }
+      const Real a = a0 + a1, ad = d0 + d1;
       const Real f = l == 0 ? f0 : f1, fd = l == 0 ? fd0 : fd1;
       const Real R = f * a;
       const Real Rd = DERIV ? (fd * a + f * ad) : Real(0);
@@ -172,11 +262,14 @@ __device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const R
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
 constexpr int kPassWarps = 4;
-// Minimum resident blocks per SM: 4 (<= 128 registers) where the FP32 kernels fit without
-// spilling (L <= 3), 3 otherwise (measured: the FP64 kernels and L >= 4 run faster at 3).
+// Minimum resident blocks per SM: 4 (<= 128 registers) for the FP32 kernels up to L = 3 and the
+// L = 4 gate passes, 3 otherwise (measured: the L = 4 outer pass spills and runs slower at 128
+// registers; the FP64 kernels spill more).
 
 template <int L, typename Real, int MODE, bool KAHAN, int BF>
-__global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) == 4) ? 4 : 3) atom_pass_kernel(PassArgs<Real> a) {
+__global__ void __launch_bounds__(kPassWarps * kWarp,
+                                  (sizeof(Real) == 4 && (L <= 3 || (L == 4 && MODE != kModeOuter))) ? 4 : 3)
+    atom_pass_kernel(PassArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;
@@ -190,23 +283,24 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
   Real* sm = reinterpret_cast<Real*>(smem_raw);
   Real* s_coeff = sm;
   Real* s_scal = s_coeff + F * B;
-  Real* s_w0 = s_scal + 2 * dm.nblk * C * C;
-  Real* s_w1 = s_w0 + C * F;
-  Real* s_wa = s_w1 + C * F;
-  Real* wbase = s_wa + C * F + pass_warp_size<Real>(F, H, M, K) * warp;
-  Real* stage = wbase;                              // [32][F + H + 1]
-  Real* v = stage + kWarp * (F + H + 1);            // [M]
-  Real* adj = v + M;                                // [M]
-  Real* abar = adj + M;                             // [K][H]
+  Real* s_pw = s_scal + 2 * dm.nblk * C * C;        // [C^2][F] x0(t_i) x1(t_j)
+  Real* s_pa = s_pw + C * C * F;                    // [C^2][F] x0(t_i) wadd(t_j)
+  Real* wbase = sm + efs_table_size(C, F, B, dm.nblk) + pass_warp_size<Real>(F, H, M, K) * warp;
+  const int sw = stage_stride(F, H), yoff = stage_yoff(F);
+  Real* stage = wbase;                              // [32][sw]: u at [0, F), Y at [yoff, yoff + H)
+  Real* v = stage + kWarp * sw;                     // [M]
+  const bool adj_staged = adj_in_stage(F, H, M);
+  Real* adj = adj_staged ? stage : v + M;           // [M]
+  Real* abar = v + M + (adj_staged ? 0 : M);        // [K][H]
   Real* hbar = abar + K * H;                        // [F]
-  const int sw = F + H + 1;
 
   for (int q = threadIdx.x; q < F * B; q += blockDim.x) s_coeff[q] = pt.coeff[q];
   for (int q = threadIdx.x; q < 2 * dm.nblk * C * C; q += blockDim.x) s_scal[q] = pt.scal[q];
-  for (int q = threadIdx.x; q < C * F; q += blockDim.x) {
-    s_w0[q] = pt.wcenter[q];
-    s_w1[q] = pt.wsource[q];
-    s_wa[q] = pt.wadd ? pt.wadd[q] : Real(0);
+  for (int q = threadIdx.x; q < C * C * F; q += blockDim.x) {
+    const int pair = q / F, mu = q - pair * F, ti = pair / C, tj = pair - ti * C;
+    const Real x0 = pt.wcenter[ti * F + mu];
+    s_pw[q] = x0 * pt.wsource[tj * F + mu];
+    s_pa[q] = pt.wadd ? x0 * pt.wadd[tj * F + mu] : Real(0);
   }
   __syncthreads();
   const bool effect_outer = MODE == kModeOuter;
@@ -221,7 +315,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
       int l = 0;
       while ((l + 1) * (l + 1) <= lm) ++l;
       it_u[s] = kk * Lp + l;
-      it_y[s] = F + lm;
+      it_y[s] = yoff + lm;
     } else {
       it_u[s] = -1;
       it_y[s] = 0;
@@ -235,34 +329,54 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
     double vir[6] = {0, 0, 0, 0, 0, 0};
     float vhi[6] = {0, 0, 0, 0, 0, 0}, vlo[6] = {0, 0, 0, 0, 0, 0};
 
+    // edge inputs of the lane's edge in the last batch: left by the forward loop, which the
+    // per-edge adjoint then starts from (it runs the batches in reverse order)
+    EdgeIn<Real> cur{};
+    const int nbat = (e1 - e0 + kWarp - 1) / kWarp;
+    // the gate reverse pass starts with the per-atom work: its first edge batch loads meanwhile
+    if (MODE == kModeGateReverse && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
+      cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + (nbat - 1) * kWarp + lane);
     if (MODE != kModeGateReverse) {
       // ---------------- forward moments ----------------
       Real acc[kMaxItems], cmp[kMaxItems];
 #pragma unroll
       for (int s = 0; s < kMaxItems; ++s) { acc[s] = Real(0); cmp[s] = Real(0); }
+      // the next batch's edge inputs are loaded while the current batch is evaluated
+      if (e0 + lane < e1) cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + lane);
       for (int base = e0; base < e1; base += kWarp) {
         const int e = base + lane;
+        const bool more = base + kWarp < e1;
+        EdgeIn<Real> nxt = cur;
+        if (more && e + kWarp < e1) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e + kWarp);
         Real* row = stage + lane * sw;
         if (e < e1) {
-          const V4 dv = a.d4[e];
-          const int j = a.nbr[e];
-          const int tj = a.types[j];
+          const V4 dv = cur.d;
+          const int j = cur.j;
+          const int tj = cur.tj;
           const Real r = dv.w, ir = Real(1) / r;
-          Real Y[H];
+          Real Y[round4(H)];
           sph_values<L, Real>(dv.x * ir, dv.y * ir, dv.z * ir, Y);
           const bool ang = !(r >= dm.rang);
 #pragma unroll
-          for (int h = 0; h < H; ++h) row[F + h] = (h == 0 || ang) ? Y[h] : Real(0);
-          const Real* hj = effect_outer ? a.hsig + (size_t)j * F : nullptr;
-          for (int mu = 0; mu < F; ++mu) row[mu] = Real(0);
-          radial_loop<L, Real, false, BF>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real) {
-            Real x3 = s_w1[tj * F + mu];
-            if (effect_outer) x3 += s_wa[tj * F + mu] * hj[mu];
-            row[mu] = s_w0[ti * F + mu] * x3 * R;
+          for (int h = 0; h < round4(H); ++h) Y[h] = (h < H && (h == 0 || ang)) ? Y[h] : Real(0);
+          store_row<Real, round4(H)>(row + yoff, Y);
+          const int pair = ti * C + tj;
+          const Real* pw = s_pw + pair * F;
+          const Real* pa = s_pa + pair * F;
+          // Effect: the neighbour's gate signal h_j is staged in the row's u slots, each read once
+          // before its u_mu overwrites it
+          if (effect_outer) copy_row<Real>(row, a.hsig + (size_t)j * F, F);
+          else for (int mu = 0; mu < F; ++mu) row[mu] = Real(0);
+          radial_loop<L, Real, false, BF>(dm, s_coeff, s_scal, pair, r, [&](int k, int l, int mu, Real R, Real) {
+            Real w = pw[mu];
+            if (effect_outer) w += pa[mu] * row[mu];
+            row[mu] = w * R;
           });
+          if (effect_outer && !ang)
+            for (int mu = 0; mu < F; ++mu)
+              if (mu % Lp != 0) row[mu] = Real(0);
         } else {
-          for (int q = 0; q < F; ++q) row[q] = Real(0);
-          for (int h = 0; h < H; ++h) row[F + h] = Real(0);
+          for (int q = 0; q < sw; ++q) row[q] = Real(0);
         }
         __syncwarp();
         // plain sum over the batch's (<= 32) staged edges, then a compensated add of the batch
@@ -280,6 +394,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
 #pragma unroll
         for (int s = 0; s < kMaxItems; ++s) kadd<Real, KAHAN>(acc[s], cmp[s], part[s]);
         __syncwarp();
+        if (more) cur = nxt;
       }
       for (int q = lane; q < M; q += kWarp) v[q] = Real(0);
       __syncwarp();
@@ -356,41 +471,55 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, (L <= 3 && sizeof(Real) ==
     __syncwarp();
 
     // ---------------- per-edge adjoint ----------------
-    for (int e = e0 + lane; e < e1; e += kWarp) {
-      const V4 dv = a.d4[e];
-      const int j = a.nbr[e];
-      const int tj = a.types[j];
+    // batches in reverse order, the next one's edge inputs loaded while the current one runs
+    for (int bt = nbat - 1; bt >= 0; --bt) {
+      const int e = e0 + bt * kWarp + lane;
+      EdgeIn<Real> nxt = cur;
+      if (bt > 0) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e - kWarp);
+      if (e >= e1) { cur = nxt; continue; }
+      const V4 dv = cur.d;
+      const int j = cur.j;
+      const int tj = cur.tj;
+      cur = nxt;
       const Real r = dv.w, ir = Real(1) / r;
       const Real ux = dv.x * ir, uy = dv.y * ir, uz = dv.z * ir;
       const bool ang = !(r >= dm.rang);
-      Real Y[H], P[H], Qd[H];
+      // P[h] = sum_k w R_kl(h) abar[k][h] feeds the angular gradient; the radial-derivative term
+      // sum_h Qd[h] Y[h], Qd[h] = sum_k w R'_kl(h) abar[k][h], is summed per (k, l) as
+      // w R'_kl S_kl with S_kl = sum_{h in l} abar[k][h] Y[h] (no per-h Qd registers)
+      Real Y[H], P[H];
       sph_values<L, Real>(ux, uy, uz, Y);
 #pragma unroll
-      for (int h = 0; h < H; ++h) { P[h] = Real(0); Qd[h] = Real(0); if (h > 0 && !ang) Y[h] = Real(0); }
-      const Real* hj = effect_outer ? a.hsig + (size_t)j * F : nullptr;
-      Real* hc = effect_outer ? a.hcontrib + (size_t)a.rev[e] * F : nullptr;
-      radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, ti * C + tj, r, [&](int k, int l, int mu, Real R, Real Rd) {
-        const Real x0 = s_w0[ti * F + mu];
-        Real x3 = s_w1[tj * F + mu];
-        if (effect_outer) x3 += s_wa[tj * F + mu] * hj[mu];
-        const Real w = x0 * x3, wR = w * R, wRd = w * Rd;
+      for (int h = 0; h < H; ++h) { P[h] = Real(0); if (h > 0 && !ang) Y[h] = Real(0); }
+      // Effect: h_j staged in the lane's row (free after the forward reduction), overwritten in
+      // place by the hbar contributions, which then go out as one row
+      Real* hrow = stage + lane * sw;
+      if (effect_outer) copy_row<Real>(hrow, a.hsig + (size_t)j * F, F);
+      const int pair = ti * C + tj;
+      const Real* pw = s_pw + pair * F;
+      const Real* pa = s_pa + pair * F;
+      Real s = Real(0);
+      radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, pair, r, [&](int k, int l, int mu, Real R, Real Rd) {
+        Real w = pw[mu], wa = Real(0);
+        if (effect_outer) { wa = pa[mu]; w += wa * hrow[mu]; }
+        const Real wR = w * R;
         const Real* ab = abar + k * H;
         Real S = Real(0);
 #pragma unroll
         for (int h = l * l; h < (l + 1) * (l + 1); ++h) {
           const Real av = ab[h];
           P[h] += wR * av;
-          Qd[h] += wRd * av;
-          if (effect_outer) S += av * Y[h];
+          S += av * Y[h];
         }
-        if (effect_outer) hc[mu] = x0 * s_wa[tj * F + mu] * R * S;
+        s += w * Rd * S;
+        if (effect_outer) hrow[mu] = wa * R * S;
       });
-      if (effect_outer && !ang)
-        for (int mu = 0; mu < F; ++mu)
-          if (mu % Lp != 0) hc[mu] = Real(0);
-      Real s = Real(0);
-#pragma unroll
-      for (int h = 0; h < H; ++h) s += Qd[h] * Y[h];
+      if (effect_outer) {
+        if (!ang)
+          for (int mu = 0; mu < F; ++mu)
+            if (mu % Lp != 0) hrow[mu] = Real(0);
+        copy_row<Real>(a.hcontrib + (size_t)a.rev[e] * F, hrow, F);
+      }
       Real gx = Real(0), gy = Real(0), gz = Real(0);
       if (ang) sph_grad_dot<L, Real>(ux, uy, uz, P, gx, gy, gz);
       const Real ug = ux * gx + uy * gy + uz * gz;
