@@ -74,7 +74,7 @@ __global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const d
 // centre's edges are sorted by (j, image) afterwards).
 __global__ void k_bin_fill(const FramePlan* plans, const int* frame_of, const double* pos, const int* bin_of,
                            int natoms, const int* bin_start, int* cursor, const AtomFrac* frac, const AtomOff* off,
-                           BinAtom* bin_rec, BinPos* bin_pos) {
+                           BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   const int bin = bin_of[i];
@@ -85,9 +85,13 @@ __global__ void k_bin_fill(const FramePlan* plans, const int* frame_of, const do
   const int slot = bin_start[bin] + atomicAdd(cursor + bin, 1);
   bin_rec[slot] = BinAtom{f.x, f.y, f.z, i, o.x, o.y, o.z, 0};
   const double a0 = o.x, a1 = o.y, a2 = o.z;
-  bin_pos[slot] = BinPos{pos[3 * i] - (a0 * c[0] + a1 * c[3] + a2 * c[6]),
-                         pos[3 * i + 1] - (a0 * c[1] + a1 * c[4] + a2 * c[7]),
-                         pos[3 * i + 2] - (a0 * c[2] + a1 * c[5] + a2 * c[8]), i, 0};
+  const double wx = pos[3 * i] - (a0 * c[0] + a1 * c[3] + a2 * c[6]);
+  const double wy = pos[3 * i + 1] - (a0 * c[1] + a1 * c[4] + a2 * c[7]);
+  const double wz = pos[3 * i + 2] - (a0 * c[2] + a1 * c[5] + a2 * c[8]);
+  bin_pos[slot] = BinPos{wx, wy, wz, i, 0};
+  const float hx = static_cast<float>(wx), hy = static_cast<float>(wy), hz = static_cast<float>(wz);
+  bin_posf[slot] = BinPosF{hx, hy, hz, i, static_cast<float>(wx - hx), static_cast<float>(wy - hy),
+                           static_cast<float>(wz - hz), 0};
 }
 
 
@@ -103,6 +107,17 @@ __global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const 
   enumerate_edges(i, fp, pos, rc2, error,
                   [&](int, int, int, int, double, double, double, double) { ++n; });
   counts[i] = n;
+}
+
+// One cell-list edge record: components and distance already in the record's precision.
+template <typename Real>
+__device__ __forceinline__ void write_edge_rec(long long e, int j, int a, int b, int c, Real x, Real y, Real z, Real r,
+                                               int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key) {
+  nbr[e] = j;
+  typename Vec4<Real>::type v;
+  v.x = x; v.y = y; v.z = z; v.w = r;
+  d4[e] = v;
+  key[e] = edge_key(j, a, b, c);
 }
 
 template <typename Real>
@@ -145,10 +160,11 @@ constexpr int kFillWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                 const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos, const int* bin_of,
-                 const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr, typename Vec4<Real>::type* d4,
-                 unsigned long long* key, int* overflow, int* error) {
+                 const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos, const BinPosF* bin_posf,
+                 const int* bin_of, const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr,
+                 typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
+  __shared__ BinSlot slots[kFillWarps][kBinSlots];
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
@@ -158,14 +174,15 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
-  warp_bin_edges(i, fp, pos, rc2, bin_start, bin_rec, bin_pos, bin_of, frac, off, error, queue[threadIdx.x / kWarp],
-                 [&](unsigned mask, bool ok, int j, int a, int b, int c, double x, double y, double z, double r2) {
-                   if (ok) {
-                     const int k = cursor + __popc(mask & below);
-                     if (k < cap) write_edge<Real>(pad + k, j, a, b, c, x, y, z, r2, nbr, d4, key);
-                   }
-                   cursor += __popc(mask);
-                 });
+  warp_bin_edges<Real>(i, fp, pos, rc2, bin_start, bin_rec, bin_pos, bin_posf, bin_of, frac, off, error,
+                       queue[threadIdx.x / kWarp], slots[threadIdx.x / kWarp],
+                       [&](unsigned mask, bool ok, int j, int a, int b, int c, Real x, Real y, Real z, Real r) {
+                         if (ok) {
+                           const int k = cursor + __popc(mask & below);
+                           if (k < cap) write_edge_rec<Real>(pad + k, j, a, b, c, x, y, z, r, nbr, d4, key);
+                         }
+                         cursor += __popc(mask);
+                       });
   if (lane == 0) {
     counts[i] = min(cursor, cap);
     if (cursor > cap) atomicMax(overflow, cursor);
@@ -207,37 +224,88 @@ k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame
     __syncwarp();
     src = sk;
   }
-  for (int q = lane; q < n; q += kWarp) {
-    const unsigned long long k = src[q];
-    int rank = 0;
-    for (int t = 0; t < n; ++t) rank += src[t] < k;
-    key_out[e0 + rank] = k;
-    nbr_out[e0 + rank] = NB[in0 + q];
-    d4_out[e0 + rank] = D[in0 + q];
+  // up to kSortPer keys per lane per pass: their payloads load while the ranks are counted
+  constexpr int kSortPer = 4;
+  for (int q0 = 0; q0 < n; q0 += kSortPer * kWarp) {
+    unsigned long long k[kSortPer];
+    int nb[kSortPer], rank[kSortPer];
+    typename Vec4<Real>::type d[kSortPer];
+#pragma unroll
+    for (int u = 0; u < kSortPer; ++u) {
+      const int q = q0 + u * kWarp + lane;
+      k[u] = ~0ull;
+      rank[u] = 0;
+      if (q < n) {
+        k[u] = src[q];
+        nb[u] = NB[in0 + q];
+        d[u] = D[in0 + q];
+      }
+    }
+    for (int t = 0; t < n; ++t) {
+      const unsigned long long kt = src[t];
+#pragma unroll
+      for (int u = 0; u < kSortPer; ++u) rank[u] += kt < k[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kSortPer; ++u) {
+      if (q0 + u * kWarp + lane < n) {
+        key_out[e0 + rank[u]] = k[u];
+        nbr_out[e0 + rank[u]] = nb[u];
+        d4_out[e0 + rank[u]] = d[u];
+      }
+    }
   }
 }
 
 // Reverse edge of every edge (warp per centre i): for e = (i -> j, n) the edge (j -> i, -n) is
 // found by binary search in j's sorted keys.
+// Up to kRevPer searches per lane run interleaved, so their dependent loads overlap.
 __global__ void k_reverse(const int* row, const unsigned long long* key, int natoms, int* rev, int* error) {
+  constexpr int kRevPer = 4;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (i >= natoms) return;
-  for (int e = row[i] + lane; e < row[i + 1]; e += kWarp) {
-    const unsigned long long k = key[e];
-    const int j = static_cast<int>(k >> 21);
-    const int n0 = static_cast<int>((k >> 14) & 127) - 64, n1 = static_cast<int>((k >> 7) & 127) - 64,
-              n2 = static_cast<int>(k & 127) - 64;
-    const unsigned long long want = edge_key(i, -n0, -n1, -n2);
-    int lo = row[j], hi = row[j + 1] - 1, found = -1;
-    while (lo <= hi) {
-      const int mid = (lo + hi) >> 1;
-      const unsigned long long km = key[mid];
-      if (km == want) { found = mid; break; }
-      if (km < want) lo = mid + 1; else hi = mid - 1;
+  const int end = row[i + 1];
+  for (int base = row[i]; base < end; base += kRevPer * kWarp) {
+    int lo[kRevPer], hi[kRevPer], found[kRevPer];
+    unsigned long long want[kRevPer];
+#pragma unroll
+    for (int u = 0; u < kRevPer; ++u) {
+      const int e = base + u * kWarp + lane;
+      lo[u] = 0; hi[u] = -1; found[u] = -1; want[u] = 0;
+      if (e < end) {
+        const unsigned long long k = key[e];
+        const int j = static_cast<int>(k >> 21);
+        const int n0 = static_cast<int>((k >> 14) & 127) - 64, n1 = static_cast<int>((k >> 7) & 127) - 64,
+                  n2 = static_cast<int>(k & 127) - 64;
+        want[u] = edge_key(i, -n0, -n1, -n2);
+        lo[u] = row[j];
+        hi[u] = row[j + 1] - 1;
+      }
     }
-    if (found < 0) record_error(error, kErrReverseEdge);
-    rev[e] = found < 0 ? e : found;
+    bool active = true;
+    while (active) {
+      active = false;
+#pragma unroll
+      for (int u = 0; u < kRevPer; ++u) {
+        if (lo[u] <= hi[u]) {
+          const int mid = (lo[u] + hi[u]) >> 1;
+          const unsigned long long km = key[mid];
+          if (km == want[u]) { found[u] = mid; hi[u] = lo[u] - 1; }
+          else if (km < want[u]) lo[u] = mid + 1;
+          else hi[u] = mid - 1;
+          active = active || lo[u] <= hi[u];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kRevPer; ++u) {
+      const int e = base + u * kWarp + lane;
+      if (e < end) {
+        if (found[u] < 0) record_error(error, kErrReverseEdge);
+        rev[e] = found[u] < 0 ? e : found[u];
+      }
+    }
   }
 }
 
@@ -899,9 +967,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     ++launches_;
     bin_rec_.ensure(sizeof(BinAtom) * std::max(1, a));
     bin_pos_.ensure(sizeof(BinPos) * std::max(1, a));
+    bin_posf_.ensure(sizeof(BinPosF) * std::max(1, a));
     k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, bin_of.as<int>(), a,
                                               bin_start_.as<int>(), bin_cursor_.as<int>(), frac_.as<AtomFrac>(),
-                                              off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>());
+                                              off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
+                                              bin_posf_.as<BinPosF>());
     launches_ += 2;
   }
   const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
@@ -912,6 +982,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const int *BS = bin_start_.as<int>(), *BO = bin_of.as<int>();
   const BinAtom* BR = bin_rec_.as<BinAtom>();
   const BinPos* BP = bin_pos_.as<BinPos>();
+  const BinPosF* BPF = bin_posf_.as<BinPosF>();
   const AtomFrac* FR = frac_.as<AtomFrac>();
   const AtomOff* OF = off_.as<AtomOff>();
   int* overflow = error_.as<int>() + 1;
@@ -923,11 +994,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     pad_key_.ensure(sizeof(unsigned long long) * slots);
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
                                                                           pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;

@@ -42,6 +42,8 @@ struct __align__(16) BinAtom { float x, y, z; int j; int ox, oy, oz, pad; };
 // atom's index: the exact test forms x_j + n.cell - x_i as wrapped x_j + ((w + off_i) . cell - x_i),
 // whose second term is one constant per (centre, neighbouring bin).
 struct __align__(16) BinPos { double x, y, z; int j, pad; };
+// FP32 engines: the wrapped position as double-float parts x = xh + xl (xh = fl32(x)).
+struct __align__(16) BinPosF { float xh, yh, zh; int j; float xl, yl, zl; int pad; };
 
 __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, int n2) {
   return (static_cast<unsigned long long>(j) << 21) |
@@ -87,35 +89,66 @@ __device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, cons
 
 // Cell-list frames, one warp per centre i: the 27 neighbouring bins' atom ranges are laid end to
 // end (prefix sums over lanes) and lanes take consecutive candidates of that flat list, two per
-// lane per iteration (independent loads in flight).  Candidates
-// that pass the FP32 prefilter are appended to a per-warp queue in shared memory (`queue`, 128
-// entries); whenever 32 are queued the warp runs the exact FP64 test on a full warp of them, so
-// the FP64 work (1/64 of the FP32 rate on this GPU) is spent on prefilter survivors only rather
-// than on mostly idle lanes.  Accepted edges of each FP64 round are reported through
-// Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r2), so the caller can count or write them
-// with one ballot per round.
+// lane per iteration (independent loads in flight).  The bin slot of a candidate comes from the
+// window's slot boundaries (a 64-candidate window touches two or three bins) and a per-warp slot
+// table in shared memory.  Candidates that pass the FP32 prefilter are appended to a per-warp
+// queue in shared memory (`queue`, 128 entries); whenever 32 are queued the warp tests a full
+// warp of them:
+//   * FP64 engines: x_j + n.cell - x_i and r^2 in FP64;
+//   * FP32 engines: the same vector from double-float (hi, lo) parts in FP32 arithmetic, with the
+//     FP64 test only for the rare entries whose FP32 r^2 lies within 1e-4 relative of r_c^2
+//     (FP64 runs at 1/64 of the FP32 rate on this GPU).
+// Either way the accepted set is exactly {r^2 < r_c^2} in FP64.  Accepted edges of each round are
+// reported through Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r) (Real components and
+// distance), so the caller can count or write them with one ballot per round.
 constexpr int kEdgeQueue = 128;
 __device__ __forceinline__ int pack_image(int n0, int n1, int n2) {
   return ((n0 + 64) << 14) | ((n1 + 64) << 7) | (n2 + 64);
 }
-template <typename Round>
+// One neighbouring bin of the centre: record index offset (start - exclusive offset), the image
+// base w + off_i, and the FP32 fractional shift w - frac_i.
+struct __align__(16) BinSlot { int rec0, nb0, nb1, nb2; float dx, dy, dz; int pad; };
+constexpr int kBinSlots = 27;
+
+// double-float sum (ah + al) + (bh + bl), rounded to FP32 (two-sum of the high parts)
+__device__ __forceinline__ float df_add(float ah, float al, float bh, float bl) {
+  const float s = ah + bh;
+  const float v = s - ah;
+  const float e = (ah - (s - v)) + (bh - v);
+  return s + (e + (al + bl));
+}
+
+template <typename Real, typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
                                                const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos,
-                                               const int* bin_of, const AtomFrac* frac, const AtomOff* off,
-                                               int* error, int2* queue, Round&& round) {
+                                               const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac,
+                                               const AtomOff* off, int* error, int2* queue, BinSlot* slots,
+                                               Round&& round) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const int local = bin_of[i] - fp.bin0;
   const int bi0 = local / (fp.nb[1] * fp.nb[2]), bi1 = (local / fp.nb[2]) % fp.nb[1], bi2 = local % fp.nb[2];
-  int start = 0, len = 0, w0 = 0, w1 = 0, w2 = 0;
-  if (lane < 27) {
+  const AtomFrac fi = frac[i];
+  const AtomOff oi = off[i];
+  const double* c = fp.cell;
+  const float* cf = fp.cellf;
+  int len = 0, start = 0;
+  // lane k < 27: bin slot k; its shift (w_k + off_i) . cell - x_i for the exact test
+  double sx = 0, sy = 0, sz = 0;
+  if (lane < kBinSlots) {
     const int raw0 = bi0 + lane / 9 - 1, raw1 = bi1 + (lane / 3) % 3 - 1, raw2 = bi2 + lane % 3 - 1;
-    w0 = raw0 < 0 ? -1 : (raw0 >= fp.nb[0] ? 1 : 0);
-    w1 = raw1 < 0 ? -1 : (raw1 >= fp.nb[1] ? 1 : 0);
-    w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
+    const int w0 = raw0 < 0 ? -1 : (raw0 >= fp.nb[0] ? 1 : 0);
+    const int w1 = raw1 < 0 ? -1 : (raw1 >= fp.nb[1] ? 1 : 0);
+    const int w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
     const int bin = fp.bin0 + ((raw0 - w0 * fp.nb[0]) * fp.nb[1] + (raw1 - w1 * fp.nb[1])) * fp.nb[2] + (raw2 - w2 * fp.nb[2]);
     start = bin_start[bin];
     len = bin_start[bin + 1] - start;
+    const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
+    sx = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
+    sy = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
+    sz = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
+    slots[lane] = BinSlot{0, w0 + oi.x, w1 + oi.y, w2 + oi.z, static_cast<float>(w0) - fi.x,
+                          static_cast<float>(w1) - fi.y, static_cast<float>(w2) - fi.z, 0};
   }
   // inclusive scan of len over lanes
   int incl = len;
@@ -126,22 +159,25 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
   }
   const int total = __shfl_sync(0xffffffffu, incl, 31);
   const int excl = incl - len;
-  const AtomFrac fi = frac[i];
-  const AtomOff oi = off[i];
-  const double* c = fp.cell;
-  const float* cf = fp.cellf;
-  // lane k < 27: shift of bin slot k, (w_k + off_i) . cell - x_i
-  double sx = 0, sy = 0, sz = 0;
-  if (lane < 27) {
-    const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
-    sx = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
-    sy = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
-    sz = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
+  // exclusive offset of slot `lane` in the flat candidate list (lanes without a slot: never <= a candidate)
+  int slot_excl = 0x7fffffff;
+  if (lane < kBinSlots) {
+    slots[lane].rec0 = start - excl;
+    slot_excl = excl;
   }
+  // FP32 engines: double-float parts of the slot shifts
+  float shx = 0, slx = 0, shy = 0, sly = 0, shz = 0, slz = 0;
+  if (sizeof(Real) == 4) {
+    shx = static_cast<float>(sx); slx = static_cast<float>(sx - static_cast<double>(shx));
+    shy = static_cast<float>(sy); sly = static_cast<float>(sy - static_cast<double>(shy));
+    shz = static_cast<float>(sz); slz = static_cast<float>(sz - static_cast<double>(shz));
+  }
+  __syncwarp();
   const float screen = static_cast<float>(rc2 + fp.band);
+  const float lo2 = static_cast<float>(rc2 * (1.0 - 1e-4)), hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
   int queued = 0;  // warp-uniform
-  // exact FP64 test of queue entries [0, n) (one per lane) and the round callback
-  // queue entry: (bin slot, packed image | neighbouring-bin index k << 21)
+  // test of queue entries [0, n) (one per lane) and the round callback
+  // queue entry: (bin record index, packed image | neighbouring-bin index k << 21)
   auto drain = [&](int n) {
     bool ok = false;
     int j = 0, n0 = 0, n1 = 0, n2 = 0, k = 0;
@@ -149,47 +185,70 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     if (lane < n) {
       q = queue[lane];
       k = q.y >> 21;
-    }
-    const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
-                 kz = __shfl_sync(0xffffffffu, sz, k);
-    double vx = 0, vy = 0, vz = 0, r2 = 0;
-    if (lane < n) {
-      const BinPos bp = bin_pos[q.x];
-      j = bp.j;
       n0 = ((q.y >> 14) & 127) - 64; n1 = ((q.y >> 7) & 127) - 64; n2 = (q.y & 127) - 64;
-      vx = bp.x + kx;
-      vy = bp.y + ky;
-      vz = bp.z + kz;
-      r2 = vx * vx + vy * vy + vz * vz;
-      ok = r2 < rc2;
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, ok);
-    round(mask, ok, j, n0, n1, n2, vx, vy, vz, r2);
+    if constexpr (sizeof(Real) == 8) {
+      const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
+                   kz = __shfl_sync(0xffffffffu, sz, k);
+      double vx = 0, vy = 0, vz = 0, r2 = 0;
+      if (lane < n) {
+        const BinPos bp = bin_pos[q.x];
+        j = bp.j;
+        vx = bp.x + kx;
+        vy = bp.y + ky;
+        vz = bp.z + kz;
+        r2 = vx * vx + vy * vy + vz * vz;
+        ok = r2 < rc2;
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, ok);
+      round(mask, ok, j, n0, n1, n2, Real(vx), Real(vy), Real(vz), Real(sqrt(r2)));
+    } else {
+      const float kxh = __shfl_sync(0xffffffffu, shx, k), kxl = __shfl_sync(0xffffffffu, slx, k);
+      const float kyh = __shfl_sync(0xffffffffu, shy, k), kyl = __shfl_sync(0xffffffffu, sly, k);
+      const float kzh = __shfl_sync(0xffffffffu, shz, k), kzl = __shfl_sync(0xffffffffu, slz, k);
+      float vx = 0, vy = 0, vz = 0, r2 = 0;
+      bool near = false;
+      if (lane < n) {
+        const BinPosF bp = bin_posf[q.x];
+        j = bp.j;
+        vx = df_add(bp.xh, bp.xl, kxh, kxl);
+        vy = df_add(bp.yh, bp.yl, kyh, kyl);
+        vz = df_add(bp.zh, bp.zl, kzh, kzl);
+        r2 = vx * vx + vy * vy + vz * vz;
+        ok = r2 < lo2;
+        near = !ok && r2 < hi2;
+      }
+      if (__ballot_sync(0xffffffffu, near)) {
+        // entries near the cutoff: the FP64 test decides
+        const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
+                     kz = __shfl_sync(0xffffffffu, sz, k);
+        if (near) {
+          const BinPos bp = bin_pos[q.x];
+          const double dx = bp.x + kx, dy = bp.y + ky, dz = bp.z + kz;
+          const double d2 = dx * dx + dy * dy + dz * dz;
+          ok = d2 < rc2;
+          vx = static_cast<float>(dx); vy = static_cast<float>(dy); vz = static_cast<float>(dz);
+          r2 = static_cast<float>(d2);
+        }
+      }
+      const unsigned mask = __ballot_sync(0xffffffffu, ok);
+      round(mask, ok, j, n0, n1, n2, vx, vy, vz, sqrtf(r2));
+    }
   };
-  // candidate cand of the flattened list: FP32 prefilter; returns the packed image with the
-  // neighbouring-bin index (or -1) and the candidate's bin slot
-  auto screen_candidate = [&](int cand, int& slot) -> int {
-    // bin slot k of this candidate: the last lane whose exclusive offset is <= cand
-    int k = 0;
-#pragma unroll
-    for (int step = 16; step > 0; step >>= 1) {
-      const int probe = k + step;
-      const int ex = __shfl_sync(0xffffffffu, excl, probe < 27 ? probe : 26);
-      if (probe < 27 && ex <= cand) k = probe;
-    }
-    const int kstart = __shfl_sync(0xffffffffu, start, k), kex = __shfl_sync(0xffffffffu, excl, k);
-    const int W0 = __shfl_sync(0xffffffffu, w0, k), W1 = __shfl_sync(0xffffffffu, w1, k), W2 = __shfl_sync(0xffffffffu, w2, k);
+  // FP32 prefilter of candidate cand (bin slot k): returns the packed image with k (or -1) and
+  // the candidate's bin record index
+  auto screen_candidate = [&](int cand, int k, int& rec_index) -> int {
     if (cand >= total) return -1;
-    slot = kstart + cand - kex;
-    const BinAtom rec = bin_rec[slot];
+    const BinSlot sl = slots[k];
+    rec_index = sl.rec0 + cand;
+    const BinAtom rec = bin_rec[rec_index];
     const int j = rec.j;
-    const float sx = rec.x + static_cast<float>(W0) - fi.x, sy = rec.y + static_cast<float>(W1) - fi.y,
-                sz = rec.z + static_cast<float>(W2) - fi.z;
-    const float fx = sx * cf[0] + sy * cf[3] + sz * cf[6];
-    const float fy = sx * cf[1] + sy * cf[4] + sz * cf[7];
-    const float fz = sx * cf[2] + sy * cf[5] + sz * cf[8];
+    const float sx32 = rec.x + sl.dx, sy32 = rec.y + sl.dy, sz32 = rec.z + sl.dz;
+    const float fx = sx32 * cf[0] + sy32 * cf[3] + sz32 * cf[6];
+    const float fy = sx32 * cf[1] + sy32 * cf[4] + sz32 * cf[7];
+    const float fz = sx32 * cf[2] + sy32 * cf[5] + sz32 * cf[8];
     if (fx * fx + fy * fy + fz * fz >= screen) return -1;
-    const int n0 = W0 + oi.x - rec.ox, n1 = W1 + oi.y - rec.oy, n2 = W2 + oi.z - rec.oz;
+    const int n0 = sl.nb0 - rec.ox, n1 = sl.nb1 - rec.oy, n2 = sl.nb2 - rec.oz;
     if (i == j && n0 == 0 && n1 == 0 && n2 == 0) return -1;
     if (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63) {
       record_error(error, kErrImageRange);
@@ -197,19 +256,29 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     }
     return pack_image(n0, n1, n2) | (k << 21);
   };
-  auto push = [&](int packed, int slot) {
+  auto push = [&](int packed, int rec_index) {
     const bool pre = packed >= 0;
     const unsigned m = __ballot_sync(0xffffffffu, pre);
-    if (pre) queue[queued + __popc(m & below)] = make_int2(slot, packed);
+    if (pre) queue[queued + __popc(m & below)] = make_int2(rec_index, packed);
     queued += __popc(m);
   };
   // two independent candidates per lane per iteration (their loads overlap)
   for (int base = 0; base < total; base += 64) {
-    int ja = 0, jb = 0;
-    const int pa = screen_candidate(base + lane, ja);
-    const int pb = screen_candidate(base + 32 + lane, jb);
-    push(pa, ja);
-    push(pb, jb);
+    // slot of the window's first candidate, then the (few) slot boundaries inside the window
+    const int k0 = __popc(__ballot_sync(0xffffffffu, slot_excl <= base)) - 1;
+    const unsigned inside = __ballot_sync(0xffffffffu, slot_excl > base && slot_excl < base + 64);
+    int ka = k0, kb = k0;
+    for (unsigned m = inside; m; m &= m - 1) {
+      const int s = __ffs(m) - 1;
+      const int p = __shfl_sync(0xffffffffu, slot_excl, s) - base;
+      if (lane >= p) ka = s;
+      if (lane + 32 >= p) kb = s;
+    }
+    int ra = 0, rb = 0;
+    const int pa = screen_candidate(base + lane, ka, ra);
+    const int pb = screen_candidate(base + 32 + lane, kb, rb);
+    push(pa, ra);
+    push(pb, rb);
     __syncwarp();
     while (queued >= 32) {
       drain(32);
