@@ -158,13 +158,13 @@ __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const d
 // with the step's error check (it then grows the capacity and repeats the step).
 constexpr int kFillWarps = 8;
 template <typename Real>
-__global__ void __launch_bounds__(kFillWarps * kWarp)
+__global__ void __launch_bounds__(kFillWarps * kWarp, 4)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
                  const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos, const BinPosF* bin_posf,
                  const int* bin_of, const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr,
                  typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
-  __shared__ BinSlot slots[kFillWarps][kBinSlots];
+  __shared__ BinWalk walk[kFillWarps];
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
@@ -175,7 +175,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const int cap = fp.cap;
   int cursor = 0;
   warp_bin_edges<Real>(i, fp, pos, rc2, bin_start, bin_rec, bin_pos, bin_posf, bin_of, frac, off, error,
-                       queue[threadIdx.x / kWarp], slots[threadIdx.x / kWarp],
+                       queue[threadIdx.x / kWarp], walk[threadIdx.x / kWarp],
                        [&](unsigned mask, bool ok, int j, int a, int b, int c, Real x, Real y, Real z, Real r) {
                          if (ok) {
                            const int k = cursor + __popc(mask & below);
@@ -918,7 +918,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     fp.bin0 = bins;
     if (fp.use_bins) {
       ++bins_frames_;
-      for (int q = 0; q < 3; ++q) fp.nb[q] = std::max(3, std::min(512, static_cast<int>(width[q] / rc)));
+      // bins at least r_c / 2 wide (the 5 x 5 x 5 stencil of the fill kernel); widths >= 3 r_c
+      // give at least 6 bins per axis, so the periodic stencil never holds a bin twice
+      for (int q = 0; q < 3; ++q) fp.nb[q] = std::max(6, std::min(512, static_cast<int>(width[q] / (0.5 * rc))));
       // FP32 prefilter: |error of r^2| <= 2 r_c |error of d|, with |error of d| bounded by the
       // rounding of the wrapped fractions (< 2^-24 each, three terms) times the cell row norms
       double rows = 0;

@@ -8,7 +8,8 @@
 //     ceil(-f - reach) .. floor(-f + reach) per axis, f = (x_j - x_i) . inv(cell),
 //     reach_q = r_c |inv(cell)[:, q]|  -- the harness's own bounds;
 //   * cell list (frames whose perpendicular widths are all >= 3 r_c): fractional bins of width
-//     >= r_c, 27 neighbouring bins with periodic wrap; each (j, n) is found exactly once.
+//     >= r_c / 2, the 125 bins within two of the centre's with periodic wrap; each (j, n) is
+//     found exactly once.
 // Afterwards each centre's edges are sorted by (j, n) -- the image-scan order -- and every edge
 // gets the index of its reverse edge (j -> i, -n) by binary search, which makes the force gather
 // F_i = sum_{e out of i} (g_e - g_rev(e)) atomic-free and deterministic.
@@ -87,28 +88,29 @@ __device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, cons
   }
 }
 
-// Cell-list frames, one warp per centre i: the 27 neighbouring bins' atom ranges are laid end to
-// end (prefix sums over lanes) and lanes take consecutive candidates of that flat list, two per
-// lane per iteration (independent loads in flight).  The bin slot of a candidate comes from the
-// window's slot boundaries (a 64-candidate window touches two or three bins) and a per-warp slot
-// table in shared memory.  Candidates that pass the FP32 prefilter are appended to a per-warp
-// queue in shared memory (`queue`, 128 entries); whenever 32 are queued the warp tests a full
-// warp of them:
+// Cell-list frames, one warp per centre i.  Bins are at least r_c / 2 wide, so every neighbour lies
+// in the 5 x 5 x 5 bins around the centre's bin (about 2.3x fewer candidates than 27 bins of width
+// r_c).  Each lane owns four of those 125 bins and walks their atoms, two candidates per
+// iteration (independent loads in flight); candidates that pass the FP32 prefilter are appended
+// to a per-warp queue in shared memory (`queue`, 128 entries) and whenever 32 are queued the warp
+// tests a full warp of them:
 //   * FP64 engines: x_j + n.cell - x_i and r^2 in FP64;
 //   * FP32 engines: the same vector from double-float (hi, lo) parts in FP32 arithmetic, with the
 //     FP64 test only for the rare entries whose FP32 r^2 lies within 1e-4 relative of r_c^2
 //     (FP64 runs at 1/64 of the FP32 rate on this GPU).
-// Either way the accepted set is exactly {r^2 < r_c^2} in FP64.  Accepted edges of each round are
-// reported through Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r) (Real components and
-// distance), so the caller can count or write them with one ballot per round.
+// Either way the accepted set is exactly {r^2 < r_c^2} in FP64.  The vector's periodic part
+// depends only on the wrap w in {-1, 0, 1}^3 of the neighbouring bin: lane k < 27 holds the shift
+// (w_k + off_i) . cell - x_i of wrap k.  Accepted edges of each round are reported through
+// Round(mask, lane_accepted, j, n0, n1, n2, x, y, z, r) (Real components and distance), so the
+// caller can count or write them with one ballot per round.
 constexpr int kEdgeQueue = 128;
+constexpr int kBinReach = 2;                       // bins on each side of the centre's bin
+constexpr int kBinSpan = 2 * kBinReach + 1;        // 5
+constexpr int kBinStencil = kBinSpan * kBinSpan * kBinSpan;  // 125
+constexpr int kBinsPerLane = 4;                    // 32 x 4 >= 125
 __device__ __forceinline__ int pack_image(int n0, int n1, int n2) {
   return ((n0 + 64) << 14) | ((n1 + 64) << 7) | (n2 + 64);
 }
-// One neighbouring bin of the centre: record index offset (start - exclusive offset), the image
-// base w + off_i, and the FP32 fractional shift w - frac_i.
-struct __align__(16) BinSlot { int rec0, nb0, nb1, nb2; float dx, dy, dz; int pad; };
-constexpr int kBinSlots = 27;
 
 // double-float sum (ah + al) + (bh + bl), rounded to FP32 (two-sum of the high parts)
 __device__ __forceinline__ float df_add(float ah, float al, float bh, float bl) {
@@ -118,11 +120,26 @@ __device__ __forceinline__ float df_add(float ah, float al, float bh, float bl) 
   return s + (e + (al + bl));
 }
 
+// Per-warp shared tables of the fill: the 27 wrap shifts (FP64 and double-float parts) and the
+// lanes' bins (start, length).
+// Per wrap w in {-1, 0, 1}^3 of a neighbouring bin (index (w0 + 1) 9 + (w1 + 1) 3 + (w2 + 1)):
+// the exact shift (w + off_i) . cell - x_i in FP64 and as double-float parts, the image base
+// w + off_i and the FP32 fractional shift w - frac_i of the prefilter.
+struct __align__(16) WrapShift {
+  double x, y, z;
+  float hx, hy, hz, lx, ly, lz;
+  int4 nb;      // (w0 + off_i.x, w1 + off_i.y, w2 + off_i.z, -)
+  float4 df;    // (w0 - frac_i.x, w1 - frac_i.y, w2 - frac_i.z, -)
+};
+struct BinWalk {
+  WrapShift shift[27];
+};
+
 template <typename Real, typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
                                                const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos,
                                                const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac,
-                                               const AtomOff* off, int* error, int2* queue, BinSlot* slots,
+                                               const AtomOff* off, int* error, int2* queue, BinWalk& walk,
                                                Round&& round) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
@@ -132,52 +149,62 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
   const AtomOff oi = off[i];
   const double* c = fp.cell;
   const float* cf = fp.cellf;
-  int len = 0, start = 0;
-  // lane k < 27: bin slot k; its shift (w_k + off_i) . cell - x_i for the exact test
-  double sx = 0, sy = 0, sz = 0;
-  if (lane < kBinSlots) {
-    const int raw0 = bi0 + lane / 9 - 1, raw1 = bi1 + (lane / 3) % 3 - 1, raw2 = bi2 + lane % 3 - 1;
-    const int w0 = raw0 < 0 ? -1 : (raw0 >= fp.nb[0] ? 1 : 0);
-    const int w1 = raw1 < 0 ? -1 : (raw1 >= fp.nb[1] ? 1 : 0);
-    const int w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
-    const int bin = fp.bin0 + ((raw0 - w0 * fp.nb[0]) * fp.nb[1] + (raw1 - w1 * fp.nb[1])) * fp.nb[2] + (raw2 - w2 * fp.nb[2]);
-    start = bin_start[bin];
-    len = bin_start[bin + 1] - start;
+  // lane k < 27: wrap k = (w0 + 1) 9 + (w1 + 1) 3 + (w2 + 1)
+  if (lane < 27) {
+    const int w0 = lane / 9 - 1, w1 = (lane / 3) % 3 - 1, w2 = lane % 3 - 1;
     const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
-    sx = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
-    sy = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
-    sz = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
-    slots[lane] = BinSlot{0, w0 + oi.x, w1 + oi.y, w2 + oi.z, static_cast<float>(w0) - fi.x,
-                          static_cast<float>(w1) - fi.y, static_cast<float>(w2) - fi.z, 0};
+    WrapShift w;
+    w.x = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
+    w.y = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
+    w.z = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
+    w.hx = static_cast<float>(w.x); w.lx = static_cast<float>(w.x - static_cast<double>(w.hx));
+    w.hy = static_cast<float>(w.y); w.ly = static_cast<float>(w.y - static_cast<double>(w.hy));
+    w.hz = static_cast<float>(w.z); w.lz = static_cast<float>(w.z - static_cast<double>(w.hz));
+    w.nb = make_int4(w0 + oi.x, w1 + oi.y, w2 + oi.z, 0);
+    w.df = make_float4(static_cast<float>(w0) - fi.x, static_cast<float>(w1) - fi.y, static_cast<float>(w2) - fi.z, 0.f);
+    walk.shift[lane] = w;
   }
-  // inclusive scan of len over lanes
-  int incl = len;
+  // the lane's bins (stencil slots 4 lane + u) laid end to end: record offset start_u - excl_u,
+  // exclusive ends excl_1..3 and the wraps packed 5 bits each
+  int off0 = 0, off1 = 0, off2 = 0, off3 = 0, ex1 = 0, ex2 = 0, ex3 = 0, kpack = 0, mine = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
+  for (int u = 0; u < kBinsPerLane; ++u) {
+    const int sl = kBinsPerLane * lane + u;
+    int bstart = 0, blen = 0, wk = 13;
+    if (sl < kBinStencil) {
+      const int raw0 = bi0 + sl / (kBinSpan * kBinSpan) - kBinReach;
+      const int raw1 = bi1 + (sl / kBinSpan) % kBinSpan - kBinReach;
+      const int raw2 = bi2 + sl % kBinSpan - kBinReach;
+      const int w0 = raw0 < 0 ? -1 : (raw0 >= fp.nb[0] ? 1 : 0);
+      const int w1 = raw1 < 0 ? -1 : (raw1 >= fp.nb[1] ? 1 : 0);
+      const int w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
+      const int bin = fp.bin0 + ((raw0 - w0 * fp.nb[0]) * fp.nb[1] + (raw1 - w1 * fp.nb[1])) * fp.nb[2] +
+                      (raw2 - w2 * fp.nb[2]);
+      bstart = bin_start[bin];
+      blen = bin_start[bin + 1] - bstart;
+      wk = (w0 + 1) * 9 + (w1 + 1) * 3 + (w2 + 1);
+    }
+    const int o = bstart - mine;
+    if (u == 0) off0 = o;
+    if (u == 1) { off1 = o; ex1 = mine; }
+    if (u == 2) { off2 = o; ex2 = mine; }
+    if (u == 3) { off3 = o; ex3 = mine; }
+    kpack |= wk << (5 * u);
+    mine += blen;
   }
-  const int total = __shfl_sync(0xffffffffu, incl, 31);
-  const int excl = incl - len;
-  // exclusive offset of slot `lane` in the flat candidate list (lanes without a slot: never <= a candidate)
-  int slot_excl = 0x7fffffff;
-  if (lane < kBinSlots) {
-    slots[lane].rec0 = start - excl;
-    slot_excl = excl;
-  }
-  // FP32 engines: double-float parts of the slot shifts
-  float shx = 0, slx = 0, shy = 0, sly = 0, shz = 0, slz = 0;
-  if (sizeof(Real) == 4) {
-    shx = static_cast<float>(sx); slx = static_cast<float>(sx - static_cast<double>(shx));
-    shy = static_cast<float>(sy); sly = static_cast<float>(sy - static_cast<double>(shy));
-    shz = static_cast<float>(sz); slz = static_cast<float>(sz - static_cast<double>(shz));
-  }
+  int most = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+  // the FP32 cell rows of the prefilter, in registers
+  float cr[9];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) cr[q] = cf[q];
   __syncwarp();
   const float screen = static_cast<float>(rc2 + fp.band);
   const float lo2 = static_cast<float>(rc2 * (1.0 - 1e-4)), hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
   int queued = 0;  // warp-uniform
   // test of queue entries [0, n) (one per lane) and the round callback
-  // queue entry: (bin record index, packed image | neighbouring-bin index k << 21)
+  // queue entry: (bin record index, packed image | wrap index k << 21)
   auto drain = [&](int n) {
     bool ok = false;
     int j = 0, n0 = 0, n1 = 0, n2 = 0, k = 0;
@@ -188,43 +215,34 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
       n0 = ((q.y >> 14) & 127) - 64; n1 = ((q.y >> 7) & 127) - 64; n2 = (q.y & 127) - 64;
     }
     if constexpr (sizeof(Real) == 8) {
-      const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
-                   kz = __shfl_sync(0xffffffffu, sz, k);
       double vx = 0, vy = 0, vz = 0, r2 = 0;
       if (lane < n) {
         const BinPos bp = bin_pos[q.x];
+        const WrapShift& w = walk.shift[k];
         j = bp.j;
-        vx = bp.x + kx;
-        vy = bp.y + ky;
-        vz = bp.z + kz;
+        vx = bp.x + w.x;
+        vy = bp.y + w.y;
+        vz = bp.z + w.z;
         r2 = vx * vx + vy * vy + vz * vz;
         ok = r2 < rc2;
       }
       const unsigned mask = __ballot_sync(0xffffffffu, ok);
       round(mask, ok, j, n0, n1, n2, Real(vx), Real(vy), Real(vz), Real(sqrt(r2)));
     } else {
-      const float kxh = __shfl_sync(0xffffffffu, shx, k), kxl = __shfl_sync(0xffffffffu, slx, k);
-      const float kyh = __shfl_sync(0xffffffffu, shy, k), kyl = __shfl_sync(0xffffffffu, sly, k);
-      const float kzh = __shfl_sync(0xffffffffu, shz, k), kzl = __shfl_sync(0xffffffffu, slz, k);
       float vx = 0, vy = 0, vz = 0, r2 = 0;
-      bool near = false;
       if (lane < n) {
         const BinPosF bp = bin_posf[q.x];
+        const WrapShift& w = walk.shift[k];
         j = bp.j;
-        vx = df_add(bp.xh, bp.xl, kxh, kxl);
-        vy = df_add(bp.yh, bp.yl, kyh, kyl);
-        vz = df_add(bp.zh, bp.zl, kzh, kzl);
+        vx = df_add(bp.xh, bp.xl, w.hx, w.lx);
+        vy = df_add(bp.yh, bp.yl, w.hy, w.ly);
+        vz = df_add(bp.zh, bp.zl, w.hz, w.lz);
         r2 = vx * vx + vy * vy + vz * vz;
         ok = r2 < lo2;
-        near = !ok && r2 < hi2;
-      }
-      if (__ballot_sync(0xffffffffu, near)) {
-        // entries near the cutoff: the FP64 test decides
-        const double kx = __shfl_sync(0xffffffffu, sx, k), ky = __shfl_sync(0xffffffffu, sy, k),
-                     kz = __shfl_sync(0xffffffffu, sz, k);
-        if (near) {
-          const BinPos bp = bin_pos[q.x];
-          const double dx = bp.x + kx, dy = bp.y + ky, dz = bp.z + kz;
+        if (!ok && r2 < hi2) {
+          // near the cutoff: the FP64 test decides
+          const BinPos bd = bin_pos[q.x];
+          const double dx = bd.x + w.x, dy = bd.y + w.y, dz = bd.z + w.z;
           const double d2 = dx * dx + dy * dy + dz * dz;
           ok = d2 < rc2;
           vx = static_cast<float>(dx); vy = static_cast<float>(dy); vz = static_cast<float>(dz);
@@ -235,21 +253,23 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
       round(mask, ok, j, n0, n1, n2, vx, vy, vz, sqrtf(r2));
     }
   };
-  // FP32 prefilter of candidate cand (bin slot k): returns the packed image with k (or -1) and
-  // the candidate's bin record index
-  auto screen_candidate = [&](int cand, int k, int& rec_index) -> int {
-    if (cand >= total) return -1;
-    const BinSlot sl = slots[k];
-    rec_index = sl.rec0 + cand;
+  // FP32 prefilter of the lane's candidate t (0 <= t < mine, else -1): packed image with the wrap
+  // index, and the bin record index
+  auto screen_candidate = [&](int t, int& rec_index) -> int {
+    if (t >= mine) return -1;
+    const int u1 = t >= ex1, u2 = t >= ex2, u3 = t >= ex3;
+    rec_index = t + (u3 ? off3 : (u2 ? off2 : (u1 ? off1 : off0)));
+    const int k = (kpack >> (5 * (u1 + u2 + u3))) & 31;
     const BinAtom rec = bin_rec[rec_index];
-    const int j = rec.j;
-    const float sx32 = rec.x + sl.dx, sy32 = rec.y + sl.dy, sz32 = rec.z + sl.dz;
-    const float fx = sx32 * cf[0] + sy32 * cf[3] + sz32 * cf[6];
-    const float fy = sx32 * cf[1] + sy32 * cf[4] + sz32 * cf[7];
-    const float fz = sx32 * cf[2] + sy32 * cf[5] + sz32 * cf[8];
+    const float4 df = walk.shift[k].df;
+    const float sx32 = rec.x + df.x, sy32 = rec.y + df.y, sz32 = rec.z + df.z;
+    const float fx = sx32 * cr[0] + sy32 * cr[3] + sz32 * cr[6];
+    const float fy = sx32 * cr[1] + sy32 * cr[4] + sz32 * cr[7];
+    const float fz = sx32 * cr[2] + sy32 * cr[5] + sz32 * cr[8];
     if (fx * fx + fy * fy + fz * fz >= screen) return -1;
-    const int n0 = sl.nb0 - rec.ox, n1 = sl.nb1 - rec.oy, n2 = sl.nb2 - rec.oz;
-    if (i == j && n0 == 0 && n1 == 0 && n2 == 0) return -1;
+    const int4 nb = walk.shift[k].nb;
+    const int n0 = nb.x - rec.ox, n1 = nb.y - rec.oy, n2 = nb.z - rec.oz;
+    if (i == rec.j && n0 == 0 && n1 == 0 && n2 == 0) return -1;
     if (n0 < -64 || n0 > 63 || n1 < -64 || n1 > 63 || n2 < -64 || n2 > 63) {
       record_error(error, kErrImageRange);
       return -1;
@@ -262,21 +282,11 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
     if (pre) queue[queued + __popc(m & below)] = make_int2(rec_index, packed);
     queued += __popc(m);
   };
-  // two independent candidates per lane per iteration (their loads overlap)
-  for (int base = 0; base < total; base += 64) {
-    // slot of the window's first candidate, then the (few) slot boundaries inside the window
-    const int k0 = __popc(__ballot_sync(0xffffffffu, slot_excl <= base)) - 1;
-    const unsigned inside = __ballot_sync(0xffffffffu, slot_excl > base && slot_excl < base + 64);
-    int ka = k0, kb = k0;
-    for (unsigned m = inside; m; m &= m - 1) {
-      const int s = __ffs(m) - 1;
-      const int p = __shfl_sync(0xffffffffu, slot_excl, s) - base;
-      if (lane >= p) ka = s;
-      if (lane + 32 >= p) kb = s;
-    }
+  // two candidates per lane per iteration (their loads overlap)
+  for (int t = 0; t < most; t += 2) {
     int ra = 0, rb = 0;
-    const int pa = screen_candidate(base + lane, ka, ra);
-    const int pb = screen_candidate(base + 32 + lane, kb, rb);
+    const int pa = screen_candidate(t, ra);
+    const int pb = screen_candidate(t + 1, rb);
     push(pa, ra);
     push(pb, rb);
     __syncwarp();
