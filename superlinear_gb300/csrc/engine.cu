@@ -47,18 +47,39 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
   for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) frame_of[i] = f;
 }
 
-__global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms,
-                            int* bin_of, int* bin_count, AtomFrac* frac, AtomOff* off) {
+// Cell-list binning in one pass: per atom the wrapped fractions and integer cell offsets, its bin
+// (bins of frame f are bin0 .. bin0 + nb0 nb1 nb2 - 1) and its record in the bin's fixed-capacity
+// slots bin bcap .. bin bcap + bcap - 1 (order inside a bin is arbitrary: each centre's edges are
+// sorted by (j, image) afterwards).  A bin that receives more than bcap atoms raises *bin_over to
+// its count; the host then grows bcap and repeats the step.  With find_frame the atom's frame is
+// found here (binary search over the frames' first atoms) and written to frame_of.
+__global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame, int* frame_of, const double* pos,
+                            int natoms, int bcap, int* bin_of, int* bin_count, AtomFrac* frac, AtomOff* off,
+                            BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
-  const FramePlan& fp = plans[frame_of[i]];
+  int f;
+  if (find_frame) {
+    // last frame whose first atom is <= i (an empty frame shares its first atom with the next one)
+    int lo = 0, hi = nframes - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (plans[mid].a0 <= i) lo = mid; else hi = mid - 1;
+    }
+    f = lo;
+    frame_of[i] = f;
+  } else {
+    f = frame_of[i];
+  }
+  const FramePlan& fp = plans[f];
   if (!fp.use_bins) { bin_of[i] = -1; return; }
+  const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
   int b[3], o[3];
   float w32[3];
   for (int q = 0; q < 3; ++q) {
-    const double s = pos[3 * i] * fp.inv[q] + pos[3 * i + 1] * fp.inv[3 + q] + pos[3 * i + 2] * fp.inv[6 + q];
-    const double fl = floor(s);
-    const double w = s - fl;
+    const double sq = x * fp.inv[q] + y * fp.inv[3 + q] + z * fp.inv[6 + q];
+    const double fl = floor(sq);
+    const double w = sq - fl;
     o[q] = static_cast<int>(fl);
     w32[q] = static_cast<float>(w);
     b[q] = min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1);
@@ -67,33 +88,20 @@ __global__ void k_bin_count(const FramePlan* plans, const int* frame_of, const d
   off[i] = AtomOff{o[0], o[1], o[2], 0};
   const int bin = fp.bin0 + (b[0] * fp.nb[1] + b[1]) * fp.nb[2] + b[2];
   bin_of[i] = bin;
-  atomicAdd(bin_count + bin, 1);
-}
-
-// Atoms grouped by bin, as one 32-byte record per slot (order inside a bin is arbitrary: each
-// centre's edges are sorted by (j, image) afterwards).
-__global__ void k_bin_fill(const FramePlan* plans, const int* frame_of, const double* pos, const int* bin_of,
-                           int natoms, const int* bin_start, int* cursor, const AtomFrac* frac, const AtomOff* off,
-                           BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= natoms) return;
-  const int bin = bin_of[i];
-  if (bin < 0) return;
-  const AtomFrac f = frac[i];
-  const AtomOff o = off[i];
-  const double* c = plans[frame_of[i]].cell;
-  const int slot = bin_start[bin] + atomicAdd(cursor + bin, 1);
-  bin_rec[slot] = BinAtom{f.x, f.y, f.z, i, o.x, o.y, o.z, 0};
-  const double a0 = o.x, a1 = o.y, a2 = o.z;
-  const double wx = pos[3 * i] - (a0 * c[0] + a1 * c[3] + a2 * c[6]);
-  const double wy = pos[3 * i + 1] - (a0 * c[1] + a1 * c[4] + a2 * c[7]);
-  const double wz = pos[3 * i + 2] - (a0 * c[2] + a1 * c[5] + a2 * c[8]);
-  bin_pos[slot] = BinPos{wx, wy, wz, i, 0};
+  const int slot = atomicAdd(bin_count + bin, 1);
+  if (slot >= bcap) { atomicMax(bin_over, slot + 1); return; }
+  const long long rec = static_cast<long long>(bin) * bcap + slot;
+  bin_rec[rec] = BinAtom{w32[0], w32[1], w32[2], i, o[0], o[1], o[2], 0};
+  const double* c = fp.cell;
+  const double a0 = o[0], a1 = o[1], a2 = o[2];
+  const double wx = x - (a0 * c[0] + a1 * c[3] + a2 * c[6]);
+  const double wy = y - (a0 * c[1] + a1 * c[4] + a2 * c[7]);
+  const double wz = z - (a0 * c[2] + a1 * c[5] + a2 * c[8]);
+  bin_pos[rec] = BinPos{wx, wy, wz, i, 0};
   const float hx = static_cast<float>(wx), hy = static_cast<float>(wy), hz = static_cast<float>(wz);
-  bin_posf[slot] = BinPosF{hx, hy, hz, i, static_cast<float>(wx - hx), static_cast<float>(wy - hy),
-                           static_cast<float>(wz - hz), 0};
+  bin_posf[rec] = BinPosF{hx, hy, hz, i, static_cast<float>(wx - hx), static_cast<float>(wy - hy),
+                          static_cast<float>(wz - hz), 0};
 }
-
 
 // Image-scan frames: one thread per centre (cell-list frames are left to the warp kernels).
 __global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
@@ -160,8 +168,8 @@ constexpr int kFillWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp, 4)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                 const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos, const BinPosF* bin_posf,
-                 const int* bin_of, const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr,
+                 const int* bin_count, int bin_cap, const BinAtom* bin_rec, const BinPos* bin_pos,
+                 const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr,
                  typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
   __shared__ BinWalk walk[kFillWarps];
@@ -174,7 +182,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
-  warp_bin_edges<Real>(i, fp, pos, rc2, bin_start, bin_rec, bin_pos, bin_posf, bin_of, frac, off, error,
+  warp_bin_edges<Real>(i, fp, pos, rc2, bin_count, bin_cap, bin_rec, bin_pos, bin_posf, bin_of, frac, off, error,
                        queue[threadIdx.x / kWarp], walk[threadIdx.x / kWarp],
                        [&](unsigned mask, bool ok, int j, int a, int b, int c, Real x, Real y, Real z, Real r) {
                          if (ok) {
@@ -427,39 +435,56 @@ __global__ void k_iota(int* v, long long n) {
   if (e < n) v[e] = static_cast<int>(e);
 }
 
-// Per-frame energy and virial in two deterministic steps: block (f, s) reduces the atoms
-// a0 + s * 256 + t, a0 + (S + s) * 256 + t, ... of frame f with a fixed-order tree into
-// partial[f][s][7]; k_frame_finish then adds the S slices of each frame in slice order.
-__global__ void k_frame_partial(const FramePlan* plans, int nframes, int S, const double* site,
-                                const double* vir_atom, double* partial) {
+// Per-frame energy and virial (FP64), one launch: block (f, slice) sums the site energies and
+// per-atom virials of its atoms (a fixed strided order per thread, then shuffle trees and the
+// block's warps in order) into partial[f][slice][7] and copies the site energies out when asked;
+// the block of frame f that arrives last (arrivals[f], reset by that block) adds the frame's
+// slices in slice order.  The result does not depend on which block arrives last.
+constexpr int kFrameThreads = 256;
+__global__ void __launch_bounds__(kFrameThreads)
+k_frame_reduce(const FramePlan* plans, int nframes, int S, const double* site, const double* vir_atom,
+               double* site_out, double* partial, unsigned* arrivals, double* energy, double* virial) {
   const int f = blockIdx.x, sl = blockIdx.y;
   if (f >= nframes) return;
-  __shared__ double sh[7][256];
   double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (int i = plans[f].a0 + sl * 256 + threadIdx.x; i < plans[f].a1; i += S * 256) {
-    acc[0] += site[i];
+  for (int i = plans[f].a0 + sl * kFrameThreads + threadIdx.x; i < plans[f].a1; i += S * kFrameThreads) {
+    const double e = site[i];
+    acc[0] += e;
+    if (site_out) site_out[i] = e;
     for (int c = 0; c < 6; ++c) acc[1 + c] += vir_atom[6 * (size_t)i + c];
   }
-  for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] = acc[c];
+  __shared__ double sh[kFrameThreads / kWarp][7];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x / kWarp;
+#pragma unroll
+  for (int c = 0; c < 7; ++c) {
+    double v = acc[c];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][c] = v;
+  }
   __syncthreads();
-  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
-    if (threadIdx.x < st)
-      for (int c = 0; c < 7; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
-    __syncthreads();
+  if (threadIdx.x < 7) {
+    double v = 0.0;
+    for (int w = 0; w < kFrameThreads / kWarp; ++w) v += sh[w][threadIdx.x];
+    partial[(static_cast<size_t>(f) * S + sl) * 7 + threadIdx.x] = v;
+    __threadfence();
   }
-  if (threadIdx.x < 7) partial[(static_cast<size_t>(f) * S + sl) * 7 + threadIdx.x] = sh[threadIdx.x][0];
-}
-
-__global__ void k_frame_finish(int nframes, int S, const double* partial, double* energy, double* virial) {
-  const int f = blockIdx.x * blockDim.y + threadIdx.y, c = threadIdx.x;
-  if (f >= nframes || c >= 7) return;
-  double v = 0.0;
-  for (int sl = 0; sl < S; ++sl) v += partial[(static_cast<size_t>(f) * S + sl) * 7 + c];
-  if (c == 0) {
-    if (energy) energy[f] = v;
-  } else if (virial) {
-    virial[6 * f + c - 1] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(arrivals + f, 1u) == static_cast<unsigned>(S - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < 7) {
+    const int c = threadIdx.x;
+    double v = 0.0;
+    for (int q = 0; q < S; ++q) v += __ldcg(partial + (static_cast<size_t>(f) * S + q) * 7 + c);
+    if (c == 0) {
+      if (energy) energy[f] = v;
+    } else if (virial) {
+      virial[6 * f + c - 1] = v;
+    }
   }
+  if (threadIdx.x == 0) arrivals[f] = 0u;
 }
 
 // Caller-provided edges (owned centres, LAMMPS layout): count per centre.
@@ -677,9 +702,10 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   if (model_.gated && !unique(model_.gate_nodes)) throw Error(3, "SUS2 model: duplicate gate scalar moments");
   if (model_.K > kMaxK) throw Error(3, "SUS2 model: sh_k_max above 8 is not supported by the GPU engine");
   plans_ = new std::vector<FramePlan>();
-  SUS2G_CUDA(cudaMallocHost(&host_total_, 4 * sizeof(int)));
-  error_.ensure(2 * sizeof(int));  // [0] error code, [1] cell-list capacity overflow (largest count)
-  SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 2 * sizeof(int), stream_));
+  SUS2G_CUDA(cudaMallocHost(&host_total_, 8 * sizeof(int)));
+  // [0] error code, [1] cell-list edge capacity overflow (largest count), [2] bin capacity overflow
+  error_.ensure(3 * sizeof(int));
+  SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 3 * sizeof(int), stream_));
   upload_model();
 }
 
@@ -820,13 +846,19 @@ long long Engine::nedges() {
 }
 
 void Engine::check_device_error() {
-  SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 2, error_.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 4, error_.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
   SUS2G_CUDA(cudaStreamSynchronize(stream_));
-  const int h = host_total_[2], over = host_total_[3];
-  if (over > 0) {
-    SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 2 * sizeof(int), stream_));
-    cap_scale_ *= 2.0;
-    min_cap_ = std::max(min_cap_, over);
+  const int h = host_total_[4], over = host_total_[5], bin_over = host_total_[6];
+  if (over > 0 || bin_over > 0) {
+    SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 3 * sizeof(int), stream_));
+    if (over > 0) {
+      cap_scale_ *= 2.0;
+      min_cap_ = std::max(min_cap_, over);
+    }
+    if (bin_over > 0) {
+      bin_cap_scale_ *= 2.0;
+      min_bin_cap_ = std::max(min_bin_cap_, bin_over);
+    }
     reset_step_graph();
     throw EdgeOverflow();
   }
@@ -896,7 +928,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const double rc = model_.max_dist, rc2 = rc * rc;
   std::vector<FramePlan>& plans = *plans_;
   plans.assign(nframes, FramePlan{});
-  int a = 0, bins = 0;
+  int a = 0, bins = 0, bin_cap = min_bin_cap_;
   long long pad_total = 0;
   bins_frames_ = 0;
   for (int f = 0; f < nframes; ++f) {
@@ -935,6 +967,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                        fp.cell[2] * (fp.cell[3] * fp.cell[7] - fp.cell[4] * fp.cell[6]);
       const double mean = frame_natoms[f] / std::abs(c) * (4.0 / 3.0) * 3.141592653589793 * rc * rc2;
       fp.cap = std::max(min_cap_, static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0)));
+      // bin capacity: twice the frame's mean atoms per bin plus 8 (grown after an overflow)
+      const double per_bin = frame_natoms[f] / static_cast<double>(fp.nb[0] * fp.nb[1] * fp.nb[2]);
+      bin_cap = std::max(bin_cap, static_cast<int>(std::min(1.0e6, std::ceil(bin_cap_scale_ * per_bin) + 8.0)));
       fp.pad0 = pad_total;
       pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
     }
@@ -954,27 +989,27 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   row_.ensure(sizeof(int) * (a + 1));
   bin_count_.ensure(sizeof(int) * (bins + 1));
   bin_start_.ensure(sizeof(int) * (bins + 1));
-  bin_cursor_.ensure(sizeof(int) * (bins + 1));
   DevBuf& bin_of = bin_of_;
   bin_of.ensure(sizeof(int) * std::max(1, a));
-  if (nframes) { k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>()); ++launches_; }
+  // batches with cell lists only: the binning kernel finds each atom's frame itself
+  const bool find_frame = bins && bins_frames_ == nframes;
+  if (nframes && !find_frame) {
+    k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>());
+    ++launches_;
+  }
   if (bins) {
     SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
-    SUS2G_CUDA(cudaMemsetAsync(bin_cursor_.ptr, 0, sizeof(int) * (bins + 1), s));
     frac_.ensure(sizeof(AtomFrac) * a);
     off_.ensure(sizeof(AtomOff) * a);
-    k_bin_count<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, a, bin_of.as<int>(),
-                                               bin_count_.as<int>(), frac_.as<AtomFrac>(), off_.as<AtomOff>());
-    k_exclusive_scan<<<1, 1024, 0, s>>>(bin_count_.as<int>(), bins, bin_start_.as<int>(), error_.as<int>());
+    const size_t slots = static_cast<size_t>(bins) * bin_cap;
+    bin_rec_.ensure(sizeof(BinAtom) * slots);
+    bin_pos_.ensure(sizeof(BinPos) * slots);
+    bin_posf_.ensure(sizeof(BinPosF) * slots);
+    k_bin_place<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, find_frame, frame_of_.as<int>(), d_pos, a,
+                                               bin_cap, bin_of.as<int>(), bin_count_.as<int>(), frac_.as<AtomFrac>(),
+                                               off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
+                                               bin_posf_.as<BinPosF>(), error_.as<int>() + 2);
     ++launches_;
-    bin_rec_.ensure(sizeof(BinAtom) * std::max(1, a));
-    bin_pos_.ensure(sizeof(BinPos) * std::max(1, a));
-    bin_posf_.ensure(sizeof(BinPosF) * std::max(1, a));
-    k_bin_fill<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), frame_of_.as<int>(), d_pos, bin_of.as<int>(), a,
-                                              bin_start_.as<int>(), bin_cursor_.as<int>(), frac_.as<AtomFrac>(),
-                                              off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
-                                              bin_posf_.as<BinPosF>());
-    launches_ += 2;
   }
   const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
   const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);
@@ -996,11 +1031,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     pad_key_.ensure(sizeof(unsigned long long) * slots);
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, BS, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
                                                                           pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;
@@ -1264,14 +1299,21 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (nframes_) {
       int largest = 0;
       for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
-      const int S = std::max(1, std::min(64, (largest + 255) / 256));
+      const int S = std::max(1, std::min(64, (largest + kFrameThreads - 1) / kFrameThreads));
       frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
-      k_frame_partial<<<dim3(nframes_, S), 256, 0, s>>>(plan_.as<FramePlan>(), nframes_, S, site_.as<double>(),
-                                                        vir_atom_.as<double>(), frame_partial_.as<double>());
-      k_frame_finish<<<(nframes_ + 7) / 8, dim3(8, 8), 0, s>>>(nframes_, S, frame_partial_.as<double>(), d_energy, d_virial);
-      launches_ += 2;
+      if (nframes_ > arrivals_frames_) {
+        // arrival counters start at zero; each launch leaves them at zero
+        frame_arrivals_.ensure(sizeof(unsigned) * nframes_);
+        SUS2G_CUDA(cudaMemsetAsync(frame_arrivals_.ptr, 0, sizeof(unsigned) * nframes_, s));
+        arrivals_frames_ = nframes_;
+      }
+      k_frame_reduce<<<dim3(nframes_, S), kFrameThreads, 0, s>>>(
+          plan_.as<FramePlan>(), nframes_, S, site_.as<double>(), vir_atom_.as<double>(), d_site,
+          frame_partial_.as<double>(), frame_arrivals_.as<unsigned>(), d_energy, d_virial);
+      ++launches_;
+    } else if (d_site && N) {
+      SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
     }
-    if (d_site && N) SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
     mark_end();
   }
 }
@@ -1504,6 +1546,8 @@ void Engine::step_frames(int nframes, const int* frame_natoms, const double* cel
     key.push_back(ptr(p));
   key.push_back(cap_scale_);
   key.push_back(min_cap_);
+  key.push_back(bin_cap_scale_);
+  key.push_back(min_bin_cap_);
   // the same layout as the previous step, with no other edge build, staged call or parameter
   // upload since (those may have regrown the buffers whose addresses a graph holds)
   const bool same = step_graphs_ && !timing_ && key == step_key_ && edge_generation_ == step_gen_;

@@ -182,12 +182,14 @@ class Engine {
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
   DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
-  DevBuf bin_count_, bin_start_, bin_cursor_, bin_rec_, bin_pos_, bin_posf_;
+  DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf hbar_atom_, bin_of_, frac_, off_, in_row_, in_edge_;  // in_*: caller edges grouped by neighbour
   DevBuf pad_nbr_, pad_d4_, pad_key_;  // padded single-pass staging of cell-list frames
   double cap_scale_ = 2.0;      // padded capacity = cap_scale x mean neighbour count + 64 (grows on overflow)
+  double bin_cap_scale_ = 2.0;  // bin capacity = bin_cap_scale x mean atoms per bin + 8 (grows on overflow)
+  int min_bin_cap_ = 0;          // lower bound of the bin capacity after an overflow
   bool sort_from_pad_ = false;
   int* host_total_ = nullptr;   // pinned [4]
   // stage timer (cudaEvent pairs per stage, enabled by set_timing)
@@ -203,7 +205,8 @@ class Engine {
   int open_stage_ = -1;
   cudaEvent_t open_event_ = nullptr;
   // step buffers
-  DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_, frame_partial_;
+  DevBuf g_, hsig_, hcontrib_, gmom_, site_, vir_atom_, error_, frame_partial_, frame_arrivals_;
+  int arrivals_frames_ = 0;     // frame_arrivals_ entries known to be zero
   DevBuf scratch_;
   DevBuf io_[8];
 };

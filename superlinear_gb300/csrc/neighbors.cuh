@@ -137,7 +137,8 @@ struct BinWalk {
 
 template <typename Real, typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
-                                               const int* bin_start, const BinAtom* bin_rec, const BinPos* bin_pos,
+                                               const int* bin_count, int bin_cap, const BinAtom* bin_rec,
+                                               const BinPos* bin_pos,
                                                const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac,
                                                const AtomOff* off, int* error, int2* queue, BinWalk& walk,
                                                Round&& round) {
@@ -180,8 +181,8 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
       const int w2 = raw2 < 0 ? -1 : (raw2 >= fp.nb[2] ? 1 : 0);
       const int bin = fp.bin0 + ((raw0 - w0 * fp.nb[0]) * fp.nb[1] + (raw1 - w1 * fp.nb[1])) * fp.nb[2] +
                       (raw2 - w2 * fp.nb[2]);
-      bstart = bin_start[bin];
-      blen = bin_start[bin + 1] - bstart;
+      bstart = bin * bin_cap;
+      blen = min(bin_count[bin], bin_cap);
       wk = (w0 + 1) * 9 + (w1 + 1) * 3 + (w2 + 1);
     }
     const int o = bstart - mine;
