@@ -474,14 +474,20 @@ k_frame_reduce(const FramePlan* plans, int nframes, int S, const double* site, c
   __syncthreads();
   if (!last) return;
   __threadfence();
-  if (threadIdx.x < 7) {
-    const int c = threadIdx.x;
-    double v = 0.0;
-    for (int q = 0; q < S; ++q) v += __ldcg(partial + (static_cast<size_t>(f) * S + q) * 7 + c);
-    if (c == 0) {
-      if (energy) energy[f] = v;
-    } else if (virial) {
-      virial[6 * f + c - 1] = v;
+  // warp c < 7 sums component c over the S <= 64 slices: lane q holds slices q and q + 32, then a
+  // fixed shuffle tree (all loads in flight at once)
+  if (warp < 7) {
+    const int c = warp;
+    const double* pf = partial + static_cast<size_t>(f) * S * 7 + c;
+    double v = lane < S ? __ldcg(pf + 7 * lane) : 0.0;
+    if (lane + kWarp < S) v += __ldcg(pf + 7 * (lane + kWarp));
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      if (c == 0) {
+        if (energy) energy[f] = v;
+      } else if (virial) {
+        virial[6 * f + c - 1] = v;
+      }
     }
   }
   if (threadIdx.x == 0) arrivals[f] = 0u;
