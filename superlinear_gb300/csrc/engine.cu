@@ -54,8 +54,8 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
 // its count; the host then grows bcap and repeats the step.  With find_frame the atom's frame is
 // found here (binary search over the frames' first atoms) and written to frame_of.
 __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame, int* frame_of, const double* pos,
-                            int natoms, int bcap, int* bin_of, int* bin_count, AtomFrac* frac, AtomOff* off,
-                            BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over) {
+                            int natoms, int bcap, int* bin_of, int* rec_of, int* bin_count, AtomFrac* frac,
+                            AtomOff* off, BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   int f;
@@ -89,8 +89,9 @@ __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame
   const int bin = fp.bin0 + (b[0] * fp.nb[1] + b[1]) * fp.nb[2] + b[2];
   bin_of[i] = bin;
   const int slot = atomicAdd(bin_count + bin, 1);
-  if (slot >= bcap) { atomicMax(bin_over, slot + 1); return; }
+  if (slot >= bcap) { atomicMax(bin_over, slot + 1); rec_of[i] = 0; return; }
   const long long rec = static_cast<long long>(bin) * bcap + slot;
+  rec_of[i] = static_cast<int>(rec);
   bin_rec[rec] = BinAtom{w32[0], w32[1], w32[2], i, o[0], o[1], o[2], 0};
   const double* c = fp.cell;
   const double a0 = o[0], a1 = o[1], a2 = o[2];
@@ -169,7 +170,8 @@ template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp, 4)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
                  const int* bin_count, int bin_cap, const BinAtom* bin_rec, const BinPos* bin_pos,
-                 const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac, const AtomOff* off, int* counts, int* nbr,
+                 const BinPosF* bin_posf, const int* bin_of, const int* rec_of, const AtomFrac* frac, const AtomOff* off,
+                 int* counts, int* nbr,
                  typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
   __shared__ BinWalk walk[kFillWarps];
@@ -182,7 +184,7 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
-  warp_bin_edges<Real>(i, fp, pos, rc2, bin_count, bin_cap, bin_rec, bin_pos, bin_posf, bin_of, frac, off, error,
+  warp_bin_edges<Real>(i, fp, pos, rc2, bin_count, bin_cap, bin_rec, bin_pos, bin_posf, bin_of, rec_of, frac, off, error,
                        queue[threadIdx.x / kWarp], walk[threadIdx.x / kWarp],
                        [&](unsigned mask, bool ok, int j, int a, int b, int c, Real x, Real y, Real z, Real r) {
                          if (ok) {
@@ -965,7 +967,14 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       for (int q = 0; q < 3; ++q)
         rows += std::sqrt(fp.cell[3 * q] * fp.cell[3 * q] + fp.cell[3 * q + 1] * fp.cell[3 * q + 1] + fp.cell[3 * q + 2] * fp.cell[3 * q + 2]);
       fp.band = 2.0 * rc * (4.0 * 6.0e-8 * rows) * 4.0 + 1e-6;
-      for (int q = 0; q < 9; ++q) fp.cellf[q] = static_cast<float>(fp.cell[q]);
+      for (int q = 0; q < 9; ++q) {
+        fp.cellf[q] = static_cast<float>(fp.cell[q]);
+        fp.celll[q] = static_cast<float>(fp.cell[q] - static_cast<double>(fp.cellf[q]));
+      }
+      fp.screen2 = static_cast<float>(rc2 + fp.band);
+      // FP32 r^2 of the double-float edge vector is within ~1e-6 relative of the exact one
+      fp.lo2 = static_cast<float>(rc2 * (1.0 - 1e-4));
+      fp.hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
       bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
       // padded staging capacity: cap_scale x the mean neighbour count of the frame's density + 64
       const double c = fp.cell[0] * (fp.cell[4] * fp.cell[8] - fp.cell[5] * fp.cell[7]) -
@@ -1007,12 +1016,14 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
     frac_.ensure(sizeof(AtomFrac) * a);
     off_.ensure(sizeof(AtomOff) * a);
+    rec_of_.ensure(sizeof(int) * a);
     const size_t slots = static_cast<size_t>(bins) * bin_cap;
     bin_rec_.ensure(sizeof(BinAtom) * slots);
     bin_pos_.ensure(sizeof(BinPos) * slots);
     bin_posf_.ensure(sizeof(BinPosF) * slots);
     k_bin_place<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, find_frame, frame_of_.as<int>(), d_pos, a,
-                                               bin_cap, bin_of.as<int>(), bin_count_.as<int>(), frac_.as<AtomFrac>(),
+                                               bin_cap, bin_of.as<int>(), rec_of_.as<int>(), bin_count_.as<int>(),
+                                               frac_.as<AtomFrac>(),
                                                off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
                                                bin_posf_.as<BinPosF>(), error_.as<int>() + 2);
     ++launches_;
@@ -1037,11 +1048,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     pad_key_.ensure(sizeof(unsigned long long) * slots);
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF, counts_.as<int>(),
                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, FR, OF, counts_.as<int>(),
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF, counts_.as<int>(),
                                                                           pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
                                                                           pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
     ++launches_;

@@ -182,7 +182,7 @@ class Engine {
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
   DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
-  DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_;
+  DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf hbar_atom_, bin_of_, frac_, off_, in_row_, in_edge_;  // in_*: caller edges grouped by neighbour

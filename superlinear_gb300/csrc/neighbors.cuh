@@ -29,7 +29,10 @@ struct FramePlan {
   int cap;          // cell-list frames: edge slots per centre in the padded staging buffers
   long long pad0;   // cell-list frames: first padded slot of the frame (centre i: pad0 + (i - a0) cap)
   float cellf[9];   // FP32 copy of the cell for the candidate prefilter
+  float celll[9];   // cell - cellf: with cellf the double-float form of the cell rows
   double band;      // |r^2 error| bound of the FP32 prefilter; candidates within it get the FP64 test
+  float screen2;    // FP32 prefilter threshold r_c^2 + band
+  float lo2, hi2;   // FP32 engines: r^2 below lo2 is inside, above hi2 outside, else the FP64 test
 };
 
 // Per-atom wrapped fractional coordinates (FP32, in [0,1)) and the integer cell offsets
@@ -139,9 +142,9 @@ template <typename Real, typename Round>
 __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const double* pos, double rc2,
                                                const int* bin_count, int bin_cap, const BinAtom* bin_rec,
                                                const BinPos* bin_pos,
-                                               const BinPosF* bin_posf, const int* bin_of, const AtomFrac* frac,
-                                               const AtomOff* off, int* error, int2* queue, BinWalk& walk,
-                                               Round&& round) {
+                                               const BinPosF* bin_posf, const int* bin_of, const int* rec_of,
+                                               const AtomFrac* frac, const AtomOff* off, int* error, int2* queue,
+                                               BinWalk& walk, Round&& round) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const int local = bin_of[i] - fp.bin0;
@@ -150,17 +153,46 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
   const AtomOff oi = off[i];
   const double* c = fp.cell;
   const float* cf = fp.cellf;
-  // lane k < 27: wrap k = (w0 + 1) 9 + (w1 + 1) 3 + (w2 + 1)
+  const int self_rec = rec_of[i];  // the centre's own bin record
+  // lane k < 27: wrap k = (w0 + 1) 9 + (w1 + 1) 3 + (w2 + 1).  Its shift (w + off_i) . cell - x_i =
+  // w . cell - (x_i wrapped into the home cell): FP64 engines in FP64; FP32 engines as double-float
+  // parts from the cell's and the centre record's (hi, lo) parts in FP32 arithmetic (their exact
+  // FP64 shift is formed only for the rare entries near the cutoff)
   if (lane < 27) {
     const int w0 = lane / 9 - 1, w1 = (lane / 3) % 3 - 1, w2 = lane % 3 - 1;
-    const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
     WrapShift w;
-    w.x = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
-    w.y = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
-    w.z = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
-    w.hx = static_cast<float>(w.x); w.lx = static_cast<float>(w.x - static_cast<double>(w.hx));
-    w.hy = static_cast<float>(w.y); w.ly = static_cast<float>(w.y - static_cast<double>(w.hy));
-    w.hz = static_cast<float>(w.z); w.lz = static_cast<float>(w.z - static_cast<double>(w.hz));
+    if constexpr (sizeof(Real) == 8) {
+      const double a0 = w0 + oi.x, a1 = w1 + oi.y, a2 = w2 + oi.z;
+      w.x = a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i];
+      w.y = a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1];
+      w.z = a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2];
+      w.hx = w.hy = w.hz = w.lx = w.ly = w.lz = 0.f;
+    } else {
+      const BinPosF me = bin_posf[self_rec];
+      const float* cl = fp.celll;
+      float h[3], l[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        // w0 row0 + w1 row1 + w2 row2 - x_i, each term an exact (hi, lo) pair
+        float sh = -(q == 0 ? me.xh : (q == 1 ? me.yh : me.zh));
+        float sl = -(q == 0 ? me.xl : (q == 1 ? me.yl : me.zl));
+        const int wq[3] = {w0, w1, w2};
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          const float th = static_cast<float>(wq[r]) * cf[3 * r + q], tl = static_cast<float>(wq[r]) * cl[3 * r + q];
+          const float s2 = sh + th, v = s2 - sh;
+          const float e = (sh - (s2 - v)) + (th - v);
+          const float lo = e + (sl + tl);
+          sh = s2 + lo;
+          sl = lo - (sh - s2);
+        }
+        h[q] = sh;
+        l[q] = sl;
+      }
+      w.x = w.y = w.z = 0.0;
+      w.hx = h[0]; w.hy = h[1]; w.hz = h[2];
+      w.lx = l[0]; w.ly = l[1]; w.lz = l[2];
+    }
     w.nb = make_int4(w0 + oi.x, w1 + oi.y, w2 + oi.z, 0);
     w.df = make_float4(static_cast<float>(w0) - fi.x, static_cast<float>(w1) - fi.y, static_cast<float>(w2) - fi.z, 0.f);
     walk.shift[lane] = w;
@@ -201,8 +233,7 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
 #pragma unroll
   for (int q = 0; q < 9; ++q) cr[q] = cf[q];
   __syncwarp();
-  const float screen = static_cast<float>(rc2 + fp.band);
-  const float lo2 = static_cast<float>(rc2 * (1.0 - 1e-4)), hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
+  const float screen = fp.screen2, lo2 = fp.lo2, hi2 = fp.hi2;
   int queued = 0;  // warp-uniform
   // test of queue entries [0, n) (one per lane) and the round callback
   // queue entry: (bin record index, packed image | wrap index k << 21)
@@ -241,9 +272,12 @@ __device__ __forceinline__ void warp_bin_edges(int i, const FramePlan& fp, const
         r2 = vx * vx + vy * vy + vz * vz;
         ok = r2 < lo2;
         if (!ok && r2 < hi2) {
-          // near the cutoff: the FP64 test decides
+          // near the cutoff: the FP64 test decides, x_j + (w + off_i) . cell - x_i in FP64
           const BinPos bd = bin_pos[q.x];
-          const double dx = bd.x + w.x, dy = bd.y + w.y, dz = bd.z + w.z;
+          const double a0 = k / 9 - 1 + oi.x, a1 = (k / 3) % 3 - 1 + oi.y, a2 = k % 3 - 1 + oi.z;
+          const double dx = bd.x + (a0 * c[0] + a1 * c[3] + a2 * c[6] - pos[3 * i]);
+          const double dy = bd.y + (a0 * c[1] + a1 * c[4] + a2 * c[7] - pos[3 * i + 1]);
+          const double dz = bd.z + (a0 * c[2] + a1 * c[5] + a2 * c[8] - pos[3 * i + 2]);
           const double d2 = dx * dx + dy * dy + dz * dz;
           ok = d2 < rc2;
           vx = static_cast<float>(dx); vy = static_cast<float>(dy); vz = static_cast<float>(dz);
