@@ -36,7 +36,8 @@ struct PassArgs {
   DevModel<Real> dm;
   int natoms;
   const int* types;
-  const int* row;          // [natoms + 1] CSR by centre
+  const int* row;          // [natoms] first edge of each centre
+  const int* row_end;      // [natoms] one past its last edge (row + 1 for CSR layouts)
   const int* nbr;          // [E]
   const int* rev;          // [E] reverse edge
   const typename Vec4<Real>::type* d4;  // [E] (dx, dy, dz, r)
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp,
 
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
     const int ti = a.types[atom];
-    const int e0 = a.row[atom], e1 = a.row[atom + 1];
+    const int e0 = a.row[atom], e1 = a.row_end[atom];
     // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form
     double vir[6] = {0, 0, 0, 0, 0, 0};
     float vhi[6] = {0, 0, 0, 0, 0, 0}, vlo[6] = {0, 0, 0, 0, 0, 0};

@@ -207,24 +207,38 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
 constexpr int kSortWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kSortWarps * kWarp)
-k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame_of, int stage,
-            const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
+k_edge_sort(int* row, int* row_end, const int* counts, int natoms, const FramePlan* plans, const int* frame_of,
+            int stage, const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
             const unsigned long long* pkey, const int* pnbr, const typename Vec4<Real>::type* pd4,
             unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   extern __shared__ unsigned long long sort_keys[];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
-  const int e0 = row[warp], n = row[warp + 1] - e0;
-  long long in0 = e0;
+  // row_end == null: CSR output at row[i] .. row[i + 1]; otherwise (cell lists only) the sorted
+  // edges stay in the centre's padded slots and the row bounds are written here
+  int e0, n;
+  long long in0;
   const unsigned long long* K = key_in;
   const int* NB = nbr_in;
   const typename Vec4<Real>::type* D = d4_in;
-  if (plans) {
+  if (row_end) {
     const FramePlan& fp = plans[frame_of[warp]];
-    if (fp.use_bins) {
-      in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
-      K = pkey; NB = pnbr; D = pd4;
+    in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
+    e0 = static_cast<int>(in0);
+    n = counts[warp];
+    K = pkey; NB = pnbr; D = pd4;
+    if (lane == 0) { row[warp] = e0; row_end[warp] = e0 + n; }
+  } else {
+    e0 = row[warp];
+    n = row[warp + 1] - e0;
+    in0 = e0;
+    if (plans) {
+      const FramePlan& fp = plans[frame_of[warp]];
+      if (fp.use_bins) {
+        in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
+        K = pkey; NB = pnbr; D = pd4;
+      }
     }
   }
   const unsigned long long* src = K + in0;
@@ -270,12 +284,13 @@ k_edge_sort(const int* row, int natoms, const FramePlan* plans, const int* frame
 // Reverse edge of every edge (warp per centre i): for e = (i -> j, n) the edge (j -> i, -n) is
 // found by binary search in j's sorted keys.
 // Up to kRevPer searches per lane run interleaved, so their dependent loads overlap.
-__global__ void k_reverse(const int* row, const unsigned long long* key, int natoms, int* rev, int* error) {
+__global__ void k_reverse(const int* row, const int* row_end, const unsigned long long* key, int natoms, int* rev,
+                          int* error) {
   constexpr int kRevPer = 4;
   const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (i >= natoms) return;
-  const int end = row[i + 1];
+  const int end = row_end[i];
   for (int base = row[i]; base < end; base += kRevPer * kWarp) {
     int lo[kRevPer], hi[kRevPer], found[kRevPer];
     unsigned long long want[kRevPer];
@@ -290,7 +305,7 @@ __global__ void k_reverse(const int* row, const unsigned long long* key, int nat
                   n2 = static_cast<int>(k & 127) - 64;
         want[u] = edge_key(i, -n0, -n1, -n2);
         lo[u] = row[j];
-        hi[u] = row[j + 1] - 1;
+        hi[u] = row_end[j] - 1;
       }
     }
     bool active = true;
@@ -322,13 +337,14 @@ __global__ void k_reverse(const int* row, const unsigned long long* key, int nat
 // F_i = sum over i's edges of (g_e - g_rev(e)), warp per atom: FP64 accumulation for FP64 edge
 // gradients, compensated FP32 (two-sum, FP64 result) for FP32 ones.
 template <typename Real>
-__global__ void k_force_gather(const int* row, const int* rev, const Real* g, int natoms, double* force) {
+__global__ void k_force_gather(const int* row, const int* row_end, const int* rev, const Real* g, int natoms,
+                               double* force) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
   double f[3] = {0, 0, 0};
   float hi[3] = {0, 0, 0}, lo[3] = {0, 0, 0};
-  for (int e = row[warp] + lane; e < row[warp + 1]; e += kWarp) {
+  for (int e = row[warp] + lane; e < row_end[warp]; e += kWarp) {
     const int r = rev[e];
     for (int c = 0; c < 3; ++c) {
       if (sizeof(Real) == 4) {
@@ -845,9 +861,13 @@ void Engine::upload_model() {
 
 long long Engine::nedges() {
   if (!nedges_exact_) {
-    SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 2, row_.as<int>() + ncentres_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+    // padded layout: the sum of the per-centre counts
+    std::vector<int> counts(static_cast<size_t>(std::max(0, ncentres_)));
+    if (ncentres_)
+      SUS2G_CUDA(cudaMemcpyAsync(counts.data(), counts_.ptr, sizeof(int) * ncentres_, cudaMemcpyDeviceToHost, stream_));
     SUS2G_CUDA(cudaStreamSynchronize(stream_));
-    exact_edges_ = host_total_[2];
+    exact_edges_ = 0;
+    for (int c : counts) exact_edges_ += c;
     nedges_exact_ = true;
   }
   return exact_edges_;
@@ -1067,13 +1087,14 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   }
   long long total = 0;
   if (bins_frames_ == nframes) {
-    // cell lists only: no host synchronisation.  The edge arrays are sized by the padded
-    // capacity; the exact total stays on the device (row[a]) and an overflow is reported by the
+    // cell lists only: no host synchronisation and no CSR compaction.  The sorted edges stay in
+    // their centres' padded slots (row[i] .. row_end[i]); the edge arrays are sized by the padded
+    // capacity, the exact total is the sum of the counts, and an overflow is reported by the
     // step's check_device_error.
-    k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
-    ++launches_;
     total = pad_total;
     nedges_exact_ = false;
+    padded_ = true;
+    row_end_.ensure(sizeof(int) * std::max(1, a));
   } else {
     for (int attempt = 0;; ++attempt) {
       k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
@@ -1107,6 +1128,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
     }
     nedges_exact_ = true;
+    padded_ = false;
   }
   if (total > 2147483647LL) throw Error(4, "edge build: more than 2^31 - 1 edge slots");
   nedges_ = total;
@@ -1143,14 +1165,15 @@ void Engine::finalize_edges() {
       for (const FramePlan& fp : *plans_) stage = std::max(stage, fp.use_bins ? fp.cap : 0);
     stage = std::min(stage, 512);
     const size_t smem = sizeof(unsigned long long) * kSortWarps * stage;
+    int* RE = padded_ ? row_end_.as<int>() : nullptr;
     if (precision_ == kFP32)
       k_edge_sort<float><<<blocks, kSortWarps * kWarp, smem, s>>>(
-          row_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+          row_.as<int>(), RE, counts_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
           tmp_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
           key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeF>());
     else
       k_edge_sort<double><<<blocks, kSortWarps * kWarp, smem, s>>>(
-          row_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
+          row_.as<int>(), RE, counts_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
           tmp_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
           key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
     ++launches_;
@@ -1179,7 +1202,7 @@ void Engine::finalize_edges() {
     }
   } else if (nedges_ && a) {
     k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, s>>>(
-        row_.as<int>(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
+        row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
     ++launches_;
   }
 }
@@ -1188,6 +1211,7 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
   SUS2G_CUDA(cudaSetDevice(device_));
   ++edge_generation_;
   sort_from_pad_ = false;
+  padded_ = false;
   if (nowned < 0 || nall < nowned || nedges < 0) throw Error(1, "invalid atom layout");
   cudaStream_t s = stream_;
   ncentres_ = nowned;
@@ -1253,6 +1277,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   a.natoms = ncentres_;
   a.types = d_types_;
   a.row = row_.as<int>();
+  a.row_end = d_row_end();
   a.nbr = nbr_.as<int>();
   a.rev = rev_.as<int>();
   a.d4 = static_cast<const typename Vec4<Real>::type*>(d4_.ptr);
@@ -1310,7 +1335,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
         k_force_gather_user<Real><<<static_cast<unsigned>((static_cast<long long>(N) * kWarp + 255) / 256), 256, 0, s>>>(
             row_.as<int>(), ncentres_, in_row_.as<int>(), in_edge_.as<int>(), g_.as<Real>(), N, d_forces);
       else
-        k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), rev_.as<int>(), g_.as<Real>(), ncentres_, d_forces);
+        k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), d_row_end(), rev_.as<int>(),
+                                                                     g_.as<Real>(), ncentres_, d_forces);
       ++launches_;
     }
     if (nframes_) {
@@ -1432,6 +1458,7 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
   a.natoms = ncentres_;
   a.types = d_types_;
   a.row = row_.as<int>();
+  a.row_end = d_row_end();
   a.nbr = nbr_.as<int>();
   a.rev = rev_.as<int>();
   a.d4 = static_cast<const typename Vec4<Real>::type*>(d4_.ptr);
@@ -1518,6 +1545,7 @@ int Engine::static_pass_external(int natoms, const int* types, const int* row, c
   a.natoms = natoms;
   a.types = types;
   a.row = row;
+  a.row_end = row + 1;
   a.nbr = nbr;
   a.rev = nullptr;
   a.d4 = static_cast<const EdgeF*>(d4);

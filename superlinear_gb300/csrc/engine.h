@@ -140,6 +140,9 @@ class Engine {
 
   // internal buffers exposed for the tests / parameter-gradient pass
   const int* d_row() const { return row_.as<int>(); }
+  // one past each centre's last edge: a separate array for cell-list batches (edges in padded
+  // per-centre slots), row + 1 for CSR layouts
+  const int* d_row_end() const { return padded_ ? row_end_.as<int>() : row_.as<int>() + 1; }
   const int* d_nbr() const { return nbr_.as<int>(); }
   const int* d_rev() const { return rev_.as<int>(); }
 
@@ -181,7 +184,8 @@ class Engine {
   int min_cap_ = 0;              // lower bound of the padded capacity after an overflow
   std::vector<FramePlan>* plans_ = nullptr;
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
-  DevBuf counts_, row_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
+  DevBuf counts_, row_, row_end_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
+  bool padded_ = false;         // cell-list batch: edges left in padded per-centre slots (row_end_)
   DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather

@@ -40,6 +40,7 @@ struct GradArgs {
   int natoms;
   const int* types;
   const int* row;
+  const int* row_end;      // one past each centre's last edge (row + 1 for CSR layouts)
   const int* nbr;
   const int* rev;
   const typename Vec4<Real>::type* d4;
@@ -226,7 +227,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
 
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
     const int ti = a.types[atom];
-    const int e0 = a.row[atom], e1 = a.row[atom + 1];
+    const int e0 = a.row[atom], e1 = a.row_end[atom];
     const double* Sw = a.sw + 9 * a.frame_of[atom];
     const Real S00 = Real(Sw[0]), S01 = Real(Sw[1]), S02 = Real(Sw[2]), S10 = Real(Sw[3]), S11 = Real(Sw[4]),
                S12 = Real(Sw[5]), S20 = Real(Sw[6]), S21 = Real(Sw[7]), S22 = Real(Sw[8]);

@@ -114,11 +114,12 @@ __global__ void k_loss(int nframes, const int* fbegin, const double* E, const do
 // Effect gate-x L2 term of one frame (block per frame; MLMTPR::AddTwoLayerGateX2Penalty,
 // dev_src/mtpr_sh.cpp:5869-6047):  P_f = sum over edges (i -> j) of norm(t_j) sum_mu (alpha(t_j, mu)
 // h_j[mu])^2 with norm(t) = coeff / (active types x F x edges whose neighbour type is t).  Edges
-// are symmetric, so the edges with neighbour j number deg(j) = row[j + 1] - row[j].  Adds P_f to
+// are symmetric, so the edges with neighbour j number deg(j) = row_end[j] - row[j].  Adds P_f to
 // loss_f[f]; writes dP/dh_j to extra_h[j] (the gate-chain seed) and the frame's dP/dalpha to
 // agrad[f][t F + mu]; fixed-order sums throughout.
 template <typename Real>
-__global__ void k_gatex_frame(int nframes, const int* fbegin, const int* row, const int* types, const Real* h,
+__global__ void k_gatex_frame(int nframes, const int* fbegin, const int* row, const int* row_end, const int* types,
+                              const Real* h,
                               const Real* alpha, int C, int F, double coeff, double* extra_h, double* loss_f,
                               double* agrad) {
   const int f = blockIdx.x;
@@ -129,12 +130,12 @@ __global__ void k_gatex_frame(int nframes, const int* fbegin, const int* row, co
   for (int t = threadIdx.x; t < C; t += blockDim.x) count[t] = 0;
   __syncthreads();
   for (int j = a0 + threadIdx.x; j < a1; j += blockDim.x)
-    atomicAdd(&count[types[j]], static_cast<unsigned long long>(row[j + 1] - row[j]));
+    atomicAdd(&count[types[j]], static_cast<unsigned long long>(row_end[j] - row[j]));
   __syncthreads();
   int active = 0;
   for (int t = 0; t < C; ++t) active += count[t] > 0;
   auto weight = [&](int j) {  // deg(j) norm(t_j)
-    const int t = types[j], deg = row[j + 1] - row[j];
+    const int t = types[j], deg = row_end[j] - row[j];
     return deg > 0 ? coeff * deg / (double(active) * F * double(count[t])) : 0.0;
   };
   double pen = 0.0;
@@ -484,13 +485,15 @@ class Trainer {
     const Model& m = eng_.model();
     if (gatex_) {
       if (eng_.precision() == kFP32)
-        k_gatex_frame<float><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), types_.as<int>(),
+        k_gatex_frame<float><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), eng_.d_row_end(),
+                                                      types_.as<int>(),
                                                       static_cast<const float*>(eng_.d_gate_signal()),
                                                       static_cast<const float*>(eng_.d_gate_additive()), m.C, m.F,
                                                       cfg_.gate_x_l2, extra_h_.as<double>(), lossf_.as<double>(),
                                                       agrad_.as<double>());
       else
-        k_gatex_frame<double><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), types_.as<int>(),
+        k_gatex_frame<double><<<nframes_, 256, 0, s>>>(nframes_, fbegin_.as<int>(), eng_.d_row(), eng_.d_row_end(),
+                                                       types_.as<int>(),
                                                        static_cast<const double*>(eng_.d_gate_signal()),
                                                        static_cast<const double*>(eng_.d_gate_additive()), m.C, m.F,
                                                        cfg_.gate_x_l2, extra_h_.as<double>(), lossf_.as<double>(),
