@@ -196,29 +196,43 @@ int sus2g_calc_efs_host(sus2g_engine e, int nframes, const int* natoms, const do
       need(types[i] >= 0 && types[i] < eng.model().C, "atom species index out of range");
     cudaStream_t s = eng.stream();
     cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
-    Slot pos(eng, 0, sizeof(double) * 3 * n), typ(eng, 1, sizeof(int) * n);
-    Slot out_e(eng, 2, sizeof(double) * nframes), out_f(eng, 3, sizeof(double) * 3 * n),
-        out_v(eng, 4, sizeof(double) * 6 * nframes), out_s(eng, 5, sizeof(double) * n);
+    // one pinned staging area and one transfer each way: inputs [positions 3n][types n], outputs
+    // [energy nf][forces 3n][virial 6 nf][site n] (doubles; types as int after the positions)
+    const size_t in_bytes = sizeof(double) * 3 * n + sizeof(int) * n;
+    const size_t out_doubles = static_cast<size_t>(nframes) * 7 + 4 * static_cast<size_t>(n);
+    char* stage = static_cast<char*>(eng.pinned(std::max(in_bytes, sizeof(double) * out_doubles)));
+    Slot in(eng, 0, in_bytes), out(eng, 2, sizeof(double) * out_doubles);
+    double* d_pos = in.as<double>();
+    int* d_typ = reinterpret_cast<int*>(in.as<char>() + sizeof(double) * 3 * n);
+    double* d_e = out.as<double>();
+    double* d_f = d_e + nframes;
+    double* d_v = d_f + 3 * n;
+    double* d_s = d_v + 6 * static_cast<size_t>(nframes);
     if (n) {
-      cuda(cudaMemcpyAsync(pos.p, positions, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s), "positions copy");
-      cuda(cudaMemcpyAsync(typ.p, types, sizeof(int) * n, cudaMemcpyHostToDevice, s), "types copy");
+      std::memcpy(stage, positions, sizeof(double) * 3 * n);
+      std::memcpy(stage + sizeof(double) * 3 * n, types, sizeof(int) * n);
+      cuda(cudaMemcpyAsync(in.p, stage, in_bytes, cudaMemcpyHostToDevice, s), "input copy");
     }
     for (int attempt = 0;; ++attempt) {
+      eng.step_frames(nframes, natoms, cells, d_pos, d_typ, energy ? d_e : nullptr, forces ? d_f : nullptr,
+                      virial ? d_v : nullptr, site_energy ? d_s : nullptr);
+      // the outputs and the error words come back together; one synchronisation
+      if (out_doubles)
+        cuda(cudaMemcpyAsync(stage, out.p, sizeof(double) * out_doubles, cudaMemcpyDeviceToHost, s), "output copy");
+      eng.enqueue_error_read();
+      cuda(cudaStreamSynchronize(s), "stream synchronize");
       try {
-        eng.step_frames(nframes, natoms, cells, pos.as<double>(), typ.as<int>(), energy ? out_e.as<double>() : nullptr,
-                        forces ? out_f.as<double>() : nullptr, virial ? out_v.as<double>() : nullptr,
-                        site_energy ? out_s.as<double>() : nullptr);
-        eng.check_device_error();
+        eng.check_error_read();
         break;
       } catch (const sus2g::EdgeOverflow&) {
         if (attempt >= 4) throw;  // the capacity has been grown: repeat the step
       }
     }
-    if (energy && nframes) cuda(cudaMemcpyAsync(energy, out_e.p, sizeof(double) * nframes, cudaMemcpyDeviceToHost, s), "energy copy");
-    if (forces && n) cuda(cudaMemcpyAsync(forces, out_f.p, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s), "force copy");
-    if (virial && nframes) cuda(cudaMemcpyAsync(virial, out_v.p, sizeof(double) * 6 * nframes, cudaMemcpyDeviceToHost, s), "virial copy");
-    if (site_energy && n) cuda(cudaMemcpyAsync(site_energy, out_s.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s), "site copy");
-    cuda(cudaStreamSynchronize(s), "stream synchronize");
+    const double* h = reinterpret_cast<const double*>(stage);
+    if (energy && nframes) std::memcpy(energy, h, sizeof(double) * nframes);
+    if (forces && n) std::memcpy(forces, h + nframes, sizeof(double) * 3 * n);
+    if (virial && nframes) std::memcpy(virial, h + nframes + 3 * n, sizeof(double) * 6 * nframes);
+    if (site_energy && n) std::memcpy(site_energy, h + 7 * static_cast<size_t>(nframes) + 3 * n, sizeof(double) * n);
   });
 }
 

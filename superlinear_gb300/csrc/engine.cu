@@ -716,6 +716,9 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   SUS2G_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
   SUS2G_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
   stream_ = own_stream_;
+  SUS2G_CUDA(cudaStreamCreateWithFlags(&aux_stream_, cudaStreamNonBlocking));
+  for (cudaEvent_t* e : {&ev_fork_, &ev_rev_, &ev_fork2_, &ev_join2_})
+    SUS2G_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   SUS2G_CUDA(upload_pass_constants<float>());
   SUS2G_CUDA(upload_pass_constants<double>());
   SUS2G_CUDA(upload_grad_constants<float>());
@@ -737,10 +740,24 @@ Engine::~Engine() {
   reset_step_graph();
   delete plans_;
   if (host_total_) cudaFreeHost(host_total_);
+  if (pinned_) cudaFreeHost(pinned_);
   for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
   if (precision_ == kFP32) delete static_cast<DevModel<float>*>(dev_model_);
   else delete static_cast<DevModel<double>*>(dev_model_);
+  for (cudaEvent_t e : {ev_fork_, ev_rev_, ev_fork2_, ev_join2_})
+    if (e) cudaEventDestroy(e);
+  if (aux_stream_) cudaStreamDestroy(aux_stream_);
   if (own_stream_) cudaStreamDestroy(own_stream_);
+}
+
+// Work on the second stream forks from the engine stream after an event and joins it back
+// before the first consumer; the stage timer keeps everything on one stream.
+bool Engine::may_fork() const { return !timing_; }
+
+void Engine::wait_reverse() {
+  if (!rev_pending_) return;
+  SUS2G_CUDA(cudaStreamWaitEvent(stream_, ev_rev_, 0));
+  rev_pending_ = false;
 }
 
 template <typename Real>
@@ -860,6 +877,7 @@ void Engine::upload_model() {
 }
 
 long long Engine::nedges() {
+  wait_reverse();
   if (!nedges_exact_) {
     // padded layout: the sum of the per-centre counts
     std::vector<int> counts(static_cast<size_t>(std::max(0, ncentres_)));
@@ -873,9 +891,29 @@ long long Engine::nedges() {
   return exact_edges_;
 }
 
+void* Engine::pinned(size_t bytes) {
+  if (bytes > pinned_bytes_) {
+    if (pinned_) cudaFreeHost(pinned_);
+    pinned_ = nullptr;
+    pinned_bytes_ = 0;
+    SUS2G_CUDA(cudaMallocHost(&pinned_, bytes));
+    pinned_bytes_ = bytes;
+  }
+  return pinned_;
+}
+
 void Engine::check_device_error() {
-  SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 4, error_.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  enqueue_error_read();
   SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  check_error_read();
+}
+
+void Engine::enqueue_error_read() {
+  wait_reverse();
+  SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 4, error_.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, stream_));
+}
+
+void Engine::check_error_read() {
   const int h = host_total_[4], over = host_total_[5], bin_over = host_total_[6];
   if (over > 0 || bin_over > 0) {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 3 * sizeof(int), stream_));
@@ -1201,9 +1239,23 @@ void Engine::finalize_edges() {
       launches_ += 2;
     }
   } else if (nedges_ && a) {
-    k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, s>>>(
+    // reverse edges on the second stream: the Static pass and the Effect gate-forward pass do not
+    // read them, so they overlap; wait_reverse() joins before the first reader
+    // (FP32 engines only: the FP64 pass is long enough that the overlap gains nothing, and its
+    // persistent grid loses SMs to the reverse kernel while that runs)
+    cudaStream_t rs = s;
+    if (may_fork() && precision_ == kFP32) {
+      SUS2G_CUDA(cudaEventRecord(ev_fork_, s));
+      SUS2G_CUDA(cudaStreamWaitEvent(aux_stream_, ev_fork_, 0));
+      rs = aux_stream_;
+    }
+    k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, rs>>>(
         row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
     ++launches_;
+    if (rs != s) {
+      SUS2G_CUDA(cudaEventRecord(ev_rev_, rs));
+      rev_pending_ = true;
+    }
   }
 }
 
@@ -1296,11 +1348,17 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   }
   // stage 1: gate forward (Effect) -- gate signals of the centre atoms
   if (stages & kStageGate) {
-    SUS2G_CUDA(cudaMemsetAsync(site_.ptr, 0, sizeof(double) * std::max(1, N), s));
-    SUS2G_CUDA(cudaMemsetAsync(vir_atom_.ptr, 0, sizeof(double) * 6 * std::max(1, N), s));
+    // every centre's site energy, virial and gate signal is written by the passes; only caller
+    // layouts with ghosts have rows that must start at zero
+    const bool ghosts = user_edges_ && N > ncentres_;
+    if (ghosts) {
+      SUS2G_CUDA(cudaMemsetAsync(site_.ptr, 0, sizeof(double) * std::max(1, N), s));
+      SUS2G_CUDA(cudaMemsetAsync(vir_atom_.ptr, 0, sizeof(double) * 6 * std::max(1, N), s));
+    }
     if (m.gated) {
       // ghost rows (caller edges) are filled by the caller's forward exchange
-      SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
+      if (ghosts)
+        SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
       mark_begin(2);
       launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
       mark_end();
@@ -1308,6 +1366,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   }
   // stage 2: Static pass, or Effect outer pass and the gate-signal adjoint per atom
   if (stages & kStageOuter) {
+    if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
     launches_ += launch_atom_pass<Real>(m.L, m.gated ? kModeOuter : kModeStatic, a, sm_count_, s);
     mark_end();
@@ -1329,7 +1388,31 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
       mark_end();
     }
+    wait_reverse();
     mark_begin(4);
+    // frame-reduction buffers first: the arrival counters must be zero before the reduction
+    // starts on either stream
+    int S = 1;
+    if (nframes_) {
+      int largest = 0;
+      for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
+      S = std::max(1, std::min(64, (largest + kFrameThreads - 1) / kFrameThreads));
+      frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
+      if (nframes_ > arrivals_frames_) {
+        // arrival counters start at zero; each launch leaves them at zero
+        frame_arrivals_.ensure(sizeof(unsigned) * nframes_);
+        SUS2G_CUDA(cudaMemsetAsync(frame_arrivals_.ptr, 0, sizeof(unsigned) * nframes_, s));
+        arrivals_frames_ = nframes_;
+      }
+    }
+    // the per-frame reduction (site energies and virials) runs on the second stream beside the
+    // force gather
+    cudaStream_t fs = s;
+    if (may_fork() && nframes_ && d_forces && N) {
+      SUS2G_CUDA(cudaEventRecord(ev_fork2_, s));
+      SUS2G_CUDA(cudaStreamWaitEvent(aux_stream_, ev_fork2_, 0));
+      fs = aux_stream_;
+    }
     if (d_forces && N) {
       if (user_edges_)
         k_force_gather_user<Real><<<static_cast<unsigned>((static_cast<long long>(N) * kWarp + 255) / 256), 256, 0, s>>>(
@@ -1340,22 +1423,16 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       ++launches_;
     }
     if (nframes_) {
-      int largest = 0;
-      for (const FramePlan& fp : *plans_) largest = std::max(largest, fp.a1 - fp.a0);
-      const int S = std::max(1, std::min(64, (largest + kFrameThreads - 1) / kFrameThreads));
-      frame_partial_.ensure(sizeof(double) * 7 * static_cast<size_t>(nframes_) * S);
-      if (nframes_ > arrivals_frames_) {
-        // arrival counters start at zero; each launch leaves them at zero
-        frame_arrivals_.ensure(sizeof(unsigned) * nframes_);
-        SUS2G_CUDA(cudaMemsetAsync(frame_arrivals_.ptr, 0, sizeof(unsigned) * nframes_, s));
-        arrivals_frames_ = nframes_;
-      }
-      k_frame_reduce<<<dim3(nframes_, S), kFrameThreads, 0, s>>>(
+      k_frame_reduce<<<dim3(nframes_, S), kFrameThreads, 0, fs>>>(
           plan_.as<FramePlan>(), nframes_, S, site_.as<double>(), vir_atom_.as<double>(), d_site,
           frame_partial_.as<double>(), frame_arrivals_.as<unsigned>(), d_energy, d_virial);
       ++launches_;
     } else if (d_site && N) {
       SUS2G_CUDA(cudaMemcpyAsync(d_site, site_.ptr, sizeof(double) * ncentres_, cudaMemcpyDeviceToDevice, s));
+    }
+    if (fs != s) {
+      SUS2G_CUDA(cudaEventRecord(ev_join2_, fs));
+      SUS2G_CUDA(cudaStreamWaitEvent(s, ev_join2_, 0));
     }
     mark_end();
   }
@@ -1521,6 +1598,7 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
 void Engine::combination_grad(const double* d_ew, const double* d_fw, const double* d_sw, double* d_grad,
                               const double* d_extra_h) {
   SUS2G_CUDA(cudaSetDevice(device_));
+  wait_reverse();
   if (precision_ == kFP32) run_grad<float>(d_ew, d_fw, d_sw, d_grad, d_extra_h);
   else run_grad<double>(d_ew, d_fw, d_sw, d_grad, d_extra_h);
 }

@@ -130,6 +130,12 @@ class Engine {
   // Grow-only device staging buffer `slot` (0..7) of at least `bytes`, owned by the engine, for
   // entry points that copy host arrays in and out.
   void* io(int slot, size_t bytes) { io_[slot].ensure(bytes ? bytes : 1); return io_[slot].ptr; }
+  // Pinned host staging of the host-buffer entry points (grows; freed with the engine).
+  void* pinned(size_t bytes);
+  // check_device_error in two halves: queue the copy of the error words, then (after the caller's
+  // own synchronisation of the engine stream) evaluate them.
+  void enqueue_error_read();
+  void check_error_read();
 
   // Static FP32 pass on caller / external buffers (used by the allocation-free entry point):
   // natoms centres, CSR edges (row, nbr) with edge records d4 (EdgeF), outputs g[3E], site[natoms],
@@ -213,6 +219,15 @@ class Engine {
   int arrivals_frames_ = 0;     // frame_arrivals_ entries known to be zero
   DevBuf scratch_;
   DevBuf io_[8];
+  // second stream for independent work inside a step (reverse edges beside the first pass, the
+  // frame reduction beside the force gather)
+  cudaStream_t aux_stream_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_rev_ = nullptr, ev_fork2_ = nullptr, ev_join2_ = nullptr;
+  bool rev_pending_ = false;
+  bool may_fork() const;
+  void wait_reverse();
+  void* pinned_ = nullptr;
+  size_t pinned_bytes_ = 0;
 };
 
 }  // namespace sus2g

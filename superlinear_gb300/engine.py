@@ -129,6 +129,11 @@ class Engine:
     # -- periodic frames ------------------------------------------------------------------------
     @staticmethod
     def pack_frames(frames):
+        if len(frames) == 1:
+            # one frame: its arrays as they are when they already have the layout of the C ABI
+            f = frames[0]
+            return (np.array([f.natoms], dtype=np.int32), np.ascontiguousarray(f.cell, dtype=np.float64).reshape(1, 3, 3),
+                    np.ascontiguousarray(f.positions, dtype=np.float64), np.ascontiguousarray(f.types, dtype=np.int32))
         natoms = np.array([f.natoms for f in frames], dtype=np.int32)
         cells = np.ascontiguousarray(np.stack([f.cell for f in frames]) if frames else np.zeros((0, 3, 3)),
                                      dtype=np.float64)
@@ -142,10 +147,10 @@ class Engine:
         """Host arrays in and out: returns (energy[nf], forces[N,3], virial[nf,6], site[N])."""
         natoms, cells, pos, types = self.pack_frames(frames)
         nf, n = natoms.size, int(natoms.sum())
-        e = np.zeros(nf)
-        f = np.zeros((n, 3))
-        v = np.zeros((nf, 6))
-        s = np.zeros(n)
+        e = np.empty(nf)
+        f = np.empty((n, 3))
+        v = np.empty((nf, 6))
+        s = np.empty(n)
         check(load().sus2g_calc_efs_host(self._h, nf, _i(natoms), _d(cells), _d(pos), _i(types), _d(e), _d(f),
                                          _d(v), _d(s)))
         return e, f, v, s
