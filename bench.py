@@ -415,17 +415,17 @@ def run_ours(args):
         torch.cuda.synchronize()
         if sampler:
             sampler.start()
-        total = 0.0
-        for _ in range(steps):
+        # every timed step between its own event pair, queued back to back behind its L2 flush (not
+        # timed) so that host submission does not leave the device idle inside a step; one
+        # synchronisation at the end
+        marks = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for a, b in marks:
             flush.fill_(1.0)  # L2 flush between timed steps (not timed)
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
             a.record(stream)
             step(eng)
             b.record(stream)
-            b.synchronize()
-            total += a.elapsed_time(b)
         torch.cuda.synchronize()
+        total = sum(a.elapsed_time(b) for a, b in marks)
         clocks = sampler.stop() if sampler else None
         launches = eng.take_launch_count()
         return total / steps, stage_times(eng, steps), launches, clocks

@@ -166,36 +166,82 @@ __global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const d
 // count above cap is clamped to cap and raises *overflow to the full count, which the host reads
 // with the step's error check (it then grows the capacity and repeats the step).
 constexpr int kFillWarps = 8;
+constexpr int kFillSortStage = 256;  // keys per warp kept in shared memory for the in-kernel sort
+constexpr int kFillSortPer = 4;
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp, 4)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
                  const int* bin_count, int bin_cap, const BinAtom* bin_rec, const BinPos* bin_pos,
                  const BinPosF* bin_posf, const int* bin_of, const int* rec_of, const AtomFrac* frac, const AtomOff* off,
                  int* counts, int* nbr,
-                 typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error) {
+                 typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error, int* row,
+                 int* row_end, unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
   __shared__ BinWalk walk[kFillWarps];
+  __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
   if (!fp.use_bins) return;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, w = threadIdx.x / kWarp;
   const unsigned below = (1u << lane) - 1u;
   const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
   const int cap = fp.cap;
   int cursor = 0;
   warp_bin_edges<Real>(i, fp, pos, rc2, bin_count, bin_cap, bin_rec, bin_pos, bin_posf, bin_of, rec_of, frac, off, error,
-                       queue[threadIdx.x / kWarp], walk[threadIdx.x / kWarp],
+                       queue[w], walk[w],
                        [&](unsigned mask, bool ok, int j, int a, int b, int c, Real x, Real y, Real z, Real r) {
                          if (ok) {
                            const int k = cursor + __popc(mask & below);
-                           if (k < cap) write_edge_rec<Real>(pad + k, j, a, b, c, x, y, z, r, nbr, d4, key);
+                           if (k < cap) {
+                             write_edge_rec<Real>(pad + k, j, a, b, c, x, y, z, r, nbr, d4, key);
+                             if (k < kFillSortStage) skeys[w][k] = edge_key(j, a, b, c);
+                           }
                          }
                          cursor += __popc(mask);
                        });
+  const int n = min(cursor, cap);
   if (lane == 0) {
-    counts[i] = min(cursor, cap);
+    counts[i] = n;
     if (cursor > cap) atomicMax(overflow, cursor);
+  }
+  if (!row_end) return;
+  // cell lists only: sort the centre's edges by key into the final arrays at the same slots (rank
+  // of each key among the centre's keys; keys are unique within a centre)
+  __syncwarp();
+  const unsigned long long* src = n <= kFillSortStage ? skeys[w] : key + pad;
+  for (int q0 = 0; q0 < n; q0 += kFillSortPer * kWarp) {
+    unsigned long long kk[kFillSortPer];
+    int nb[kFillSortPer], rank[kFillSortPer];
+    typename Vec4<Real>::type dd[kFillSortPer];
+#pragma unroll
+    for (int u = 0; u < kFillSortPer; ++u) {
+      const int q = q0 + u * kWarp + lane;
+      kk[u] = ~0ull;
+      rank[u] = 0;
+      if (q < n) {
+        kk[u] = src[q];
+        nb[u] = nbr[pad + q];
+        dd[u] = d4[pad + q];
+      }
+    }
+    for (int t = 0; t < n; ++t) {
+      const unsigned long long kt = src[t];
+#pragma unroll
+      for (int u = 0; u < kFillSortPer; ++u) rank[u] += kt < kk[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kFillSortPer; ++u) {
+      if (q0 + u * kWarp + lane < n) {
+        key_out[pad + rank[u]] = kk[u];
+        nbr_out[pad + rank[u]] = nb[u];
+        d4_out[pad + rank[u]] = dd[u];
+      }
+    }
+  }
+  if (lane == 0) {
+    row[i] = static_cast<int>(pad);
+    row_end[i] = static_cast<int>(pad) + n;
   }
 }
 
@@ -1099,20 +1145,34 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   const AtomOff* OF = off_.as<AtomOff>();
   int* overflow = error_.as<int>() + 1;
   // cell-list frames: one pass into padded staging slots (repeated with a larger capacity on overflow)
+  // cell-list batches sort each centre's edges inside the fill kernel, into the final arrays
+  const bool fused = bins && bins_frames_ == nframes;
   auto fill_bins = [&]() {
     const size_t slots = static_cast<size_t>(std::max<long long>(1, pad_total));
     pad_nbr_.ensure(sizeof(int) * slots);
     pad_d4_.ensure(rsz * slots);
     pad_key_.ensure(sizeof(unsigned long long) * slots);
+    if (fused) {
+      nbr_.ensure(sizeof(int) * slots);
+      d4_.ensure(rsz * slots);
+      key_.ensure(sizeof(unsigned long long) * slots);
+      row_end_.ensure(sizeof(int) * std::max(1, a));
+    }
+    int* RW = fused ? row_.as<int>() : nullptr;
+    int* RE = fused ? row_end_.as<int>() : nullptr;
+    unsigned long long* KO = fused ? key_.as<unsigned long long>() : nullptr;
+    int* NO = fused ? nbr_.as<int>() : nullptr;
     SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF, counts_.as<int>(),
-                                                                         pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
-                                                                         pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
+      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+          P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
+          counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), overflow,
+          error_.as<int>(), RW, RE, KO, NO, fused ? d4_.as<EdgeF>() : nullptr);
     else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF, counts_.as<int>(),
-                                                                          pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
-                                                                          pad_key_.as<unsigned long long>(), overflow, error_.as<int>());
+      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+          P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
+          counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), overflow,
+          error_.as<int>(), RW, RE, KO, NO, fused ? d4_.as<EdgeD>() : nullptr);
     ++launches_;
   };
   if (a) {
@@ -1132,7 +1192,6 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     total = pad_total;
     nedges_exact_ = false;
     padded_ = true;
-    row_end_.ensure(sizeof(int) * std::max(1, a));
   } else {
     for (int attempt = 0;; ++attempt) {
       k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
@@ -1172,10 +1231,16 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   nedges_ = total;
   if (nedges_exact_) exact_edges_ = total;
   const size_t E = std::max<long long>(1, total);
-  nbr_.ensure(sizeof(int) * E); tmp_nbr_.ensure(sizeof(int) * E);
+  nbr_.ensure(sizeof(int) * E);
   rev_.ensure(sizeof(int) * E);
-  d4_.ensure(rsz * E); tmp_d4_.ensure(rsz * E);
-  key_.ensure(sizeof(unsigned long long) * E); tmp_key_.ensure(sizeof(unsigned long long) * E);
+  d4_.ensure(rsz * E);
+  key_.ensure(sizeof(unsigned long long) * E);
+  if (!fused) {
+    // CSR staging of the image-scan frames (and the merge of mixed batches)
+    tmp_nbr_.ensure(sizeof(int) * E);
+    tmp_d4_.ensure(rsz * E);
+    tmp_key_.ensure(sizeof(unsigned long long) * E);
+  }
   if (a && bins_frames_ < nframes) {
     unsigned long long* KY = tmp_key_.as<unsigned long long>();
     if (precision_ == kFP32)
@@ -1194,7 +1259,8 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
 void Engine::finalize_edges() {
   cudaStream_t s = stream_;
   const int a = ncentres_;
-  if (a) {
+  // (cell-list batches were sorted by the fill kernel)
+  if (a && !padded_) {
     const int blocks = (a + kSortWarps - 1) / kSortWarps;
     const FramePlan* P = sort_from_pad_ ? plan_.as<FramePlan>() : nullptr;
     // shared-memory key staging up to the largest padded capacity (at most 512 keys per warp)
