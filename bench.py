@@ -234,7 +234,7 @@ def bench_training(sg, torch, steps, warmup):
     out = {"workload": "effect_l3k4r2o2_train256", "frames": len(frames), "atoms": int(sum(f.natoms for f in frames)),
            "weights": {"energy": TRAIN_WEIGHTS[0], "force": TRAIN_WEIGHTS[1], "stress": TRAIN_WEIGHTS[2]}}
     losses = {}
-    for prec, key, nsteps in ((sg.FP32, "fp32", steps), (sg.FP64, "fp64", max(3, steps // 4))):
+    for prec, key, nsteps in ((sg.FP32, "fp32", steps), (sg.FP64, "fp64", max(5, steps // 2))):
         eng = sg.Engine(model, 0, prec)
         tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
         for _ in range(warmup):
