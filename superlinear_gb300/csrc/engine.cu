@@ -330,10 +330,14 @@ k_edge_sort(int* row, int* row_end, const int* counts, int natoms, const FramePl
 // Reverse edge of every edge (warp per centre i): for e = (i -> j, n) the edge (j -> i, -n) is
 // found by binary search in j's sorted keys.
 // Up to kRevPer searches per lane run interleaved, so their dependent loads overlap.
+// It also clears the first nzero bin counters (their last reader, the fill kernel, is done), so
+// that the next step's binning starts from zero without a memset.
 __global__ void k_reverse(const int* row, const int* row_end, const unsigned long long* key, int natoms, int* rev,
-                          int* error) {
+                          int* error, int* zero, int nzero) {
   constexpr int kRevPer = 4;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const long long tid = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (long long q = tid; q < nzero; q += static_cast<long long>(gridDim.x) * blockDim.x) zero[q] = 0;
+  const int i = static_cast<int>(tid / kWarp);
   const int lane = threadIdx.x & 31;
   if (i >= natoms) return;
   const int end = row_end[i];
@@ -1106,7 +1110,13 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   frame_of_.ensure(sizeof(int) * std::max(1, a));
   counts_.ensure(sizeof(int) * (a + 1));
   row_.ensure(sizeof(int) * (a + 1));
-  bin_count_.ensure(sizeof(int) * (bins + 1));
+  {
+    // bin counters: zero at the start of a binning pass; the reverse-edge kernel of the previous
+    // step cleared the ones it used, so only new or reallocated entries need a memset
+    const void* before = bin_count_.ptr;
+    bin_count_.ensure(sizeof(int) * (bins + 1));
+    if (bin_count_.ptr != before) bin_zeroed_ = 0;
+  }
   bin_start_.ensure(sizeof(int) * (bins + 1));
   DevBuf& bin_of = bin_of_;
   bin_of.ensure(sizeof(int) * std::max(1, a));
@@ -1117,7 +1127,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     ++launches_;
   }
   if (bins) {
-    SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
+    if (bin_zeroed_ < bins + 1) SUS2G_CUDA(cudaMemsetAsync(bin_count_.ptr, 0, sizeof(int) * (bins + 1), s));
+    bin_zeroed_ = 0;          // counted into from here on
+    bins_used_ = bins + 1;    // cleared again by this step's reverse-edge kernel
     frac_.ensure(sizeof(AtomFrac) * a);
     off_.ensure(sizeof(AtomOff) * a);
     rec_of_.ensure(sizeof(int) * a);
@@ -1162,7 +1174,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     int* RE = fused ? row_end_.as<int>() : nullptr;
     unsigned long long* KO = fused ? key_.as<unsigned long long>() : nullptr;
     int* NO = fused ? nbr_.as<int>() : nullptr;
-    SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
+    // the overflow word is zero between steps (the step's error check clears it after an
+    // overflow); the host-synchronised retry below re-arms it itself
+    if (!fused) SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
     if (precision_ == kFP32)
       k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
           P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
@@ -1176,7 +1190,8 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     ++launches_;
   };
   if (a) {
-    SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
+    // (every centre's count is written by the fill kernels; the CSR scan also reads entry a)
+    if (!fused) SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
     if (bins) fill_bins();
     if (bins_frames_ < nframes) {
       k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, counts_.as<int>(), error_.as<int>());
@@ -1316,8 +1331,10 @@ void Engine::finalize_edges() {
       rs = aux_stream_;
     }
     k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, rs>>>(
-        row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>());
+        row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>(),
+        bin_count_.as<int>(), sort_from_pad_ ? bins_used_ : 0);
     ++launches_;
+    if (sort_from_pad_) bin_zeroed_ = bins_used_;
     if (rs != s) {
       SUS2G_CUDA(cudaEventRecord(ev_rev_, rs));
       rev_pending_ = true;

@@ -192,6 +192,8 @@ class Engine {
   DevBuf plan_, frame_of_, frame_begin_, types_copy_;
   DevBuf counts_, row_, row_end_, nbr_, rev_, d4_, key_, tmp_key_, tmp_d4_, tmp_nbr_;
   bool padded_ = false;         // cell-list batch: edges left in padded per-centre slots (row_end_)
+  int bin_zeroed_ = 0;          // leading bin counters known to be zero on the device
+  int bins_used_ = 0;           // bin counters used by the current cell-list build
   DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
