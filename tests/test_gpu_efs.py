@@ -142,6 +142,29 @@ def test_cell_list_capacity_overflow_is_retried(lib, oracle_lib, golden):
     assert rel_err(V.cpu().numpy()[0], vo) < FP64_TOL
 
 
+def test_bin_capacity_overflow_is_retried(lib, oracle_lib, golden):
+    """A compact 729-atom cluster (1.0 A spacing) in a 30 A box: up to 27 atoms fall in a
+    half-width bin of the cluster against a bin capacity sized from the box's mean density (9),
+    and the padded edge capacity overflows too; both capacities grow and the step is repeated,
+    in FP64 and FP32, with the oracle's edge set."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    rng = np.random.default_rng(11)
+    grid = np.stack(np.meshgrid(*[np.arange(9)] * 3, indexing="ij"), -1).reshape(-1, 3) * 1.0
+    pos = grid + 4.0 + rng.normal(0, 0.02, grid.shape)
+    fr = Frame(np.eye(3) * 30.0, pos, np.zeros(len(pos), dtype=np.int32))
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+    e, f, v, s = g64.calc_efs([fr])
+    assert g64.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
+    # FP32: the exact edge set; values to FP32 accuracy (this unphysically dense cluster has ~500
+    # neighbours per atom, outside the conditions of the 1e-5 eV/A bar)
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    assert g32.edge_count() == ne
+    assert np.max(np.abs(f32 - fo)) <= 1e-4 * np.max(np.abs(fo)) and abs(e32[0] - eo) <= 1e-5 * abs(eo)
+
+
 def test_triclinic_cell(lib, oracle_lib, golden):
     path = os.path.join(golden, "models", "static_l2k3o2_c2.sus2")
     m, g64, _ = engines(lib, path)
