@@ -48,6 +48,11 @@ int sus2g_model_cutoff(sus2g_model model, double* cutoff);
 int sus2g_model_param_count(sus2g_model model, int* count);
 int sus2g_model_get_params(sus2g_model model, double* out, int n);
 int sus2g_model_set_params(sus2g_model model, const double* in, int n);
+/* The model's global radial scaling (the .sus2 `scaling` field, MLMTPR::scaling; not part of the
+ * parameter vector).  set: positive and finite; an engine picks it up through
+ * sus2g_engine_update_params, and sus2g_model_save writes it. */
+int sus2g_model_get_scaling(sus2g_model model, double* scaling);
+int sus2g_model_set_scaling(sus2g_model model, double scaling);
 /* Write the model with its current parameter vector as a .sus2 file the reference loads
  * (replaces MLMTPR::Save, dev_src/mtpr.cpp:6893): the loaded fields in file order, the trainable
  * blocks replaced by the current values in %.17e (bit-exact on reload). */
@@ -189,6 +194,15 @@ int sus2g_trainer_metrics(sus2g_trainer trainer, const double* params, double* o
  * centre factor 1, shift = constant - 1, readout = solution.  params (host) in/out; the engine's
  * parameters become the result. */
 int sus2g_trainer_train_linear(sus2g_trainer trainer, double* params);
+/* Rescale step before the linear solve, replacing Rescale (dev_src/mlp/mtpr_train.cpp:1504-1748,
+ * run by MTPR_trainer when do-lin rescaling is on, dev_src/mtpr_trainer.cpp:4040-4046): a search over
+ * the model's global radial `scaling` in which every trial runs the linear warm-up above on at most
+ * five of the frames (largest, second largest, median, second smallest, smallest by atom count)
+ * and is judged by the median and spread of log|readout coefficient|.  params (host, in/out, the
+ * trainer's Coeff() order) becomes the chosen trial's coefficients, *scaling its scaling; the
+ * trainer's engine keeps both (sus2g_model_set_scaling puts the scaling into a model to save).
+ * *solves (may be NULL) = linear solves run. */
+int sus2g_trainer_rescale(sus2g_trainer trainer, double* params, double* scaling, int* solves);
 /* Replay the evaluation as one CUDA graph (enabled = 1, default) or launch it eagerly (0). */
 int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
 /* Dense BFGS from params (in/out) for at most max_iter accepted steps or until |grad| <= gtol:

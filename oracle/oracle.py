@@ -41,6 +41,9 @@ def lib():
         L.orc_param_count.argtypes = [ctypes.c_void_p]
         L.orc_get_params.argtypes = [ctypes.c_void_p, _dp]
         L.orc_set_params.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_get_scaling.restype = ctypes.c_double
+        L.orc_get_scaling.argtypes = [ctypes.c_void_p]
+        L.orc_set_scaling.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_efs.restype = ctypes.c_longlong
         L.orc_efs.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_int,
                               ctypes.c_char_p, ctypes.c_int]
@@ -92,6 +95,15 @@ class OracleModel:
         p = np.ascontiguousarray(p, dtype=np.float64)
         assert p.size == self.nparams
         lib().orc_set_params(self._h, _d(p))
+
+    @property
+    def scaling(self) -> float:
+        return lib().orc_get_scaling(self._h)
+
+    @scaling.setter
+    def scaling(self, s: float) -> None:
+        if lib().orc_set_scaling(self._h, float(s)) != 0:
+            raise ValueError("scaling must be positive and finite")
 
     def efs(self, cell, pos, types, threads: int = 1):
         """One periodic frame -> (energy, forces[n,3], virial6, site[n], n_edges)."""
@@ -349,3 +361,146 @@ def train_linear(model: "OracleModel", frames, wE: float, wF: float, wS: float, 
     p[lay["o_linear"]: lay["o_linear"] + heads * S] = x[C:]
     model.set_params(p)
     return p
+
+
+def rescale_subset(natoms):
+    """Frames the rescale step solves on, restating BuildRescaleSubsetIndices
+    (dev_src/mlp/mtpr_train.cpp:646-690): all frames when there are at most five, else the largest,
+    second largest, median, second smallest and smallest by atom count (stable order), unique."""
+    n = len(natoms)
+    if n <= 5:
+        return list(range(n))
+    order = sorted(range(n), key=lambda f: (natoms[f], f))
+    picks = []
+    for f in (order[n - 1], order[n - 2], order[n // 2], order[1], order[0]):
+        if f not in picks:
+            picks.append(f)
+    return picks
+
+
+def moment_stats(params, o_linear: int, nread: int):
+    """Median (upper) and RMS spread of log|c| over the scalar-readout coefficients |c| > 1e-12,
+    restating ComputeMomentCoeffStats (dev_src/mlp/mtpr_train.cpp:279-307); None when empty."""
+    logs = sorted(float(np.log(abs(c))) for c in params[o_linear:o_linear + nread] if abs(c) > 1e-12)
+    if not logs:
+        return None
+    center = logs[len(logs) // 2]
+    spread = float(np.sqrt(sum((v - center) ** 2 for v in logs) / len(logs)))
+    return center, spread
+
+
+def expansion_direction(seed, lower, upper):
+    """First bracket-expansion direction (SelectRescaleExpansionDirection,
+    dev_src/rescale_search.h:10-27): -1 / +1 for the probe that improves |median log| most, 0 when
+    neither does; a probe is None when invalid."""
+    best, d = abs(seed), 0
+    if lower is not None and abs(lower) < best:
+        best, d = abs(lower), -1
+    if upper is not None and abs(upper) < best:
+        d = 1
+    return d
+
+
+def rescale(model: "OracleModel", frames, wE: float, wF: float, wS: float, weighting: str = "vibrations",
+            norm_by_forces: int = 0):
+    """The rescale step around the linear warm-up, restating Rescale
+    (dev_src/mlp/mtpr_train.cpp:1504-1748): returns (params, scaling, linear solves); the model keeps
+    both.  Each trial sets the scaling and runs train_linear on the subset frames; the search
+    brackets the median log coefficient at 0, refines it by secant steps in log scaling and ends
+    with five fine trials judged by spread^2 + 3 median^2 (RescaleMetric, :309)."""
+    lay = model.layout()
+    heads = lay["C"] if lay["species_readout"] else 1
+    nread, o_lin = heads * lay["S"], lay["o_linear"]
+    sub = [frames[f] for f in rescale_subset([fr.natoms for fr in frames])]
+    solves = [0]
+
+    def evaluate(s):
+        model.scaling = s
+        p = train_linear(model, sub, wE, wF, wS, weighting, norm_by_forces)
+        solves[0] += 1
+        return {"scaling": s, "p": p, "st": moment_stats(p, o_lin, nread)}
+
+    floor, factors = 1e-12, (1.0 / 1.08, 1.0 / 1.03, 1.0, 1.03, 1.08)
+    center = evaluate(model.scaling)
+    if center["st"] is None:
+        return center["p"], center["scaling"], solves[0]
+    state = {"best": center, "pos": None, "neg": None}
+
+    def consider(e):
+        if e is None or e["st"] is None:
+            return
+        c = e["st"][0]
+        if abs(c) < abs(state["best"]["st"][0]):
+            state["best"] = e
+        if c >= 0.0:
+            if state["pos"] is None or c < state["pos"]["st"][0]:
+                state["pos"] = e
+        elif state["neg"] is None or c > state["neg"]["st"][0]:
+            state["neg"] = e
+
+    def bracketed():
+        return state["pos"] is not None and state["neg"] is not None
+
+    consider(center)
+    if abs(center["st"][0]) >= 0.15:
+        lower = upper = None
+        ls = max(floor, center["scaling"] / 2.0)
+        if ls < center["scaling"]:
+            lower = evaluate(ls)
+            consider(lower)
+        if not bracketed():
+            us = center["scaling"] * 2.0
+            if np.isfinite(us):
+                upper = evaluate(us)
+                consider(upper)
+        if not bracketed():
+            lc = lower["st"][0] if lower is not None and lower["st"] is not None else None
+            uc = upper["st"][0] if upper is not None and upper["st"] is not None else None
+            d = expansion_direction(center["st"][0], lc, uc)
+            edge = lower if d < 0 else upper
+            for _ in range(6):
+                if d == 0 or bracketed():
+                    break
+                ts = max(floor, edge["scaling"] / 2.0) if d < 0 else edge["scaling"] * 2.0
+                if not (ts > 0.0) or not np.isfinite(ts) or ts == edge["scaling"]:
+                    break
+                trial = evaluate(ts)
+                if trial["st"] is None:
+                    break
+                prev = abs(edge["st"][0])
+                consider(trial)
+                edge = trial
+                if not bracketed() and abs(trial["st"][0]) >= prev:
+                    break
+    if bracketed():
+        for _ in range(6):
+            pos, neg = state["pos"], state["neg"]
+            lp, ln = np.log(pos["scaling"]), np.log(neg["scaling"])
+            lt = 0.5 * (lp + ln)
+            cp, cn = pos["st"][0], neg["st"][0]
+            if abs(cp - cn) > 1e-12:
+                lt = (lp * cn - ln * cp) / (cn - cp)
+                lt = max(min(lt, max(lp, ln)), min(lp, ln))
+                span = abs(lp - ln)
+                if abs(lt - lp) < 0.1 * span or abs(lt - ln) < 0.1 * span:
+                    lt = 0.5 * (lp + ln)
+            trial = evaluate(max(floor, float(np.exp(lt))))
+            if trial["st"] is None:
+                break
+            consider(trial)
+            if abs(trial["st"][0]) < 0.15:
+                state["best"] = trial
+                break
+    base = state["best"]["scaling"]
+    best_metric, best_s, best_p = np.inf, base, state["best"]["p"]
+    for f in factors:
+        trial = evaluate(max(floor, base * f))
+        if trial["st"] is None:
+            continue
+        c, sp = trial["st"]
+        metric = sp * sp + 3.0 * c * c
+        if metric < best_metric:
+            best_metric, best_s, best_p = metric, trial["scaling"], trial["p"]
+    model.scaling = best_s
+    model.set_params(best_p)
+    return best_p, best_s, solves[0]

@@ -11,6 +11,11 @@
 // Usage: ref-grad --linear MODEL CFG wE wF wS [weighting]
 //   MTPR_trainer::TrainLinear on the labelled CFG; prints {"coeffs": [...]} after the solve.
 //
+// Usage: ref-grad --rescale MODEL CFG wE wF wS [weighting]
+//   Rescale (dev_src/mlp/mtpr_train.cpp:1504, the scaling search around TrainLinear) on the labelled
+//   CFG as the reference trainer's training set; prints {"scaling": s, "coeffs": [...]} (its log
+//   lines go to stderr).
+//
 // Usage: ref-grad --write MODEL OUT VALUES
 //   Loads MODEL, replaces its parameter vector by the whitespace-separated VALUES (same length
 //   and order as Coeff()), and saves it with MLMTPR::Save, so that the written .sus2 is in the
@@ -22,11 +27,15 @@
 #include "configuration.h"
 #include "non_linear_regression.h"
 #include "mtpr_trainer.h"
+#include "mlp/mtpr_train.h"
 #include <cstdio>
 #include <string>
 #include <fstream>
 #include <iostream>
 #include <vector>
+
+// the reference trainer's training set (a global of dev_src/mlp/mtpr_train.cpp, read by Rescale)
+extern std::vector<Configuration> training_set;
 
 static void vec(const double* v, int n) {
   std::printf("[");
@@ -85,6 +94,23 @@ int main(int argc, char** argv) {
     std::printf(", \"metrics\": ");
     vec(metrics, 6);
     std::printf(", \"configs\": %zu}\n", train.size());
+    return 0;
+  }
+  if (std::string(argv[1]) == "--rescale") {
+    if (argc < 7) { std::fprintf(stderr, "usage: ref-grad --rescale MODEL CFG wE wF wS [weighting]\n"); return 2; }
+    MLMTPR mtpr(argv[2]);
+    MTPR_trainer trainer(&mtpr, std::stod(argv[4]), std::stod(argv[5]), std::stod(argv[6]));
+    if (argc > 7) trainer.weighting = argv[7];
+    std::ifstream in(argv[3]);
+    Configuration c;
+    training_set.clear();
+    while (c.Load(in)) training_set.push_back(c);
+    std::streambuf* keep = std::cout.rdbuf(std::cerr.rdbuf());  // the search's log lines
+    Rescale(trainer, mtpr, nullptr);
+    std::cout.rdbuf(keep);
+    std::printf("{\"scaling\": %.17g, \"coeffs\": ", mtpr.scaling);
+    vec(mtpr.Coeff(), mtpr.CoeffCount());
+    std::printf(", \"configs\": %zu}\n", training_set.size());
     return 0;
   }
   if (std::string(argv[1]) == "--linear") {

@@ -942,6 +942,14 @@ int orc_get_params(void* mp, double* out) {
   return 0;
 }
 
+// The global radial scaling (the .sus2 `scaling` field; MLMTPR::scaling).
+double orc_get_scaling(void* mp) { return static_cast<Model*>(mp)->scaling; }
+int orc_set_scaling(void* mp, double s) {
+  if (!(s > 0) || !std::isfinite(s)) return 1;
+  static_cast<Model*>(mp)->scaling = s;
+  return 0;
+}
+
 int orc_set_params(void* mp, const double* in) {
   Model& m = *static_cast<Model*>(mp);
   for (int w = 0; w < 12; ++w) {

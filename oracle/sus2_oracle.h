@@ -16,6 +16,8 @@ void orc_free(void* model);
 int orc_param_count(void* model);
 int orc_get_params(void* model, double* out);
 int orc_set_params(void* model, const double* in);
+double orc_get_scaling(void* model);
+int orc_set_scaling(void* model, double scaling);
 /* One periodic frame: cell rows are lattice vectors.  Outputs energy, forces[3n], virial[6]
  * (xx, yy, zz, xy, xz, yz), site energies[n] (any may be NULL).  threads <= 0: all cores.
  * Returns the number of directed edges, or -1 on error (message in err). */

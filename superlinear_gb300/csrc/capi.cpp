@@ -127,6 +127,14 @@ int sus2g_engine_create(sus2g_model model, int device, int precision, sus2g_engi
 
 void sus2g_engine_free(sus2g_engine e) { delete e; }
 
+int sus2g_model_get_scaling(sus2g_model m, double* scaling) {
+  return guarded([&] { need(m && scaling, "model/scaling"); *scaling = m->model.scaling; });
+}
+
+int sus2g_model_set_scaling(sus2g_model m, double scaling) {
+  return guarded([&] { need(m, "model"); m->model.set_scaling(scaling); });
+}
+
 int sus2g_engine_update_params(sus2g_engine e, sus2g_model model) {
   return guarded([&] {
     need(e && model, "engine/model");

@@ -42,6 +42,7 @@ class Engine {
   void upload_model();
   // Replace the engine's parameter vector (trainer order) and re-upload the device tables.
   void set_params(const double* params) { model_.set_params(params); upload_model(); }
+  void set_scaling(double s) { model_.set_scaling(s); upload_model(); }
   // Incremented by every build_edges / set_edges: a caller that captured work on this engine's
   // buffers (a CUDA graph) must rebuild it when the generation it recorded has changed, since a
   // rebuild may reallocate the edge and step buffers.

@@ -414,6 +414,18 @@ std::vector<Model::Block> Model::layout() const {
   return out;
 }
 
+void Model::set_scaling(double s) {
+  if (!(s > 0) || !std::isfinite(s)) throw Error(1, "scaling must be positive and finite");
+  scaling = s;
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%.17e", s);
+  if (!fields.count("scaling")) {
+    auto it = std::find(field_order.begin(), field_order.end(), "version");
+    field_order.insert(it == field_order.end() ? field_order.begin() : it + 1, "scaling");
+  }
+  fields["scaling"] = buf;
+}
+
 void Model::save(const std::string& path) const {
   std::map<std::string, std::string> out = fields;
   std::vector<std::string> order = field_order;

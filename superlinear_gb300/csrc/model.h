@@ -91,6 +91,9 @@ struct Model {
   int param_count() const;
   void get_params(double* out) const;
   void set_params(const double* in);
+  // The global radial scaling (the `scaling` field, MLMTPR::scaling): not a trained coefficient,
+  // set by the trainer's rescale step and written back by save().
+  void set_scaling(double s);
   double gate_weight(int mu, int q) const;  // sus2_sl_kernel.cpp:314-317
 
  private:

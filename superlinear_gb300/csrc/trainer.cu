@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <string>
 #include <vector>
@@ -413,6 +414,13 @@ class Trainer {
     nparams_ = eng_.model().param_count();
     natoms_list_.assign(natoms, natoms + nframes);
     cells_.assign(cells, cells + 9 * nframes);
+    // host copies: the rescale step builds a trainer on a subset of the frames
+    pos_h_.assign(pos, pos + 3 * static_cast<size_t>(n));
+    types_h_.assign(types, types + n);
+    E0_h_.assign(E0, E0 + nframes);
+    F0_h_.assign(F0, F0 + 3 * static_cast<size_t>(n));
+    S0_h_.assign(S0, S0 + 9 * static_cast<size_t>(nframes));
+    has_h_.assign(has, has + nframes);
     pos_.ensure(sizeof(double) * 3 * std::max(1, natoms_));
     types_.ensure(sizeof(int) * std::max(1, natoms_));
     E0_.ensure(sizeof(double) * std::max(1, nframes));
@@ -730,6 +738,181 @@ class Trainer {
     eng_.set_params(params);
   }
 
+  // Rescale step before the linear solve (Rescale, dev_src/mlp/mtpr_train.cpp:1504-1748): a search
+  // over the model's global radial scaling for which the linear warm-up's scalar-readout
+  // coefficients sit at a typical magnitude of 1.  On at most five frames (largest, second largest,
+  // median, second smallest, smallest by atom count, BuildRescaleSubsetIndices :646) when the set
+  // has more than five, else on all: each trial sets the scaling and runs train_linear; the
+  // statistics are the median (upper) and RMS spread of log|c| over readout coefficients |c| > 1e-12
+  // (ComputeMomentCoeffStats :279).  Bracket the median log at 0 (halve / double the seed, expand in
+  // the improving direction, SelectRescaleExpansionDirection, dev_src/rescale_search.h), refine by
+  // secant steps in log scaling (up to 6, tolerance 0.15), then try the refined scaling times
+  // 1/1.08, 1/1.03, 1, 1.03, 1.08 and keep the trial with the least spread^2 + 3 median^2
+  // (RescaleMetric :309).  params (host, in/out) ends as that trial's coefficients; *scaling is
+  // set to its scaling and the engine keeps both.  Returns the number of linear solves.
+  int rescale(double* params, double* scaling_out) {
+    const Model& m = eng_.model();
+    const int C = m.C, heads = m.species_readout ? C : 1, nread = heads * m.S;
+    int o_linear = -1;
+    for (const auto& blk : m.layout())
+      if (blk.name == "moment_coeffs") o_linear = blk.offset;
+    struct Stats { double center = 0, spread = 0; size_t count = 0; bool valid = false; };
+    struct Eval { double scaling = 0; Stats st; std::vector<double> p; bool valid = false; };
+    auto stats_of = [&](const std::vector<double>& p) {
+      Stats st;
+      std::vector<double> logs;
+      for (int q = 0; q < nread; ++q) {
+        const double a = std::abs(p[o_linear + q]);
+        if (a > 1e-12) logs.push_back(std::log(a));
+      }
+      if (logs.empty()) return st;
+      std::sort(logs.begin(), logs.end());
+      st.count = logs.size();
+      st.center = logs[logs.size() / 2];
+      double sq = 0.0;
+      for (double v : logs) sq += (v - st.center) * (v - st.center);
+      st.spread = std::sqrt(sq / logs.size());
+      st.valid = true;
+      return st;
+    };
+    // the frames the trial solves run on
+    std::unique_ptr<Trainer> sub;
+    if (nframes_ > 5) {
+      std::vector<int> order(nframes_);
+      for (int f = 0; f < nframes_; ++f) order[f] = f;
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int a, int b) { return natoms_list_[a] < natoms_list_[b]; });
+      std::vector<int> picks;
+      auto push = [&](int f) { if (std::find(picks.begin(), picks.end(), f) == picks.end()) picks.push_back(f); };
+      const int n = nframes_;
+      push(order[n - 1]); push(order[n - 2]); push(order[n / 2]); push(order[1]); push(order[0]);
+      std::vector<int> na, hs;
+      std::vector<double> cl, ps, e0, f0, s0;
+      std::vector<int> ty;
+      for (int f : picks) {
+        const int a0 = fbegin_host_[f], a1 = fbegin_host_[f + 1];
+        na.push_back(a1 - a0);
+        cl.insert(cl.end(), cells_.begin() + 9 * f, cells_.begin() + 9 * f + 9);
+        ps.insert(ps.end(), pos_h_.begin() + 3 * a0, pos_h_.begin() + 3 * a1);
+        ty.insert(ty.end(), types_h_.begin() + a0, types_h_.begin() + a1);
+        e0.push_back(E0_h_[f]);
+        f0.insert(f0.end(), F0_h_.begin() + 3 * a0, F0_h_.begin() + 3 * a1);
+        s0.insert(s0.end(), S0_h_.begin() + 9 * f, S0_h_.begin() + 9 * f + 9);
+        hs.push_back(has_h_[f]);
+      }
+      sub = std::make_unique<Trainer>(eng_, static_cast<int>(picks.size()), na.data(), cl.data(), ps.data(), ty.data(),
+                                      e0.data(), f0.data(), s0.data(), hs.data(), cfg_);
+    }
+    Trainer& T = sub ? *sub : *this;
+    std::vector<double> cur(params, params + nparams_);  // coefficients carried from trial to trial
+    int solves = 0;
+    auto evaluate = [&](double s) {
+      Eval r;
+      r.scaling = s;
+      eng_.set_scaling(s);
+      T.train_linear(cur.data());
+      ++solves;
+      r.p = cur;
+      r.st = stats_of(cur);
+      r.valid = r.st.valid;
+      return r;
+    };
+    constexpr int kCenterMaxIters = 6, kExpandMaxIters = 6;
+    constexpr double kCenterTol = 0.15, kFloor = 1e-12, kBracket = 2.0;
+    const double factors[5] = {1.0 / 1.08, 1.0 / 1.03, 1.0, 1.03, 1.08};
+    Eval center = evaluate(m.scaling);
+    if (!center.valid) {
+      // no readout coefficient above the floor: the reference leaves the model as the seed solve
+      std::copy(center.p.begin(), center.p.end(), params);
+      *scaling_out = center.scaling;
+      eng_.set_params(params);
+      return solves;
+    }
+    Eval best = center, pos, neg;
+    bool have_pos = false, have_neg = false;
+    auto consider = [&](const Eval& e) {
+      if (!e.valid) return;
+      if (std::abs(e.st.center) < std::abs(best.st.center)) best = e;
+      if (e.st.center >= 0.0) {
+        if (!have_pos || e.st.center < pos.st.center) pos = e;
+        have_pos = true;
+      } else {
+        if (!have_neg || e.st.center > neg.st.center) neg = e;
+        have_neg = true;
+      }
+    };
+    consider(center);
+    if (std::abs(center.st.center) >= kCenterTol) {
+      Eval lower, upper;
+      const double ls = std::max(kFloor, center.scaling / kBracket);
+      if (ls < center.scaling) {
+        lower = evaluate(ls);
+        if (lower.valid) consider(lower);
+      }
+      if (!(have_pos && have_neg)) {
+        const double us = center.scaling * kBracket;
+        if (std::isfinite(us)) {
+          upper = evaluate(us);
+          if (upper.valid) consider(upper);
+        }
+      }
+      if (!(have_pos && have_neg)) {
+        // first expansion direction: the probe that improves |median log| most, else none
+        int dir = 0;
+        double err = std::abs(center.st.center);
+        if (lower.valid && std::abs(lower.st.center) < err) { err = std::abs(lower.st.center); dir = -1; }
+        if (upper.valid && std::abs(upper.st.center) < err) dir = 1;
+        Eval edge = dir < 0 ? lower : upper;
+        for (int it = 0; dir != 0 && it < kExpandMaxIters && !(have_pos && have_neg); ++it) {
+          const double ts = dir < 0 ? std::max(kFloor, edge.scaling / kBracket) : edge.scaling * kBracket;
+          if (!(ts > 0.0) || !std::isfinite(ts) || ts == edge.scaling) break;
+          Eval trial = evaluate(ts);
+          if (!trial.valid) break;
+          const double prev = std::abs(edge.st.center);
+          consider(trial);
+          edge = trial;
+          if (!(have_pos && have_neg) && std::abs(trial.st.center) >= prev) break;
+        }
+      }
+    }
+    if (have_pos && have_neg) {
+      for (int it = 0; it < kCenterMaxIters; ++it) {
+        const double lp = std::log(pos.scaling), ln = std::log(neg.scaling);
+        double lt = 0.5 * (lp + ln);
+        const double cp = pos.st.center, cn = neg.st.center;
+        if (std::abs(cp - cn) > 1e-12) {
+          lt = (lp * cn - ln * cp) / (cn - cp);
+          lt = std::max(std::min(lt, std::max(lp, ln)), std::min(lp, ln));
+          const double span = std::abs(lp - ln);
+          if (std::abs(lt - lp) < 0.1 * span || std::abs(lt - ln) < 0.1 * span) lt = 0.5 * (lp + ln);
+        }
+        Eval trial = evaluate(std::max(kFloor, std::exp(lt)));
+        if (!trial.valid) break;
+        consider(trial);
+        if (std::abs(trial.st.center) < kCenterTol) { best = trial; break; }
+      }
+    }
+    // fine trials around the centred scaling: least spread^2 + 3 median^2
+    const double base = best.scaling;
+    double best_metric = std::numeric_limits<double>::infinity(), best_scaling = base;
+    std::vector<double> best_p = best.p;
+    for (int j = 0; j < 5; ++j) {
+      Eval trial = evaluate(std::max(kFloor, base * factors[j]));
+      if (!trial.valid) continue;
+      const double metric = trial.st.spread * trial.st.spread + 3.0 * trial.st.center * trial.st.center;
+      if (metric < best_metric) {
+        best_metric = metric;
+        best_scaling = trial.scaling;
+        best_p = trial.p;
+      }
+    }
+    std::copy(best_p.begin(), best_p.end(), params);
+    *scaling_out = best_scaling;
+    eng_.set_scaling(best_scaling);
+    eng_.set_params(params);
+    return solves;
+  }
+
   int graph_builds() const { return graph_builds_; }
 
  private:
@@ -738,6 +921,8 @@ class Trainer {
   LossConfig cfg_;
   std::vector<int> fbegin_host_, natoms_list_;
   std::vector<double> cells_;
+  std::vector<double> pos_h_, E0_h_, F0_h_, S0_h_;
+  std::vector<int> types_h_, has_h_;
   DevBuf pos_, types_, E0_, F0_, S0_, has_, fbegin_;
   DevBuf E_, F_, V_, ew_, fw_, sw_, lossf_, loss_, grad_;
   bool gatex_ = false;
@@ -822,6 +1007,14 @@ int sus2g_trainer_metrics(sus2g_trainer t, const double* params, double* out6) {
   return train_guarded([&] {
     if (!t || !params || !out6) throw sus2g::Error(1, "invalid argument: trainer/params/out");
     t->trainer->metrics(params, out6);
+  });
+}
+
+int sus2g_trainer_rescale(sus2g_trainer t, double* params, double* scaling, int* solves) {
+  return train_guarded([&] {
+    if (!t || !params || !scaling) throw sus2g::Error(1, "invalid argument: trainer/params/scaling");
+    const int n = t->trainer->rescale(params, scaling);
+    if (solves) *solves = n;
   });
 }
 

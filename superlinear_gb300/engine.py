@@ -73,6 +73,17 @@ class Model:
         v = np.ascontiguousarray(values, dtype=np.float64)
         check(load().sus2g_model_set_params(self._h, _d(v), v.size))
 
+    @property
+    def scaling(self) -> float:
+        """The global radial scaling (the .sus2 `scaling` field; not a trained parameter)."""
+        v = ctypes.c_double()
+        check(load().sus2g_model_get_scaling(self._h, ctypes.byref(v)))
+        return v.value
+
+    @scaling.setter
+    def scaling(self, value: float) -> None:
+        check(load().sus2g_model_set_scaling(self._h, float(value)))
+
     def save(self, path: str) -> None:
         """Write the model with its current parameters as a ``.sus2`` file (MLMTPR::Save)."""
         check(load().sus2g_model_save(self._h, str(path).encode()))

@@ -8,6 +8,8 @@ Mirrors the reference trainer's objective / optimiser surface for this path:
   * ``Trainer.bfgs(params, ...)``  ~ the dense BFGS loop of MTPR_trainer::Train over BFGS::Iterate
                                      (src/common/bfgs.cpp:251-329)
   * ``Trainer.train_linear(params)`` ~ MTPR_trainer::TrainLinear, the linear warm-up before BFGS
+  * ``Trainer.rescale(params)``      ~ Rescale (dev_src/mlp/mtpr_train.cpp:1504), the scaling search
+                                       around it
                                      (dev_src/mtpr_trainer.cpp:1455)
   * ``Trainer.metrics(params)``    ~ the trainer's energy / force / stress MAE and RMSE
 ``weighting`` takes the reference's names: "vibrations", "structures", "molecules".  ``gate_x_l2``
@@ -112,6 +114,18 @@ class Trainer:
             raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
         check(load().sus2g_trainer_train_linear(self._h, _d(p)))
         return p
+
+    def rescale(self, params):
+        """Rescale step before the linear solve (the reference trainer's Rescale): returns
+        (params, scaling, linear solves).  The trainer's engine keeps the new scaling; put it into a
+        model to save with ``model.scaling = scaling``."""
+        p = np.array(params, dtype=np.float64)
+        if p.size != self.nparams:
+            raise ValueError(f"expected {self.nparams} parameters, got {p.size}")
+        s = ctypes.c_double()
+        n = ctypes.c_int()
+        check(load().sus2g_trainer_rescale(self._h, _d(p), ctypes.byref(s), ctypes.byref(n)))
+        return p, s.value, n.value
 
     def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
         """Runs BFGS from ``params``; returns (params, loss history)."""

@@ -166,6 +166,7 @@ def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--reference", default=os.environ.get("SUS2_REFERENCE", "/root/reference"))
     ap.add_argument("--oracle", default=os.path.join(REPO, "oracle", "_ref"))
+    ap.add_argument("--rescale-only", action="store_true", help="only regenerate the rescale-step goldens")
     args = ap.parse_args()
     emb = os.path.join(args.oracle, "embedded-efs")
     mlp = os.path.join(args.oracle, "mlp-sus2")
@@ -173,6 +174,9 @@ def main():
     for tool in (emb, mlp, refgrad):
         if not os.path.exists(tool):
             sys.exit(f"missing {tool}: build it with make -C oracle ref _ref/ref-grad")
+    if args.rescale_only:
+        golden_rescale(refgrad)
+        return
 
     # 1. the reference's own golden fixtures
     src = os.path.join(args.reference, "interfaces/lammps/tests/fixtures/two_cutoff")
@@ -295,8 +299,22 @@ def main():
             json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
                        "weighting": "vibrations", "source": "reference MTPR_trainer::TrainLinear",
                        "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
+    golden_rescale(refgrad)
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+def golden_rescale(refgrad):
+    """7. rescale step: the reference trainer's Rescale (scaling search around TrainLinear) on the
+    labelled sets (the Effect set has six frames, so its five-frame subset is exercised)."""
+    for name, _, weights in LOSS_CASES():
+        model = os.path.join(HERE, "models", f"{name}.sus2")
+        cfg = os.path.join(HERE, "frames", f"{name}__labelled.cfg")
+        res = json.loads(run([refgrad, "--rescale", model, cfg, *(str(w) for w in weights)]))
+        with open(os.path.join(HERE, "linear", f"{name}__rescale.json"), "w") as fh:
+            json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
+                       "weighting": "vibrations", "source": "reference Rescale (dev_src/mlp/mtpr_train.cpp)",
+                       "scaling": res["scaling"], "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
 
 
 if __name__ == "__main__":

@@ -167,7 +167,8 @@ def test_trainer_survives_other_use_of_its_engine(sg, golden):
     assert first[0] == again[0] and np.array_equal(first[1], again[1])
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*.json"))),
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear",
+                                                            "*__labelled.json"))),
                          ids=os.path.basename)
 def test_linear_warmup_matches_reference_trainer(sg, golden, path):
     """Trainer.train_linear (GPU components, device normal equations) against the reference's
@@ -188,3 +189,27 @@ def test_linear_warmup_matches_reference_trainer(sg, golden, path):
     assert after < before
     ref_after, _ = tr.loss_grad(p, want_grad=False)
     assert abs(after - ref_after) <= 1e-3 * abs(ref_after)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear",
+                                                            "*__rescale.json"))),
+                         ids=os.path.basename)
+def test_rescale_matches_reference_trainer(sg, golden, path):
+    """Trainer.rescale (a linear warm-up on the GPU per trial) against the reference's Rescale: the
+    chosen scaling and the final coefficients; the model saves the new scaling."""
+    data = load_json(path)
+    model = sg.Model(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, *data["weights"], weighting=data["weighting"], gate_x_l2=0.0)
+    p, s, solves = tr.rescale(model.params())
+    assert abs(s - data["scaling"]) <= 1e-8 * data["scaling"]
+    assert np.max(np.abs(p - np.asarray(data["coeffs"])) / (1.0 + np.abs(data["coeffs"]))) < 1e-7
+    assert solves >= 6
+    # the trainer keeps evaluating with the new scaling; the model carries it into a saved file
+    loss_after, _ = tr.loss_grad(p, want_grad=False)
+    model.scaling = s
+    model.set_params(p)
+    fresh = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, *data["weights"], weighting=data["weighting"],
+                       gate_x_l2=0.0)
+    loss_fresh, _ = fresh.loss_grad(p, want_grad=False)
+    assert abs(loss_fresh - loss_after) <= 1e-12 * abs(loss_after)

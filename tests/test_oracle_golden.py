@@ -120,7 +120,11 @@ def test_descriptor_goldens(oracle_lib, golden, path):
 
 
 def linear_cases():
-    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*.json")))
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*__labelled.json")))
+
+
+def rescale_cases():
+    return sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "linear", "*__rescale.json")))
 
 
 @pytest.mark.parametrize("path", linear_cases(), ids=os.path.basename)
@@ -131,3 +135,33 @@ def test_linear_warmup_goldens(oracle_lib, golden, path):
     frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
     p = oracle_lib.train_linear(m, frames, *data["weights"], weighting=data["weighting"])
     assert rel_err(p, data["coeffs"]) < 1e-9
+
+
+@pytest.mark.parametrize("path", rescale_cases(), ids=os.path.basename)
+def test_rescale_goldens(oracle_lib, golden, path):
+    """The rescale step (scaling search around the linear warm-up) against the reference's Rescale:
+    the chosen scaling and the final coefficients (the Effect set's six frames exercise the
+    five-frame subset)."""
+    data = load_json(path)
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    p, s, solves = oracle_lib.rescale(m, frames, *data["weights"], weighting=data["weighting"])
+    assert abs(s - data["scaling"]) <= 1e-9 * data["scaling"]
+    assert rel_err(p, data["coeffs"]) < 1e-8
+    assert solves >= 6 and m.scaling == s
+
+
+def test_rescale_helpers_known_answers(oracle_lib):
+    """Expansion-direction and subset selection known answers: the former from the reference's own
+    self-test (dev_src/mlp/dev_self_test.cpp:3033-3053), the latter by its definition."""
+    d = oracle_lib.expansion_direction
+    assert d(-5.26730719706032, -8.27303159671854, -2.25) == 1
+    assert d(5.0, 2.0, 8.0) == -1
+    assert d(-1.0, -2.0, -3.0) == 0
+    assert d(-4.0, None, -1.0) == 1
+    assert oracle_lib.rescale_subset([10, 20, 30]) == [0, 1, 2]
+    # sizes 5 3 9 3 7 1 -> stable order 5(1) 1(3) 3(3) 0(5) 4(7) 2(9): max 2, second max 4,
+    # median order[3] = 0, second min 1, min 5
+    assert oracle_lib.rescale_subset([5, 3, 9, 3, 7, 1]) == [2, 4, 0, 1, 5]
+    st = oracle_lib.moment_stats(np.array([0.0, np.e, 1.0, 1e-13, -np.e ** 2]), 1, 4)
+    assert st is not None and abs(st[0] - 1.0) < 1e-15
