@@ -142,6 +142,32 @@ def test_cell_list_capacity_overflow_is_retried(lib, oracle_lib, golden):
     assert rel_err(V.cpu().numpy()[0], vo) < FP64_TOL
 
 
+@pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l3k4r2o2"])
+def test_mixed_cell_list_and_image_scan_batch(lib, oracle_lib, golden, name):
+    """One call over a 1,728-atom diamond (cell list) between two small frames (image scan): the
+    mixed batch is merged into one CSR edge list; every frame matches the oracle (FP64) and its
+    own single-frame evaluation bit for bit (FP32 and FP64)."""
+    path = os.path.join(golden, "models", f"{name}.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    C = m.dims["C"]
+    small = training_frames(2, 20, 40, 3.2, 3.8, 0.1, seed=21, species=C)
+    big = diamond(6, sigma=0.05, seed=5, species=C)
+    frames = [small[0], big, small[1]]
+    for g in (g64, g32):
+        e, f, v, s = g.calc_efs(frames)
+        off = 0
+        for k, fr in enumerate(frames):
+            sl = slice(off, off + fr.natoms)
+            e1, f1, v1, s1 = g.calc_efs([fr])
+            assert e1[0] == e[k] and np.array_equal(f1, f[sl]) and np.array_equal(v1[0], v[k])
+            if g is g64:
+                eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+                assert rel_err(e[k], eo) < FP64_TOL and rel_err(f[sl], fo) < FP64_TOL
+                assert rel_err(v[k], vo) < FP64_TOL
+            off += fr.natoms
+
+
 def test_bin_capacity_overflow_is_retried(lib, oracle_lib, golden):
     """A compact 729-atom cluster (1.0 A spacing) in a 30 A box: up to 27 atoms fall in a
     half-width bin of the cluster against a bin capacity sized from the box's mean density (9),
