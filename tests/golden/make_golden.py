@@ -167,6 +167,7 @@ def main():
     ap.add_argument("--reference", default=os.environ.get("SUS2_REFERENCE", "/root/reference"))
     ap.add_argument("--oracle", default=os.path.join(REPO, "oracle", "_ref"))
     ap.add_argument("--rescale-only", action="store_true", help="only regenerate the rescale-step goldens")
+    ap.add_argument("--config5-only", action="store_true", help="only regenerate the L5 (config 5) model")
     args = ap.parse_args()
     emb = os.path.join(args.oracle, "embedded-efs")
     mlp = os.path.join(args.oracle, "mlp-sus2")
@@ -176,6 +177,9 @@ def main():
             sys.exit(f"missing {tool}: build it with make -C oracle ref _ref/ref-grad")
     if args.rescale_only:
         golden_rescale(refgrad)
+        return
+    if args.config5_only:
+        golden_config5(mlp)
         return
 
     # 1. the reference's own golden fixtures
@@ -300,8 +304,35 @@ def main():
                        "weighting": "vibrations", "source": "reference MTPR_trainer::TrainLinear",
                        "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
     golden_rescale(refgrad)
+    golden_config5(mlp)
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+# Config 5 topology: Effect L5/K8/R2/O2, three species.  The reference's init-sh writes it, but its
+# model loader rejects sh_l_max > 4, so the seeded parameters are written with this package's
+# writer (no reference round trip) and the L5 evaluations have no reference values: GPU and oracle
+# are checked against each other and against finite differences.
+CONFIG5 = ("effect_l5k8r2o2_c3", "coordination-effect",
+           dict(species_count=3, l_max=5, radial_channels=8, neighbor_cutoff=5.0,
+                coordination=dict(channels=2, body_order=4, channel_coupling="cross"),
+                interaction=dict(channels=2, body_order=4, channel_coupling="diagonal")), (15, 3.0, 8.0))
+
+
+def golden_config5(mlp):
+    name, kind, spec, (seed, rscale, oscale) = CONFIG5
+    with tempfile.TemporaryDirectory() as tmp:
+        ypath = os.path.join(tmp, f"{name}.yaml")
+        with open(ypath, "w") as fh:
+            fh.write(yaml_for(kind, spec, f"{name}.sus2"))
+        run([mlp, "init-sh", ypath], cwd=tmp)
+        fields = read_sus2(os.path.join(tmp, f"{name}.sus2"))
+        vec = random_vector(fields, seed, rscale, oscale)
+        vector_to_fields(fields, vec)
+        model = os.path.join(HERE, "models", f"{name}.sus2")
+        write_sus2(model, fields)
+        assert np.array_equal(fields_to_vector(read_sus2(model)), vec)
+    print(name, "written (init-sh topology, seeded parameters)")
 
 
 def golden_rescale(refgrad):
