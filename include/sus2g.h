@@ -101,6 +101,13 @@ int sus2g_calc_efs_device(sus2g_engine engine, int nframes, const int* natoms, c
  * stage timer or a neighbour-capacity overflow makes the next call eager again.
  * enabled = 1 (default) or 0. */
 int sus2g_engine_set_step_graph(sus2g_engine engine, int enabled);
+/* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
+ * the model runs with both compiled register budgets (3 and 4 resident blocks per SM; basis size 8)
+ * over `reps` launches each and keeps the faster for later evaluations (results are identical
+ * either way).  blocks4[mode] (may be NULL) = the chosen budgets per pass (0 Static, 1 gate
+ * forward, 2 outer, 3 gate reverse; 0 for passes the model does not run), ms8[2 mode + budget - 3]
+ * (may be NULL) = milliseconds per launch. */
+int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* ms8);
 
 /* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
  * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors

@@ -164,6 +164,17 @@ int sus2g_engine_set_timing(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_timing(enabled != 0); });
 }
 
+int sus2g_engine_autotune(sus2g_engine e, int reps, int* blocks4, double* ms8) {
+  return guarded([&] {
+    need(e && reps > 0, "engine/reps");
+    int b[4];
+    double ms[8];
+    e->engine->autotune(reps, b, ms);
+    if (blocks4) std::memcpy(blocks4, b, sizeof(b));
+    if (ms8) std::memcpy(ms8, ms, sizeof(ms));
+  });
+}
+
 int sus2g_engine_set_step_graph(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_step_graphs(enabled != 0); });
 }

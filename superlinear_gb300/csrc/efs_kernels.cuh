@@ -263,14 +263,17 @@ __device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const R
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
 constexpr int kPassWarps = 4;
-// Minimum resident blocks per SM: 4 (<= 128 registers) for the FP32 kernels up to L = 3 and the
-// L = 4 gate passes, 3 otherwise (measured: the L = 4 outer pass spills and runs slower at 128
-// registers; the FP64 kernels spill more).
+// Minimum resident blocks per SM (the register budget: 4 blocks = 128 registers, 3 = 168).  Both
+// budgets are compiled for the B = 8 passes and the engine's autotuner times them on the caller's
+// layout; without tuning: 4 for the FP32 kernels up to L = 3 and the L = 4 gate passes, 3
+// otherwise (measured: the L = 4 outer pass spills and runs slower at 128 registers; the FP64
+// kernels spill more).
+__host__ __device__ constexpr int default_min_blocks(int L, bool fp32, int mode) {
+  return (fp32 && (L <= 3 || (L == 4 && mode != kModeOuter))) ? 4 : 3;
+}
 
-template <int L, typename Real, int MODE, bool KAHAN, int BF>
-__global__ void __launch_bounds__(kPassWarps * kWarp,
-                                  (sizeof(Real) == 4 && (L <= 3 || (L == 4 && MODE != kModeOuter))) ? 4 : 3)
-    atom_pass_kernel(PassArgs<Real> a) {
+template <int L, typename Real, int MODE, bool KAHAN, int BF, int MINB>
+__global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(PassArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;

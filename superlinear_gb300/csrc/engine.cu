@@ -1399,9 +1399,8 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
 }
 
 template <typename Real>
-void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages) {
+PassArgs<Real> Engine::pass_args() {
   const Model& m = model_;
-  cudaStream_t s = stream_;
   const int N = natoms_;
   const size_t E = std::max<long long>(1, nedges_);
   g_.ensure(sizeof(Real) * 3 * E);
@@ -1429,6 +1428,15 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     a.hcontrib = hcontrib_.as<Real>();
     a.gmom = gmom_.as<Real>();
   }
+  return a;
+}
+
+template <typename Real>
+void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages) {
+  const Model& m = model_;
+  cudaStream_t s = stream_;
+  const int N = natoms_;
+  PassArgs<Real> a = pass_args<Real>();
   // stage 1: gate forward (Effect) -- gate signals of the centre atoms
   if (stages & kStageGate) {
     // every centre's site energy, virial and gate signal is written by the passes; only caller
@@ -1443,7 +1451,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       if (ghosts)
         SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
       mark_begin(2);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s, pass_blocks_[kModeGateForward]);
       mark_end();
     }
   }
@@ -1451,7 +1459,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
   if (stages & kStageOuter) {
     if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
-    launches_ += launch_atom_pass<Real>(m.L, m.gated ? kModeOuter : kModeStatic, a, sm_count_, s);
+    const int mode = m.gated ? kModeOuter : kModeStatic;
+    launches_ += launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, pass_blocks_[mode]);
     mark_end();
     if (m.gated && user_edges_) {
       hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
@@ -1468,7 +1477,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) {
       if (user_edges_) a.hbar_atom = hbar_atom_.as<double>();
       mark_begin(3);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s, pass_blocks_[kModeGateReverse]);
       mark_end();
     }
     wait_reverse();
@@ -1723,6 +1732,59 @@ void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d
     throw Error(1, "Effect models on a ghost layout need the caller's gate-signal exchange: use the staged calls");
   if (precision_ == kFP32) run_efs<float>(d_energy, d_forces, d_virial, d_site, kStageAll);
   else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
+}
+
+// Pass-kernel autotuner: on the current layout (the last evaluation's edges), times each pass the
+// model runs with both register budgets (3 and 4 resident blocks per SM), `reps` launches each
+// after one warm-up launch, and keeps the faster budget per pass.  The passes read the state the
+// evaluation before them left (gate signals, node adjoints), so a full evaluation runs first; the
+// gate reverse pass accumulates into the edge gradients, so the next evaluation recomputes them.
+template <typename Real>
+void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
+  const Model& m = model_;
+  cudaStream_t s = stream_;
+  const int N = natoms_;
+  double* scratch = static_cast<double*>(io(7, sizeof(double) * (7 * static_cast<size_t>(std::max(1, nframes_)) +
+                                                                  4 * static_cast<size_t>(std::max(1, N)))));
+  run_efs<Real>(scratch, scratch + 7 * std::max(1, nframes_), scratch + std::max(1, nframes_), nullptr, kStageAll);
+  PassArgs<Real> a = pass_args<Real>();
+  const int modes_static[] = {kModeStatic};
+  const int modes_gated[] = {kModeGateForward, kModeOuter, kModeGateReverse};
+  const int* modes = m.gated ? modes_gated : modes_static;
+  const int nmodes = m.gated ? 3 : 1;
+  for (int q = 0; q < 4; ++q) { blocks_out[q] = 0; ms_out[2 * q] = ms_out[2 * q + 1] = 0.0; }
+  cudaEvent_t e0 = take_event(), e1 = take_event();
+  for (int k = 0; k < nmodes; ++k) {
+    const int mode = modes[k];
+    double best = 0.0;
+    int choice = 0;
+    for (int blocks = 3; blocks <= 4; ++blocks) {
+      launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+      SUS2G_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r) launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+      SUS2G_CUDA(cudaEventRecord(e1, s));
+      SUS2G_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      const double per = double(ms) / std::max(1, reps);
+      ms_out[2 * mode + (blocks - 3)] = per;
+      if (choice == 0 || per < best) { best = per; choice = blocks; }
+    }
+    pass_blocks_[mode] = choice;
+    blocks_out[mode] = choice;
+  }
+  event_next_ = 0;
+  reset_step_graph();  // a captured step holds the previous budgets
+}
+
+void Engine::autotune(int reps, int* blocks_out, double* ms_out) {
+  SUS2G_CUDA(cudaSetDevice(device_));
+  if (natoms_ <= 0 || ncentres_ <= 0) throw Error(1, "autotune needs an evaluated layout: evaluate once first");
+  if (timing_) throw Error(1, "autotune: turn the stage timer off first");
+  wait_reverse();
+  if (precision_ == kFP32) autotune_passes<float>(reps, blocks_out, ms_out);
+  else autotune_passes<double>(reps, blocks_out, ms_out);
+  check_device_error();
 }
 
 void Engine::reset_step_graph() {

@@ -11,6 +11,8 @@
 
 namespace sus2g {
 
+template <typename Real> struct PassArgs;  // efs_kernels.cuh
+
 enum Precision : int { kFP64 = 0, kFP32 = 1 };
 
 // Grow-only device buffer.
@@ -66,6 +68,10 @@ class Engine {
   void step_frames(int nframes, const int* frame_natoms, const double* cells, const double* d_pos, const int* d_types,
                    double* d_energy, double* d_forces, double* d_virial, double* d_site);
   void set_step_graphs(bool on) { step_graphs_ = on; if (!on) reset_step_graph(); }
+  // Pass-kernel autotuner on the current layout (see engine.cu): blocks_out[mode] = the chosen
+  // register budget (3 or 4 resident blocks per SM; 0 for passes the model does not run),
+  // ms_out[2 mode + (budget - 3)] = the timed milliseconds per launch.
+  void autotune(int reps, int* blocks_out, double* ms_out);
   void reset_step_graph();
 
   // --- evaluation ---------------------------------------------------------------------------
@@ -155,6 +161,8 @@ class Engine {
 
  private:
   template <typename Real> void upload_tables();
+  template <typename Real> PassArgs<Real> pass_args();
+  template <typename Real> void autotune_passes(int reps, int* blocks_out, double* ms_out);
   enum : int { kStageGate = 1, kStageOuter = 2, kStageFinish = 4, kStageAll = 7 };
   template <typename Real>
   void run_efs(double* d_energy, double* d_forces, double* d_virial, double* d_site, int stages);
@@ -222,6 +230,7 @@ class Engine {
   int arrivals_frames_ = 0;     // frame_arrivals_ entries known to be zero
   DevBuf scratch_;
   DevBuf io_[8];
+  int pass_blocks_[4] = {0, 0, 0, 0};  // register budget per pass mode (0: the default)
   // second stream for independent work inside a step (reverse edges beside the first pass, the
   // frame reduction beside the force gather)
   cudaStream_t aux_stream_ = nullptr;

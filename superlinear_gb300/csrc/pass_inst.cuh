@@ -13,10 +13,10 @@
 namespace sus2g {
 namespace pass_detail {
 
-template <typename Real, int L, int MODE, int BF>
+template <typename Real, int L, int MODE, int BF, int MINB>
 int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream) {
   constexpr bool kKahan = sizeof(Real) == 4;
-  auto kern = atom_pass_kernel<L, Real, MODE, kKahan, BF>;
+  auto kern = atom_pass_kernel<L, Real, MODE, kKahan, BF, MINB>;
   const auto& dm = a.dm;
   const int H = (L + 1) * (L + 1);
   const size_t smem = sizeof(Real) *
@@ -39,13 +39,27 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream) {
   return 1;
 }
 
+template <typename Real, int L, int MODE>
+constexpr int min_blocks() { return default_min_blocks(L, sizeof(Real) == 4, MODE); }
+
+// B = 8: the register budget min_blocks (3 or 4 resident blocks per SM; 0 = the default);
+// other basis sizes: the default only.
+template <typename Real, int L, int MODE, int BF>
+int launch_budget(int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+  if constexpr (BF == 8) {
+    if (blocks == 3) return launch_one<Real, L, MODE, BF, 3>(a, sm_count, s);
+    if (blocks == 4) return launch_one<Real, L, MODE, BF, 4>(a, sm_count, s);
+  }
+  return launch_one<Real, L, MODE, BF, min_blocks<Real, L, MODE>()>(a, sm_count, s);
+}
+
 template <typename Real, int L, int BF>
-int launch_mode(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
   switch (mode) {
-    case kModeStatic: return launch_one<Real, L, kModeStatic, BF>(a, sm_count, s);
-    case kModeGateForward: return launch_one<Real, L, kModeGateForward, BF>(a, sm_count, s);
-    case kModeOuter: return launch_one<Real, L, kModeOuter, BF>(a, sm_count, s);
-    case kModeGateReverse: return launch_one<Real, L, kModeGateReverse, BF>(a, sm_count, s);
+    case kModeStatic: return launch_budget<Real, L, kModeStatic, BF>(blocks, a, sm_count, s);
+    case kModeGateForward: return launch_budget<Real, L, kModeGateForward, BF>(blocks, a, sm_count, s);
+    case kModeOuter: return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s);
+    case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s);
   }
   throw std::runtime_error("unknown pass mode");
 }
@@ -55,9 +69,9 @@ int launch_mode(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s)
 // B = 8 (the basis size the reference's model initialisation writes) runs the variant with the
 // basis size fixed at compile time; other sizes run the generic variant.
 template <typename Real, int L>
-int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
-  if (a.dm.B == 8) return pass_detail::launch_mode<Real, L, 8>(mode, a, sm_count, s);
-  return pass_detail::launch_mode<Real, L, 0>(mode, a, sm_count, s);
+int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks) {
+  if (a.dm.B == 8) return pass_detail::launch_mode<Real, L, 8>(mode, blocks, a, sm_count, s);
+  return pass_detail::launch_mode<Real, L, 0>(mode, 0, a, sm_count, s);
 }
 
 template <typename Real, int L>
@@ -66,5 +80,5 @@ cudaError_t upload_pass_constants_l() { return sph_norm_upload(); }
 }  // namespace sus2g
 
 #define SUS2G_INSTANTIATE_PASS(REAL, L)                                                               \
-  template int launch_atom_pass_l<REAL, L>(int, const PassArgs<REAL>&, int, cudaStream_t);            \
+  template int launch_atom_pass_l<REAL, L>(int, const PassArgs<REAL>&, int, cudaStream_t, int);       \
   template cudaError_t upload_pass_constants_l<REAL, L>();

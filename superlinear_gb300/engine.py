@@ -121,6 +121,16 @@ class Engine:
         check(load().sus2g_engine_edge_count(self._h, ctypes.byref(n)))
         return n.value
 
+    PASSES = ("static", "gate_forward", "outer", "gate_reverse")
+
+    def autotune(self, reps: int = 5):
+        """Times both register budgets of every pass on the last evaluation's layout and keeps the
+        faster; returns {pass: (chosen blocks per SM, {blocks: ms per launch})}."""
+        b = (ctypes.c_int * 4)()
+        ms = (ctypes.c_double * 8)()
+        check(load().sus2g_engine_autotune(self._h, int(reps), b, ms))
+        return {name: (b[q], {3: ms[2 * q], 4: ms[2 * q + 1]}) for q, name in enumerate(self.PASSES) if b[q]}
+
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))

@@ -168,6 +168,29 @@ def test_mixed_cell_list_and_image_scan_batch(lib, oracle_lib, golden, name):
             off += fr.natoms
 
 
+@pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l4k8r2o3"])
+def test_autotune_keeps_results_and_chooses_budgets(lib, golden, name):
+    """The pass autotuner times both register budgets on the evaluated layout; the chosen kernels
+    compute the same values (bit for bit), before and after, through the step graph too."""
+    path = os.path.join(golden, "models", f"{name}.sus2")
+    m = lib.Model(path)
+    fr = diamond(6, sigma=0.05, seed=9, species=m.dims["C"])
+    for prec in (lib.FP32, lib.FP64):
+        g = lib.Engine(m, 0, prec)
+        with pytest.raises(lib.Sus2Error):
+            g.autotune()                    # nothing evaluated yet
+        before = g.calc_efs([fr])
+        choice = g.autotune(reps=2)
+        modes = {"static"} if not m.dims["gated"] else {"gate_forward", "outer", "gate_reverse"}
+        assert set(choice) == modes
+        for blocks, times in choice.values():
+            assert blocks in (3, 4) and times[blocks] == min(times.values()) and times[blocks] > 0
+        for _ in range(3):
+            after = g.calc_efs([fr])
+            for x, y in zip(before, after):
+                assert np.array_equal(x, y)
+
+
 def test_bin_capacity_overflow_is_retried(lib, oracle_lib, golden):
     """A compact 729-atom cluster (1.0 A spacing) in a 30 A box: up to 27 atoms fall in a
     half-width bin of the cluster against a bin capacity sized from the box's mean density (9),
