@@ -237,6 +237,8 @@ def bench_training(sg, torch, steps, warmup):
     for prec, key, nsteps in ((sg.FP32, "fp32", steps), (sg.FP64, "fp64", max(5, steps // 2))):
         eng = sg.Engine(model, 0, prec)
         tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
+        tr.loss_grad(p)
+        out.setdefault("autotune", {})[key] = {q: c[0] for q, c in eng.autotune(reps=2).items()}
         for _ in range(warmup):
             tr.loss_grad(p)
         torch.cuda.synchronize()

@@ -1775,6 +1775,9 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
   }
   event_next_ = 0;
   reset_step_graph();  // a captured step holds the previous budgets
+  // graphs captured elsewhere (a trainer's evaluation graph) hold them too: a new edge generation
+  // makes their owners rebind and capture again
+  ++edge_generation_;
 }
 
 void Engine::autotune(int reps, int* blocks_out, double* ms_out) {

@@ -213,3 +213,19 @@ def test_rescale_matches_reference_trainer(sg, golden, path):
                        gate_x_l2=0.0)
     loss_fresh, _ = fresh.loss_grad(p, want_grad=False)
     assert abs(loss_fresh - loss_after) <= 1e-12 * abs(loss_after)
+
+
+def test_trainer_after_autotune(sg, golden):
+    """Tuning the engine's passes on the trainer's layout: the trainer captures its graph again and
+    its objective and gradient are unchanged bit for bit."""
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    model = sg.Model(path)
+    frames = read_cfg(os.path.join(golden, "frames", "effect_l3k4r2o2__labelled.cfg"))
+    for prec in (sg.FP64, sg.FP32):
+        eng = sg.Engine(model, 0, prec)
+        tr = sg.Trainer(eng, frames)
+        l0, g0 = tr.loss_grad(model.params())
+        choice = eng.autotune(reps=2)
+        assert set(choice) == {"gate_forward", "outer", "gate_reverse"}
+        l1, g1 = tr.loss_grad(model.params())
+        assert l1 == l0 and np.array_equal(g1, g0)
