@@ -10,7 +10,7 @@
 namespace sus2g {
 namespace grad_detail {
 
-constexpr int kGradWarps = 2;
+constexpr int kGradMaxWarps = 4;  // warps per block considered by the launch configuration
 template <typename Real>
 using GradKernel = void (*)(GradArgs<Real>);
 
@@ -48,20 +48,28 @@ GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, in
                        ? 0
                        : grad_acc_cols(Lp, dm.B, dm.C, dm.scaling_mode, mode == kGradOuter && dm.gated);
   GradLaunch cfg;
-  cfg.warps = kGradWarps;
   cfg.acc_cols = cols;
   auto bytes = [&](int warps, int c) {
     return sizeof(Real) * (table + warps * (per_warp + static_cast<size_t>(c) * kAccStride));
   };
-  if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) cfg.warps = 1;
-  if (bytes(cfg.warps, cols) > static_cast<size_t>(optin)) { cfg.warps = kGradWarps; cfg.acc_cols = 0; }
+  if (bytes(1, cols) > static_cast<size_t>(optin)) cfg.acc_cols = 0;  // columns do not fit: shuffle trees
+  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (err != cudaSuccess) throw std::runtime_error(std::string("gradient shared memory: ") + cudaGetErrorString(err));
+  // warps per block: the most resident warps per SM (registers and shared memory), fewer warps
+  // per block on ties (finer work distribution)
+  int per_sm = 0, best_warps = 0;
+  for (int w = 1; w <= kGradMaxWarps; ++w) {
+    const size_t smem = bytes(w, cfg.acc_cols);
+    if (smem > static_cast<size_t>(optin)) break;
+    int blocks = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, w * kWarp, smem);
+    if (blocks * w > per_sm * best_warps) { per_sm = blocks; best_warps = w; }
+  }
+  if (best_warps == 0 || per_sm < 1)
+    throw std::runtime_error("gradient kernel does not fit on an SM (shared memory " + std::to_string(bytes(1, cfg.acc_cols)) + " B)");
+  cfg.warps = best_warps;
   cfg.block = cfg.warps * kWarp;
   cfg.smem = bytes(cfg.warps, cfg.acc_cols);
-  cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(cfg.smem));
-  if (err != cudaSuccess) throw std::runtime_error(std::string("gradient shared memory: ") + cudaGetErrorString(err));
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, cfg.block, cfg.smem);
-  if (per_sm < 1) throw std::runtime_error("gradient kernel does not fit on an SM (shared memory " + std::to_string(cfg.smem) + " B)");
   const int need = std::max(1, (natoms + cfg.warps - 1) / cfg.warps);
   cfg.grid = std::max(1, std::min(need, per_sm * sm_count));
   return cfg;

@@ -62,9 +62,13 @@ struct GradArgs {
 
 constexpr int kAccStride = kWarp + 1;
 
+// Per-warp scratch: staged rows [32][2F + 2H + 1], node values and tangents v, vd [M] each, the
+// node adjoints lam, mu [M] each (in the staged rows when they fit: those are dead once the forward
+// reduction is done, and the per-edge loop recomputes its geometry), abar rows [2][K][H], hbar [2F].
+__host__ __device__ constexpr bool grad_adj_in_stage(int F, int H, int M) { return 2 * M <= kWarp * (2 * F + 2 * H + 1); }
 template <typename Real>
 __host__ __device__ inline int grad_warp_size(int F, int H, int M, int K) {
-  return kWarp * (2 * F + 2 * H + 1) + 4 * M + 2 * K * H + 2 * F + 4;
+  return kWarp * (2 * F + 2 * H + 1) + 2 * M + (grad_adj_in_stage(F, H, M) ? 0 : 2 * M) + 2 * K * H + 2 * F + 4;
 }
 
 // Accumulator columns per radial index k: Chebyshev coefficients [l][b], species factors [t][l]
@@ -189,9 +193,10 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
   Real* stage = wbase;
   Real* v = stage + kWarp * sw;
   Real* vd = v + M;
-  Real* lam = vd + M;
+  const bool adj_staged = grad_adj_in_stage(F, H, M);
+  Real* lam = adj_staged ? stage : vd + M;
   Real* mu = lam + M;
-  Real* abl = mu + M;
+  Real* abl = vd + M + (adj_staged ? 0 : 2 * M);
   Real* abm = abl + K * H;
   Real* hb = abm + K * H;  // [2F]
   Real* accs = wbase + grad_warp_size<Real>(F, H, M, K);  // [ncol][kAccStride]
