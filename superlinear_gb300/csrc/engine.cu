@@ -104,20 +104,6 @@ __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame
                           static_cast<float>(wz - hz), 0};
 }
 
-// Image-scan frames: one thread per centre (cell-list frames are left to the warp kernels).
-__global__ void k_edge_count(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                             const int* bin_start, const int* bin_of, const AtomFrac* frac,
-                             const AtomOff* off, int* counts, int* error) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= natoms) return;
-  const FramePlan& fp = plans[frame_of[i]];
-  if (fp.use_bins) return;
-  int n = 0;
-  enumerate_edges(i, fp, pos, rc2, error,
-                  [&](int, int, int, int, double, double, double, double) { ++n; });
-  counts[i] = n;
-}
-
 // One cell-list edge record: components and distance already in the record's precision.
 template <typename Real>
 __device__ __forceinline__ void write_edge_rec(long long e, int j, int a, int b, int c, Real x, Real y, Real z, Real r,
@@ -143,31 +129,56 @@ __device__ __forceinline__ void write_edge(long long e, int j, int a, int b, int
   key[e] = edge_key(j, a, b, c);
 }
 
-template <typename Real>
-__global__ void k_edge_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
-                            const int* bin_start, const int* bin_of, const AtomFrac* frac,
-                            const AtomOff* off, const int* row, int* nbr, typename Vec4<Real>::type* d4,
-                            unsigned long long* key, int* error) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= natoms) return;
-  const FramePlan& fp = plans[frame_of[i]];
-  if (fp.use_bins) return;
-  int e = row[i];
-  const int end = row[i + 1];
-  enumerate_edges(i, fp, pos, rc2, error,
-                  [&](int j, int a, int b, int c, double x, double y, double z, double r2) {
-                    if (e >= end) { record_error(error, kErrEdgeCapacity); return; }
-                    write_edge<Real>(e++, j, a, b, c, x, y, z, r2, nbr, d4, key);
-                  });
-}
-
-// Cell-list frames: one warp per centre over the flattened 27-bin candidate list, one pass.  The
-// centre's edges go to its padded slots pad0 + (i - a0) cap .. + cap of the staging buffers; a
-// count above cap is clamped to cap and raises *overflow to the full count, which the host reads
-// with the step's error check (it then grows the capacity and repeats the step).
 constexpr int kFillWarps = 8;
 constexpr int kFillSortStage = 256;  // keys per warp kept in shared memory for the in-kernel sort
 constexpr int kFillSortPer = 4;
+
+// Sorts a centre's n staged edges (slots pad .. pad + n - 1) by key into the final arrays at the
+// same slots: each key's rank among the centre's keys (unique within a centre), up to
+// kFillSortPer keys per lane per pass with their payloads loaded while the ranks are counted;
+// keys from shared memory when the centre has at most kFillSortStage of them.
+template <typename Real>
+__device__ __forceinline__ void sort_centre_edges(int lane, int n, long long pad, const unsigned long long* skeys,
+                                                  const unsigned long long* key, const int* nbr,
+                                                  const typename Vec4<Real>::type* d4, unsigned long long* key_out,
+                                                  int* nbr_out, typename Vec4<Real>::type* d4_out) {
+  const unsigned long long* src = n <= kFillSortStage ? skeys : key + pad;
+  for (int q0 = 0; q0 < n; q0 += kFillSortPer * kWarp) {
+    unsigned long long kk[kFillSortPer];
+    int nb[kFillSortPer], rank[kFillSortPer];
+    typename Vec4<Real>::type dd[kFillSortPer];
+#pragma unroll
+    for (int u = 0; u < kFillSortPer; ++u) {
+      const int q = q0 + u * kWarp + lane;
+      kk[u] = ~0ull;
+      rank[u] = 0;
+      if (q < n) {
+        kk[u] = src[q];
+        nb[u] = nbr[pad + q];
+        dd[u] = d4[pad + q];
+      }
+    }
+    for (int t = 0; t < n; ++t) {
+      const unsigned long long kt = src[t];
+#pragma unroll
+      for (int u = 0; u < kFillSortPer; ++u) rank[u] += kt < kk[u];
+    }
+#pragma unroll
+    for (int u = 0; u < kFillSortPer; ++u) {
+      if (q0 + u * kWarp + lane < n) {
+        key_out[pad + rank[u]] = kk[u];
+        nbr_out[pad + rank[u]] = nb[u];
+        d4_out[pad + rank[u]] = dd[u];
+      }
+    }
+  }
+}
+
+// Cell-list frames: one warp per centre over its 125 stencil bins (warp_bin_edges), one pass.  The
+// centre's edges go to its padded slots pad0 + (i - a0) cap .. + cap of the staging buffers; a
+// count above cap is clamped to cap and raises *overflow to the full count, which the host reads
+// with the step's error check (it then grows the capacity and repeats the step).  With row_end the
+// kernel then sorts the centre's edges into the final arrays at the same slots.
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp, 4)
 k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2,
@@ -206,87 +217,97 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
     if (cursor > cap) atomicMax(overflow, cursor);
   }
   if (!row_end) return;
-  // cell lists only: sort the centre's edges by key into the final arrays at the same slots (rank
-  // of each key among the centre's keys; keys are unique within a centre)
   __syncwarp();
-  const unsigned long long* src = n <= kFillSortStage ? skeys[w] : key + pad;
-  for (int q0 = 0; q0 < n; q0 += kFillSortPer * kWarp) {
-    unsigned long long kk[kFillSortPer];
-    int nb[kFillSortPer], rank[kFillSortPer];
-    typename Vec4<Real>::type dd[kFillSortPer];
-#pragma unroll
-    for (int u = 0; u < kFillSortPer; ++u) {
-      const int q = q0 + u * kWarp + lane;
-      kk[u] = ~0ull;
-      rank[u] = 0;
-      if (q < n) {
-        kk[u] = src[q];
-        nb[u] = nbr[pad + q];
-        dd[u] = d4[pad + q];
-      }
-    }
-    for (int t = 0; t < n; ++t) {
-      const unsigned long long kt = src[t];
-#pragma unroll
-      for (int u = 0; u < kFillSortPer; ++u) rank[u] += kt < kk[u];
-    }
-#pragma unroll
-    for (int u = 0; u < kFillSortPer; ++u) {
-      if (q0 + u * kWarp + lane < n) {
-        key_out[pad + rank[u]] = kk[u];
-        nbr_out[pad + rank[u]] = nb[u];
-        d4_out[pad + rank[u]] = dd[u];
-      }
-    }
-  }
+  sort_centre_edges<Real>(lane, n, pad, skeys[w], key, nbr, d4, key_out, nbr_out, d4_out);
   if (lane == 0) {
     row[i] = static_cast<int>(pad);
     row_end[i] = static_cast<int>(pad) + n;
   }
 }
 
-// Sort one centre's edges by key into CSR order (warp per centre, rank sort; keys within a centre
-// are unique).  Cell-list centres read their padded staging slots, the others their CSR range of
-// the staging buffers (plans may be null when no frame uses cell lists).  Keys of centres with at
-// most `stage` edges are staged in shared memory (the rank loop then reads broadcast shared
-// memory); longer lists rank from global memory.
+// Periodic frames too small for cell lists (a perpendicular width below 3 r_c, or at most 512
+// atoms): warp per centre i, lanes over the frame's atoms j.  For each j the image range per axis
+// is ceil(-f - reach) .. floor(-f + reach), f = (x_j - x_i) . inv(cell), and every image n in it
+// is tested exactly in FP64 (r^2 = |x_j + n.cell - x_i|^2 < r_c^2).  Accepted edges take the
+// centre's next padded slot (a shared-memory counter) and are then sorted by (j, n) like the
+// cell-list edges, so every periodic batch ends in the same padded layout without host
+// synchronisation; a count above cap raises *overflow as in the cell-list kernel.
+template <typename Real>
+__global__ void __launch_bounds__(kFillWarps * kWarp)
+k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2, int* counts,
+                  int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error, int* row,
+                  int* row_end, unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
+  __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
+  __shared__ int cursor[kFillWarps];
+  const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
+  if (i >= natoms) return;
+  const FramePlan& fp = plans[frame_of[i]];
+  if (fp.use_bins) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x / kWarp;
+  const long long pad = fp.pad0 + static_cast<long long>(i - fp.a0) * fp.cap;
+  const int cap = fp.cap;
+  if (lane == 0) cursor[w] = 0;
+  __syncwarp();
+  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  const double* c = fp.cell;
+  const double* inv = fp.inv;
+  for (int j = fp.a0 + lane; j < fp.a1; j += kWarp) {
+    const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
+    int lo[3], hi[3];
+    for (int q = 0; q < 3; ++q) {
+      const double f = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
+      lo[q] = static_cast<int>(ceil(-f - fp.reach[q]));
+      hi[q] = static_cast<int>(floor(-f + fp.reach[q]));
+    }
+    for (int a = lo[0]; a <= hi[0]; ++a)
+      for (int b = lo[1]; b <= hi[1]; ++b)
+        for (int cc = lo[2]; cc <= hi[2]; ++cc) {
+          if (i == j && a == 0 && b == 0 && cc == 0) continue;
+          const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
+          const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
+          const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
+          const double r2 = vx * vx + vy * vy + vz * vz;
+          if (!(r2 < rc2)) continue;
+          if (a < -64 || a > 63 || b < -64 || b > 63 || cc < -64 || cc > 63) { record_error(error, kErrImageRange); continue; }
+          const int k = atomicAdd(&cursor[w], 1);
+          if (k < cap) {
+            write_edge<Real>(pad + k, j, a, b, cc, vx, vy, vz, r2, nbr, d4, key);
+            if (k < kFillSortStage) skeys[w][k] = edge_key(j, a, b, cc);
+          }
+        }
+  }
+  __syncwarp();
+  const int total = cursor[w], n = min(total, cap);
+  if (lane == 0) {
+    counts[i] = n;
+    if (total > cap) atomicMax(overflow, total);
+  }
+  sort_centre_edges<Real>(lane, n, pad, skeys[w], key, nbr, d4, key_out, nbr_out, d4_out);
+  if (lane == 0) {
+    row[i] = static_cast<int>(pad);
+    row_end[i] = static_cast<int>(pad) + n;
+  }
+}
+
+// Sort one centre's edges of a user edge list by key into CSR order (warp per centre, rank sort;
+// keys within a centre are unique).  Keys of centres with at most `stage` edges are staged in
+// shared memory (the rank loop then reads broadcast shared memory); longer lists rank from global
+// memory.  Periodic batches are sorted inside their fill kernels.
 constexpr int kSortWarps = 8;
 template <typename Real>
 __global__ void __launch_bounds__(kSortWarps * kWarp)
-k_edge_sort(int* row, int* row_end, const int* counts, int natoms, const FramePlan* plans, const int* frame_of,
-            int stage, const unsigned long long* key_in, const int* nbr_in, const typename Vec4<Real>::type* d4_in,
-            const unsigned long long* pkey, const int* pnbr, const typename Vec4<Real>::type* pd4,
-            unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
+k_edge_sort(const int* row, int natoms, int stage, const unsigned long long* key_in, const int* nbr_in,
+            const typename Vec4<Real>::type* d4_in, unsigned long long* key_out, int* nbr_out,
+            typename Vec4<Real>::type* d4_out) {
   extern __shared__ unsigned long long sort_keys[];
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
-  // row_end == null: CSR output at row[i] .. row[i + 1]; otherwise (cell lists only) the sorted
-  // edges stay in the centre's padded slots and the row bounds are written here
-  int e0, n;
-  long long in0;
+  const int e0 = row[warp], n = row[warp + 1] - e0;
+  const long long in0 = e0;
   const unsigned long long* K = key_in;
   const int* NB = nbr_in;
   const typename Vec4<Real>::type* D = d4_in;
-  if (row_end) {
-    const FramePlan& fp = plans[frame_of[warp]];
-    in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
-    e0 = static_cast<int>(in0);
-    n = counts[warp];
-    K = pkey; NB = pnbr; D = pd4;
-    if (lane == 0) { row[warp] = e0; row_end[warp] = e0 + n; }
-  } else {
-    e0 = row[warp];
-    n = row[warp + 1] - e0;
-    in0 = e0;
-    if (plans) {
-      const FramePlan& fp = plans[frame_of[warp]];
-      if (fp.use_bins) {
-        in0 = fp.pad0 + static_cast<long long>(warp - fp.a0) * fp.cap;
-        K = pkey; NB = pnbr; D = pd4;
-      }
-    }
-  }
   const unsigned long long* src = K + in0;
   if (n <= stage) {
     unsigned long long* sk = sort_keys + (threadIdx.x / kWarp) * stage;
@@ -1084,18 +1105,19 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       fp.lo2 = static_cast<float>(rc2 * (1.0 - 1e-4));
       fp.hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
       bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
-      // padded staging capacity: cap_scale x the mean neighbour count of the frame's density + 64
-      const double c = fp.cell[0] * (fp.cell[4] * fp.cell[8] - fp.cell[5] * fp.cell[7]) -
-                       fp.cell[1] * (fp.cell[3] * fp.cell[8] - fp.cell[5] * fp.cell[6]) +
-                       fp.cell[2] * (fp.cell[3] * fp.cell[7] - fp.cell[4] * fp.cell[6]);
-      const double mean = frame_natoms[f] / std::abs(c) * (4.0 / 3.0) * 3.141592653589793 * rc * rc2;
-      fp.cap = std::max(min_cap_, static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0)));
       // bin capacity: twice the frame's mean atoms per bin plus 8 (grown after an overflow)
       const double per_bin = frame_natoms[f] / static_cast<double>(fp.nb[0] * fp.nb[1] * fp.nb[2]);
       bin_cap = std::max(bin_cap, static_cast<int>(std::min(1.0e6, std::ceil(bin_cap_scale_ * per_bin) + 8.0)));
-      fp.pad0 = pad_total;
-      pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
     }
+    // padded edge slots of every frame: cap_scale x the mean neighbour count of the frame's density
+    // + 64 per centre (grown after an overflow)
+    const double vol = std::abs(fp.cell[0] * (fp.cell[4] * fp.cell[8] - fp.cell[5] * fp.cell[7]) -
+                                fp.cell[1] * (fp.cell[3] * fp.cell[8] - fp.cell[5] * fp.cell[6]) +
+                                fp.cell[2] * (fp.cell[3] * fp.cell[7] - fp.cell[4] * fp.cell[6]));
+    const double mean = vol > 0 ? frame_natoms[f] / vol * (4.0 / 3.0) * 3.141592653589793 * rc * rc2 : 0.0;
+    fp.cap = std::max(min_cap_, static_cast<int>(std::min(1.0e6, std::ceil(cap_scale_ * mean) + 64.0)));
+    fp.pad0 = pad_total;
+    pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
   }
   natoms_ = ncentres_ = a;
   nframes_ = nframes;
@@ -1117,7 +1139,6 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     bin_count_.ensure(sizeof(int) * (bins + 1));
     if (bin_count_.ptr != before) bin_zeroed_ = 0;
   }
-  bin_start_.ensure(sizeof(int) * (bins + 1));
   DevBuf& bin_of = bin_of_;
   bin_of.ensure(sizeof(int) * std::max(1, a));
   // batches with cell lists only: the binning kernel finds each atom's frame itself
@@ -1144,129 +1165,65 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                                                bin_posf_.as<BinPosF>(), error_.as<int>() + 2);
     ++launches_;
   }
-  const unsigned thread_blocks = static_cast<unsigned>((a + 127) / 128);
   const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);
   const size_t rsz = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
   const FramePlan* P = plan_.as<FramePlan>();
   const int* FO = frame_of_.as<int>();
-  const int *BS = bin_start_.as<int>(), *BO = bin_of.as<int>();
+  const int* BO = bin_of.as<int>();
   const BinAtom* BR = bin_rec_.as<BinAtom>();
   const BinPos* BP = bin_pos_.as<BinPos>();
   const BinPosF* BPF = bin_posf_.as<BinPosF>();
   const AtomFrac* FR = frac_.as<AtomFrac>();
   const AtomOff* OF = off_.as<AtomOff>();
   int* overflow = error_.as<int>() + 1;
-  // cell-list frames: one pass into padded staging slots (repeated with a larger capacity on overflow)
-  // cell-list batches sort each centre's edges inside the fill kernel, into the final arrays
-  const bool fused = bins && bins_frames_ == nframes;
-  auto fill_bins = [&]() {
-    const size_t slots = static_cast<size_t>(std::max<long long>(1, pad_total));
-    pad_nbr_.ensure(sizeof(int) * slots);
-    pad_d4_.ensure(rsz * slots);
-    pad_key_.ensure(sizeof(unsigned long long) * slots);
-    if (fused) {
-      nbr_.ensure(sizeof(int) * slots);
-      d4_.ensure(rsz * slots);
-      key_.ensure(sizeof(unsigned long long) * slots);
-      row_end_.ensure(sizeof(int) * std::max(1, a));
-    }
-    int* RW = fused ? row_.as<int>() : nullptr;
-    int* RE = fused ? row_end_.as<int>() : nullptr;
-    unsigned long long* KO = fused ? key_.as<unsigned long long>() : nullptr;
-    int* NO = fused ? nbr_.as<int>() : nullptr;
-    // the overflow word is zero between steps (the step's error check clears it after an
-    // overflow); the host-synchronised retry below re-arms it itself
-    if (!fused) SUS2G_CUDA(cudaMemsetAsync(overflow, 0, sizeof(int), s));
-    if (precision_ == kFP32)
-      k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
-          P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
-          counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), overflow,
-          error_.as<int>(), RW, RE, KO, NO, fused ? d4_.as<EdgeF>() : nullptr);
-    else
-      k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
-          P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
-          counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), overflow,
-          error_.as<int>(), RW, RE, KO, NO, fused ? d4_.as<EdgeD>() : nullptr);
-    ++launches_;
-  };
+  // every periodic batch: the fill kernels (cell lists and image scan) write each centre's edges
+  // to its padded slots and sort them there into the final arrays; no compaction, no host
+  // synchronisation.  The edge arrays are sized by the padded capacity, the exact total is the sum
+  // of the counts, and an overflow is reported by the step's check_device_error.
+  const size_t slots = static_cast<size_t>(std::max<long long>(1, pad_total));
+  if (pad_total > 2147483647LL) throw Error(4, "edge build: more than 2^31 - 1 edge slots");
+  pad_nbr_.ensure(sizeof(int) * slots);
+  pad_d4_.ensure(rsz * slots);
+  pad_key_.ensure(sizeof(unsigned long long) * slots);
+  nbr_.ensure(sizeof(int) * slots);
+  rev_.ensure(sizeof(int) * slots);
+  d4_.ensure(rsz * slots);
+  key_.ensure(sizeof(unsigned long long) * slots);
+  row_end_.ensure(sizeof(int) * std::max(1, a));
   if (a) {
-    // (every centre's count is written by the fill kernels; the CSR scan also reads entry a)
-    if (!fused) SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (a + 1), s));
-    if (bins) fill_bins();
+    int* RW = row_.as<int>();
+    int* RE = row_end_.as<int>();
+    unsigned long long* KO = key_.as<unsigned long long>();
+    int* NO = nbr_.as<int>();
+    if (bins) {
+      if (precision_ == kFP32)
+        k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+            P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
+            counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), overflow,
+            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>());
+      else
+        k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+            P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
+            counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), overflow,
+            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>());
+      ++launches_;
+    }
     if (bins_frames_ < nframes) {
-      k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, counts_.as<int>(), error_.as<int>());
+      if (precision_ == kFP32)
+        k_edge_image_fill<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+            P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>());
+      else
+        k_edge_image_fill<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+            P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>());
       ++launches_;
     }
   }
-  long long total = 0;
-  if (bins_frames_ == nframes) {
-    // cell lists only: no host synchronisation and no CSR compaction.  The sorted edges stay in
-    // their centres' padded slots (row[i] .. row_end[i]); the edge arrays are sized by the padded
-    // capacity, the exact total is the sum of the counts, and an overflow is reported by the
-    // step's check_device_error.
-    total = pad_total;
-    nedges_exact_ = false;
-    padded_ = true;
-  } else {
-    for (int attempt = 0;; ++attempt) {
-      k_exclusive_scan<<<1, 1024, 0, s>>>(counts_.as<int>(), a, row_.as<int>(), error_.as<int>());
-      ++launches_;
-      // the edge total sizes the edge arrays (image-scan frames have no capacity bound), and the
-      // overflow word says whether a cell-list centre had more edges than its padded capacity
-      SUS2G_CUDA(cudaMemcpyAsync(host_total_, row_.as<int>() + a, sizeof(int), cudaMemcpyDeviceToHost, s));
-      SUS2G_CUDA(cudaMemcpyAsync(host_total_ + 1, overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
-      SUS2G_CUDA(cudaStreamSynchronize(s));
-      total = host_total_[0];
-      const int over = bins ? host_total_[1] : 0;
-      if (over <= 0) break;
-      if (attempt >= 8) throw Error(4, "edge build: padded capacity did not converge");
-      // grow every cell-list frame's capacity to at least the largest count seen, and re-run
-      cap_scale_ *= 2.0;
-      min_cap_ = std::max(min_cap_, over);
-      pad_total = 0;
-      for (int f = 0; f < nframes; ++f) {
-        FramePlan& fp = plans[f];
-        if (!fp.use_bins) continue;
-        fp.cap = std::max(2 * fp.cap, over);
-        fp.pad0 = pad_total;
-        pad_total += static_cast<long long>(frame_natoms[f]) * fp.cap;
-      }
-      SUS2G_CUDA(cudaMemcpyAsync(plan_.ptr, plans.data(), sizeof(FramePlan) * nframes, cudaMemcpyHostToDevice, s));
-      fill_bins();
-      if (bins_frames_ < nframes) {
-        k_edge_count<<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, counts_.as<int>(), error_.as<int>());
-        ++launches_;
-      }
-      SUS2G_CUDA(cudaStreamSynchronize(s));  // the plans' host copy is reused by the next attempt
-    }
-    nedges_exact_ = true;
-    padded_ = false;
-  }
-  if (total > 2147483647LL) throw Error(4, "edge build: more than 2^31 - 1 edge slots");
-  nedges_ = total;
-  if (nedges_exact_) exact_edges_ = total;
-  const size_t E = std::max<long long>(1, total);
-  nbr_.ensure(sizeof(int) * E);
-  rev_.ensure(sizeof(int) * E);
-  d4_.ensure(rsz * E);
-  key_.ensure(sizeof(unsigned long long) * E);
-  if (!fused) {
-    // CSR staging of the image-scan frames (and the merge of mixed batches)
-    tmp_nbr_.ensure(sizeof(int) * E);
-    tmp_d4_.ensure(rsz * E);
-    tmp_key_.ensure(sizeof(unsigned long long) * E);
-  }
-  if (a && bins_frames_ < nframes) {
-    unsigned long long* KY = tmp_key_.as<unsigned long long>();
-    if (precision_ == kFP32)
-      k_edge_fill<float><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, row_.as<int>(),
-                                                       tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), KY, error_.as<int>());
-    else
-      k_edge_fill<double><<<thread_blocks, 128, 0, s>>>(P, FO, d_pos, a, rc2, BS, BO, FR, OF, row_.as<int>(),
-                                                        tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), KY, error_.as<int>());
-    ++launches_;
-  }
-  sort_from_pad_ = bins > 0;
+  nedges_ = pad_total;
+  nedges_exact_ = false;
+  padded_ = true;
+  clear_bins_ = bins > 0;
   finalize_edges();
   mark_end();
 }
@@ -1274,26 +1231,19 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
 void Engine::finalize_edges() {
   cudaStream_t s = stream_;
   const int a = ncentres_;
-  // (cell-list batches were sorted by the fill kernel)
+  // (periodic batches were sorted by their fill kernels)
   if (a && !padded_) {
     const int blocks = (a + kSortWarps - 1) / kSortWarps;
-    const FramePlan* P = sort_from_pad_ ? plan_.as<FramePlan>() : nullptr;
-    // shared-memory key staging up to the largest padded capacity (at most 512 keys per warp)
-    int stage = 0;
-    if (sort_from_pad_)
-      for (const FramePlan& fp : *plans_) stage = std::max(stage, fp.use_bins ? fp.cap : 0);
-    stage = std::min(stage, 512);
+    // centres with at most 128 edges rank from shared memory
+    constexpr int stage = 128;
     const size_t smem = sizeof(unsigned long long) * kSortWarps * stage;
-    int* RE = padded_ ? row_end_.as<int>() : nullptr;
     if (precision_ == kFP32)
       k_edge_sort<float><<<blocks, kSortWarps * kWarp, smem, s>>>(
-          row_.as<int>(), RE, counts_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
-          tmp_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+          row_.as<int>(), a, stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(),
           key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeF>());
     else
       k_edge_sort<double><<<blocks, kSortWarps * kWarp, smem, s>>>(
-          row_.as<int>(), RE, counts_.as<int>(), a, P, frame_of_.as<int>(), stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(),
-          tmp_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+          row_.as<int>(), a, stage, tmp_key_.as<unsigned long long>(), tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(),
           key_.as<unsigned long long>(), nbr_.as<int>(), d4_.as<EdgeD>());
     ++launches_;
   }
@@ -1332,9 +1282,9 @@ void Engine::finalize_edges() {
     }
     k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, rs>>>(
         row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>(),
-        bin_count_.as<int>(), sort_from_pad_ ? bins_used_ : 0);
+        bin_count_.as<int>(), clear_bins_ ? bins_used_ : 0);
     ++launches_;
-    if (sort_from_pad_) bin_zeroed_ = bins_used_;
+    if (clear_bins_) bin_zeroed_ = bins_used_;
     if (rs != s) {
       SUS2G_CUDA(cudaEventRecord(ev_rev_, rs));
       rev_pending_ = true;
@@ -1345,7 +1295,7 @@ void Engine::finalize_edges() {
 void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, const int* d_i, const int* d_j, const double* d_d) {
   SUS2G_CUDA(cudaSetDevice(device_));
   ++edge_generation_;
-  sort_from_pad_ = false;
+  clear_bins_ = false;
   padded_ = false;
   if (nowned < 0 || nall < nowned || nedges < 0) throw Error(1, "invalid atom layout");
   cudaStream_t s = stream_;
@@ -1829,9 +1779,9 @@ void Engine::step_frames(int nframes, const int* frame_natoms, const double* cel
     nedges_exact_ = false;
     return;
   }
-  // cell-list batches build their edges without host synchronisation: the second step of a
-  // layout is captured and launched, later ones replay (a one-off layout is never captured)
-  if (same && nframes > 0 && bins_frames_ == nframes) {
+  // periodic batches build their edges without host synchronisation: the second step of a layout
+  // is captured and launched, later ones replay (a one-off layout is never captured)
+  if (same && nframes > 0) {
     reset_step_graph();
     const int before = launches_;
     capturing_ = true;

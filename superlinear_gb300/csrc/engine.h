@@ -203,7 +203,7 @@ class Engine {
   bool padded_ = false;         // cell-list batch: edges left in padded per-centre slots (row_end_)
   int bin_zeroed_ = 0;          // leading bin counters known to be zero on the device
   int bins_used_ = 0;           // bin counters used by the current cell-list build
-  DevBuf bin_count_, bin_start_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
+  DevBuf bin_count_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather
   DevBuf hbar_atom_, bin_of_, frac_, off_, in_row_, in_edge_;  // in_*: caller edges grouped by neighbour
@@ -211,7 +211,7 @@ class Engine {
   double cap_scale_ = 2.0;      // padded capacity = cap_scale x mean neighbour count + 64 (grows on overflow)
   double bin_cap_scale_ = 2.0;  // bin capacity = bin_cap_scale x mean atoms per bin + 8 (grows on overflow)
   int min_bin_cap_ = 0;          // lower bound of the bin capacity after an overflow
-  bool sort_from_pad_ = false;
+  bool clear_bins_ = false;
   int* host_total_ = nullptr;   // pinned [4]
   // stage timer (cudaEvent pairs per stage, enabled by set_timing)
   bool timing_ = false;

@@ -56,41 +56,6 @@ __device__ __forceinline__ unsigned long long edge_key(int j, int n0, int n1, in
          static_cast<unsigned long long>(n2 + 64);
 }
 
-// Image scan of centre i (frames without cell lists): for each j of the frame the image range
-// ceil(-f - reach) .. floor(-f + reach) per axis, f = (x_j - x_i) . inv(cell); Emit(j, n0, n1, n2,
-// dx, dy, dz, r2) for every image inside the cutoff.  The per-centre order is fixed afterwards by
-// sorting on the (j, n) key.
-template <typename Emit>
-__device__ __forceinline__ void enumerate_edges(int i, const FramePlan& fp, const double* pos, double rc2, int* error,
-                                                Emit&& emit) {
-  const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
-  const double* c = fp.cell;
-  const double* inv = fp.inv;
-  for (int j = fp.a0; j < fp.a1; ++j) {
-    const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
-    double f[3];
-    int lo[3], hi[3];
-    for (int q = 0; q < 3; ++q) {
-      f[q] = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
-      lo[q] = static_cast<int>(ceil(-f[q] - fp.reach[q]));
-      hi[q] = static_cast<int>(floor(-f[q] + fp.reach[q]));
-    }
-    for (int a = lo[0]; a <= hi[0]; ++a)
-      for (int b = lo[1]; b <= hi[1]; ++b)
-        for (int cc = lo[2]; cc <= hi[2]; ++cc) {
-          if (i == j && a == 0 && b == 0 && cc == 0) continue;
-          const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
-          const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
-          const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
-          const double r2 = vx * vx + vy * vy + vz * vz;
-          if (r2 < rc2) {
-            if (a < -64 || a > 63 || b < -64 || b > 63 || cc < -64 || cc > 63) { record_error(error, kErrImageRange); continue; }
-            emit(j, a, b, cc, vx, vy, vz, r2);
-          }
-        }
-  }
-}
-
 // Cell-list frames, one warp per centre i.  Bins are at least r_c / 2 wide, so every neighbour lies
 // in the 5 x 5 x 5 bins around the centre's bin (about 2.3x fewer candidates than 27 bins of width
 // r_c).  Each lane owns four of those 125 bins and walks their atoms, two candidates per
