@@ -11,7 +11,9 @@ eager steps under the stage timer.  The inputs are smaller than L2, so L2 is flu
 write) between timed steps, outside the step's events.
 
 The training loss + gradient throughput (frames/s, FP32 bulk vs FP64 plain) over a batch of 256
-uneven Effect L3/K4/R2/O2 frames is reported alongside under "train_effect_l3k4r2o2_256".
+uneven Effect L3/K4/R2/O2 frames is reported alongside under "train_effect_l3k4r2o2_256", and the
+same for 2,048 Effect L5/K8/R2/O2 frames with three species (sizes log-uniform in [16, 512], plus
+timed BFGS iterations) under "train_effect_l5k8r2o2_2048".
 
 --impl reference times the CPU reference path on the host cores instead: the FP64 CPU
 restatement of the reference algorithm (the reference's own sources do not travel to the GPU
@@ -42,7 +44,8 @@ METRIC = "atom-steps/s E/F/virial; train loss+grad frames/s; FP32-bulk vs FP64, 
 MODEL = os.path.join(ROOT, "tests", "golden", "models", "static_l3k4o2.sus2")
 EFFECT_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l4k8r2o3.sus2")
 TRAIN_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l3k4r2o2.sus2")
-TRAIN_WEIGHTS = (1.0, 0.01, 0.0)  # energy + force MSE
+C5_MODEL = os.path.join(ROOT, "tests", "golden", "models", "effect_l5k8r2o2_c3.sus2")
+TRAIN_WEIGHTS = (1.0, 0.01, 0.001)  # energy + force + stress MSE (the example training profile's weights)
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "dram_traffic.txt")
 
@@ -256,6 +259,70 @@ def bench_training(sg, torch, steps, warmup):
     out["fp32_error"] = {"loss_rel": abs(l32 - l64) / abs(l64),
                          "grad_rel_norm": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))}
     return frames, out
+
+
+def config5_set(sg, nframes=2048, seed=53):
+    """2,048 uneven periodic frames (sizes log-uniform in [16, 512], fcc/bcc/diamond, a in
+    [2.8, 4.5] A, sigma 0.15 A, three species uniform) labelled by a teacher of the same Effect
+    L5/K8/R2/O2 topology at 2% perturbed parameters (FP64 GPU evaluation, outside any timed region)."""
+    from superlinear_gb300.synth import training_frames
+    frames = training_frames(nframes, 16, 512, 2.8, 4.5, 0.15, seed=seed, species=3, log_uniform=True)
+    teacher = sg.Model(C5_MODEL)
+    p0 = teacher.params()
+    teacher.set_params(p0 * (1 + 0.02 * np.random.default_rng(seed + 1).normal(size=p0.size)))
+    e, f, v, _ = sg.Engine(teacher, 0, sg.FP64).calc_efs(frames)
+    a = 0
+    for k, fr in enumerate(frames):
+        fr.energy = float(e[k])
+        fr.forces = f[a:a + fr.natoms].copy()
+        xx, yy, zz, xy, xz, yz = v[k]
+        fr.stress = np.array([[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]])
+        a += fr.natoms
+    return frames
+
+
+def bench_config5(sg, torch, steps, warmup, bfgs_iters):
+    """Loss + gradient frames/s over the 2,048-frame L5 batch (FP32 bulk and FP64 plain, one step =
+    one Trainer.loss_grad as a BFGS iteration calls it), then bfgs_iters BFGS iterations in FP32
+    (each: line-search evaluations through the captured loss+gradient graph and the device-side
+    inverse-Hessian update)."""
+    frames = config5_set(sg)
+    model = sg.Model(C5_MODEL)
+    p = model.params()
+    out = {"workload": "effect_l5k8r2o2_c3_train2048", "frames": len(frames),
+           "atoms": int(sum(f.natoms for f in frames)),
+           "weights": {"energy": TRAIN_WEIGHTS[0], "force": TRAIN_WEIGHTS[1], "stress": TRAIN_WEIGHTS[2]}}
+    losses = {}
+    for prec, key, nw, nsteps in ((sg.FP32, "fp32", warmup, steps), (sg.FP64, "fp64", 1, 2)):
+        eng = sg.Engine(model, 0, prec)
+        tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
+        tr.loss_grad(p)
+        out.setdefault("autotune", {})[key] = {q: c[0] for q, c in eng.autotune(reps=1).items()}
+        for _ in range(nw):
+            tr.loss_grad(p)
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(nsteps):
+            t0 = time.perf_counter()
+            loss, g = tr.loss_grad(p)
+            t.append(time.perf_counter() - t0)
+        ms = 1e3 * float(np.mean(t))
+        losses[key] = (loss, g)
+        out[key] = {"ms_per_step": ms, "frames_per_s": len(frames) / (ms / 1e3), "edges": eng.edge_count()}
+        if prec == sg.FP32 and bfgs_iters > 0:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            _, hist = tr.bfgs(p, max_iter=bfgs_iters)
+            dt = time.perf_counter() - t0
+            out["bfgs_fp32"] = {"iterations": int(hist.size - 1), "seconds": dt,
+                                "ms_per_iteration": 1e3 * dt / max(1, hist.size - 1),
+                                "loss_first": float(hist[0]), "loss_last": float(hist[-1])}
+        del tr, eng
+    out["fp32_over_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
+    (l32, g32), (l64, g64) = losses["fp32"], losses["fp64"]
+    out["fp32_error"] = {"loss_rel": abs(l32 - l64) / abs(l64),
+                         "grad_rel_norm": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))}
+    return out
 
 
 def cpu_train_sample(frames, min_seconds=8.0):
@@ -541,6 +608,11 @@ def run_ours(args):
                                  "sample": f"loss + gradient of the first {nd} frames of the batch by the FP64 "
                                            "CPU restatement (one thread)"}
 
+    # training loss + gradient and BFGS over the 2,048-frame Effect L5/K8/R2/O2 batch
+    c5 = None
+    if not args.skip_config5:
+        c5 = bench_config5(sg, torch, 3, 3, args.bfgs_iters)
+
     line = {
         "metric": METRIC, "value": n * world / (ms32 / 1e3), "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
@@ -578,6 +650,7 @@ def run_ours(args):
         "autotune": {k: {p: c[0] for p, c in v.items()} for k, v in tuned.items()},
         "effect_l4k8r2o3_110592": extra or None,
         "train_effect_l3k4r2o2_256": train,
+        "train_effect_l5k8r2o2_2048": c5,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -601,6 +674,11 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="with --profile-train: eager launches instead of the graph")
     ap.add_argument("--profile-effect", action="store_true",
                     help="only FP32 Effect L4/K8/R2/O3 steps on a --cells diamond (for ncu captures)")
+    ap.add_argument("--skip-config5", action="store_true",
+                    help="skip the 2,048-frame L5 training loss+gradient and BFGS measurement")
+    ap.add_argument("--bfgs-iters", type=int, default=10, help="timed FP32 BFGS iterations on the L5 batch")
+    ap.add_argument("--config5-only", action="store_true",
+                    help="only the 2,048-frame L5 training measurement; prints its JSON object")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -610,6 +688,12 @@ def main():
         return run_profile_train(args)
     if args.profile_effect:
         return run_profile_effect(args)
+    if args.config5_only:
+        import torch
+
+        import superlinear_gb300 as sg
+        print(json.dumps(bench_config5(sg, torch, 3, 3, args.bfgs_iters)), flush=True)
+        return 0
     return run_ours(args)
 
 

@@ -220,6 +220,12 @@ int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
 int sus2g_trainer_bfgs(sus2g_trainer trainer, double* params, int max_iter, double gtol, double* history,
                        int* steps);
 
+/* Initial inverse Hessian of the following sus2g_trainer_bfgs calls: diag[n] (n = the parameter
+ * count; finite, positive) on the diagonal, zero elsewhere; n = 0 restores the identity.  Replaces
+ * BFGS::SetInvHessDiagonal (src/common/bfgs.h:395), which the reference trainer calls with its
+ * per-coefficient scaling before BFGS (dev_src/mtpr_trainer.cpp:4011-4072). */
+int sus2g_trainer_set_inv_hess_diagonal(sus2g_trainer trainer, const double* diag, int n);
+
 /* ---- allocation-free Static E / F / virial ------------------------------------------------------
  * No counterpart in the reference: this entry point exists for callers that cannot allocate device
  * memory during a step -- code recording into a CUDA stream capture, MD drivers whose device memory

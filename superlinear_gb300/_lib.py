@@ -66,6 +66,7 @@ SIGNATURES = {
     "sus2g_trainer_metrics": (ctypes.c_int, [_vp, _dp, _dp]),
     "sus2g_trainer_train_linear": (ctypes.c_int, [_vp, _dp]),
     "sus2g_trainer_bfgs": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_double, _dp, _ip]),
+    "sus2g_trainer_set_inv_hess_diagonal": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
 }
 
 _lib = None

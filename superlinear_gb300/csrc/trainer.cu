@@ -389,6 +389,13 @@ __global__ void k_scaled_identity(int n, double* H, double diag) {
   H[t] = i == j ? diag : 0.0;
 }
 
+__global__ void k_diagonal_matrix(int n, double* H, const double* diag) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * n) return;
+  const int i = static_cast<int>(t / n), j = static_cast<int>(t - static_cast<long long>(i) * n);
+  H[t] = i == j ? diag[i] : 0.0;
+}
+
 __global__ void k_axpy_to(int n, const double* x, double a, const double* p, double* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = x[i] + a * p[i];
@@ -551,17 +558,30 @@ class Trainer {
   }
 
   // Dense BFGS on the device (BFGS::Iterate / UpdateInvHess, src/common/bfgs.cpp:251-329, 428-502):
-  // H starts at the identity (BFGS::Restart, bfgs.cpp:529-534); each iteration takes p = -H g, a line
-  // search x + a p from a = 1 until the strong Wolfe conditions f <= f0 + c1 a p.g0 and
-  // |p.g| <= c2 |p.g0| hold (c1 = 0.1, c2 = 0.5, bfgs.h:384-385), then the rank-2 update of H with
-  // s = a p, y = g - g0, skipped when s.y <= 64 eps.  The trial points bracket by doubling and
-  // bisection (the reference interpolates inside its bracket; accepted points satisfy the same
-  // conditions).  params (host) in/out; history[max_iter + 1] receives the loss after each
-  // accepted step (history[0] = initial).  Returns the number of accepted steps.
+  // H starts at the identity, or at the diagonal given by set_inv_hess_diagonal (BFGS::Restart and
+  // SetInvHessDiagonal, bfgs.cpp:529-534, bfgs.h:395); each iteration takes p = -H g, a line search
+  // x + a p from a = 1 until the strong Wolfe conditions f <= f0 + c1 a p.g0 and |p.g| <= c2 |p.g0|
+  // hold (c1 = 0.1, c2 = 0.5, bfgs.h:384-385), then the rank-2 update of H with s = a p,
+  // y = g - g0, skipped when s.y <= 64 eps.  params (host) in/out; history[max_iter + 1] receives
+  // the loss after each accepted step (history[0] = initial).  Returns the number of accepted steps.
+  //
+  // Trial steps (a bracketing search that interpolates, as Linesearch::Iterate, bfgs.h:100-290,
+  // does; every trial has the loss and its slope p.g).  lo = the last trial with sufficient
+  // decrease and a negative slope (initially a = 0), hi = the first trial past the minimum:
+  //   * sufficient decrease fails: hi = a; next = the minimiser of the parabola through f(lo),
+  //     the slope at lo and f(a), kept within lo + [0.01, 0.5] (a - lo); a non-finite loss takes
+  //     a quarter of the step (ReduceStep(0.25) in BFGS::Iterate);
+  //   * slope still negative and steep: lo = a; inside a bracket as below, else the zero of the
+  //     secant through the slopes at the previous lo and a, kept within [2a, 8a];
+  //   * slope positive and steep: hi = a; next = the zero of the secant through the slopes at lo
+  //     and hi, kept within lo + [0.1, 0.9] (hi - lo) (the parabola again when hi failed the
+  //     decrease test).
+  void set_inv_hess_diagonal(const double* diag, int n) { h0_diag_.assign(diag, diag + n); }
+
   int bfgs(double* params, int max_iter, double gtol, double* history) {
     const int n = nparams_;
     cudaStream_t s = eng_.stream();
-    DevBuf H, x, g, p, xn, gn, sv, yv, Hy, sc;
+    DevBuf H, x, g, p, xn, gn, sv, yv, Hy, sc, dg;
     H.ensure(sizeof(double) * static_cast<size_t>(n) * n);
     for (DevBuf* b : {&x, &g, &p, &xn, &gn, &sv, &yv, &Hy}) b->ensure(sizeof(double) * n);
     sc.ensure(sizeof(double) * 8);
@@ -578,7 +598,13 @@ class Trainer {
     double f = loss_grad(xh.data(), nullptr);
     TRAIN_CUDA(cudaMemcpyAsync(x.ptr, xh.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
     TRAIN_CUDA(cudaMemcpyAsync(g.ptr, grad_.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    k_scaled_identity<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), 1.0);
+    if (static_cast<int>(h0_diag_.size()) == n && n) {
+      dg.ensure(sizeof(double) * n);
+      TRAIN_CUDA(cudaMemcpyAsync(dg.ptr, h0_diag_.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      k_diagonal_matrix<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), dg.as<double>());
+    } else {
+      k_scaled_identity<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), 1.0);
+    }
     if (history) history[0] = f;
     int accepted = 0;
     const double c1 = 0.1, c2 = 0.5, floor = 64.0 * 2.220446049250313e-16;
@@ -587,8 +613,26 @@ class Trainer {
       k_symv<<<row_blocks, 256, 0, s>>>(n, H.as<double>(), g.as<double>(), -1.0, p.as<double>());
       const double gp = dot(g.as<double>(), p.as<double>());
       if (!(gp < 0)) throw Error(5, "BFGS: search direction is not a descent direction");
-      double alpha = 1.0, lo = 0.0, hi = -1.0, fn = f;
+      double alpha = 1.0, fn = f;
+      double lo = 0.0, f_lo = f, g_lo = gp;             // bracket start: sufficient decrease, slope < 0
+      double hi = -1.0, f_hi = 0.0, g_hi = 0.0;         // bracket end (hi < 0: none yet)
+      bool hi_failed = false;                            // hi failed the sufficient-decrease test
       bool ok = false;
+      // the parabola through f(lo), the slope at lo and f(b), minimised, within lo + [0.01, 0.5] (b - lo)
+      auto parabola = [&](double b, double fb) {
+        const double d = b - lo, den = 2.0 * (fb - f_lo - g_lo * d);
+        if (!std::isfinite(fb)) return lo + 0.25 * d;
+        double t = den > 0 ? lo - g_lo * d * d / den : lo + 0.5 * d;
+        if (!std::isfinite(t)) t = lo + 0.5 * d;
+        return std::min(std::max(t, lo + 0.01 * d), lo + 0.5 * d);
+      };
+      // the zero of the secant through the slopes at lo and hi, within lo + [0.1, 0.9] (hi - lo)
+      auto secant = [&]() {
+        const double d = hi - lo;
+        double t = g_hi > g_lo ? lo - g_lo * d / (g_hi - g_lo) : lo + 0.5 * d;
+        if (!std::isfinite(t)) t = lo + 0.5 * d;
+        return std::min(std::max(t, lo + 0.1 * d), lo + 0.9 * d);
+      };
       for (int ls = 0; ls < 31; ++ls) {
         k_axpy_to<<<n_blocks, 256, 0, s>>>(n, x.as<double>(), alpha, p.as<double>(), xn.as<double>());
         TRAIN_CUDA(cudaMemcpyAsync(xh.data(), xn.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
@@ -596,14 +640,25 @@ class Trainer {
         fn = loss_grad(xh.data(), nullptr);
         TRAIN_CUDA(cudaMemcpyAsync(gn.ptr, grad_.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
         if (!std::isfinite(fn) || fn > f + c1 * alpha * gp) {
-          hi = alpha;
-        } else {
-          const double gpn = dot(gn.as<double>(), p.as<double>());
-          if (std::abs(gpn) <= c2 * std::abs(gp)) { ok = true; break; }
-          if (gpn < 0) lo = alpha;  // still descending steeply: longer step
-          else hi = alpha;          // past the minimum along p
+          hi = alpha; f_hi = fn; hi_failed = true;
+          alpha = parabola(hi, f_hi);
+          continue;
         }
-        alpha = hi < 0 ? 2.0 * alpha : 0.5 * (lo + hi);
+        const double gpn = dot(gn.as<double>(), p.as<double>());
+        if (std::abs(gpn) <= c2 * std::abs(gp)) { ok = true; break; }
+        if (gpn < 0) {
+          const double lo_prev = lo, g_prev = g_lo;
+          lo = alpha; f_lo = fn; g_lo = gpn;
+          if (hi < 0) {
+            double t = gpn > g_prev ? alpha - gpn * (alpha - lo_prev) / (gpn - g_prev) : 4.0 * alpha;
+            if (!std::isfinite(t)) t = 4.0 * alpha;
+            alpha = std::min(std::max(t, 2.0 * alpha), 8.0 * alpha);
+            continue;
+          }
+        } else {
+          hi = alpha; f_hi = fn; g_hi = gpn; hi_failed = false;
+        }
+        alpha = hi_failed ? parabola(hi, f_hi) : secant();
       }
       if (!ok) break;  // line search exhausted: keep the last accepted point
       k_sub<<<n_blocks, 256, 0, s>>>(n, xn.as<double>(), x.as<double>(), sv.as<double>());
@@ -930,6 +985,7 @@ class Trainer {
   DevBuf metric_part_;
   DevBuf lin_cm_, lin_alpha_, lin_rhs_, lin_A_, lin_b_;  // linear warm-up
   double* host_scalars_ = nullptr;
+  std::vector<double> h0_diag_;  // initial inverse-Hessian diagonal of bfgs (empty: the identity)
   bool use_graph_ = true;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
@@ -1022,6 +1078,16 @@ int sus2g_trainer_train_linear(sus2g_trainer t, double* params) {
   return train_guarded([&] {
     if (!t || !params) throw sus2g::Error(1, "invalid argument: trainer/params");
     t->trainer->train_linear(params);
+  });
+}
+
+int sus2g_trainer_set_inv_hess_diagonal(sus2g_trainer t, const double* diag, int n) {
+  return train_guarded([&] {
+    if (!t || n < 0 || (n && !diag)) throw sus2g::Error(1, "invalid argument: trainer/diag/n");
+    if (n && n != t->trainer->nparams()) throw sus2g::Error(1, "inverse-Hessian diagonal: length is not the parameter count");
+    for (int i = 0; i < n; ++i)
+      if (!(std::isfinite(diag[i]) && diag[i] > 0)) throw sus2g::Error(1, "inverse-Hessian diagonal: entries must be finite and positive");
+    t->trainer->set_inv_hess_diagonal(diag, n);
   });
 }
 

@@ -127,6 +127,16 @@ class Trainer:
         check(load().sus2g_trainer_rescale(self._h, _d(p), ctypes.byref(s), ctypes.byref(n)))
         return p, s.value, n.value
 
+    def set_inv_hess_diagonal(self, diag=None) -> None:
+        """Initial inverse Hessian of later ``bfgs`` calls: ``diag`` (one finite positive entry per
+        parameter) on the diagonal; ``None`` restores the identity (BFGS::SetInvHessDiagonal,
+        src/common/bfgs.h:395)."""
+        if diag is None:
+            check(load().sus2g_trainer_set_inv_hess_diagonal(self._h, None, 0))
+            return
+        d = np.ascontiguousarray(diag, dtype=np.float64)
+        check(load().sus2g_trainer_set_inv_hess_diagonal(self._h, _d(d), int(d.size)))
+
     def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
         """Runs BFGS from ``params``; returns (params, loss history)."""
         p = np.array(params, dtype=np.float64)

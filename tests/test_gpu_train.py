@@ -109,6 +109,31 @@ def test_bfgs_decreases_loss(sg, golden):
     assert abs(loss - hist[-1]) <= 1e-12 * abs(hist[-1])
 
 
+def test_bfgs_initial_inverse_hessian_diagonal(sg, golden):
+    """A diagonal of ones is the default start (bit for bit); a scaled diagonal starts elsewhere
+    and still descends; bad diagonals are rejected."""
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    p0 = model.params()
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames)
+    p_ref, h_ref = tr.bfgs(p0, max_iter=5)
+    tr.set_inv_hess_diagonal(np.ones(p0.size))
+    p_one, h_one = tr.bfgs(p0, max_iter=5)
+    assert np.array_equal(h_one, h_ref) and np.array_equal(p_one, p_ref)
+    diag = np.full(p0.size, 0.25)
+    diag[: p0.size // 2] = 2.0
+    tr.set_inv_hess_diagonal(diag)
+    p_d, h_d = tr.bfgs(p0, max_iter=5)
+    assert h_d.size >= 3 and np.all(np.diff(h_d) <= 0.0) and h_d[-1] < h_d[0]
+    assert not np.array_equal(p_d, p_ref)
+    tr.set_inv_hess_diagonal(None)
+    p_back, h_back = tr.bfgs(p0, max_iter=5)
+    assert np.array_equal(h_back, h_ref)
+    for bad in (np.ones(p0.size - 1), -np.ones(p0.size), np.full(p0.size, np.nan)):
+        with pytest.raises(sg.Sus2Error):
+            tr.set_inv_hess_diagonal(bad)
+
+
 def test_trainer_rejects_invalid_inputs(sg, golden):
     model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
     frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
