@@ -95,12 +95,19 @@ int sus2g_calc_efs_device(sus2g_engine engine, int nframes, const int* natoms, c
                           const double* positions, const int* types, double* energy, double* forces,
                           double* virial, double* site_energy);
 /* Step graph of the two calls above: when two consecutive calls have the same layout (frame
- * sizes, cells, buffer addresses, stream) and every frame uses cell lists, the second is captured
+ * sizes, cells, buffer addresses, stream) of periodic frames, the second is captured
  * as one CUDA graph (edge build + E/F/virial) and later ones replay it -- positions may change
  * between calls, as in an MD run.  Another edge build on the engine, a parameter update, the
  * stage timer or a neighbour-capacity overflow makes the next call eager again.
  * enabled = 1 (default) or 0. */
 int sus2g_engine_set_step_graph(sus2g_engine engine, int enabled);
+/* Programmatic dependent launch between the kernels of an E/F/virial evaluation: a kernel may be
+ * scheduled, and stage its model tables, while the previous kernel of the stream drains.  sites =
+ * a bit mask of launch sites: 1 the edge fill (after binning), 2 the first per-atom pass (after
+ * the edge fill), 4 the Effect outer and gate-reverse passes (after the previous pass), 8 the
+ * force gather (after the last pass); 0 = none, -1 = the model's default (Static 1 | 2, Effect 1:
+ * the sites that measured faster on GB300).  Results are identical for every mask. */
+int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
  * the model runs with both compiled register budgets (3 and 4 resident blocks per SM; basis size 8)
  * over `reps` launches each and keeps the faster for later evaluations (results are identical

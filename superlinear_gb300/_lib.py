@@ -36,6 +36,7 @@ SIGNATURES = {
     "sus2g_engine_edge_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "sus2g_engine_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_set_step_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sus2g_engine_set_pdl": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp]),
     "sus2g_model_get_scaling": (ctypes.c_int, [_vp, _dp]),
     "sus2g_model_set_scaling": (ctypes.c_int, [_vp, ctypes.c_double]),

@@ -179,6 +179,13 @@ int sus2g_engine_set_step_graph(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_step_graphs(enabled != 0); });
 }
 
+int sus2g_engine_set_pdl(sus2g_engine e, int sites) {
+  return guarded([&] {
+    need(e && sites >= -1 && sites <= 15, "engine/sites");
+    e->engine->set_pdl(sites);
+  });
+}
+
 int sus2g_engine_take_stage_times(sus2g_engine e, double* ms, int* counts) {
   return guarded([&] { need(e, "engine"); e->engine->take_stage_times(ms, counts); });
 }

@@ -99,6 +99,53 @@ struct DevModel {
 
 __device__ __forceinline__ int warp_lane() { return threadIdx.x & (kWarp - 1); }
 
+// Programmatic dependent launch (griddepcontrol, sm_90 and later).  A kernel launched with the
+// programmatic-serialization attribute may start while the previous kernel of its stream is still
+// draining, once every block of that kernel has called pdl_launch_dependents() or exited; it must
+// call pdl_wait() -- which returns when all its prerequisite grids have completed and their memory
+// is visible -- before it reads anything those grids (or earlier work) wrote, and every block must
+// execute it so that the grid's completion implies its prerequisites' completion.  Without the
+// attribute both are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// kernel<<<grid, block, smem, stream>>>(args...), with the programmatic-serialization attribute
+// when pdl is set.  Returns the launch status.
+template <typename... P, typename... A>
+inline cudaError_t launch_kernel(bool pdl, void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
+                                 cudaStream_t stream, A&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = pdl ? attr : nullptr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
+// kernel<<<grid, block, smem, stream>>>(args...) at the given scheduling priority (a stream
+// priority value; lower is more urgent): its blocks are placed ahead of lower-priority pending
+// blocks when SM resources free up, also inside a captured graph.
+template <typename... P, typename... A>
+inline cudaError_t launch_kernel_priority(int priority, void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
+                                          cudaStream_t stream, A&&... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = priority;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

@@ -298,6 +298,10 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   Real* abar = v + M + (adj_staged ? 0 : M);        // [K][H]
   Real* hbar = abar + K * H;                        // [F]
 
+  // the next kernel may be scheduled as soon as every block has started; the model tables staged
+  // here are written only by host uploads, which completed before the launch chain began, so
+  // they are read before the wait for the previous kernel's edges and signals
+  pdl_launch_dependents();
   for (int q = threadIdx.x; q < F * B; q += blockDim.x) s_coeff[q] = pt.coeff[q];
   for (int q = threadIdx.x; q < 2 * dm.nblk * C * C; q += blockDim.x) s_scal[q] = pt.scal[q];
   for (int q = threadIdx.x; q < C * C * F; q += blockDim.x) {
@@ -307,6 +311,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     s_pa[q] = pt.wadd ? x0 * pt.wadd[tj * F + mu] : Real(0);
   }
   __syncthreads();
+  pdl_wait();
   const bool effect_outer = MODE == kModeOuter;
 
   // Lane-owned moment items for the forward reduction: item t = lane + 32 s <-> (k, lm).

@@ -56,6 +56,7 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
 __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame, int* frame_of, const double* pos,
                             int natoms, int bcap, int* bin_of, int* rec_of, int* bin_count, AtomFrac* frac,
                             AtomOff* off, BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over) {
+  pdl_launch_dependents();  // the fill kernel's blocks may become resident while this grid runs
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
   int f;
@@ -190,6 +191,8 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
   __shared__ int2 queue[kFillWarps][kEdgeQueue];
   __shared__ BinWalk walk[kFillWarps];
   __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
+  pdl_wait();  // the bins and frame map of the previous kernel
+  pdl_launch_dependents();
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
@@ -239,6 +242,8 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
                   int* row_end, unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
   __shared__ int cursor[kFillWarps];
+  pdl_wait();  // the frame map (and, in mixed batches, the cell-list fill) of the previous kernels
+  pdl_launch_dependents();
   const int i = static_cast<int>((static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x) / kWarp);
   if (i >= natoms) return;
   const FramePlan& fp = plans[frame_of[i]];
@@ -410,6 +415,7 @@ __global__ void k_reverse(const int* row, const int* row_end, const unsigned lon
 template <typename Real>
 __global__ void k_force_gather(const int* row, const int* row_end, const int* rev, const Real* g, int natoms,
                                double* force) {
+  pdl_wait();  // the pass's dE/dd per edge
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
   const int lane = threadIdx.x & 31;
   if (warp >= natoms) return;
@@ -783,11 +789,16 @@ PassTables<Real> bind_pass(const PassOffsets& o, const int* I, const Real* R) {
 
 Engine::Engine(const Model& model, int device, int precision) : model_(model), device_(device), precision_(precision) {
   if (precision != kFP64 && precision != kFP32) throw Error(1, "precision must be 0 (FP64) or 1 (FP32 bulk)");
+  pdl_ = default_pdl();
   SUS2G_CUDA(cudaSetDevice(device));
   SUS2G_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
   SUS2G_CUDA(cudaStreamCreateWithFlags(&own_stream_, cudaStreamNonBlocking));
   stream_ = own_stream_;
-  SUS2G_CUDA(cudaStreamCreateWithFlags(&aux_stream_, cudaStreamNonBlocking));
+  // the second stream runs the reverse-edge search beside the first pass: at the most urgent
+  // priority, so that its blocks take SM slots ahead of that pass's pending blocks
+  int least = 0;
+  SUS2G_CUDA(cudaDeviceGetStreamPriorityRange(&least, &urgent_priority_));
+  SUS2G_CUDA(cudaStreamCreateWithPriority(&aux_stream_, cudaStreamNonBlocking, urgent_priority_));
   for (cudaEvent_t* e : {&ev_fork_, &ev_rev_, &ev_fork2_, &ev_join2_})
     SUS2G_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   SUS2G_CUDA(upload_pass_constants<float>());
@@ -1197,26 +1208,26 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     int* NO = nbr_.as<int>();
     if (bins) {
       if (precision_ == kFP32)
-        k_edge_fill_bins<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+        SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_fill_bins<float>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
             P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
             counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(), pad_key_.as<unsigned long long>(), overflow,
-            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>());
+            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>()));
       else
-        k_edge_fill_bins<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+        SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_fill_bins<double>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
             P, FO, d_pos, a, rc2, bin_count_.as<int>(), bin_cap, BR, BP, BPF, BO, rec_of_.as<int>(), FR, OF,
             counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(), pad_key_.as<unsigned long long>(), overflow,
-            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>());
+            error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>()));
       ++launches_;
     }
     if (bins_frames_ < nframes) {
       if (precision_ == kFP32)
-        k_edge_image_fill<float><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+        SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<float>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
             P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
-            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>());
+            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>()));
       else
-        k_edge_image_fill<double><<<warp_blocks, kFillWarps * kWarp, 0, s>>>(
+        SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<double>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
             P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
-            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>());
+            pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>()));
       ++launches_;
     }
   }
@@ -1280,9 +1291,10 @@ void Engine::finalize_edges() {
       SUS2G_CUDA(cudaStreamWaitEvent(aux_stream_, ev_fork_, 0));
       rs = aux_stream_;
     }
-    k_reverse<<<static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256), 256, 0, rs>>>(
+    SUS2G_CUDA(launch_kernel_priority(rs != s ? urgent_priority_ : 0, k_reverse,
+        dim3(static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256)), dim3(256), 0, rs,
         row_.as<int>(), d_row_end(), key_.as<unsigned long long>(), a, rev_.as<int>(), error_.as<int>(),
-        bin_count_.as<int>(), clear_bins_ ? bins_used_ : 0);
+        bin_count_.as<int>(), clear_bins_ ? bins_used_ : 0));
     ++launches_;
     if (clear_bins_) bin_zeroed_ = bins_used_;
     if (rs != s) {
@@ -1401,7 +1413,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       if (ghosts)
         SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
       mark_begin(2);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s, pass_blocks_[kModeGateForward]);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s, pass_blocks_[kModeGateForward], (pdl_ & kPdlFirstPass) != 0);
       mark_end();
     }
   }
@@ -1410,7 +1422,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
     const int mode = m.gated ? kModeOuter : kModeStatic;
-    launches_ += launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, pass_blocks_[mode]);
+    launches_ += launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, pass_blocks_[mode], (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
     mark_end();
     if (m.gated && user_edges_) {
       hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
@@ -1427,7 +1439,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) {
       if (user_edges_) a.hbar_atom = hbar_atom_.as<double>();
       mark_begin(3);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s, pass_blocks_[kModeGateReverse]);
+      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s, pass_blocks_[kModeGateReverse], (pdl_ & kPdlBetweenPasses) != 0);
       mark_end();
     }
     wait_reverse();
@@ -1460,8 +1472,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
         k_force_gather_user<Real><<<static_cast<unsigned>((static_cast<long long>(N) * kWarp + 255) / 256), 256, 0, s>>>(
             row_.as<int>(), ncentres_, in_row_.as<int>(), in_edge_.as<int>(), g_.as<Real>(), N, d_forces);
       else
-        k_force_gather<Real><<<(N * kWarp + 255) / 256, 256, 0, s>>>(row_.as<int>(), d_row_end(), rev_.as<int>(),
-                                                                     g_.as<Real>(), ncentres_, d_forces);
+        SUS2G_CUDA(launch_kernel((pdl_ & kPdlGather) != 0, k_force_gather<Real>, dim3((N * kWarp + 255) / 256), dim3(256), 0, s,
+                                 row_.as<int>(), d_row_end(), rev_.as<int>(), g_.as<Real>(), ncentres_, d_forces));
       ++launches_;
     }
     if (nframes_) {

@@ -68,6 +68,19 @@ class Engine {
   void step_frames(int nframes, const int* frame_natoms, const double* cells, const double* d_pos, const int* d_types,
                    double* d_energy, double* d_forces, double* d_virial, double* d_site);
   void set_step_graphs(bool on) { step_graphs_ = on; if (!on) reset_step_graph(); }
+  // programmatic dependent launch between the kernels of an E/F/virial step, per launch site
+  // (kPdl* bits; negative = the model's default); a change drops a captured step graph.
+  // Measured on GB300 (graph replay): the Static 4,096-atom step 0.151 ms with no site, 0.145 ms
+  // with the fill and first-pass sites; the Effect L4 110,592-atom step 14.22 ms with none,
+  // 14.26 ms with the fill site, 14.37 ms with the first-pass site, 14.44 ms with the gather site
+  // (the gather site also slows the Static step).  Defaults: Static fill + first pass, Effect fill.
+  static constexpr int kPdlFill = 1, kPdlFirstPass = 2, kPdlBetweenPasses = 4, kPdlGather = 8;
+  int default_pdl() const { return model_.gated ? kPdlFill : kPdlFill | kPdlFirstPass; }
+  void set_pdl(int sites) {
+    if (sites < 0) sites = default_pdl();
+    if (sites != pdl_) reset_step_graph();
+    pdl_ = sites;
+  }
   // Pass-kernel autotuner on the current layout (see engine.cu): blocks_out[mode] = the chosen
   // register budget (3 or 4 resident blocks per SM; 0 for passes the model does not run),
   // ms_out[2 mode + (budget - 3)] = the timed milliseconds per launch.
@@ -170,6 +183,8 @@ class Engine {
   double* desc_out_ = nullptr;
   // step graph (step_frames)
   bool step_graphs_ = true, capturing_ = false;
+  int pdl_ = -1;  // set from the model in the constructor
+  int urgent_priority_ = 0;  // the device's most urgent stream priority
   cudaGraph_t step_graph_ = nullptr;
   cudaGraphExec_t step_exec_ = nullptr;
   std::vector<double> step_key_;

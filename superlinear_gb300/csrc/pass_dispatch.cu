@@ -8,15 +8,15 @@
 namespace sus2g {
 
 template <typename Real>
-int launch_atom_pass(int L, int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks) {
+int launch_atom_pass(int L, int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks, bool pdl) {
   if (a.dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
   switch (L) {
-    case 0: return launch_atom_pass_l<Real, 0>(mode, a, sm_count, s, blocks);
-    case 1: return launch_atom_pass_l<Real, 1>(mode, a, sm_count, s, blocks);
-    case 2: return launch_atom_pass_l<Real, 2>(mode, a, sm_count, s, blocks);
-    case 3: return launch_atom_pass_l<Real, 3>(mode, a, sm_count, s, blocks);
-    case 4: return launch_atom_pass_l<Real, 4>(mode, a, sm_count, s, blocks);
-    case 5: return launch_atom_pass_l<Real, 5>(mode, a, sm_count, s, blocks);
+    case 0: return launch_atom_pass_l<Real, 0>(mode, a, sm_count, s, blocks, pdl);
+    case 1: return launch_atom_pass_l<Real, 1>(mode, a, sm_count, s, blocks, pdl);
+    case 2: return launch_atom_pass_l<Real, 2>(mode, a, sm_count, s, blocks, pdl);
+    case 3: return launch_atom_pass_l<Real, 3>(mode, a, sm_count, s, blocks, pdl);
+    case 4: return launch_atom_pass_l<Real, 4>(mode, a, sm_count, s, blocks, pdl);
+    case 5: return launch_atom_pass_l<Real, 5>(mode, a, sm_count, s, blocks, pdl);
   }
   throw std::runtime_error("sh_l_max above 5 is not supported");
 }
@@ -67,8 +67,8 @@ cudaError_t upload_grad_constants() {
   return cudaSuccess;
 }
 
-template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t, int);
-template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t, int);
+template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t, int, bool);
+template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t, int, bool);
 template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int);
 template GradLaunch grad_pass_config<double>(int, int, const DevModel<double>&, int, int);
 template int launch_grad_pass<float>(int, int, const GradArgs<float>&, const GradLaunch&, cudaStream_t);

@@ -14,7 +14,7 @@ namespace sus2g {
 namespace pass_detail {
 
 template <typename Real, int L, int MODE, int BF, int MINB>
-int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream) {
+int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool pdl) {
   constexpr bool kKahan = sizeof(Real) == 4;
   auto kern = atom_pass_kernel<L, Real, MODE, kKahan, BF, MINB>;
   const auto& dm = a.dm;
@@ -33,8 +33,7 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream) {
   const int need = (a.natoms + kPassWarps - 1) / kPassWarps;
   const int grid = std::max(1, std::min(need, per_sm * sm_count));
   if (a.natoms == 0) return 0;
-  kern<<<grid, kPassWarps * kWarp, smem, stream>>>(a);
-  cudaError_t err = cudaGetLastError();
+  cudaError_t err = launch_kernel(pdl, kern, dim3(grid), dim3(kPassWarps * kWarp), smem, stream, a);
   if (err != cudaSuccess) throw std::runtime_error(std::string("pass launch: ") + cudaGetErrorString(err));
   return 1;
 }
@@ -45,21 +44,21 @@ constexpr int min_blocks() { return default_min_blocks(L, sizeof(Real) == 4, MOD
 // B = 8: the register budget min_blocks (3 or 4 resident blocks per SM; 0 = the default);
 // other basis sizes: the default only.
 template <typename Real, int L, int MODE, int BF>
-int launch_budget(int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+int launch_budget(int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s, bool pdl) {
   if constexpr (BF == 8) {
-    if (blocks == 3) return launch_one<Real, L, MODE, BF, 3>(a, sm_count, s);
-    if (blocks == 4) return launch_one<Real, L, MODE, BF, 4>(a, sm_count, s);
+    if (blocks == 3) return launch_one<Real, L, MODE, BF, 3>(a, sm_count, s, pdl);
+    if (blocks == 4) return launch_one<Real, L, MODE, BF, 4>(a, sm_count, s, pdl);
   }
-  return launch_one<Real, L, MODE, BF, min_blocks<Real, L, MODE>()>(a, sm_count, s);
+  return launch_one<Real, L, MODE, BF, min_blocks<Real, L, MODE>()>(a, sm_count, s, pdl);
 }
 
 template <typename Real, int L, int BF>
-int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cudaStream_t s, bool pdl) {
   switch (mode) {
-    case kModeStatic: return launch_budget<Real, L, kModeStatic, BF>(blocks, a, sm_count, s);
-    case kModeGateForward: return launch_budget<Real, L, kModeGateForward, BF>(blocks, a, sm_count, s);
-    case kModeOuter: return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s);
-    case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s);
+    case kModeStatic: return launch_budget<Real, L, kModeStatic, BF>(blocks, a, sm_count, s, pdl);
+    case kModeGateForward: return launch_budget<Real, L, kModeGateForward, BF>(blocks, a, sm_count, s, pdl);
+    case kModeOuter: return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s, pdl);
+    case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s, pdl);
   }
   throw std::runtime_error("unknown pass mode");
 }
@@ -69,9 +68,9 @@ int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cud
 // B = 8 (the basis size the reference's model initialisation writes) runs the variant with the
 // basis size fixed at compile time; other sizes run the generic variant.
 template <typename Real, int L>
-int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks) {
-  if (a.dm.B == 8) return pass_detail::launch_mode<Real, L, 8>(mode, blocks, a, sm_count, s);
-  return pass_detail::launch_mode<Real, L, 0>(mode, 0, a, sm_count, s);
+int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks, bool pdl) {
+  if (a.dm.B == 8) return pass_detail::launch_mode<Real, L, 8>(mode, blocks, a, sm_count, s, pdl);
+  return pass_detail::launch_mode<Real, L, 0>(mode, 0, a, sm_count, s, pdl);
 }
 
 template <typename Real, int L>
@@ -80,5 +79,5 @@ cudaError_t upload_pass_constants_l() { return sph_norm_upload(); }
 }  // namespace sus2g
 
 #define SUS2G_INSTANTIATE_PASS(REAL, L)                                                               \
-  template int launch_atom_pass_l<REAL, L>(int, const PassArgs<REAL>&, int, cudaStream_t, int);       \
+  template int launch_atom_pass_l<REAL, L>(int, const PassArgs<REAL>&, int, cudaStream_t, int, bool); \
   template cudaError_t upload_pass_constants_l<REAL, L>();

@@ -21,11 +21,13 @@ template <typename Real>
 int launch_grad_pass(int L, int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t stream);
 
 // Launches atom_pass_kernel<L, Real, mode, Kahan = (Real is float)> sized as a multiple of the SM
-// count, with the register budget of `blocks` resident blocks per SM (3 or 4; 0 = the default).
-// Returns the number of kernels launched (1) or throws on a configuration error.
+// count, with the register budget of `blocks` resident blocks per SM (3 or 4; 0 = the default),
+// as a programmatic dependent launch when pdl is set (the kernel stages its model tables while
+// the previous kernel of the stream drains).  Returns the number of kernels launched (1) or
+// throws on a configuration error.
 template <typename Real>
 int launch_atom_pass(int L, int mode, const PassArgs<Real>& args, int sm_count, cudaStream_t stream,
-                     int blocks = 0);
+                     int blocks = 0, bool pdl = false);
 
 // Per-translation-unit constant-table upload (spherical-harmonic normalisation) of every unit.
 template <typename Real>
@@ -35,7 +37,7 @@ cudaError_t upload_grad_constants();
 
 // Per-L entry points, explicitly instantiated in the pass_fp*_l* / grad_fp*_l* units.
 template <typename Real, int L>
-int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks);
+int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStream_t s, int blocks, bool pdl);
 template <typename Real, int L>
 cudaError_t upload_pass_constants_l();
 template <typename Real, int L>

@@ -135,6 +135,13 @@ class Engine:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))
 
+    PDL_FILL, PDL_FIRST_PASS, PDL_BETWEEN_PASSES, PDL_GATHER = 1, 2, 4, 8
+
+    def set_pdl(self, sites: int = -1) -> None:
+        """Programmatic dependent launch between the kernels of an evaluation, per launch site (a
+        mask of the PDL_* bits; 0 none, -1 the model's default)."""
+        check(load().sus2g_engine_set_pdl(self._h, int(sites)))
+
     STAGES = ("edges", "outer", "gate_forward", "gate_reverse", "gather")
 
     def set_timing(self, on: bool) -> None:
