@@ -16,6 +16,7 @@ enum DeviceError : int {
   kErrImageRange = 2,     // periodic image index outside the packed range
   kErrReverseEdge = 3,    // a directed edge had no reverse partner
   kErrBadDistance = 4,    // zero or non-finite edge length
+  kErrBadPosition = 5,    // a non-finite atom coordinate in a periodic frame
 };
 
 __device__ __forceinline__ void record_error(int* flag, int code) {

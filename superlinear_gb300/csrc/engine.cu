@@ -55,7 +55,8 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
 // found here (binary search over the frames' first atoms) and written to frame_of.
 __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame, int* frame_of, const double* pos,
                             int natoms, int bcap, int* bin_of, int* rec_of, int* bin_count, AtomFrac* frac,
-                            AtomOff* off, BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over) {
+                            AtomOff* off, BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over,
+                            int* error) {
   pdl_launch_dependents();  // the fill kernel's blocks may become resident while this grid runs
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
@@ -75,15 +76,24 @@ __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame
   const FramePlan& fp = plans[f];
   if (!fp.use_bins) { bin_of[i] = -1; return; }
   const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+  // fractional coordinates, checked before any conversion to an integer: a non-finite coordinate,
+  // or one more than 2^30 cells from the home cell, is reported and the atom binned inertly at
+  // fraction 0 of bin 0 with non-finite wrapped positions (every distance test then rejects it)
+  double sq[3];
+  bool finite = true;
+  for (int q = 0; q < 3; ++q) {
+    sq[q] = x * fp.inv[q] + y * fp.inv[3 + q] + z * fp.inv[6 + q];
+    finite = finite && fabs(sq[q]) < 1073741824.0;  // false for NaN and infinities too
+  }
+  if (!finite) record_error(error, kErrBadPosition);
   int b[3], o[3];
   float w32[3];
   for (int q = 0; q < 3; ++q) {
-    const double sq = x * fp.inv[q] + y * fp.inv[3 + q] + z * fp.inv[6 + q];
-    const double fl = floor(sq);
-    const double w = sq - fl;
+    const double fl = finite ? floor(sq[q]) : 0.0;
+    const double w = finite ? sq[q] - fl : 0.0;
     o[q] = static_cast<int>(fl);
     w32[q] = static_cast<float>(w);
-    b[q] = min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1);
+    b[q] = max(0, min(static_cast<int>(w * fp.nb[q]), fp.nb[q] - 1));
   }
   frac[i] = AtomFrac{w32[0], w32[1], w32[2], 0};
   off[i] = AtomOff{o[0], o[1], o[2], 0};
@@ -96,9 +106,10 @@ __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame
   bin_rec[rec] = BinAtom{w32[0], w32[1], w32[2], i, o[0], o[1], o[2], 0};
   const double* c = fp.cell;
   const double a0 = o[0], a1 = o[1], a2 = o[2];
-  const double wx = x - (a0 * c[0] + a1 * c[3] + a2 * c[6]);
-  const double wy = y - (a0 * c[1] + a1 * c[4] + a2 * c[7]);
-  const double wz = z - (a0 * c[2] + a1 * c[5] + a2 * c[8]);
+  const double bad = finite ? 0.0 : nan("");
+  const double wx = x - (a0 * c[0] + a1 * c[3] + a2 * c[6]) + bad;
+  const double wy = y - (a0 * c[1] + a1 * c[4] + a2 * c[7]) + bad;
+  const double wz = z - (a0 * c[2] + a1 * c[5] + a2 * c[8]) + bad;
   bin_pos[rec] = BinPos{wx, wy, wz, i, 0};
   const float hx = static_cast<float>(wx), hy = static_cast<float>(wy), hz = static_cast<float>(wz);
   bin_posf[rec] = BinPosF{hx, hy, hz, i, static_cast<float>(wx - hx), static_cast<float>(wy - hy),
@@ -254,15 +265,27 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
   if (lane == 0) cursor[w] = 0;
   __syncwarp();
   const double xi = pos[3 * i], yi = pos[3 * i + 1], zi = pos[3 * i + 2];
+  // a non-finite centre is reported and gets no edges; a non-finite neighbour is skipped (it
+  // reports itself as a centre); image ranges are clamped to the packable [-64, 63] before any
+  // conversion to an integer, and a range that reaches past it is reported
+  const bool centre_ok = isfinite(xi) && isfinite(yi) && isfinite(zi);
+  if (lane == 0 && !centre_ok) record_error(error, kErrBadPosition);
   const double* c = fp.cell;
   const double* inv = fp.inv;
-  for (int j = fp.a0 + lane; j < fp.a1; j += kWarp) {
+  for (int j = fp.a0 + lane; centre_ok && j < fp.a1; j += kWarp) {
     const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
+    if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) continue;
     int lo[3], hi[3];
     for (int q = 0; q < 3; ++q) {
       const double f = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
-      lo[q] = static_cast<int>(ceil(-f - fp.reach[q]));
-      hi[q] = static_cast<int>(floor(-f + fp.reach[q]));
+      double l = ceil(-f - fp.reach[q]), h = floor(-f + fp.reach[q]);
+      if (l < -64.0 || h > 63.0) {
+        record_error(error, kErrImageRange);
+        l = fmax(l, -64.0);
+        h = fmin(h, 63.0);
+      }
+      lo[q] = static_cast<int>(l);
+      hi[q] = static_cast<int>(fmax(h, l - 1.0));
     }
     for (int a = lo[0]; a <= hi[0]; ++a)
       for (int b = lo[1]; b <= hi[1]; ++b)
@@ -1014,8 +1037,8 @@ void Engine::check_error_read() {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
     static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
                                 "periodic image index outside [-64, 63]", "a directed edge has no reverse partner",
-                                "zero or non-finite edge length"};
-    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 5 ? msg[h] : "unknown"));
+                                "zero or non-finite edge length", "non-finite atom coordinate"};
+    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 6 ? msg[h] : "unknown"));
   }
 }
 
@@ -1173,7 +1196,7 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                                                bin_cap, bin_of.as<int>(), rec_of_.as<int>(), bin_count_.as<int>(),
                                                frac_.as<AtomFrac>(),
                                                off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
-                                               bin_posf_.as<BinPosF>(), error_.as<int>() + 2);
+                                               bin_posf_.as<BinPosF>(), error_.as<int>() + 2, error_.as<int>());
     ++launches_;
   }
   const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);

@@ -34,6 +34,12 @@ def _i(a):
     return a.ctypes.data_as(_ip) if a is not None else None
 
 
+def _addr(a):
+    """Address of an array for the c_void_p arguments of the per-step entry points.  Unlike
+    data_as it holds no reference: the caller keeps ``a`` alive in a local across the call."""
+    return a.ctypes.data
+
+
 DIM_NAMES = ("C", "L", "K", "B", "F", "M", "NB", "P", "S", "Q", "gated", "nparams", "outer_rank", "gate_rank",
              "split", "reserved")
 
@@ -179,8 +185,8 @@ class Engine:
         f = np.empty((n, 3))
         v = np.empty((nf, 6))
         s = np.empty(n)
-        check(load().sus2g_calc_efs_host(self._h, nf, _i(natoms), _d(cells), _d(pos), _i(types), _d(e), _d(f),
-                                         _d(v), _d(s)))
+        check(load().sus2g_calc_efs_host(self._h, nf, _addr(natoms), _addr(cells), _addr(pos), _addr(types),
+                                         _addr(e), _addr(f), _addr(v), _addr(s)))
         return e, f, v, s
 
     def calc_descriptors(self, frames) -> np.ndarray:
@@ -196,9 +202,9 @@ class Engine:
         """Device pointers (e.g. ``tensor.data_ptr()``) for positions/types/outputs; host natoms/cells."""
         natoms = np.ascontiguousarray(natoms, dtype=np.int32)
         cells = np.ascontiguousarray(cells, dtype=np.float64)
-        vp = ctypes.c_void_p
-        check(load().sus2g_calc_efs_device(self._h, natoms.size, _i(natoms), _d(cells), vp(pos_ptr), vp(types_ptr),
-                                           vp(energy_ptr), vp(forces_ptr), vp(virial_ptr), vp(site_ptr)))
+        check(load().sus2g_calc_efs_device(self._h, natoms.size, _addr(natoms), _addr(cells), pos_ptr or None,
+                                           types_ptr or None, energy_ptr or None, forces_ptr or None,
+                                           virial_ptr or None, site_ptr or None))
 
     def combination_grad(self, frames, ene_w, frc_w, str_w, grad=None):
         """d/dtheta of sum_i ene_w_i E_i + sum_e (frc_w_i - frc_w_j + str_w d_e) . dE/dd_e (host arrays).

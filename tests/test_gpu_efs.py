@@ -328,6 +328,27 @@ def test_invalid_inputs_raise(lib, golden):
         lib.Engine(m, 0, 7)
 
 
+
+@pytest.mark.parametrize("cells", [3, 7])
+def test_non_finite_coordinates_raise(lib, golden, cells):
+    """A NaN or infinite coordinate in a periodic frame (image scan at 216 atoms, cell lists at
+    2,744) is reported by the edge build's device check; the engine stays usable."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    good = diamond(cells, sigma=0.05, seed=31)
+    ref = g64.calc_efs([good])
+    for value in (np.nan, np.inf, -np.inf):
+        bad = diamond(cells, sigma=0.05, seed=31)
+        bad.positions = bad.positions.copy()
+        bad.positions[good.natoms // 2, 1] = value
+        for eng in (g64, g32):
+            with pytest.raises(lib.Sus2Error, match="non-finite atom coordinate"):
+                eng.calc_efs([bad])
+    again = g64.calc_efs([good])
+    for x, y in zip(again, ref):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "desc", "*.json"))),
                          ids=os.path.basename)
 def test_descriptors_match_reference(lib, golden, path):
