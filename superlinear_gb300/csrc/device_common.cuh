@@ -17,6 +17,7 @@ enum DeviceError : int {
   kErrReverseEdge = 3,    // a directed edge had no reverse partner
   kErrBadDistance = 4,    // zero or non-finite edge length
   kErrBadPosition = 5,    // a non-finite atom coordinate in a periodic frame
+  kErrBadSpecies = 6,     // an atom species index outside [0, C)
 };
 
 __device__ __forceinline__ void record_error(int* flag, int code) {

@@ -126,13 +126,17 @@ struct EdgeIn {
   typename Vec4<Real>::type d;
   int j, tj;
 };
+// (species indices are clamped to [0, C): an index out of range, which the edge build or the
+// caller-edge checks report, must not reach the per-species tables within the same step)
+__device__ __forceinline__ int species_of(const int* types, int i, int C) { return min(max(types[i], 0), C - 1); }
+
 template <typename Real>
 __device__ __forceinline__ EdgeIn<Real> load_edge(const typename Vec4<Real>::type* d4, const int* nbr,
-                                                  const int* types, int e) {
+                                                  const int* types, int e, int C) {
   EdgeIn<Real> x;
   x.d = d4[e];
   x.j = nbr[e];
-  x.tj = types[x.j];
+  x.tj = species_of(types, x.j, C);
   return x;
 }
 
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   }
 
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
-    const int ti = a.types[atom];
+    const int ti = species_of(a.types, atom, C);
     const int e0 = a.row[atom], e1 = a.row_end[atom];
     // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form
     double vir[6] = {0, 0, 0, 0, 0, 0};
@@ -344,19 +348,19 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     const int nbat = (e1 - e0 + kWarp - 1) / kWarp;
     // the gate reverse pass starts with the per-atom work: its first edge batch loads meanwhile
     if (MODE == kModeGateReverse && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
-      cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + (nbat - 1) * kWarp + lane);
+      cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + (nbat - 1) * kWarp + lane, C);
     if (MODE != kModeGateReverse) {
       // ---------------- forward moments ----------------
       Real acc[kMaxItems], cmp[kMaxItems];
 #pragma unroll
       for (int s = 0; s < kMaxItems; ++s) { acc[s] = Real(0); cmp[s] = Real(0); }
       // the next batch's edge inputs are loaded while the current batch is evaluated
-      if (e0 + lane < e1) cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + lane);
+      if (e0 + lane < e1) cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + lane, C);
       for (int base = e0; base < e1; base += kWarp) {
         const int e = base + lane;
         const bool more = base + kWarp < e1;
         EdgeIn<Real> nxt = cur;
-        if (more && e + kWarp < e1) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e + kWarp);
+        if (more && e + kWarp < e1) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e + kWarp, C);
         Real* row = stage + lane * sw;
         if (e < e1) {
           const V4 dv = cur.d;
@@ -484,7 +488,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     for (int bt = nbat - 1; bt >= 0; --bt) {
       const int e = e0 + bt * kWarp + lane;
       EdgeIn<Real> nxt = cur;
-      if (bt > 0) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e - kWarp);
+      if (bt > 0) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e - kWarp, C);
       if (e >= e1) { cur = nxt; continue; }
       const V4 dv = cur.d;
       const int j = cur.j;

@@ -56,7 +56,7 @@ __global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
 __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame, int* frame_of, const double* pos,
                             int natoms, int bcap, int* bin_of, int* rec_of, int* bin_count, AtomFrac* frac,
                             AtomOff* off, BinAtom* bin_rec, BinPos* bin_pos, BinPosF* bin_posf, int* bin_over,
-                            int* error) {
+                            int* error, const int* types, int C) {
   pdl_launch_dependents();  // the fill kernel's blocks may become resident while this grid runs
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= natoms) return;
@@ -74,6 +74,7 @@ __global__ void k_bin_place(const FramePlan* plans, int nframes, bool find_frame
     f = frame_of[i];
   }
   const FramePlan& fp = plans[f];
+  if (types[i] < 0 || types[i] >= C) record_error(error, kErrBadSpecies);
   if (!fp.use_bins) { bin_of[i] = -1; return; }
   const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
   // fractional coordinates, checked before any conversion to an integer: a non-finite coordinate,
@@ -248,7 +249,8 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
 // synchronisation; a count above cap raises *overflow as in the cell-list kernel.
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
-k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos, int natoms, double rc2, int* counts,
+k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos, const int* types, int C,
+                  int natoms, double rc2, int* counts,
                   int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error, int* row,
                   int* row_end, unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
@@ -270,6 +272,7 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
   // conversion to an integer, and a range that reaches past it is reported
   const bool centre_ok = isfinite(xi) && isfinite(yi) && isfinite(zi);
   if (lane == 0 && !centre_ok) record_error(error, kErrBadPosition);
+  if (lane == 0 && (types[i] < 0 || types[i] >= C)) record_error(error, kErrBadSpecies);
   const double* c = fp.cell;
   const double* inv = fp.inv;
   for (int j = fp.a0 + lane; centre_ok && j < fp.a1; j += kWarp) {
@@ -1037,8 +1040,9 @@ void Engine::check_error_read() {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
     static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
                                 "periodic image index outside [-64, 63]", "a directed edge has no reverse partner",
-                                "zero or non-finite edge length", "non-finite atom coordinate"};
-    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 6 ? msg[h] : "unknown"));
+                                "zero or non-finite edge length", "non-finite atom coordinate",
+                                "atom species index out of range"};
+    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 7 ? msg[h] : "unknown"));
   }
 }
 
@@ -1196,7 +1200,8 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
                                                bin_cap, bin_of.as<int>(), rec_of_.as<int>(), bin_count_.as<int>(),
                                                frac_.as<AtomFrac>(),
                                                off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
-                                               bin_posf_.as<BinPosF>(), error_.as<int>() + 2, error_.as<int>());
+                                               bin_posf_.as<BinPosF>(), error_.as<int>() + 2, error_.as<int>(), d_types,
+                                               model_.C);
     ++launches_;
   }
   const unsigned warp_blocks = static_cast<unsigned>((static_cast<long long>(a) * kWarp + 255) / 256);
@@ -1245,11 +1250,11 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     if (bins_frames_ < nframes) {
       if (precision_ == kFP32)
         SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<float>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
-            P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+            P, FO, d_pos, d_types, model_.C, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
             pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>()));
       else
         SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<double>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
-            P, FO, d_pos, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+            P, FO, d_pos, d_types, model_.C, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
             pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>()));
       ++launches_;
     }

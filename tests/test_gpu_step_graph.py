@@ -192,3 +192,25 @@ def test_programmatic_launch_matches_serial_launches(sg, golden, name, precision
                 b.pos += d
         for x, y in zip(pdl.calc_efs(frames), serial.calc_efs(frames)):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("cells", [3, 7])
+def test_device_species_out_of_range_raise(sg, golden, cells):
+    """Species indices given in device memory are checked by the edge build (image scan at 216
+    atoms, cell lists at 2,744); the passes never index their tables with them, and the engine is
+    usable afterwards."""
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    m = sg.Model(path)
+    for prec in (sg.FP64, sg.FP32):
+        eng = sg.Engine(m, 0, prec)
+        frames = [diamond(cells, sigma=0.05, seed=41, species=2)]
+        a = DeviceFrames(frames)
+        ref = a.step(eng)
+        good = a.types.clone()
+        for bad in (2, -1, 1 << 20):
+            a.types[frames[0].natoms // 3] = bad
+            with pytest.raises(sg.Sus2Error, match="species index out of range"):
+                a.step(eng)
+            a.types.copy_(good)
+        for x, y in zip(a.step(eng), ref):
+            assert np.array_equal(x, y)
