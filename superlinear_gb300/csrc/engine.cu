@@ -278,7 +278,74 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
   for (int j = fp.a0 + lane; centre_ok && j < fp.a1; j += kWarp) {
     const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
     if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) continue;
+    auto accept = [&](int a, int b, int cc, double vx, double vy, double vz, double r2) {
+      const int k = atomicAdd(&cursor[w], 1);
+      if (k < cap) {
+        write_edge<Real>(pad + k, j, a, b, cc, vx, vy, vz, r2, nbr, d4, key);
+        if (k < kFillSortStage) skeys[w][k] = edge_key(j, a, b, cc);
+      }
+    };
+    // exact FP64 test of image n (every image in FP64 engines; the FP32 screen's survivors)
+    auto exact = [&](int a, int b, int cc) {
+      const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
+      const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
+      const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
+      const double r2 = vx * vx + vy * vy + vz * vz;
+      if (r2 < rc2) accept(a, b, cc, vx, vy, vz, r2);
+    };
     int lo[3], hi[3];
+    if constexpr (sizeof(Real) == 4) {
+      // FP32 engines: an FP32 screen rejects the images clearly outside the cutoff, and the
+      // rest take the exact FP64 test and vector (so accepted edges carry the FP64 vector
+      // rounded once, as in the FP64 loop).
+      //  * Ranges: f = dx . inv(cell) in FP32 errs by at most ~6 2^-24 S, S = sum |dx_r inv_rq|;
+      //    widening reach by 1e-4 + 1e-6 S keeps every image of the FP64 range (extra images are
+      //    rejected by the distance test).
+      //  * Screen: v = dx + n . cell in FP32 (three FMAs a component).  Every partial sum of
+      //    component q is at most M_q = |dx_q| + sum_r |n_r|max |cell_rq|, each of the ~6
+      //    roundings errs by at most 2^-24 of that, so |v - v_exact| <= E = 6 2^-24 |M| and r^2
+      //    near r_c^2 errs by at most 2 r_c E + E^2: below 5e-5 r_c^2 when |M| <= 64 r_c.  An FP32
+      //    r^2 at or above hi2 = (1 + 1e-4) r_c^2 is then outside in FP64 too: the accepted set is
+      //    the FP64 set.  Pairs with larger |M| take the FP64 loop.
+      const float fx = static_cast<float>(dx), fy = static_cast<float>(dy), fz = static_cast<float>(dz);
+      const float* cf = fp.cellf;
+      float mq[3] = {fabsf(fx), fabsf(fy), fabsf(fz)};
+      bool fast = true;
+      for (int q = 0; q < 3; ++q) {
+        const float i0 = fp.invf[q], i1 = fp.invf[3 + q], i2 = fp.invf[6 + q];
+        const float f = fx * i0 + fy * i1 + fz * i2;
+        const float S = fabsf(fx * i0) + fabsf(fy * i1) + fabsf(fz * i2);
+        const float reach = fp.reachf[q] + 1e-4f + 1e-6f * S;
+        float l = ceilf(-f - reach), h = floorf(-f + reach);
+        if (!(l >= -64.0f && h <= 63.0f)) { fast = false; break; }  // (the FP64 loop reports it)
+        lo[q] = static_cast<int>(l);
+        hi[q] = static_cast<int>(h);
+      }
+      if (fast) {
+        for (int r = 0; r < 3; ++r) {
+          const float n = static_cast<float>(max(abs(lo[r]), abs(hi[r])));
+          mq[0] += n * fabsf(cf[3 * r]);
+          mq[1] += n * fabsf(cf[3 * r + 1]);
+          mq[2] += n * fabsf(cf[3 * r + 2]);
+        }
+        fast = mq[0] * mq[0] + mq[1] * mq[1] + mq[2] * mq[2] <= 4096.0f * fp.rc2f;
+      }
+      if (fast) {
+        const float hi2 = fp.hi2;
+        for (int a = lo[0]; a <= hi[0]; ++a) {
+          const float ax = fmaf(a, cf[0], fx), ay = fmaf(a, cf[1], fy), az = fmaf(a, cf[2], fz);
+          for (int b = lo[1]; b <= hi[1]; ++b) {
+            const float px = fmaf(b, cf[3], ax), py = fmaf(b, cf[4], ay), pz = fmaf(b, cf[5], az);
+            for (int cc = lo[2]; cc <= hi[2]; ++cc) {
+              const float vx = fmaf(cc, cf[6], px), vy = fmaf(cc, cf[7], py), vz = fmaf(cc, cf[8], pz);
+              const float r2 = vx * vx + vy * vy + vz * vz;
+              if (r2 < hi2 && !(i == j && a == 0 && b == 0 && cc == 0)) exact(a, b, cc);
+            }
+          }
+        }
+        continue;
+      }
+    }
     for (int q = 0; q < 3; ++q) {
       const double f = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
       double l = ceil(-f - fp.reach[q]), h = floor(-f + fp.reach[q]);
@@ -292,20 +359,8 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
     }
     for (int a = lo[0]; a <= hi[0]; ++a)
       for (int b = lo[1]; b <= hi[1]; ++b)
-        for (int cc = lo[2]; cc <= hi[2]; ++cc) {
-          if (i == j && a == 0 && b == 0 && cc == 0) continue;
-          const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
-          const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
-          const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
-          const double r2 = vx * vx + vy * vy + vz * vz;
-          if (!(r2 < rc2)) continue;
-          if (a < -64 || a > 63 || b < -64 || b > 63 || cc < -64 || cc > 63) { record_error(error, kErrImageRange); continue; }
-          const int k = atomicAdd(&cursor[w], 1);
-          if (k < cap) {
-            write_edge<Real>(pad + k, j, a, b, cc, vx, vy, vz, r2, nbr, d4, key);
-            if (k < kFillSortStage) skeys[w][k] = edge_key(j, a, b, cc);
-          }
-        }
+        for (int cc = lo[2]; cc <= hi[2]; ++cc)
+          if (!(i == j && a == 0 && b == 0 && cc == 0)) exact(a, b, cc);
   }
   __syncwarp();
   const int total = cursor[w], n = min(total, cap);
@@ -1134,19 +1189,24 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
       for (int q = 0; q < 3; ++q)
         rows += std::sqrt(fp.cell[3 * q] * fp.cell[3 * q] + fp.cell[3 * q + 1] * fp.cell[3 * q + 1] + fp.cell[3 * q + 2] * fp.cell[3 * q + 2]);
       fp.band = 2.0 * rc * (4.0 * 6.0e-8 * rows) * 4.0 + 1e-6;
-      for (int q = 0; q < 9; ++q) {
-        fp.cellf[q] = static_cast<float>(fp.cell[q]);
-        fp.celll[q] = static_cast<float>(fp.cell[q] - static_cast<double>(fp.cellf[q]));
-      }
       fp.screen2 = static_cast<float>(rc2 + fp.band);
-      // FP32 r^2 of the double-float edge vector is within ~1e-6 relative of the exact one
-      fp.lo2 = static_cast<float>(rc2 * (1.0 - 1e-4));
-      fp.hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
       bins += fp.nb[0] * fp.nb[1] * fp.nb[2];
       // bin capacity: twice the frame's mean atoms per bin plus 8 (grown after an overflow)
       const double per_bin = frame_natoms[f] / static_cast<double>(fp.nb[0] * fp.nb[1] * fp.nb[2]);
       bin_cap = std::max(bin_cap, static_cast<int>(std::min(1.0e6, std::ceil(bin_cap_scale_ * per_bin) + 8.0)));
     }
+    // FP32 cell rows (hi, lo) and the band of r^2 around r_c^2 that FP32 engines decide in FP64
+    // (the cell-list fill's double-float r^2 is within ~1e-6 relative of the exact one, the
+    // image scan's FP32 r^2 within ~5e-5)
+    for (int q = 0; q < 9; ++q) {
+      fp.cellf[q] = static_cast<float>(fp.cell[q]);
+      fp.celll[q] = static_cast<float>(fp.cell[q] - static_cast<double>(fp.cellf[q]));
+    }
+    fp.lo2 = static_cast<float>(rc2 * (1.0 - 1e-4));
+    fp.hi2 = static_cast<float>(rc2 * (1.0 + 1e-4));
+    for (int q = 0; q < 9; ++q) fp.invf[q] = static_cast<float>(fp.inv[q]);
+    for (int q = 0; q < 3; ++q) fp.reachf[q] = static_cast<float>(fp.reach[q]);
+    fp.rc2f = static_cast<float>(rc2);
     // padded edge slots of every frame: cap_scale x the mean neighbour count of the frame's density
     // + 64 per centre (grown after an overflow)
     const double vol = std::abs(fp.cell[0] * (fp.cell[4] * fp.cell[8] - fp.cell[5] * fp.cell[7]) -

@@ -33,6 +33,7 @@ struct FramePlan {
   double band;      // |r^2 error| bound of the FP32 prefilter; candidates within it get the FP64 test
   float screen2;    // FP32 prefilter threshold r_c^2 + band
   float lo2, hi2;   // FP32 engines: r^2 below lo2 is inside, above hi2 outside, else the FP64 test
+  float invf[9], reachf[3], rc2f;  // FP32 copies for the image scan's FP32 ranges and bound
 };
 
 // Per-atom wrapped fractional coordinates (FP32, in [0,1)) and the integer cell offsets
