@@ -1256,7 +1256,9 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     bin_rec_.ensure(sizeof(BinAtom) * slots);
     bin_pos_.ensure(sizeof(BinPos) * slots);
     bin_posf_.ensure(sizeof(BinPosF) * slots);
-    k_bin_place<<<(a + 255) / 256, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, find_frame, frame_of_.as<int>(), d_pos, a,
+    // one warp per block: each atom costs ~40 FP64 operations (1/64 of the FP32 rate on this
+    // GPU), so small frames are spread over as many SMs as possible (4,096 atoms: 128 SMs)
+    k_bin_place<<<(a + kWarp - 1) / kWarp, kWarp, 0, s>>>(plan_.as<FramePlan>(), nframes, find_frame, frame_of_.as<int>(), d_pos, a,
                                                bin_cap, bin_of.as<int>(), rec_of_.as<int>(), bin_count_.as<int>(),
                                                frac_.as<AtomFrac>(),
                                                off_.as<AtomOff>(), bin_rec_.as<BinAtom>(), bin_pos_.as<BinPos>(),
