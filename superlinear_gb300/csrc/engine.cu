@@ -41,10 +41,21 @@ void DevBuf::release() {
 // ------------------------------------------------------------------------------------------------
 namespace {
 
-__global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of) {
+// Frame of every atom; with posh / posl (FP32 engines with image-scan frames) also its position
+// as double-float parts x = xh + xl, xh = fl32(x), for the image scan's FP32 arithmetic.
+__global__ void k_frame_of(const FramePlan* plans, int nframes, int* frame_of, const double* pos, float4* posh,
+                           float4* posl) {
   const int f = blockIdx.x;
   if (f >= nframes) return;
-  for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) frame_of[i] = f;
+  for (int i = plans[f].a0 + threadIdx.x; i < plans[f].a1; i += blockDim.x) {
+    frame_of[i] = f;
+    if (posh) {
+      const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+      const float xh = static_cast<float>(x), yh = static_cast<float>(y), zh = static_cast<float>(z);
+      posh[i] = make_float4(xh, yh, zh, 0.f);
+      posl[i] = make_float4(static_cast<float>(x - xh), static_cast<float>(y - yh), static_cast<float>(z - zh), 0.f);
+    }
+  }
 }
 
 // Cell-list binning in one pass: per atom the wrapped fractions and integer cell offsets, its bin
@@ -249,8 +260,8 @@ k_edge_fill_bins(const FramePlan* plans, const int* frame_of, const double* pos,
 // synchronisation; a count above cap raises *overflow as in the cell-list kernel.
 template <typename Real>
 __global__ void __launch_bounds__(kFillWarps * kWarp)
-k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos, const int* types, int C,
-                  int natoms, double rc2, int* counts,
+k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos, const float4* posh,
+                  const float4* posl, const int* types, int C, int natoms, double rc2, int* counts,
                   int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key, int* overflow, int* error, int* row,
                   int* row_end, unsigned long long* key_out, int* nbr_out, typename Vec4<Real>::type* d4_out) {
   __shared__ unsigned long long skeys[kFillWarps][kFillSortStage];
@@ -275,9 +286,9 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
   if (lane == 0 && (types[i] < 0 || types[i] >= C)) record_error(error, kErrBadSpecies);
   const double* c = fp.cell;
   const double* inv = fp.inv;
+  float4 cih = make_float4(0.f, 0.f, 0.f, 0.f), cil = cih;
+  if (posh) { cih = posh[i]; cil = posl[i]; }
   for (int j = fp.a0 + lane; centre_ok && j < fp.a1; j += kWarp) {
-    const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
-    if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) continue;
     auto accept = [&](int a, int b, int cc, double vx, double vy, double vz, double r2) {
       const int k = atomicAdd(&cursor[w], 1);
       if (k < cap) {
@@ -285,67 +296,85 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
         if (k < kFillSortStage) skeys[w][k] = edge_key(j, a, b, cc);
       }
     };
-    // exact FP64 test of image n (every image in FP64 engines; the FP32 screen's survivors)
-    auto exact = [&](int a, int b, int cc) {
-      const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
-      const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
-      const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
-      const double r2 = vx * vx + vy * vy + vz * vz;
-      if (r2 < rc2) accept(a, b, cc, vx, vy, vz, r2);
-    };
     int lo[3], hi[3];
     if constexpr (sizeof(Real) == 4) {
-      // FP32 engines: an FP32 screen rejects the images clearly outside the cutoff, and the
-      // rest take the exact FP64 test and vector (so accepted edges carry the FP64 vector
-      // rounded once, as in the FP64 loop).
-      //  * Ranges: f = dx . inv(cell) in FP32 errs by at most ~6 2^-24 S, S = sum |dx_r inv_rq|;
+      // FP32 engines: double-float arithmetic on the (hi, lo) positions, FP64 only near the cutoff.
+      //  * dx = x_j - x_i and every image vector v = dx + n . cell are accumulated as double-float
+      //    pairs (exact two-sums, m cell_hi split exactly by an FMA): their absolute error is a few
+      //    dozen 2^-48 of M, the largest magnitude involved, M = |dx| + sum_r |n_r| |cell_r|.  The
+      //    vector is then rounded once to FP32 and r^2 formed in FP32: with M <= 1e6 r_c, r^2 near
+      //    r_c^2 errs by well under 1e-6 r_c^2, so r^2 below lo2 = (1 - 1e-4) r_c^2 is inside and
+      //    above hi2 = (1 + 1e-4) r_c^2 outside in FP64 too, and the band takes the exact FP64 test.
+      //    The accepted set is the FP64 set; accepted vectors are the exact ones rounded once.
+      //  * Ranges: f = dx_hi . inv(cell) in FP32 errs by at most ~7 2^-24 S, S = sum |dx_r inv_rq|;
       //    widening reach by 1e-4 + 1e-6 S keeps every image of the FP64 range (extra images are
       //    rejected by the distance test).
-      //  * Screen: v = dx + n . cell in FP32 (three FMAs a component).  Every partial sum of
-      //    component q is at most M_q = |dx_q| + sum_r |n_r|max |cell_rq|, each of the ~6
-      //    roundings errs by at most 2^-24 of that, so |v - v_exact| <= E = 6 2^-24 |M| and r^2
-      //    near r_c^2 errs by at most 2 r_c E + E^2: below 5e-5 r_c^2 when |M| <= 64 r_c.  An FP32
-      //    r^2 at or above hi2 = (1 + 1e-4) r_c^2 is then outside in FP64 too: the accepted set is
-      //    the FP64 set.  Pairs with larger |M| take the FP64 loop.
-      const float fx = static_cast<float>(dx), fy = static_cast<float>(dy), fz = static_cast<float>(dz);
-      const float* cf = fp.cellf;
-      float mq[3] = {fabsf(fx), fabsf(fy), fabsf(fz)};
+      //  Non-finite positions, ranges outside the packable [-64, 63] and larger M take the FP64 loop,
+      //  which reports the first two.
+      const float4 hj = posh[j], lj = posl[j];
+      float xh = hj.x, xl = lj.x, yh = hj.y, yl = lj.y, zh = hj.z, zl = lj.z;
+      df_acc(xh, xl, -cih.x, -cil.x);
+      df_acc(yh, yl, -cih.y, -cil.y);
+      df_acc(zh, zl, -cih.z, -cil.z);
+      const float* ch = fp.cellf;
+      const float* cl = fp.celll;
       bool fast = true;
       for (int q = 0; q < 3; ++q) {
         const float i0 = fp.invf[q], i1 = fp.invf[3 + q], i2 = fp.invf[6 + q];
-        const float f = fx * i0 + fy * i1 + fz * i2;
-        const float S = fabsf(fx * i0) + fabsf(fy * i1) + fabsf(fz * i2);
+        const float f = xh * i0 + yh * i1 + zh * i2;
+        const float S = fabsf(xh * i0) + fabsf(yh * i1) + fabsf(zh * i2);
         const float reach = fp.reachf[q] + 1e-4f + 1e-6f * S;
-        float l = ceilf(-f - reach), h = floorf(-f + reach);
-        if (!(l >= -64.0f && h <= 63.0f)) { fast = false; break; }  // (the FP64 loop reports it)
+        const float l = ceilf(-f - reach), h = floorf(-f + reach);
+        if (!(l >= -64.0f && h <= 63.0f)) { fast = false; break; }
         lo[q] = static_cast<int>(l);
         hi[q] = static_cast<int>(h);
       }
       if (fast) {
-        for (int r = 0; r < 3; ++r) {
-          const float n = static_cast<float>(max(abs(lo[r]), abs(hi[r])));
-          mq[0] += n * fabsf(cf[3 * r]);
-          mq[1] += n * fabsf(cf[3 * r + 1]);
-          mq[2] += n * fabsf(cf[3 * r + 2]);
-        }
-        fast = mq[0] * mq[0] + mq[1] * mq[1] + mq[2] * mq[2] <= 4096.0f * fp.rc2f;
+        float m = fabsf(xh) + fabsf(yh) + fabsf(zh);
+        for (int r = 0; r < 3; ++r)
+          m += static_cast<float>(max(abs(lo[r]), abs(hi[r]))) *
+               (fabsf(ch[3 * r]) + fabsf(ch[3 * r + 1]) + fabsf(ch[3 * r + 2]));
+        fast = m * m <= 1e12f * fp.rc2f;
       }
       if (fast) {
-        const float hi2 = fp.hi2;
+        const float lo2 = fp.lo2, hi2 = fp.hi2;
         for (int a = lo[0]; a <= hi[0]; ++a) {
-          const float ax = fmaf(a, cf[0], fx), ay = fmaf(a, cf[1], fy), az = fmaf(a, cf[2], fz);
+          float axh = xh, axl = xl, ayh = yh, ayl = yl, azh = zh, azl = zl;
+          df_acc_mul(axh, axl, a, ch[0], cl[0]);
+          df_acc_mul(ayh, ayl, a, ch[1], cl[1]);
+          df_acc_mul(azh, azl, a, ch[2], cl[2]);
           for (int b = lo[1]; b <= hi[1]; ++b) {
-            const float px = fmaf(b, cf[3], ax), py = fmaf(b, cf[4], ay), pz = fmaf(b, cf[5], az);
+            float pxh = axh, pxl = axl, pyh = ayh, pyl = ayl, pzh = azh, pzl = azl;
+            df_acc_mul(pxh, pxl, b, ch[3], cl[3]);
+            df_acc_mul(pyh, pyl, b, ch[4], cl[4]);
+            df_acc_mul(pzh, pzl, b, ch[5], cl[5]);
             for (int cc = lo[2]; cc <= hi[2]; ++cc) {
-              const float vx = fmaf(cc, cf[6], px), vy = fmaf(cc, cf[7], py), vz = fmaf(cc, cf[8], pz);
+              float vxh = pxh, vxl = pxl, vyh = pyh, vyl = pyl, vzh = pzh, vzl = pzl;
+              df_acc_mul(vxh, vxl, cc, ch[6], cl[6]);
+              df_acc_mul(vyh, vyl, cc, ch[7], cl[7]);
+              df_acc_mul(vzh, vzl, cc, ch[8], cl[8]);
+              const float vx = vxh + vxl, vy = vyh + vyl, vz = vzh + vzl;
               const float r2 = vx * vx + vy * vy + vz * vz;
-              if (r2 < hi2 && !(i == j && a == 0 && b == 0 && cc == 0)) exact(a, b, cc);
+              if (!(r2 < hi2) || (i == j && a == 0 && b == 0 && cc == 0)) continue;
+              if (r2 < lo2) {
+                accept(a, b, cc, vx, vy, vz, r2);
+              } else {
+                const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
+                const double ex = dx + a * c[0] + b * c[3] + cc * c[6];
+                const double ey = dy + a * c[1] + b * c[4] + cc * c[7];
+                const double ez = dz + a * c[2] + b * c[5] + cc * c[8];
+                const double d2 = ex * ex + ey * ey + ez * ez;
+                if (d2 < rc2) accept(a, b, cc, ex, ey, ez, d2);
+              }
             }
           }
         }
         continue;
       }
     }
+    // FP64: the exact test of every image (FP64 engines; FP32 engines' fallback)
+    const double dx = pos[3 * j] - xi, dy = pos[3 * j + 1] - yi, dz = pos[3 * j + 2] - zi;
+    if (!(isfinite(dx) && isfinite(dy) && isfinite(dz))) continue;
     for (int q = 0; q < 3; ++q) {
       const double f = dx * inv[q] + dy * inv[3 + q] + dz * inv[6 + q];
       double l = ceil(-f - fp.reach[q]), h = floor(-f + fp.reach[q]);
@@ -359,8 +388,14 @@ k_edge_image_fill(const FramePlan* plans, const int* frame_of, const double* pos
     }
     for (int a = lo[0]; a <= hi[0]; ++a)
       for (int b = lo[1]; b <= hi[1]; ++b)
-        for (int cc = lo[2]; cc <= hi[2]; ++cc)
-          if (!(i == j && a == 0 && b == 0 && cc == 0)) exact(a, b, cc);
+        for (int cc = lo[2]; cc <= hi[2]; ++cc) {
+          if (i == j && a == 0 && b == 0 && cc == 0) continue;
+          const double vx = dx + a * c[0] + b * c[3] + cc * c[6];
+          const double vy = dy + a * c[1] + b * c[4] + cc * c[7];
+          const double vz = dz + a * c[2] + b * c[5] + cc * c[8];
+          const double r2 = vx * vx + vy * vy + vz * vz;
+          if (r2 < rc2) accept(a, b, cc, vx, vy, vz, r2);
+        }
   }
   __syncwarp();
   const int total = cursor[w], n = min(total, cap);
@@ -1242,7 +1277,10 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
   // batches with cell lists only: the binning kernel finds each atom's frame itself
   const bool find_frame = bins && bins_frames_ == nframes;
   if (nframes && !find_frame) {
-    k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>());
+    const bool split = precision_ == kFP32 && bins_frames_ < nframes;
+    if (split) posf_.ensure(2 * sizeof(float4) * std::max(1, a));
+    k_frame_of<<<nframes, 256, 0, s>>>(plan_.as<FramePlan>(), nframes, frame_of_.as<int>(), d_pos,
+                                       split ? posf_.as<float4>() : nullptr, split ? posf_.as<float4>() + a : nullptr);
     ++launches_;
   }
   if (bins) {
@@ -1312,11 +1350,13 @@ void Engine::build_edges(int nframes, const int* frame_natoms, const double* cel
     if (bins_frames_ < nframes) {
       if (precision_ == kFP32)
         SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<float>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
-            P, FO, d_pos, d_types, model_.C, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
+            P, FO, d_pos, posf_.as<float4>(), posf_.as<float4>() + a, d_types, model_.C, a, rc2, counts_.as<int>(),
+            pad_nbr_.as<int>(), pad_d4_.as<EdgeF>(),
             pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeF>()));
       else
         SUS2G_CUDA(launch_kernel((pdl_ & kPdlFill) != 0, k_edge_image_fill<double>, dim3(warp_blocks), dim3(kFillWarps * kWarp), 0, s,
-            P, FO, d_pos, d_types, model_.C, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(), pad_d4_.as<EdgeD>(),
+            P, FO, d_pos, nullptr, nullptr, d_types, model_.C, a, rc2, counts_.as<int>(), pad_nbr_.as<int>(),
+            pad_d4_.as<EdgeD>(),
             pad_key_.as<unsigned long long>(), overflow, error_.as<int>(), RW, RE, KO, NO, d4_.as<EdgeD>()));
       ++launches_;
     }

@@ -218,6 +218,7 @@ class Engine {
   bool padded_ = false;         // cell-list batch: edges left in padded per-centre slots (row_end_)
   int bin_zeroed_ = 0;          // leading bin counters known to be zero on the device
   int bins_used_ = 0;           // bin counters used by the current cell-list build
+  DevBuf posf_;  // double-float positions of image-scan batches (FP32 engines)
   DevBuf bin_count_, bin_rec_, bin_pos_, bin_posf_, rec_of_;
   const int* d_types_ = nullptr;
   bool user_edges_ = false;     // caller-supplied edges: no reverse partners, scatter instead of gather

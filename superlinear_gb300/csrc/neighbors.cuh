@@ -89,6 +89,23 @@ __device__ __forceinline__ float df_add(float ah, float al, float bh, float bl) 
   return s + (e + (al + bl));
 }
 
+// Double-float accumulation (h, l) += (bh, bl) (Knuth two-sum of the leading parts, the trailing
+// parts added once): absolute error a few 2^-48 of the operands' magnitudes.
+__device__ __forceinline__ void df_acc(float& h, float& l, float bh, float bl) {
+  const float s = h + bh;
+  const float v = s - h;
+  const float e = (h - (s - v)) + (bh - v) + (l + bl);
+  h = s + e;
+  l = e - (h - s);
+}
+
+// (h, l) += m (ch, cl) for a small integer m (|m| <= 64): m ch is split exactly by an FMA.
+__device__ __forceinline__ void df_acc_mul(float& h, float& l, float m, float ch, float cl) {
+  const float p = m * ch;
+  const float pe = fmaf(m, ch, -p);
+  df_acc(h, l, p, fmaf(m, cl, pe));
+}
+
 // Per-warp shared tables of the fill: the 27 wrap shifts (FP64 and double-float parts) and the
 // lanes' bins (start, length).
 // Per wrap w in {-1, 0, 1}^3 of a neighbouring bin (index (w0 + 1) 9 + (w1 + 1) 3 + (w2 + 1)):
