@@ -1663,9 +1663,11 @@ __global__ void __launch_bounds__(kGwThreads) k_gate_weight_grad(int natoms, int
                                                                  const double* lh, const Real* gmom,
                                                                  const Real* gmomd, double* slots, int nparams,
                                                                  int gw_off) {
+  // staging and chunk sums in the compute precision (FP32 bulk: the products and each 32-atom
+  // chunk's sum in FP32, the chunk partials added in FP64; FP64 plain: FP64 throughout)
   extern __shared__ double gw_sh[];
-  double* sl = gw_sh;                          // [kGwChunk][2F]
-  double* sg = gw_sh + kGwChunk * 2 * F;       // [kGwChunk][2Q]
+  Real* sl = reinterpret_cast<Real*>(gw_sh);   // [kGwChunk][2F]
+  Real* sg = sl + kGwChunk * 2 * F;            // [kGwChunk][2Q]
   const int FQ = F * Q;
   double* out = slots + static_cast<size_t>(blockIdx.x) * nparams + gw_off;
   for (int tile = 0; tile < FQ; tile += kGwThreads * kGwPer) {
@@ -1675,12 +1677,12 @@ __global__ void __launch_bounds__(kGwThreads) k_gate_weight_grad(int natoms, int
     for (int base = blockIdx.x * kGwChunk; base < natoms; base += gridDim.x * kGwChunk) {
       const int n = min(kGwChunk, natoms - base);
       __syncthreads();
-      for (int t = threadIdx.x; t < n * 2 * F; t += blockDim.x) sl[t] = lh[static_cast<size_t>(base) * 2 * F + t];
+      for (int t = threadIdx.x; t < n * 2 * F; t += blockDim.x) sl[t] = Real(lh[static_cast<size_t>(base) * 2 * F + t]);
       for (int t = threadIdx.x; t < n * Q; t += blockDim.x) {
         const int a = t / Q, q = t - a * Q;
         const size_t o = static_cast<size_t>(base + a) * M + nodes[q];
-        sg[a * 2 * Q + q] = double(gmom[o]);
-        sg[a * 2 * Q + Q + q] = double(gmomd[o]);
+        sg[a * 2 * Q + q] = gmom[o];
+        sg[a * 2 * Q + Q + q] = gmomd[o];
       }
       __syncthreads();
 #pragma unroll
@@ -1688,10 +1690,10 @@ __global__ void __launch_bounds__(kGwThreads) k_gate_weight_grad(int natoms, int
         const int t = tile + k * kGwThreads + threadIdx.x;
         if (t < FQ) {
           const int m = t / Q, q = t - m * Q;
-          double v = 0.0;
+          Real v = Real(0);
           for (int a = 0; a < n; ++a)
             v += sl[a * 2 * F + m] * sg[a * 2 * Q + q] + sl[a * 2 * F + F + m] * sg[a * 2 * Q + Q + q];
-          acc[k] += v;
+          acc[k] += double(v);
         }
       }
     }
@@ -1759,8 +1761,8 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
     const int gw_off = dm.grad.gate_w_off;
     if (N && gw_off >= 0) {
       const int blocks = std::max(1, std::min(nslots, (ncentres_ + kGwChunk - 1) / kGwChunk));
-      const size_t smem = sizeof(double) * kGwChunk * 2 * (m.F + m.Q);
-      if (smem > 200 * 1024) throw Error(3, "gate weight gradient: radial functions + gate scalars above 400");
+      const size_t smem = sizeof(Real) * kGwChunk * 2 * (m.F + m.Q);
+      if (smem > 200 * 1024) throw Error(3, "gate weight gradient: radial functions + gate scalars exceed the shared-memory staging");
       if (smem > 48 * 1024)
         SUS2G_CUDA(cudaFuncSetAttribute(k_gate_weight_grad<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         static_cast<int>(smem)));
