@@ -143,15 +143,16 @@ __device__ __forceinline__ void contract_reverse_dual(const PassTables<Real>& t,
                                                       const Real* v, const Real* vd, Real* lam, Real* mu, double* slot,
                                                       int lane) {
   if (t.ndst == 0) return;
-  // rank-weight gradients first (they read lam/mu of contraction nodes, which do not change below)
+  // rank-weight gradients first (they read lam/mu of contraction nodes, which do not change below);
+  // the per-weight sum of a few products in the compute precision, added to the FP64 slice
   if (gl.rw_off >= 0)
     for (int w = lane; w < gl.nw; w += kWarp) {
-      double s = 0.0;
+      Real s = Real(0);
       for (int p = gl.w_begin[w]; p < gl.w_begin[w + 1]; ++p) {
         const int src = gl.w_src[p], dst = gl.w_dst[p];
-        s += double(lam[dst]) * double(v[src]) + double(mu[dst]) * double(vd[src]);
+        s += lam[dst] * v[src] + mu[dst] * vd[src];
       }
-      slot[gl.rw_off + w] += s;
+      slot[gl.rw_off + w] += double(s);
     }
   for (int b = lane; b < NB; b += kWarp) {
     Real sl = Real(0), sm = Real(0);
