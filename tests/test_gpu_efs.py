@@ -329,6 +329,31 @@ def test_invalid_inputs_raise(lib, golden):
 
 
 
+@pytest.mark.parametrize("n", [4, 9])
+def test_edge_set_at_the_cutoff_is_the_fp64_set(lib, oracle_lib, golden, n):
+    """Simple cubic, a = r_c / 2, positions jittered by ~1e-9 A: every second- and several
+    further-neighbour distances lie within ~1e-9 relative of r_c, deep inside the band where
+    the FP32 engines' screens hand the decision to the exact FP64 test (image scan at 64 atoms,
+    cell lists at 729).  Edge counts of both engines equal the oracle's, and so do the results
+    (FP64 within 1e-10, FP32 within its bars)."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    from superlinear_gb300.sus2_format import read_sus2
+    rc = float(read_sus2(path)["max_dist"])
+    om = oracle_lib.OracleModel(path)
+    a = rc / 2
+    grid = np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+    rng = np.random.default_rng(77 + n)
+    fr = Frame(np.eye(3) * (a * n), grid * a + rng.normal(0, 1e-9, grid.shape), np.zeros(len(grid), dtype=np.int32))
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+    e, f, v, s = g64.calc_efs([fr])
+    assert g64.edge_count() == ne
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    assert g32.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL
+    check_fp32(e32[0], f32, e[0], f, fr.natoms)
+
+
 @pytest.mark.parametrize("cells", [3, 7])
 def test_non_finite_coordinates_raise(lib, golden, cells):
     """A NaN or infinite coordinate in a periodic frame (image scan at 216 atoms, cell lists at
