@@ -193,6 +193,22 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(values, world, device):
+    """Per-rank timings -> their maximum over the ranks (replicas: the job is as slow as its slowest
+    rank); every rank receives the result."""
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def replica_throughput(units_per_rank, world, ms):
+    """Whole-job throughput of `world` replicas that each processed units_per_rank in ms."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 def read_traffic(key):
     """DRAM bytes per launch of the dominant kernel from the committed ncu summary, or None."""
     try:
@@ -532,10 +548,7 @@ def run_ours(args):
     e2e_ms = 1e3 * float(np.mean(calls))
 
     # max over ranks
-    t_rank = torch.tensor([ms32, ms64, e2e_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
-    ms32, ms64, e2e_ms = (float(x) for x in t_rank.cpu())
+    ms32, ms64, e2e_ms = max_over_ranks([ms32, ms64, e2e_ms], world, dev)
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -614,14 +627,14 @@ def run_ours(args):
         c5 = bench_config5(sg, torch, 3, 3, args.bfgs_iters)
 
     line = {
-        "metric": METRIC, "value": n * world / (ms32 / 1e3), "unit": "atom-steps/s", "n_gpus": world,
+        "metric": METRIC, "value": replica_throughput(n, world, ms32), "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "static_l3k4o2_diamond4096", "model": "Static L3/K4/O2 (1 species, C)", "atoms": n,
                    "edges": edges, "cutoff": 5.0, "cells": "8x8x8", "a": 3.567, "sigma": 0.08,
                    "step": "GPU edge build + energy/forces/virial", "l2": "flushed (256 MiB write) between steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "fp64_plain": {"ms_per_step": ms64, "value": n / (ms64 / 1e3), "fp32_over_fp64": ms64 / ms32},
+        "fp64_plain": {"ms_per_step": ms64, "value": replica_throughput(n, world, ms64), "fp32_over_fp64": ms64 / ms32},
         "stages_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in st32.items() if v[1]},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
@@ -641,7 +654,7 @@ def run_ours(args):
                          "sample": f"{nev} E/F/virial evaluations of the same 4,096-atom frame by the FP64 CPU "
                                    f"restatement on {threads} threads, edge build excluded "
                                    f"({1e3 * te / max(nev, 1):.1f} ms each)"},
-        "e2e": {"value": n / (e2e_ms / 1e3), "unit": "atom-steps/s",
+        "e2e": {"value": replica_throughput(n, world, e2e_ms), "unit": "atom-steps/s",
                 "h2d_bytes_per_step": n * 3 * 8 + n * 4 + 9 * 8,
                 "d2h_bytes_per_step": 8 + n * 3 * 8 + 6 * 8 + n * 8, "ms_per_step": e2e_ms,
                 "api": "sus2g_calc_efs_host (C ABI, host buffers)"},
