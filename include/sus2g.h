@@ -235,21 +235,25 @@ int sus2g_trainer_set_inv_hess_diagonal(sus2g_trainer trainer, const double* dia
 
 /* ---- allocation-free Static E / F / virial ------------------------------------------------------
  * No counterpart in the reference: this entry point exists for callers that cannot allocate device
- * memory during a step -- code recording into a CUDA stream capture, MD drivers whose device memory
- * comes from a pre-sized arena, integrations that forbid driver allocations in their time loop.
- * Every other entry point may grow engine-owned buffers with cudaMalloc; this one allocates
- * nothing: its scratch is a fixed file-scope device array.
+ * memory during a step -- MD drivers whose device memory comes from a pre-sized arena, and
+ * integrations that forbid driver allocations in their time loop.  Every other entry point may
+ * grow engine-owned buffers with cudaMalloc; this one allocates nothing: its scratch is a fixed
+ * file-scope device array (about 22 MiB, held by every GPU that loads the library until exit).
  *   All array arguments are DEVICE pointers on the engine's device; the engine must hold a Static
  *   model in FP32-bulk form.  natoms centre atoms (0..natoms-1) of nall >= natoms atoms;
- *   types[nall]; edges in CSR by centre: row[natoms + 1] (row[0] = 0, row[natoms] = nedges),
- *   nbr[nedges] (0..nall-1), vec[3 * nedges] = x_j - x_i (A).  Outputs (device, any may be NULL):
- *   energy[1], forces[3 * nall] (overwritten), virial[6] (xx, yy, zz, xy, xz, yz),
+ *   types[nall]; edges in CSR by centre: row[natoms + 1] (row[0] = 0, row[natoms] = nedges,
+ *   non-decreasing), nbr[nedges] (0..nall-1), vec[3 * nedges] = x_j - x_i (A).  Outputs (device,
+ *   any may be NULL): energy[1], forces[3 * nall] (overwritten), virial[6] (xx, yy, zz, xy, xz, yz),
  *   site_energy[natoms].
- *   Limits: natoms <= 16384 and nedges <= 524288; larger calls are rejected with an error.
+ *   Limits: natoms <= 16384, nall <= 65536 and nedges <= 524288; larger calls are rejected with an
+ *   error (code 6).  Bad rows or neighbour indices return 21, a species outside [0, C) 26, a zero
+ *   or non-finite edge length 24; the device reads only sanitised copies of rows and neighbour
+ *   indices, so bad input causes no out-of-range access.  Forces are gathered per atom in a fixed
+ *   order (no floating-point atomics): results are bitwise reproducible.
  *   The first call on a device looks up the scratch array's device address for that device
- *   (cudaGetSymbolAddress); make that first call before any stream capture.  Calls share the
- *   scratch array: calls that overlap on the GPU race and must be serialised by the caller.
- *   The call synchronises the engine's stream to report input errors. */
+ *   (cudaGetSymbolAddress).  Calls share the scratch array: calls that overlap on the GPU race and
+ *   must be serialised by the caller.  The call synchronises the engine's stream to report input
+ *   errors. */
 int sus2g_static_efs_noalloc(sus2g_engine engine, int natoms, int nall, const int* types, const int* row,
                              const int* nbr, const double* vec, long long nedges, double* energy, double* forces,
                              double* virial, double* site_energy);
