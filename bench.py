@@ -297,7 +297,7 @@ def config5_set(sg, nframes=2048, seed=53):
     return frames
 
 
-def bench_config5(sg, torch, steps, warmup, bfgs_iters):
+def bench_config5(sg, torch, steps, warmup, bfgs_iters, cpu_frames=0):
     """Loss + gradient frames/s over the 2,048-frame L5 batch (FP32 bulk and FP64 plain, one step =
     one Trainer.loss_grad as a BFGS iteration calls it), then bfgs_iters BFGS iterations in FP32
     (each: line-search evaluations through the captured loss+gradient graph and the device-side
@@ -338,18 +338,45 @@ def bench_config5(sg, torch, steps, warmup, bfgs_iters):
     (l32, g32), (l64, g64) = losses["fp32"], losses["fp64"]
     out["fp32_error"] = {"loss_rel": abs(l32 - l64) / abs(l64),
                          "grad_rel_norm": float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))}
+    if cpu_frames > 0:
+        sample = frames[::max(1, len(frames) // cpu_frames)][:cpu_frames]
+        nd, tcpu, nw = cpu_train_parallel(sample, C5_MODEL)
+        out["cpu_baseline"] = {"value": nd / tcpu, "unit": "frames/s", "cores": nw, "kind": "port",
+                               "sample": f"loss + gradient of {nd} frames (every {max(1, len(frames) // cpu_frames)}"
+                                         f"th of the batch, {sum(f.natoms for f in sample)} atoms) by the FP64 CPU "
+                                         f"restatement, {nw} processes: {tcpu:.2f} s"}
+        out["fp32_over_cpu"] = out["fp32"]["frames_per_s"] / out["cpu_baseline"]["value"]
     return out
 
 
-def cpu_train_sample(frames, min_seconds=8.0):
-    """Oracle port loss + gradient frames/s over the first frames of the batch (one thread)."""
+def _cpu_train_warm(_):
     import oracle as orc
-    m = orc.OracleModel(TRAIN_MODEL)
-    done, t0 = 0, time.perf_counter()
-    while done == 0 or (done < len(frames) and time.perf_counter() - t0 < min_seconds):
-        orc.loss_grad(m, frames[done:done + 1], *TRAIN_WEIGHTS)
-        done += 1
-    return done, time.perf_counter() - t0
+    orc.lib()
+    time.sleep(0.2)  # keeps this worker busy so that the warm-up tasks reach every worker
+    return 0
+
+
+def _cpu_train_chunk(job):
+    model_path, frames = job
+    import oracle as orc
+    orc.loss_grad(orc.OracleModel(model_path), frames, *TRAIN_WEIGHTS)
+    return len(frames)
+
+
+def cpu_train_parallel(frames, model_path, workers=None):
+    """Loss + gradient of `frames` by the FP64 CPU restatement in `workers` processes (all host
+    cores by default), frames dealt round-robin; returns (frames done, wall seconds).  The pool is
+    started with spawn and warmed (library loaded in every worker) outside the timed region."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    workers = max(1, min(workers or (os.cpu_count() or 1), len(frames)))
+    chunks = [frames[k::workers] for k in range(workers)]
+    with cf.ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+        list(ex.map(_cpu_train_warm, range(workers)))
+        t0 = time.perf_counter()
+        done = sum(ex.map(_cpu_train_chunk, [(model_path, c) for c in chunks]))
+        dt = time.perf_counter() - t0
+    return done, dt, workers
 
 
 def cpu_sample(frame, threads, min_seconds=8.0, max_evals=50):
@@ -587,6 +614,7 @@ def run_ours(args):
         F4 = torch.zeros(fr4.natoms, 3, dtype=torch.float64, device=dev)
         c4 = fr4.cell.reshape(1, 9).copy()
         n4 = np.array([fr4.natoms], np.int32)
+        results = {}
         for prec, key, reps in ((sg.FP32, "fp32", 5), (sg.FP64, "fp64", 2)):
             e4 = sg.Engine(m4, device, prec)
             e4.set_stream(stream.cuda_stream)
@@ -602,6 +630,7 @@ def run_ours(args):
             b.record(stream)
             b.synchronize()
             ms = a.elapsed_time(b) / reps
+            results[key] = (float(E.cpu()[0]), F4.cpu().numpy().copy())
             extra[key] = {"ms_per_step": ms, "atom_steps_per_s": fr4.natoms / (ms / 1e3), "edges": e4.edge_count()}
             if prec == sg.FP32:
                 e4.set_timing(True)
@@ -611,20 +640,43 @@ def run_ours(args):
                 e4.set_timing(False)
             del e4
         extra["fp32_over_fp64"] = extra["fp64"]["ms_per_step"] / extra["fp32"]["ms_per_step"]
+        (e32, f32), (e64, f64) = results["fp32"], results["fp64"]
+        dfn = np.linalg.norm(f32 - f64, axis=1)
+        extra["fp32_error"] = {"against": "FP64 plain GPU path on the same box (pinned to the FP64 oracle at "
+                                          "13,824 atoms of the same model and lattice by the GPU tests)",
+                               "force_max_ev_per_a": float(np.max(np.abs(f32 - f64))),
+                               "force_rms_ev_per_a": float(np.sqrt(np.mean(dfn ** 2))),
+                               "energy_ev_per_atom": abs(e32 - e64) / fr4.natoms,
+                               "bars": {"force_ev_per_a": 1e-5, "energy_ev_per_atom": 1e-6}}
+        if not args.skip_cpu_large:
+            # CPU baseline at this size: the FP64 CPU restatement, all host cores, one evaluation
+            # (edge build excluded and reported separately)
+            import oracle as orc
+            om4 = orc.OracleModel(EFFECT_MODEL)
+            threads = os.cpu_count() or 1
+            _, ne4, te4, tc4 = om4.efs_timed(fr4.cell, fr4.positions, fr4.types, threads=threads)
+            cpu4 = fr4.natoms / tc4
+            extra["cpu_baseline"] = {"value": cpu4, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                                     "sample": f"one E/F/virial evaluation of the 110,592-atom box ({ne4} edges) by the "
+                                               f"FP64 CPU restatement on {threads} threads: {tc4:.2f} s; edge build "
+                                               f"excluded ({te4:.2f} s)"}
+            extra["fp32_over_cpu"] = extra["fp32"]["atom_steps_per_s"] / cpu4
+            extra["fp64_over_cpu"] = extra["fp64"]["atom_steps_per_s"] / cpu4
 
     # training loss + gradient over the 256-frame Effect L3/K4/R2/O2 batch
     train = None
     if not args.skip_train:
         tframes, train = bench_training(sg, torch, max(3, args.steps // 2), args.warmup)
-        nd, tcpu = cpu_train_sample(tframes)
-        train["cpu_baseline"] = {"value": nd / tcpu, "unit": "frames/s", "cores": 1, "kind": "port",
-                                 "sample": f"loss + gradient of the first {nd} frames of the batch by the FP64 "
-                                           "CPU restatement (one thread)"}
+        nd, tcpu, nw = cpu_train_parallel(tframes, TRAIN_MODEL)
+        train["cpu_baseline"] = {"value": nd / tcpu, "unit": "frames/s", "cores": nw, "kind": "port",
+                                 "sample": f"loss + gradient of all {nd} frames of the batch by the FP64 CPU "
+                                           f"restatement, {nw} processes over interleaved frame shards: {tcpu:.2f} s"}
+        train["fp32_over_cpu"] = train["fp32"]["frames_per_s"] / train["cpu_baseline"]["value"]
 
     # training loss + gradient and BFGS over the 2,048-frame Effect L5/K8/R2/O2 batch
     c5 = None
     if not args.skip_config5:
-        c5 = bench_config5(sg, torch, 3, 3, args.bfgs_iters)
+        c5 = bench_config5(sg, torch, 3, 3, args.bfgs_iters, cpu_frames=128)
 
     line = {
         "metric": METRIC, "value": replica_throughput(n, world, ms32), "unit": "atom-steps/s", "n_gpus": world,
@@ -679,6 +731,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-effect", action="store_true", help="skip the 110,592-atom Effect measurement")
     ap.add_argument("--skip-train", action="store_true", help="skip the 256-frame training loss+gradient measurement")
+    ap.add_argument("--skip-cpu-large", action="store_true",
+                    help="skip the CPU baseline evaluation of the 110,592-atom box")
     ap.add_argument("--profile-only", action="store_true",
                     help="only the FP32 timed steps (for ncu captures); prints a short JSON line")
     ap.add_argument("--cells", type=int, default=8, help="diamond cells per edge (8 -> the 4,096-atom workload)")

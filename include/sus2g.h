@@ -71,6 +71,14 @@ int sus2g_engine_set_stream(sus2g_engine engine, void* cuda_stream);
 int sus2g_engine_take_launch_count(sus2g_engine engine, int* count);
 /* Number of directed edges of the last evaluation. */
 int sus2g_engine_edge_count(sus2g_engine engine, long long* count);
+/* The directed edge set of the last evaluation, copied to host arrays in centre order (each centre's
+ * edges sorted by neighbour, then periodic image): centre[k], neighbour[k] (atom indices within the
+ * batch), d[3k..3k+2] = x_j - x_i in the compute precision's record widened to double.  At most cap
+ * edges are written (any array may be NULL); *count receives the total.  Replaces reading the
+ * reference's neighbour lists: Neighborhoods::InitNbhs (src/neighborhoods.cpp:358) and the embedded
+ * harness's edge list (interfaces/lammps/tests/embedded_efs.cpp:46-66).  Synchronises. */
+int sus2g_engine_copy_edges(sus2g_engine engine, long long cap, int* centre, int* neighbour, double* d,
+                            long long* count);
 /* Stage timer (CUDA events on the engine's stream), the counterpart of the reference's
  * profile_every stage timers and Kernel::outer_profile (pair_sus2_embedded.cpp:261-264,320-361;
  * sus2_sl_kernel.h:33-35).  Stages: 0 edge build, 1 Static/outer pass, 2 gate forward pass,
@@ -221,11 +229,24 @@ int sus2g_trainer_rescale(sus2g_trainer trainer, double* params, double* scaling
 int sus2g_trainer_set_graph(sus2g_trainer trainer, int enabled);
 /* Dense BFGS from params (in/out) for at most max_iter accepted steps or until |grad| <= gtol:
  * replaces the MTPR_trainer::Train BFGS loop (dev_src/mtpr_trainer.cpp:4985-4997) over
- * BFGS::Iterate / UpdateInvHess (src/common/bfgs.cpp:251-329, 428-502); inverse Hessian,
- * direction and update in FP64 on the device.  history[max_iter + 1] (may be NULL) receives the
- * loss before the first and after each accepted step; *steps the accepted step count. */
+ * BFGS::Iterate / Linesearch::Iterate / UpdateInvHess (src/common/bfgs.cpp:251-329, 428-502,
+ * bfgs.h:121-290) on the raw parameter vector; inverse Hessian, direction and update in FP64 on
+ * the device.  Ends early, keeping the last accepted point, when a line search stagnates or
+ * takes more than 30 trials (dev_src/mtpr_trainer.cpp:5328-5333).  history[max_iter + 1] (may be
+ * NULL) receives the loss before the first and after each accepted step; *steps the accepted
+ * step count; params the last accepted point. */
 int sus2g_trainer_bfgs(sus2g_trainer trainer, double* params, int max_iter, double gtol, double* history,
                        int* steps);
+/* Line search of the following sus2g_trainer_bfgs calls: 0 (default) the reference's Linesearch
+ * (src/common/bfgs.h:31-290; the trial sequence is the reference's), 1 an interpolating strong-Wolfe
+ * search (fewer evaluations per accepted step, not the reference's sequence). */
+int sus2g_trainer_set_line_search(sus2g_trainer trainer, int mode);
+/* Trial points of the last sus2g_trainer_bfgs call, one per objective evaluation in order: loss[k],
+ * points[k * nparams ...] and accepted[k] (1 where BFGS took the point as its new start), at most
+ * cap of them (arrays may be NULL); *count = the number recorded.  The record the reference's
+ * trainer log gives per step (dev_src/mtpr_trainer.cpp:4640-4830). */
+int sus2g_trainer_bfgs_trials(sus2g_trainer trainer, int cap, double* loss, double* points, int* accepted,
+                              int* count);
 
 /* Initial inverse Hessian of the following sus2g_trainer_bfgs calls: diag[n] (n = the parameter
  * count; finite, positive) on the diagonal, zero elsewhere; n = 0 restores the identity.  Replaces

@@ -52,6 +52,9 @@ def lib():
                                     _dp, ctypes.c_char_p, ctypes.c_int]
         L.orc_efs_edges.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _ip, ctypes.c_int, _ip, _ip, _dp,
                                     _dp, _dp, _dp, _dp, ctypes.c_char_p, ctypes.c_int]
+        L.orc_edges.restype = ctypes.c_longlong
+        L.orc_edges.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_longlong, _ip, _ip, _dp,
+                                ctypes.c_char_p, ctypes.c_int]
         L.orc_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, _ip, _dp, _dp, _dp, _dp, ctypes.c_char_p,
                                ctypes.c_int]
         L.orc_layout.argtypes = [ctypes.c_void_p, _ip]
@@ -137,6 +140,21 @@ class OracleModel:
         if ne < 0:
             raise RuntimeError(err.value.decode())
         return float(e[0]), int(ne), float(sec[0]), float(sec[1])
+
+    def edges(self, cell, pos):
+        """The frame's directed edges (centre[E], neighbour[E], d[E, 3] = x_j - x_i), centre order."""
+        cell = np.ascontiguousarray(cell, dtype=np.float64).reshape(9)
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        err = ctypes.create_string_buffer(512)
+        n = pos.shape[0]
+        ne = lib().orc_edges(self._h, n, _d(cell), _d(pos), 0, None, None, None, err, 512)
+        if ne < 0:
+            raise RuntimeError(err.value.decode())
+        ei = np.zeros(ne, np.int32)
+        ej = np.zeros(ne, np.int32)
+        d = np.zeros((ne, 3))
+        lib().orc_edges(self._h, n, _d(cell), _d(pos), ne, _i(ei), _i(ej), _d(d), err, 512)
+        return ei, ej, d
 
     def efs_edges(self, nowned, types, ei, ej, d):
         types = np.ascontiguousarray(types, dtype=np.int32)
@@ -504,3 +522,203 @@ def rescale(model: "OracleModel", frames, wE: float, wF: float, wS: float, weigh
     model.scaling = best_s
     model.set_params(best_p)
     return best_p, best_s, solves[0]
+
+
+# ------------------------------------------------------------------------------------------------
+# BFGS with the reference's line search (src/common/bfgs.h:31-290 Linesearch, src/common/bfgs.cpp
+# BFGS::Iterate :251-329, UpdateInvHess :428-502, FormDenseDirection :174).  The decision rules
+# are kept exactly -- the trial sequence must match the reference's -- in this module's own code.
+# ------------------------------------------------------------------------------------------------
+HUGE = 9.9e99            # the reference's HUGE_DOUBLE (src/common/utils.h:24), initial right_f / f_start
+RIGHT_F_SENTINEL = 9e99  # the value Linesearch::Iterate compares right_f with (bfgs.h:165); the
+                         # reset value is HUGE, so that clause only fires if a trial returns 9e99
+EPS = np.finfo(float).eps
+
+
+class RefLineSearch:
+    """One-dimensional search along the BFGS direction in reverse communication: iterate(f, g)
+    takes the objective and its slope at x and sets the next trial x (Linesearch, bfgs.h:31-290).
+    (lx, lf, lg) bracket the left end, (rx, rf, rg) the right end, (px, pf, pg) the previous
+    trial."""
+
+    def __init__(self):
+        self.lf = self.lg = self.px = self.pf = self.pg = 0.0
+        self.reset()
+
+    def reset(self, step=1.0):
+        self.stagnated = False
+        self.x = self.lx = 0.0
+        self.rx = step
+        self.rf = self.rg = HUGE
+
+    def reduce_step(self, ratio=0.25):
+        self.x = self.px + ratio * (self.x - self.px)
+
+    def _tolerance(self):
+        return 64.0 * EPS * max(1.0, abs(self.lx), abs(self.x), abs(self.rx), abs(self.px))
+
+    def _best(self, f):
+        bx, bf = self.x, f
+        if self.lf < bf:
+            bx, bf = self.lx, self.lf
+        if self.rf < bf:
+            bx = self.rx
+        return bx
+
+    def _recover(self, f, g, tol):
+        if not self.lx < self.rx:
+            return False
+        r = 0.5 * (self.lx + self.rx)
+        if abs(r - self.x) <= tol:
+            if self.x > self.lx:
+                t = float(np.nextafter(self.x, self.lx))
+                if t != self.x and t >= self.lx:
+                    r = t
+            if abs(r - self.x) <= tol and self.x < self.rx:
+                t = float(np.nextafter(self.x, self.rx))
+                if t != self.x and t <= self.rx:
+                    r = t
+        if abs(r - self.x) <= tol:
+            return False
+        self.px, self.pf, self.pg = self.x, f, g
+        self.x = r
+        return True
+
+    def _to_prev(self, f, g):
+        self.px, self.pf, self.pg = self.x, f, g
+
+    def iterate(self, f, g):
+        x = self.x
+        if x == 0:
+            self.lx, self.lf, self.lg = x, f, g
+            if g > 0:
+                raise RuntimeError("line search along an increasing direction")
+            self._to_prev(f, g)
+            self.x = self.rx
+            return
+        tol = self._tolerance()
+        if abs(self.px - x) <= tol:
+            if self._recover(f, g, tol):
+                return
+            if self.rx - self.lx <= tol:
+                self.stagnated = True
+                self.x = self._best(f)
+                return
+            raise RuntimeError("line search stagnated: unable to recover a distinct step")
+        if x == self.rx or (x > self.lx and self.rf == RIGHT_F_SENTINEL):
+            self.rx, self.rf, self.rg = x, f, g
+        if self.rg < 0 and self.rf < self.lf:
+            if x > self.rx:
+                self.lx, self.lf, self.lg = self.rx, self.rf, self.rg
+                self.rx, self.rf, self.rg = x, f, g
+        else:
+            if g < 0 and f < self.lf and x > self.lx:
+                if x > self.rx:
+                    if f > self.rf:
+                        self._to_prev(f, g)
+                        self.lx, self.lf, self.lg = self.rx, self.rf, self.rg
+                        self.rx, self.rf, self.rg = x, f, g
+                        self.x = 0.5 * (self.lx + self.rx)
+                        return
+                    self.rx, self.rf, self.rg = x, f, g
+                else:
+                    self.lx, self.lf, self.lg = x, f, g
+            if g > 0 and x < self.rx:
+                self.rx, self.rf, self.rg = x, f, g
+        lx, lf, lg, rx, rg = self.lx, self.lf, self.lg, self.rx, self.rg
+        if f > lf + 0.1 * lg * (x - lx):
+            # insufficient decrease: the minimiser of a parabola fitted to log(f - f_lin)
+            slope = -lg * (x - lx)
+            nx = lx + 0.5 * (x - lx)
+            arg = f - lf + slope
+            if slope > 0.0 and arg > 0.0 and np.isfinite(slope) and np.isfinite(arg):
+                f0, g0, f1 = np.log(slope), lg / slope, np.log(arg)
+                den = f1 - f0 - g0 * (x - lx)
+                if np.isfinite(den) and den != 0.0:
+                    nx = lx - 0.5 * g0 * (x - lx) * (x - lx) / den
+            if nx > rx and rg > 0:
+                nx = lx + 0.5 * (x - lx)
+            elif (nx - lx > 3.0 * rx - 2.0 * lx) and rg < 0:
+                nx = lx + 3.0 * (rx - lx)
+            if not np.isfinite(nx):
+                nx = lx + 0.5 * (x - lx)
+            self._to_prev(f, g)
+            self.x = float(nx)
+            return
+        if (g - self.pg) / (x - self.px) < 0.0:
+            # negative curvature along the line
+            self._to_prev(f, g)
+            self.x = 3 * rx - 2 * lx if rg < 0 else x + 0.5 * (rx - x)
+            return
+        # secant step on the slopes
+        nx = x - g * (x - self.px) / (g - self.pg) if g != self.pg else float("nan")
+        if not np.isfinite(nx):
+            nx = lx + 0.5 * (rx - lx)
+        self._to_prev(f, g)
+        self.x = nx
+        if nx > rx:
+            if rg > 0:
+                self.x = 0.5 * lx + 0.5 * rx
+            elif nx > 3 * rx - 2 * lx:
+                self.x = 3 * rx - 2 * lx
+            return
+        if nx < lx:
+            self._to_prev(f, g)
+            self.x = 0.5 * lx + 0.5 * rx
+
+
+def bfgs_reference(fg, x0, iterations, inv_hess_diagonal=None, max_evals=400, c1=0.1, c2=0.5):
+    """Minimise with BFGS as the reference's engine does (Set_x, optional SetInvHessDiagonal, then
+    Iterate once per objective evaluation).  fg(x) -> (f, g).  Returns (trials, x_accepted): every
+    evaluated point as (x, f, accepted), up to `iterations` accepted steps beyond the start, and
+    the last accepted point."""
+    x = np.array(x0, dtype=float)
+    n = x.size
+    H = np.diag(np.asarray(inv_hess_diagonal, float)) if inv_hess_diagonal is not None else np.eye(n)
+    p = np.zeros(n)
+    x_start, g_start = x.copy(), np.zeros(n)
+    f_start, pg_start = HUGE, HUGE
+    ls = RefLineSearch()
+    trials, accepted = [], -1
+    while accepted < iterations and len(trials) < max_evals:
+        f, g = fg(x)
+        xe = x.copy()
+        if not np.isfinite(f) or not np.all(np.isfinite(g)):
+            if ls.x == 0.0:
+                raise RuntimeError("non-finite objective outside a line search")
+            ls.reduce_step(0.25)
+            x = x_start + ls.x * p
+            trials.append((xe, f, False))
+            continue
+        pg = float(g @ p)
+        if f > f_start + c1 * ls.x * pg_start or abs(pg) > c2 * abs(pg_start):
+            ls.iterate(f, pg)
+            if ls.stagnated:
+                trials.append((xe, f, False))
+                break
+            x = x_start + ls.x * p
+            trials.append((xe, f, False))
+            continue
+        # accepted: inverse-Hessian update with s = alpha p, y = g - g_start (skipped while
+        # alpha p . y <= 64 eps), new direction p = -H g, a fresh line search from alpha = 1
+        alpha = ls.x
+        dg = g - g_start
+        py = float(np.sum(alpha * p * dg))
+        if not np.isfinite(py):
+            raise RuntimeError("non-finite curvature")
+        if py > 64.0 * EPS:
+            yC = H @ dg
+            foo = (py + float(yC @ dg)) / (py * py)
+            if np.isfinite(foo):
+                H += alpha * alpha * foo * np.outer(p, p) - (alpha / py) * (np.outer(p, yC) + np.outer(yC, p))
+        p = -(H @ g)
+        pg = float(g @ p)
+        ls.reset()
+        x_start, g_start, f_start, pg_start = x.copy(), g.copy(), f, pg
+        if pg > 0:
+            raise RuntimeError("BFGS: ascent direction")
+        ls.iterate(f, pg)
+        x = x_start + ls.x * p
+        trials.append((xe, f, True))
+        accepted += 1
+    return trials, x_start

@@ -8,6 +8,10 @@
 //     {"cfg": c, "grad": [...]}                       AccumulateEFSCombinationGrad
 //                                                     (src/basic_mlip.cpp:421, dev_src/mtpr.cpp:9188)
 //
+// Usage: ref-grad --bfgs MODEL CFG wE wF wS weighting ITERS [DIAG]
+//   The reference BFGS engine over Coeff() on the trainer objective (loss / K); prints every trial
+//   point and its objective value (see the mode's comment below).
+//
 // Usage: ref-grad --linear MODEL CFG wE wF wS [weighting]
 //   MTPR_trainer::TrainLinear on the labelled CFG; prints {"coeffs": [...]} after the solve.
 //
@@ -94,6 +98,70 @@ int main(int argc, char** argv) {
     std::printf(", \"metrics\": ");
     vec(metrics, 6);
     std::printf(", \"configs\": %zu}\n", train.size());
+    return 0;
+  }
+  if (std::string(argv[1]) == "--bfgs") {
+    // ref-grad --bfgs MODEL CFG wE wF wS weighting ITERS: the reference's BFGS engine
+    // (BFGS::Iterate / Linesearch::Iterate / UpdateInvHess, src/common/bfgs.{h,cpp}) in reverse
+    // communication over the raw parameter vector Coeff(), minimising the trainer objective
+    // f = loss / K, g = grad / K of NonLinearRegression::CalcObjectiveFunctionGrad (the same terms
+    // as --loss, gate-x term off), from the model's parameters and the identity inverse Hessian.
+    // Prints, per objective evaluation, {"eval": k, "f": f, "x": [...], "accepted": a} where a says
+    // whether BFGS took the evaluated point as its new line-search start; stops after ITERS
+    // accepted steps beyond the starting point (or 400 evaluations).  DIAG (optional) is a file of
+    // Coeff()-many values given to BFGS::SetInvHessDiagonal after Set_x, as the trainer does
+    // (dev_src/mtpr_trainer.cpp:3063-3068).
+    if (argc < 9) { std::fprintf(stderr, "usage: ref-grad --bfgs MODEL CFG wE wF wS weighting ITERS [DIAG]\n"); return 2; }
+    MLMTPR mtpr(argv[2]);
+    struct Objective : NonLinearRegression {
+      using NonLinearRegression::NonLinearRegression;
+      double loss() const { return loss_; }
+      const std::vector<double>& grad() const { return loss_grad_; }
+    };
+    struct TracedBFGS : BFGS {
+      const Array1D& start_x() const { return x_start; }
+    };
+    Objective obj(&mtpr, std::stod(argv[4]), std::stod(argv[5]), std::stod(argv[6]), 0.0, 0.0);
+    obj.std_scaling = 0.0;
+    obj.stdd_scaling = 0.0;
+    obj.radial_smooth_regularization = 0.0;
+    obj.fixed_atomic_energy_weight = 0.0;
+    obj.weighting = argv[7];
+    obj.gate_x_l2_regularization = 0.0;
+    const int iters = std::stoi(argv[8]);
+    std::ifstream in(argv[3]);
+    std::vector<Configuration> train;
+    Configuration c;
+    while (c.Load(in)) train.push_back(c);
+    const double K = static_cast<double>(train.size());
+    const int n = mtpr.CoeffCount();
+    TracedBFGS bfgs;
+    bfgs.Set_x(mtpr.Coeff(), n);
+    if (argc > 9) {
+      std::ifstream df(argv[9]);
+      Array1D diag(n);
+      for (int i = 0; i < n; ++i)
+        if (!(df >> diag[i])) { std::fprintf(stderr, "diagonal: expected %d values\n", n); return 3; }
+      bfgs.SetInvHessDiagonal(diag);
+    }
+    Array1D g(n);
+    std::vector<double> xe(n);
+    int accepted = -1;
+    for (int k = 0; k < 400 && accepted < iters; ++k) {
+      // the trainer writes the optimiser's point straight into Coeff(), which CalcEFS reads (no
+      // DistributeCoeffs: that rebuilds the readout block from the model's own copy)
+      for (int i = 0; i < n; ++i) xe[i] = mtpr.Coeff()[i] = bfgs.x(i);
+      obj.CalcObjectiveFunctionGrad(train);
+      const double f = obj.loss() / K;
+      for (int i = 0; i < n; ++i) g[i] = obj.grad()[i] / K;
+      bfgs.Iterate(f, g);
+      bool took = true;
+      for (int i = 0; i < n && took; ++i) took = bfgs.start_x()[i] == xe[i];
+      if (took) ++accepted;
+      std::printf("{\"eval\": %d, \"f\": %.17g, \"accepted\": %s, \"x\": ", k, f, took ? "true" : "false");
+      vec(xe.data(), n);
+      std::printf("}\n");
+    }
     return 0;
   }
   if (std::string(argv[1]) == "--rescale") {

@@ -997,6 +997,23 @@ long long orc_efs_timed(void* mp, int n, const double* cell, const double* pos, 
   }
 }
 
+long long orc_edges(void* mp, int n, const double* cell, const double* pos, long long cap, int* ei, int* ej,
+                    double* d, char* err, int errlen) {
+  try {
+    const Model& m = *static_cast<Model*>(mp);
+    const vector<Edge> edges = image_edges(n, cell, pos, m.rmax);
+    for (size_t k = 0; k < edges.size() && static_cast<long long>(k) < cap; ++k) {
+      if (ei) ei[k] = edges[k].i;
+      if (ej) ej[k] = edges[k].j;
+      if (d) for (int q = 0; q < 3; ++q) d[3 * k + q] = edges[k].d[q];
+    }
+    return static_cast<long long>(edges.size());
+  } catch (const std::exception& e) {
+    set_err(err, errlen, e.what());
+    return -1;
+  }
+}
+
 int orc_efs_edges(void* mp, int nowned, int nall, const int* types, int nedges, const int* ei, const int* ej,
                   const double* d, double* energy, double* forces, double* virial, double* site, char* err, int errlen) {
   try {

@@ -27,6 +27,11 @@ long long orc_efs(void* model, int n, const double* cell, const double* pos, con
 long long orc_efs_timed(void* model, int n, const double* cell, const double* pos, const int* types, double* energy,
                         double* forces, double* virial, double* site, int threads, double* seconds, char* err,
                         int errlen);
+/* The periodic frame's directed edge set (strict r < cutoff, self images included, d = x_j - x_i),
+ * in centre order (the image-scan rule of Neighborhoods::InitNbhs, src/neighborhoods.cpp:358):
+ * writes at most cap edges (arrays may be NULL), returns the total or -1. */
+long long orc_edges(void* model, int n, const double* cell, const double* pos, long long cap, int* ei, int* ej,
+                    double* d, char* err, int errlen);
 /* Caller edge list (single domain, owned centres 0..nowned-1 of nall atoms). */
 int orc_efs_edges(void* model, int nowned, int nall, const int* types, int nedges, const int* ei, const int* ej,
                   const double* d, double* energy, double* forces, double* virial, double* site, char* err, int errlen);

@@ -34,6 +34,8 @@ SIGNATURES = {
     "sus2g_engine_set_stream": (ctypes.c_int, [_vp, _vp]),
     "sus2g_engine_take_launch_count": (ctypes.c_int, [_vp, _ip]),
     "sus2g_engine_edge_count": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
+    "sus2g_engine_copy_edges": (ctypes.c_int, [_vp, ctypes.c_longlong, _ip, _ip, _dp,
+                                               ctypes.POINTER(ctypes.c_longlong)]),
     "sus2g_engine_set_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_set_step_graph": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_set_pdl": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -69,6 +71,8 @@ SIGNATURES = {
     "sus2g_trainer_train_linear": (ctypes.c_int, [_vp, _dp]),
     "sus2g_trainer_bfgs": (ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_double, _dp, _ip]),
     "sus2g_trainer_set_inv_hess_diagonal": (ctypes.c_int, [_vp, _dp, ctypes.c_int]),
+    "sus2g_trainer_set_line_search": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sus2g_trainer_bfgs_trials": (ctypes.c_int, [_vp, ctypes.c_int, _dp, _dp, _ip, _ip]),
 }
 
 _lib = None

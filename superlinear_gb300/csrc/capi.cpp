@@ -160,6 +160,14 @@ int sus2g_engine_edge_count(sus2g_engine e, long long* count) {
   return guarded([&] { need(e && count, "engine/count"); *count = e->engine->nedges(); });
 }
 
+int sus2g_engine_copy_edges(sus2g_engine e, long long cap, int* centre, int* neighbour, double* d,
+                            long long* count) {
+  return guarded([&] {
+    need(e && count && cap >= 0, "engine/count/capacity");
+    e->engine->copy_edges(cap, centre, neighbour, d, count);
+  });
+}
+
 int sus2g_engine_set_timing(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_timing(enabled != 0); });
 }

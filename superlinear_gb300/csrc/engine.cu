@@ -1089,6 +1089,42 @@ long long Engine::nedges() {
   return exact_edges_;
 }
 
+void Engine::copy_edges(long long cap, int* centre, int* neighbour, double* d, long long* count) {
+  const long long total = nedges();
+  *count = total;
+  const int nc = ncentres_;
+  std::vector<int> row(static_cast<size_t>(nc) + 1), row_end(static_cast<size_t>(nc));
+  std::vector<int> nbr(static_cast<size_t>(std::max<long long>(1, nedges_)));
+  const size_t rec = precision_ == kFP32 ? sizeof(EdgeF) : sizeof(EdgeD);
+  std::vector<unsigned char> d4(rec * static_cast<size_t>(std::max<long long>(1, nedges_)));
+  if (nc) {
+    SUS2G_CUDA(cudaMemcpyAsync(row.data(), row_.ptr, sizeof(int) * nc, cudaMemcpyDeviceToHost, stream_));
+    SUS2G_CUDA(cudaMemcpyAsync(row_end.data(), d_row_end(), sizeof(int) * nc, cudaMemcpyDeviceToHost, stream_));
+  }
+  if (nedges_) {
+    SUS2G_CUDA(cudaMemcpyAsync(nbr.data(), nbr_.ptr, sizeof(int) * nedges_, cudaMemcpyDeviceToHost, stream_));
+    SUS2G_CUDA(cudaMemcpyAsync(d4.data(), d4_.ptr, rec * nedges_, cudaMemcpyDeviceToHost, stream_));
+  }
+  SUS2G_CUDA(cudaStreamSynchronize(stream_));
+  long long k = 0;
+  for (int i = 0; i < nc; ++i)
+    for (int e = row[i]; e < row_end[i]; ++e, ++k) {
+      if (k >= cap) continue;
+      if (centre) centre[k] = i;
+      if (neighbour) neighbour[k] = nbr[e];
+      if (d) {
+        if (precision_ == kFP32) {
+          const EdgeF& x = reinterpret_cast<const EdgeF*>(d4.data())[e];
+          d[3 * k] = x.x; d[3 * k + 1] = x.y; d[3 * k + 2] = x.z;
+        } else {
+          const EdgeD& x = reinterpret_cast<const EdgeD*>(d4.data())[e];
+          d[3 * k] = x.x; d[3 * k + 1] = x.y; d[3 * k + 2] = x.z;
+        }
+      }
+    }
+  if (k != total) throw Error(20, "edge rows disagree with the edge count");
+}
+
 void* Engine::pinned(size_t bytes) {
   if (bytes > pinned_bytes_) {
     if (pinned_) cudaFreeHost(pinned_);

@@ -133,6 +133,11 @@ class Engine {
   // Directed edges of the last build (for cell-list-only batches read back from the device on
   // first request: the build itself does not synchronise).
   long long nedges();
+  // Copies the directed edges of the last build to host arrays in centre order, each centre's
+  // edges in the engine's order (sorted by neighbour, then image): centre[k], neighbour[k],
+  // d[3k..3k+2] = x_j - x_i (the compute precision's record, widened to double).  Writes at most
+  // cap edges (any array may be null); *count = the total.  Synchronises the stream.
+  void copy_edges(long long cap, int* centre, int* neighbour, double* d, long long* count);
   // number of kernels launched by the last build_edges + efs (for launch accounting)
   int last_launches() const { return launches_; }
   void reset_launch_count() { launches_ = 0; }

@@ -382,6 +382,14 @@ __global__ void k_bfgs_update(int n, double* H, const double* s, const double* H
   H[t] += -rho * (Hy[i] * s[j] + s[i] * Hy[j]) + (rho * rho * yHy + rho) * s[i] * s[j];
 }
 
+// H <- H + a p p^T + b (p c^T + c p^T)  (UpdateInvHess's three rank-1 updates, bfgs.cpp:470-490)
+__global__ void k_bfgs_rank2(int n, double* H, const double* p, const double* c, double a, double b) {
+  const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= static_cast<long long>(n) * n) return;
+  const int i = static_cast<int>(t / n), j = static_cast<int>(t - static_cast<long long>(i) * n);
+  H[t] += a * p[i] * p[j] + b * (p[i] * c[j] + c[i] * p[j]);
+}
+
 __global__ void k_scaled_identity(int n, double* H, double diag) {
   const long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= static_cast<long long>(n) * n) return;
@@ -407,6 +415,134 @@ __global__ void k_sub(int n, const double* a, const double* b, double* out) {
 }
 
 }  // namespace
+
+// One-dimensional search along the BFGS direction in reverse communication, with the decision rules
+// of the reference's Linesearch (src/common/bfgs.h:31-290): iterate(f, g) takes the objective and
+// its slope at the trial x and sets the next trial.  (lx, lf, lg) is the left bracket end, (rx, rf,
+// rg) the right one, (px, pf, pg) the previous trial.  The rules are kept exactly so that the trial
+// sequence is the reference's; oracle/oracle.py (RefLineSearch) restates the same rules.
+struct RefLineSearch {
+  static constexpr double kHuge = 9.9e99;          // HUGE_DOUBLE (src/common/utils.h:24)
+  static constexpr double kRightSentinel = 9e99;   // the value bfgs.h:165 compares right_f with
+  double x = 0, lx = 0, lf = 0, lg = 0, rx = 1, rf = kHuge, rg = kHuge, px = 0, pf = 0, pg = 0;
+  bool stagnated = false;
+
+  void reset(double step = 1.0) {
+    stagnated = false;
+    x = lx = 0.0;
+    rx = step;
+    rf = rg = kHuge;
+  }
+  void reduce_step(double ratio) { x = px + ratio * (x - px); }
+  void to_prev(double f, double g) { px = x; pf = f; pg = g; }
+  double tolerance() const {
+    const double scale = std::max({1.0, std::abs(lx), std::abs(x), std::abs(rx), std::abs(px)});
+    return 64.0 * std::numeric_limits<double>::epsilon() * scale;
+  }
+  double best(double f) const {
+    double bx = x, bf = f;
+    if (lf < bf) { bx = lx; bf = lf; }
+    if (rf < bf) bx = rx;
+    return bx;
+  }
+  bool recover(double f, double g, double tol) {
+    if (!(lx < rx)) return false;
+    double r = 0.5 * (lx + rx);
+    if (std::abs(r - x) <= tol) {
+      if (x > lx) {
+        const double t = std::nextafter(x, lx);
+        if (t != x && t >= lx) r = t;
+      }
+      if (std::abs(r - x) <= tol && x < rx) {
+        const double t = std::nextafter(x, rx);
+        if (t != x && t <= rx) r = t;
+      }
+    }
+    if (std::abs(r - x) <= tol) return false;
+    to_prev(f, g);
+    x = r;
+    return true;
+  }
+  void iterate(double f, double g) {
+    if (x == 0) {
+      lx = x; lf = f; lg = g;
+      if (g > 0) throw Error(5, "BFGS: line search along an increasing direction");
+      to_prev(f, g);
+      x = rx;
+      return;
+    }
+    const double tol = tolerance();
+    if (std::abs(px - x) <= tol) {
+      if (recover(f, g, tol)) return;
+      if (rx - lx <= tol) {
+        stagnated = true;
+        x = best(f);
+        return;
+      }
+      throw Error(5, "BFGS: line search stagnated without a distinct step");
+    }
+    if (x == rx || (x > lx && rf == kRightSentinel)) { rx = x; rf = f; rg = g; }
+    if (rg < 0 && rf < lf) {
+      if (x > rx) {
+        lx = rx; lf = rf; lg = rg;
+        rx = x; rf = f; rg = g;
+      }
+    } else {
+      if (g < 0 && f < lf && x > lx) {
+        if (x > rx) {
+          if (f > rf) {
+            to_prev(f, g);
+            lx = rx; lf = rf; lg = rg;
+            rx = x; rf = f; rg = g;
+            x = 0.5 * (lx + rx);
+            return;
+          }
+          rx = x; rf = f; rg = g;
+        } else {
+          lx = x; lf = f; lg = g;
+        }
+      }
+      if (g > 0 && x < rx) { rx = x; rf = f; rg = g; }
+    }
+    if (f > lf + 0.1 * lg * (x - lx)) {
+      // insufficient decrease: minimiser of a parabola fitted to log(f - f_lin)
+      const double slope = -lg * (x - lx), arg = f - lf + slope;
+      double nx = lx + 0.5 * (x - lx);
+      if (slope > 0.0 && arg > 0.0 && std::isfinite(slope) && std::isfinite(arg)) {
+        const double f0 = std::log(slope), g0 = lg / slope, f1 = std::log(arg);
+        const double den = f1 - f0 - g0 * (x - lx);
+        if (std::isfinite(den) && den != 0.0) nx = lx - 0.5 * g0 * (x - lx) * (x - lx) / den;
+      }
+      if (nx > rx && rg > 0) nx = lx + 0.5 * (x - lx);
+      else if ((nx - lx > 3.0 * rx - 2.0 * lx) && rg < 0) nx = lx + 3.0 * (rx - lx);
+      if (!std::isfinite(nx)) nx = lx + 0.5 * (x - lx);
+      to_prev(f, g);
+      x = nx;
+      return;
+    }
+    if ((g - pg) / (x - px) < 0.0) {
+      // negative curvature along the line
+      const double nx = rg < 0 ? 3 * rx - 2 * lx : x + 0.5 * (rx - x);
+      to_prev(f, g);
+      x = nx;
+      return;
+    }
+    // secant step on the slopes
+    double nx = x - g * (x - px) / (g - pg);
+    if (!std::isfinite(nx)) nx = lx + 0.5 * (rx - lx);
+    to_prev(f, g);
+    x = nx;
+    if (x > rx) {
+      if (rg > 0) x = 0.5 * lx + 0.5 * rx;
+      else if (x > 3 * rx - 2 * lx) x = 3 * rx - 2 * lx;
+      return;
+    }
+    if (x < lx) {
+      to_prev(f, g);
+      x = 0.5 * lx + 0.5 * rx;
+    }
+  }
+};
 
 class Trainer {
  public:
@@ -559,26 +695,152 @@ class Trainer {
 
   // Dense BFGS on the device (BFGS::Iterate / UpdateInvHess, src/common/bfgs.cpp:251-329, 428-502):
   // H starts at the identity, or at the diagonal given by set_inv_hess_diagonal (BFGS::Restart and
-  // SetInvHessDiagonal, bfgs.cpp:529-534, bfgs.h:395); each iteration takes p = -H g, a line search
-  // x + a p from a = 1 until the strong Wolfe conditions f <= f0 + c1 a p.g0 and |p.g| <= c2 |p.g0|
-  // hold (c1 = 0.1, c2 = 0.5, bfgs.h:384-385), then the rank-2 update of H with s = a p,
-  // y = g - g0, skipped when s.y <= 64 eps.  params (host) in/out; history[max_iter + 1] receives
-  // the loss after each accepted step (history[0] = initial).  Returns the number of accepted steps.
+  // SetInvHessDiagonal, bfgs.cpp:529-534, bfgs.h:395); p = -H g; a trial x + a p is accepted when
+  // the strong Wolfe conditions f <= f0 + c1 a p.g0 and |p.g| <= c2 |p.g0| hold (c1 = 0.1, c2 = 0.5,
+  // bfgs.h:384-385), then H takes the rank-2 update with s = a p, y = g - g0, skipped while
+  // s.y <= 64 eps.  params (host) in/out; history[max_iter + 1] receives the loss at the start and
+  // after each accepted step.  Returns the number of accepted steps; ends early when |g| <= gtol at
+  // an accepted point, or when a line search stagnates or runs more than 30 trials (the trainer's
+  // stop rule, dev_src/mtpr_trainer.cpp:5328-5333), keeping the last accepted point.
   //
-  // Trial steps (a bracketing search that interpolates, as Linesearch::Iterate, bfgs.h:100-290,
-  // does; every trial has the loss and its slope p.g).  lo = the last trial with sufficient
-  // decrease and a negative slope (initially a = 0), hi = the first trial past the minimum:
+  // Line searches (set_line_search):
+  //   kLineSearchReference (default): the reference's Linesearch in reverse communication
+  //     (RefLineSearch above), one objective evaluation per BFGS::Iterate call, non-finite
+  //     trials backed off by a quarter (ReduceStep(0.25)); every evaluated trial point and its
+  //     loss are recorded (trials()).
+  //   kLineSearchInterpolating: a bracketing search that interpolates -- lo = the last trial with
+  //     sufficient decrease and a negative slope (initially a = 0), hi = the first trial past the
+  //     minimum:
   //   * sufficient decrease fails: hi = a; next = the minimiser of the parabola through f(lo),
   //     the slope at lo and f(a), kept within lo + [0.01, 0.5] (a - lo); a non-finite loss takes
-  //     a quarter of the step (ReduceStep(0.25) in BFGS::Iterate);
+  //     a quarter of the step;
   //   * slope still negative and steep: lo = a; inside a bracket as below, else the zero of the
   //     secant through the slopes at the previous lo and a, kept within [2a, 8a];
   //   * slope positive and steep: hi = a; next = the zero of the secant through the slopes at lo
   //     and hi, kept within lo + [0.1, 0.9] (hi - lo) (the parabola again when hi failed the
   //     decrease test).
+  //   It takes fewer evaluations per accepted step on the benchmark sets (3.3 on the L5 set) but
+  //   does not reproduce the reference's trial sequence.
   void set_inv_hess_diagonal(const double* diag, int n) { h0_diag_.assign(diag, diag + n); }
+  enum : int { kLineSearchReference = 0, kLineSearchInterpolating = 1 };
+  void set_line_search(int mode) {
+    if (mode != kLineSearchReference && mode != kLineSearchInterpolating) throw Error(1, "unknown line search");
+    line_search_ = mode;
+  }
+  // evaluated trial points of the last bfgs call: losses, points [count][nparams], accepted flags
+  const std::vector<double>& trial_loss() const { return trial_f_; }
+  const std::vector<double>& trial_x() const { return trial_x_; }
+  const std::vector<int>& trial_accepted() const { return trial_acc_; }
 
   int bfgs(double* params, int max_iter, double gtol, double* history) {
+    trial_f_.clear();
+    trial_x_.clear();
+    trial_acc_.clear();
+    return line_search_ == kLineSearchReference ? bfgs_reference(params, max_iter, gtol, history)
+                                                : bfgs_interpolating(params, max_iter, gtol, history);
+  }
+
+  int bfgs_reference(double* params, int max_iter, double gtol, double* history) {
+    const int n = nparams_;
+    cudaStream_t s = eng_.stream();
+    DevBuf H, x, xs, gs, p, dg, yC, sc, dgn;
+    H.ensure(sizeof(double) * static_cast<size_t>(n) * n);
+    for (DevBuf* b : {&x, &xs, &gs, &p, &dg, &yC}) b->ensure(sizeof(double) * n);
+    sc.ensure(sizeof(double) * 8);
+    const unsigned nn_blocks = static_cast<unsigned>((static_cast<long long>(n) * n + 255) / 256);
+    const unsigned n_blocks = static_cast<unsigned>((n + 255) / 256);
+    const unsigned row_blocks = static_cast<unsigned>((static_cast<long long>(n) * kWarp + 255) / 256);
+    const double* g = grad_.as<double>();  // gradient of the last evaluation
+    auto dot = [&](const double* a, const double* b) {
+      k_dot<<<1, 256, 0, s>>>(n, a, b, sc.as<double>());
+      TRAIN_CUDA(cudaMemcpyAsync(host_scalars_ + 1, sc.ptr, sizeof(double), cudaMemcpyDeviceToHost, s));
+      TRAIN_CUDA(cudaStreamSynchronize(s));
+      return host_scalars_[1];
+    };
+    std::vector<double> xh(params, params + n);
+    // Set_x: p = 0, x_start = x, g_start = 0, f_start = p.g_start = HUGE, fresh line search
+    TRAIN_CUDA(cudaMemcpyAsync(x.ptr, xh.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    TRAIN_CUDA(cudaMemcpyAsync(xs.ptr, x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    TRAIN_CUDA(cudaMemsetAsync(p.ptr, 0, sizeof(double) * n, s));
+    TRAIN_CUDA(cudaMemsetAsync(gs.ptr, 0, sizeof(double) * n, s));
+    if (static_cast<int>(h0_diag_.size()) == n && n) {
+      dgn.ensure(sizeof(double) * n);
+      TRAIN_CUDA(cudaMemcpyAsync(dgn.ptr, h0_diag_.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+      k_diagonal_matrix<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), dgn.as<double>());
+    } else {
+      k_scaled_identity<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), 1.0);
+    }
+    const double c1 = 0.1, c2 = 0.5, floor = 64.0 * std::numeric_limits<double>::epsilon();
+    double f_start = RefLineSearch::kHuge, pg_start = RefLineSearch::kHuge;
+    RefLineSearch ls;
+    std::vector<double> accepted_x(xh);
+    int accepted = -1, trials_since = 0;
+    // the trial x = x_start + a p, built on the device and read back for the parameter upload
+    auto next_trial = [&]() {
+      k_axpy_to<<<n_blocks, 256, 0, s>>>(n, xs.as<double>(), ls.x, p.as<double>(), x.as<double>());
+      TRAIN_CUDA(cudaMemcpyAsync(xh.data(), x.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+      TRAIN_CUDA(cudaStreamSynchronize(s));
+    };
+    while (accepted < max_iter) {
+      const double f = loss_grad(xh.data(), nullptr);
+      trial_f_.push_back(f);
+      trial_x_.insert(trial_x_.end(), xh.begin(), xh.end());
+      trial_acc_.push_back(0);
+      const double gg = dot(g, g);
+      if (!std::isfinite(f) || !std::isfinite(gg)) {
+        // a non-finite trial inside a line search backs off (BFGS::Iterate, bfgs.cpp:257-268)
+        if (ls.x == 0.0) throw Error(5, "BFGS: non-finite loss or gradient at an accepted point");
+        if (++trials_since > 30) break;
+        ls.reduce_step(0.25);
+        next_trial();
+        continue;
+      }
+      const double pg = dot(g, p.as<double>());
+      if (f > f_start + c1 * ls.x * pg_start || std::abs(pg) > c2 * std::abs(pg_start)) {
+        ls.iterate(f, pg);
+        if (ls.stagnated || ++trials_since > 30) break;
+        next_trial();
+        continue;
+      }
+      // accepted: UpdateInvHess (bfgs.cpp:428-502) with the step a p of the finished line search
+      trial_acc_.back() = 1;
+      accepted_x = xh;
+      ++accepted;
+      trials_since = 0;
+      if (history) history[accepted] = f;
+      if (accepted == max_iter || !(std::sqrt(gg) > gtol)) break;
+      const double alpha = ls.x;
+      k_sub<<<n_blocks, 256, 0, s>>>(n, g, gs.as<double>(), dg.as<double>());
+      const double py = alpha * dot(p.as<double>(), dg.as<double>());
+      if (!std::isfinite(py)) throw Error(5, "BFGS: non-finite curvature in the inverse-Hessian update");
+      if (py > floor) {
+        k_symv<<<row_blocks, 256, 0, s>>>(n, H.as<double>(), dg.as<double>(), 1.0, yC.as<double>());
+        const double yCy = dot(yC.as<double>(), dg.as<double>());
+        if (!std::isfinite(yCy)) throw Error(5, "BFGS: non-finite yHy in the inverse-Hessian update");
+        const double foo = (py + yCy) / (py * py);
+        if (std::isfinite(foo))
+          k_bfgs_rank2<<<nn_blocks, 256, 0, s>>>(n, H.as<double>(), p.as<double>(), yC.as<double>(), alpha * alpha * foo,
+                                                 -alpha / py);
+      }
+      // FormDenseDirection, a fresh line search from this point (SetStart)
+      k_symv<<<row_blocks, 256, 0, s>>>(n, H.as<double>(), g, -1.0, p.as<double>());
+      const double pgn = dot(g, p.as<double>());
+      if (!std::isfinite(pgn)) throw Error(5, "BFGS: non-finite directional derivative");
+      ls.reset();
+      TRAIN_CUDA(cudaMemcpyAsync(xs.ptr, x.ptr, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      TRAIN_CUDA(cudaMemcpyAsync(gs.ptr, g, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+      f_start = f;
+      pg_start = pgn;
+      if (pgn > 0) throw Error(5, "BFGS: search direction is not a descent direction");
+      ls.iterate(f, pgn);
+      next_trial();
+    }
+    std::copy(accepted_x.begin(), accepted_x.end(), params);
+    eng_.set_params(params);
+    return std::max(0, accepted);
+  }
+
+  int bfgs_interpolating(double* params, int max_iter, double gtol, double* history) {
     const int n = nparams_;
     cudaStream_t s = eng_.stream();
     DevBuf H, x, g, p, xn, gn, sv, yv, Hy, sc, dg;
@@ -986,6 +1248,9 @@ class Trainer {
   DevBuf lin_cm_, lin_alpha_, lin_rhs_, lin_A_, lin_b_;  // linear warm-up
   double* host_scalars_ = nullptr;
   std::vector<double> h0_diag_;  // initial inverse-Hessian diagonal of bfgs (empty: the identity)
+  int line_search_ = kLineSearchReference;
+  std::vector<double> trial_f_, trial_x_;  // evaluated trials of the last bfgs call
+  std::vector<int> trial_acc_;
   bool use_graph_ = true;
   cudaGraph_t graph_ = nullptr;
   cudaGraphExec_t graph_exec_ = nullptr;
@@ -1088,6 +1353,30 @@ int sus2g_trainer_set_inv_hess_diagonal(sus2g_trainer t, const double* diag, int
     for (int i = 0; i < n; ++i)
       if (!(std::isfinite(diag[i]) && diag[i] > 0)) throw sus2g::Error(1, "inverse-Hessian diagonal: entries must be finite and positive");
     t->trainer->set_inv_hess_diagonal(diag, n);
+  });
+}
+
+int sus2g_trainer_set_line_search(sus2g_trainer t, int mode) {
+  return train_guarded([&] {
+    if (!t) throw sus2g::Error(1, "invalid argument: trainer");
+    t->trainer->set_line_search(mode);
+  });
+}
+
+int sus2g_trainer_bfgs_trials(sus2g_trainer t, int cap, double* loss, double* points, int* accepted, int* count) {
+  return train_guarded([&] {
+    if (!t || !count || cap < 0) throw sus2g::Error(1, "invalid argument: trainer/count/cap");
+    const auto& f = t->trainer->trial_loss();
+    const auto& x = t->trainer->trial_x();
+    const auto& a = t->trainer->trial_accepted();
+    const int n = t->trainer->nparams();
+    *count = static_cast<int>(f.size());
+    for (int k = 0; k < std::min(cap, *count); ++k) {
+      if (loss) loss[k] = f[k];
+      if (accepted) accepted[k] = a[k];
+      if (points) std::copy(x.begin() + static_cast<size_t>(k) * n, x.begin() + static_cast<size_t>(k + 1) * n,
+                            points + static_cast<size_t>(k) * n);
+    }
   });
 }
 

@@ -129,6 +129,18 @@ class Engine:
 
     PASSES = ("static", "gate_forward", "outer", "gate_reverse")
 
+    def edges(self):
+        """Directed edges of the last evaluation: (centre[E], neighbour[E], d[E, 3] = x_j - x_i), in
+        centre order, each centre's edges sorted by neighbour, then image."""
+        lib = load()
+        n = ctypes.c_longlong()
+        check(lib.sus2g_engine_copy_edges(self._h, 0, None, None, None, ctypes.byref(n)))
+        ci = np.zeros(n.value, np.int32)
+        cj = np.zeros(n.value, np.int32)
+        d = np.zeros((n.value, 3))
+        check(lib.sus2g_engine_copy_edges(self._h, n.value, _i(ci), _i(cj), _d(d), ctypes.byref(n)))
+        return ci, cj, d
+
     def autotune(self, reps: int = 5):
         """Times both register budgets of every pass on the last evaluation's layout and keeps the
         faster; returns {pass: (chosen blocks per SM, {blocks: ms per launch})}."""

@@ -137,8 +137,28 @@ class Trainer:
         d = np.ascontiguousarray(diag, dtype=np.float64)
         check(load().sus2g_trainer_set_inv_hess_diagonal(self._h, _d(d), int(d.size)))
 
+    LINE_SEARCHES = {"reference": 0, "interpolating": 1}
+
+    def set_line_search(self, mode: str = "reference") -> None:
+        """Line search of later ``bfgs`` calls: "reference" (default; the reference's Linesearch,
+        src/common/bfgs.h:31-290) or "interpolating" (fewer evaluations, not the reference's
+        trial sequence)."""
+        check(load().sus2g_trainer_set_line_search(self._h, self.LINE_SEARCHES[mode]))
+
+    def bfgs_trials(self):
+        """Every objective evaluation of the last ``bfgs`` call: (losses[k], points[k, nparams],
+        accepted[k])."""
+        lib = load()
+        n = ctypes.c_int()
+        check(lib.sus2g_trainer_bfgs_trials(self._h, 0, None, None, None, ctypes.byref(n)))
+        f = np.zeros(n.value)
+        x = np.zeros((n.value, self.nparams))
+        a = np.zeros(n.value, np.int32)
+        check(lib.sus2g_trainer_bfgs_trials(self._h, n.value, _d(f), _d(x), a.ctypes.data_as(_ip), ctypes.byref(n)))
+        return f, x, a.astype(bool)
+
     def bfgs(self, params, max_iter: int = 10, gtol: float = 0.0):
-        """Runs BFGS from ``params``; returns (params, loss history)."""
+        """Runs BFGS from ``params``; returns (last accepted params, loss history)."""
         p = np.array(params, dtype=np.float64)
         hist = np.zeros(max_iter + 1)
         steps = ctypes.c_int()

@@ -164,10 +164,11 @@ def golden_efs_and_grad(name, model, frame_sets, seed, tmp, emb, refgrad):
 
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--reference", default=os.environ.get("SUS2_REFERENCE", "/root/reference"))
+    ap.add_argument("--reference", default=os.environ.get("SUS2_REFERENCE", os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference")))
     ap.add_argument("--oracle", default=os.path.join(REPO, "oracle", "_ref"))
     ap.add_argument("--rescale-only", action="store_true", help="only regenerate the rescale-step goldens")
     ap.add_argument("--config5-only", action="store_true", help="only regenerate the L5 (config 5) model")
+    ap.add_argument("--bfgs-only", action="store_true", help="only regenerate the BFGS trial goldens")
     args = ap.parse_args()
     emb = os.path.join(args.oracle, "embedded-efs")
     mlp = os.path.join(args.oracle, "mlp-sus2")
@@ -180,6 +181,9 @@ def main():
         return
     if args.config5_only:
         golden_config5(mlp)
+        return
+    if args.bfgs_only:
+        golden_bfgs(refgrad)
         return
 
     # 1. the reference's own golden fixtures
@@ -304,6 +308,7 @@ def main():
                        "weighting": "vibrations", "source": "reference MTPR_trainer::TrainLinear",
                        "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
     golden_rescale(refgrad)
+    golden_bfgs(refgrad)
     golden_config5(mlp)
     with open(os.path.join(HERE, "manifest.json"), "w") as fh:
         json.dump(manifest, fh, indent=1, sort_keys=True)
@@ -346,6 +351,34 @@ def golden_rescale(refgrad):
             json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights,
                        "weighting": "vibrations", "source": "reference Rescale (dev_src/mlp/mtpr_train.cpp)",
                        "scaling": res["scaling"], "coeffs": res["coeffs"], "configs": res["configs"]}, fh)
+
+
+BFGS_CASES = (("static_l2k3o2_c2", 0.1), ("effect_l3k4r2o2", 0.1))
+
+
+def golden_bfgs(refgrad, iters=5):
+    """8. BFGS: the reference's BFGS engine (BFGS::Iterate / Linesearch::Iterate / UpdateInvHess,
+    src/common/bfgs.{h,cpp}) over the raw parameter vector on the trainer objective of each labelled
+    set, from the model's parameters and a constant initial inverse-Hessian diagonal; every trial
+    point, its objective value and whether BFGS accepted it, up to `iters` accepted steps."""
+    os.makedirs(os.path.join(HERE, "bfgs"), exist_ok=True)
+    weights = {name: w for name, _, w in LOSS_CASES()}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, diag in BFGS_CASES:
+            model = os.path.join(HERE, "models", f"{name}.sus2")
+            cfg = os.path.join(HERE, "frames", f"{name}__labelled.cfg")
+            n = len(json.loads(run([refgrad, model, "/dev/null"]).splitlines()[0])["coeffs"])
+            dfile = os.path.join(tmp, "diag.txt")
+            np.savetxt(dfile, np.full(n, diag))
+            out = run([refgrad, "--bfgs", model, cfg, *(str(w) for w in weights[name]), "vibrations", str(iters), dfile])
+            trials = [json.loads(line) for line in out.splitlines() if line.strip()]
+            assert sum(t["accepted"] for t in trials) == iters + 1, f"{name}: BFGS stopped early"
+            with open(os.path.join(HERE, "bfgs", f"{name}__labelled.json"), "w") as fh:
+                json.dump({"model": f"{name}.sus2", "frames": f"{name}__labelled.cfg", "weights": weights[name],
+                           "weighting": "vibrations", "inv_hess_diagonal": diag, "iterations": iters,
+                           "source": "reference BFGS engine (src/common/bfgs.{h,cpp}) driven by ref-grad --bfgs",
+                           "trials": [{"f": t["f"], "accepted": t["accepted"], "x": t["x"]} for t in trials]}, fh)
+            print(name, "bfgs trials", len(trials))
 
 
 if __name__ == "__main__":

@@ -387,3 +387,86 @@ def test_descriptors_match_reference(lib, golden, path):
     assert rel_err(d64, ref) < 1e-13
     d32 = g32.calc_descriptors(frames)
     assert rel_err(d32, ref) < 1e-5
+
+
+def sorted_edges(frames, ci, cj, d):
+    """Edges as sorted integer keys (centre, neighbour, lattice shift of the image), the shift
+    recovered exactly as round((d - (x_j - x_i)) C^-1) with the centre's frame cell C."""
+    pos = np.concatenate([fr.positions for fr in frames])
+    fid = np.concatenate([np.full(fr.natoms, k) for k, fr in enumerate(frames)])
+    inv = np.stack([np.linalg.inv(fr.cell) for fr in frames])
+    d = np.asarray(d)
+    base = d - (pos[cj] - pos[ci])
+    shift = np.rint(np.einsum("ea,eab->eb", base, inv[fid[ci]])).astype(np.int64)
+    keys = np.stack([ci, cj, shift[:, 0], shift[:, 1], shift[:, 2]], 1)
+    order = np.lexsort(keys.T[::-1])
+    return keys[order], d[order]
+
+
+@pytest.mark.parametrize("case", ["diamond64", "diamond4096_cells", "triclinic", "batch_mixed", "cutoff_band"])
+def test_edge_sets_equal_the_oracles(lib, oracle_lib, golden, case):
+    """The GPU edge set, as (centre, neighbour, image vector) triples, is the oracle's -- the
+    image-scan rule of the reference's Neighborhoods -- for the image-scan and cell-list builders,
+    triclinic cells, a mixed batch and distances within ~1e-9 A of r_c; FP64 records agree to
+    1e-12 A, FP32 records to their rounding (the edge decision is FP64 in both engines)."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    rng = np.random.default_rng(5)
+    if case == "diamond64":
+        frames = [diamond(2, sigma=0.08, seed=3)]
+    elif case == "diamond4096_cells":
+        frames = [diamond(8, sigma=0.08, seed=2)]
+    elif case == "triclinic":
+        cell = np.array([[7.1, 0.0, 0.0], [2.3, 6.7, 0.0], [-1.7, 0.9, 7.6]])
+        frames = [Frame(cell, rng.uniform(0, 1, (37, 3)) @ cell, np.zeros(37, np.int32))]
+    elif case == "batch_mixed":
+        frames = [diamond(2, sigma=0.05, seed=4), diamond(7, sigma=0.05, seed=5)] + \
+            training_frames(5, 8, 64, 3.0, 4.2, 0.1, seed=6, species=1)
+    else:
+        rc = m.cutoff
+        a = rc / 2
+        grid = np.stack(np.meshgrid(*[np.arange(9)] * 3, indexing="ij"), -1).reshape(-1, 3).astype(np.float64)
+        frames = [Frame(np.eye(3) * (a * 9), grid * a + rng.normal(0, 1e-9, grid.shape),
+                        np.zeros(len(grid), dtype=np.int32))]
+    oi, oj, od = [], [], []
+    off = 0
+    for fr in frames:
+        ei, ej, d = om.edges(fr.cell, fr.positions)
+        oi.append(ei + off); oj.append(ej + off); od.append(d)
+        off += fr.natoms
+    ko, do = sorted_edges(frames, np.concatenate(oi), np.concatenate(oj), np.concatenate(od))
+    for eng, tol in ((g64, 1e-12), (g32, 2e-6)):
+        eng.calc_efs(frames)
+        ci, cj, d = eng.edges()
+        assert ci.size == eng.edge_count() == ko.shape[0]
+        kg, dg = sorted_edges(frames, ci, cj, d)
+        assert np.array_equal(kg, ko)
+        assert np.max(np.abs(dg - do)) <= tol * max(1.0, float(np.max(np.abs(do))))
+        # within a centre the engine's order is (neighbour, image): centres ascending, neighbours
+        # non-decreasing
+        assert np.all(np.diff(ci) >= 0)
+        same = np.diff(ci) == 0
+        assert np.all(np.diff(cj)[same] >= 0)
+
+
+def test_effect_l4k8_13824_atoms_against_oracle(lib, oracle_lib, golden):
+    """The 110,592-atom configuration's model and lattice at 13,824 atoms (12x12x12 cells,
+    sigma 0.1 A, two species 50/50, cutoff 5.5 A, cell-list edge build): FP64 plain within 1e-10
+    of the FP64 oracle, FP32 bulk within 1e-5 eV/A (forces, max) and 1e-6 eV/atom (energy) of
+    the oracle and of FP64; equal edge counts."""
+    path = os.path.join(golden, "models", "effect_l4k8r2o3.sus2")
+    m, g64, g32 = engines(lib, path)
+    om = oracle_lib.OracleModel(path)
+    fr = diamond(12, a=3.567, sigma=0.1, seed=12, species=2, type_prob=0.5)
+    assert fr.natoms == 13824
+    eo, fo, vo, so, ne = om.efs(fr.cell, fr.positions, fr.types, threads=0)
+    e, f, v, s = g64.calc_efs([fr])
+    assert g64.edge_count() == ne
+    assert rel_err(e[0], eo) < FP64_TOL and rel_err(f, fo) < FP64_TOL and rel_err(v[0], vo) < FP64_TOL
+    assert rel_err(s, so) < FP64_TOL
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    assert g32.edge_count() == ne
+    check_fp32(e32[0], f32, e[0], f, fr.natoms)
+    check_fp32(e32[0], f32, eo, fo, fr.natoms)
+    assert rel_err(v32[0], vo) < 1e-5

@@ -109,6 +109,47 @@ def test_bfgs_decreases_loss(sg, golden):
     assert abs(loss - hist[-1]) <= 1e-12 * abs(hist[-1])
 
 
+@pytest.mark.parametrize("name", ["static_l2k3o2_c2", "effect_l3k4r2o2"])
+def test_bfgs_matches_reference_trials(sg, golden, name):
+    """Device BFGS with the reference line search (the default) against the reference's BFGS engine
+    (tests/golden/bfgs: BFGS::Iterate / Linesearch::Iterate / UpdateInvHess over the raw parameter
+    vector on the trainer objective, constant initial inverse-Hessian diagonal): every trial point
+    and loss, the accepted flags and the final parameters within 1e-8 relative (FP64)."""
+    data = load_json(os.path.join(golden, "bfgs", f"{name}__labelled.json"))
+    model = sg.Model(os.path.join(golden, "models", data["model"]))
+    frames = read_cfg(os.path.join(golden, "frames", data["frames"]))
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames, *data["weights"], weighting=data["weighting"],
+                    gate_x_l2=0.0)
+    p0 = np.asarray(data["trials"][0]["x"])
+    assert np.array_equal(p0, model.params())
+    tr.set_inv_hess_diagonal(np.full(p0.size, data["inv_hess_diagonal"]))
+    p, hist = tr.bfgs(p0, max_iter=data["iterations"])
+    f, x, acc = tr.bfgs_trials()
+    ref = data["trials"]
+    assert f.size == len(ref)
+    for k, r in enumerate(ref):
+        assert bool(acc[k]) == r["accepted"], k
+        assert abs(f[k] - r["f"]) <= 1e-8 * abs(r["f"]), k
+        rx = np.asarray(r["x"])
+        assert np.max(np.abs(x[k] - rx)) <= 1e-8 * max(1.0, float(np.max(np.abs(rx)))), k
+    last = np.asarray([r for r in ref if r["accepted"]][-1]["x"])
+    assert np.max(np.abs(p - last)) <= 1e-8 * max(1.0, float(np.max(np.abs(last))))
+    assert hist.size == data["iterations"] + 1
+    assert np.allclose(hist, [r["f"] for r in ref if r["accepted"]], rtol=1e-8, atol=0)
+
+
+def test_bfgs_interpolating_line_search_descends(sg, golden):
+    """The optional interpolating line search: monotone descent, fewer evaluations per step."""
+    model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
+    frames = read_cfg(os.path.join(golden, "frames", "static_l2k3o2_c2__labelled.cfg"))
+    tr = sg.Trainer(sg.Engine(model, 0, sg.FP64), frames)
+    tr.set_line_search("interpolating")
+    p, hist = tr.bfgs(model.params(), max_iter=8)
+    assert hist.size >= 3 and np.all(np.diff(hist) <= 0.0) and hist[-1] < 0.9 * hist[0]
+    loss, _ = tr.loss_grad(p)
+    assert abs(loss - hist[-1]) <= 1e-12 * abs(hist[-1])
+
+
 def test_bfgs_initial_inverse_hessian_diagonal(sg, golden):
     """A diagonal of ones is the default start (bit for bit); a scaled diagonal starts elsewhere
     and still descends; bad diagonals are rejected."""
