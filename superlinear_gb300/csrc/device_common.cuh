@@ -31,6 +31,32 @@ template <typename T> struct Vec4;
 template <> struct Vec4<float> { using type = EdgeF; };
 template <> struct Vec4<double> { using type = EdgeD; };
 
+// Per-atom graph program of one pass: the rank contraction and the product graph, forward and
+// reverse, as steps of lane-balanced work.  A step adds to one node array (v forward, adj reverse)
+//     T[target] += sum over a term list of c * X[a] * v[b]     (X = v forward, adj reverse)
+// where node M is a constant 1 (so a contraction row w v[src] is the term (src, M, w)).  Each
+// step's term lists are cut into chunks of about (terms / 32) terms, and the chunks are dealt to
+// the lanes longest first onto the least-loaded lane (host side).  A lane's chunks form one term
+// stream; the streams are stored lane-major -- row i holds term i of every lane, 32 consecutive
+// records -- so that a warp reads each row with one coalesced access, and are padded to the
+// step's longest stream with zero terms.  The last term of a chunk carries its flush target: the
+// node the chunk sum is added to, or a partial slot when the list was cut into several chunks;
+// the lanes combine the slots of such lists in slot order after the step (deterministic).
+template <typename Real> struct ProgRec;
+template <> struct __align__(16) ProgRec<float> { unsigned ab; int flush; float c, pad; };   // ab = a | b << 16
+template <> struct __align__(16) ProgRec<double> { unsigned ab; int flush; double c; };
+// flush: kProgNoFlush, a node index >= 0, or -(slot + 2) for a partial slot
+constexpr int kProgNoFlush = -1;
+
+template <typename Real>
+struct GraphProg {
+  int nsteps = 0, nfwd = 0;      // forward steps [0, nfwd), reverse steps [nfwd, nsteps)
+  int max_parts = 0;             // partial slots any step uses
+  const int4* steps = nullptr;   // {first row, rows, comb begin, (comb end << 1) | reverse}
+  const int4* comb = nullptr;    // {node, slot begin, slot end, 0}
+  const ProgRec<Real>* rows = nullptr;  // [row][32]
+};
+
 // Per-pass tables: the outer (energy) pass and the Effect gate pass share this layout.
 template <typename Real>
 struct PassTables {
@@ -63,6 +89,7 @@ struct PassTables {
   const int* rprod_out;
   const int* rprod_other;
   const Real* rprod_c;
+  GraphProg<Real> prog;   // the same contraction and graph as a lane-balanced program (E/F/virial passes)
 };
 
 // Parameter-vector offsets (the trainer's Coeff() order) and the gradient-only tables of one pass.
@@ -97,6 +124,7 @@ struct DevModel {
   const Real* gate_wmat;    // F x Q gate projection h = W g
   const int* gate_nodes;    // Q
   GradLayout grad;          // parameter-gradient layout
+  int prog_parts;           // partial slots of the larger of the two passes' graph programs
 };
 
 __device__ __forceinline__ int warp_lane() { return threadIdx.x & (kWarp - 1); }
@@ -171,14 +199,18 @@ __device__ __forceinline__ void csum_add_prod(float& hi, float& lo, float x, flo
   csum_add(hi, lo, p);
   lo += e;
 }
-// Warp total of compensated partials (fixed butterfly order), returned in FP64 on every lane.
-__device__ __forceinline__ double warp_csum(float hi, float lo) {
+// Warp total of compensated partials (fixed butterfly order), left as (hi, lo) on every lane.
+__device__ __forceinline__ void warp_csum_pair(float& hi, float& lo) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
     csum_add(hi, lo, oh);
     lo += ol;
   }
+}
+// The same total returned in FP64 on every lane.
+__device__ __forceinline__ double warp_csum(float hi, float lo) {
+  warp_csum_pair(hi, lo);
   return double(hi) + double(lo);
 }
 

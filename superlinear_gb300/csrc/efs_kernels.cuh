@@ -69,13 +69,14 @@ __host__ __device__ constexpr int stage_stride(int F, int H) {
 __host__ __device__ inline int efs_table_size(int C, int F, int B, int nblk) {
   return round4(F * B + 2 * nblk * C * C + 2 * C * C * F);
 }
-// Per-warp scratch: the staged edge rows, the node values v [M], the node adjoints [M] (in the
-// staging rows when they fit: those are free once the forward reduction is done), abar [K][H] and
-// hbar [F].
-__host__ __device__ constexpr bool adj_in_stage(int F, int H, int M) { return M <= kWarp * stage_stride(F, H); }
+// Per-warp scratch: the staged edge rows, the node values v [M + 1] (v[M] = 1, the graph
+// program's constant node), the node adjoints [M + 1] (in the staging rows when they fit: those
+// are free once the forward reduction is done), abar [K][H], hbar [F] and the graph program's
+// partial slots [parts].
+__host__ __device__ constexpr bool adj_in_stage(int F, int H, int M) { return M + 1 <= kWarp * stage_stride(F, H); }
 template <typename Real>
-__host__ __device__ inline int pass_warp_size(int F, int H, int M, int K) {
-  return round4(kWarp * stage_stride(F, H) + M + (adj_in_stage(F, H, M) ? 0 : M) + K * H + F + 4);
+__host__ __device__ inline int pass_warp_size(int F, int H, int M, int K, int parts) {
+  return round4(kWarp * stage_stride(F, H) + (M + 1) + (adj_in_stage(F, H, M) ? 0 : M + 1) + K * H + F + parts + 4);
 }
 
 // Kahan-compensated accumulation for the FP32 bulk form; plain sums in FP64.
@@ -263,6 +264,44 @@ __device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const R
   }
 }
 
+// Steps [s0, s1) of a pass's graph program (GraphProg, device_common.cuh) on the warp's node
+// arrays: forward steps add into v, reverse steps into adj.  Each lane runs its term stream (one
+// coalesced row per term), adding chunk sums to their target node or partial slot at the chunk's
+// last term; then the lanes combine the partial slots of lists that were cut into several chunks.
+template <typename Real>
+__device__ __forceinline__ void run_prog(const GraphProg<Real>& g, int s0, int s1, Real* v, Real* adj, Real* parts,
+                                         int lane) {
+  for (int st = s0; st < s1; ++st) {
+    const int4 info = g.steps[st];
+    const bool rev = info.w & 1;
+    Real* T = rev ? adj : v;
+    const Real* X = rev ? adj : v;
+    const ProgRec<Real>* r = g.rows + static_cast<size_t>(info.x) * kWarp + lane;
+    Real acc = Real(0);
+#pragma unroll 4
+    for (int i = 0; i < info.y; ++i) {
+      const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+      acc += p.c * X[p.ab & 0xffffu] * v[p.ab >> 16];
+      if (p.flush != kProgNoFlush) {
+        if (p.flush >= 0) T[p.flush] += acc;
+        else parts[-p.flush - 2] = acc;
+        acc = Real(0);
+      }
+    }
+    const int comb_end = info.w >> 1;
+    if (comb_end > info.z) {
+      __syncwarp();
+      for (int q = info.z + lane; q < comb_end; q += kWarp) {
+        const int4 e = g.comb[q];
+        Real s = Real(0);
+        for (int p = e.y; p < e.z; ++p) s += parts[p];
+        T[e.x] += s;
+      }
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
@@ -293,14 +332,15 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   Real* s_scal = s_coeff + F * B;
   Real* s_pw = s_scal + 2 * dm.nblk * C * C;        // [C^2][F] x0(t_i) x1(t_j)
   Real* s_pa = s_pw + C * C * F;                    // [C^2][F] x0(t_i) wadd(t_j)
-  Real* wbase = sm + efs_table_size(C, F, B, dm.nblk) + pass_warp_size<Real>(F, H, M, K) * warp;
+  Real* wbase = sm + efs_table_size(C, F, B, dm.nblk) + pass_warp_size<Real>(F, H, M, K, dm.prog_parts) * warp;
   const int sw = stage_stride(F, H), yoff = stage_yoff(F);
   Real* stage = wbase;                              // [32][sw]: u at [0, F), Y at [yoff, yoff + H)
-  Real* v = stage + kWarp * sw;                     // [M]
+  Real* v = stage + kWarp * sw;                     // [M + 1], v[M] = 1
   const bool adj_staged = adj_in_stage(F, H, M);
-  Real* adj = adj_staged ? stage : v + M;           // [M]
-  Real* abar = v + M + (adj_staged ? 0 : M);        // [K][H]
+  Real* adj = adj_staged ? stage : v + M + 1;       // [M + 1]
+  Real* abar = v + (M + 1) + (adj_staged ? 0 : M + 1);  // [K][H]
   Real* hbar = abar + K * H;                        // [F]
+  Real* parts = hbar + F;                           // [prog_parts]
 
   // the next kernel may be scheduled as soon as every block has started; the model tables staged
   // here are written only by host uploads, which completed before the launch chain began, so
@@ -318,7 +358,9 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   pdl_wait();
   const bool effect_outer = MODE == kModeOuter;
 
-  // Lane-owned moment items for the forward reduction: item t = lane + 32 s <-> (k, lm).
+  // Lane-owned moment items for the forward reduction: item t = lane + 32 s <-> (k, lm); the
+  // first nit of the kMaxItems register slots are in use.
+  const int nit = (K * H + kWarp - 1) / kWarp;
   int it_u[kMaxItems], it_y[kMaxItems];
 #pragma unroll
   for (int s = 0; s < kMaxItems; ++s) {
@@ -401,15 +443,20 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         for (int q = 0; q < nb; ++q) {
           const Real* sr = stage + q * sw;
 #pragma unroll
-          for (int s = 0; s < kMaxItems; ++s)
+          for (int s = 0; s < kMaxItems; ++s) {
+            if (s >= nit) break;  // warp-uniform: only the model's K H items are issued
             if (it_u[s] >= 0) part[s] += sr[it_u[s]] * sr[it_y[s]];
+          }
         }
 #pragma unroll
-        for (int s = 0; s < kMaxItems; ++s) kadd<Real, KAHAN>(acc[s], cmp[s], part[s]);
+        for (int s = 0; s < kMaxItems; ++s) {
+          if (s >= nit) break;
+          kadd<Real, KAHAN>(acc[s], cmp[s], part[s]);
+        }
         __syncwarp();
         if (more) cur = nxt;
       }
-      for (int q = lane; q < M; q += kWarp) v[q] = Real(0);
+      for (int q = lane; q <= M; q += kWarp) v[q] = q < M ? Real(0) : Real(1);
       __syncwarp();
 #pragma unroll
       for (int s = 0; s < kMaxItems; ++s) {
@@ -420,8 +467,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         }
       }
       __syncwarp();
-      contract_forward<Real>(pt, v, lane);
-      graph_forward<Real>(pt, v, lane);
+      run_prog<Real>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
 
       if (MODE == kModeGateForward) {
         for (int q = lane; q < M; q += kWarp) a.gmom[(size_t)atom * M + q] = v[q];
@@ -435,20 +481,25 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
       }
 
       // ---------------- readout and seeds ----------------
+      // E_i = species + shift + coef sum_q linear_q v[map q]: the sum in compensated FP32 (exact
+      // products) for the FP32 bulk form, FP64 otherwise; the seeds adj = coef linear in Real
       const double coef = dm.species_readout ? 1.0 : dm.species[ti];
+      const Real coef_r = Real(coef);
       const int off = dm.species_readout ? ti * dm.S : 0;
-      double es = 0.0;
-      for (int q = lane; q < M; q += kWarp) adj[q] = Real(0);
+      for (int q = lane; q <= M; q += kWarp) adj[q] = Real(0);
       __syncwarp();
+      double es64 = 0.0;
+      float ehi = 0.f, elo = 0.f;
       for (int q = lane; q < dm.S; q += kWarp) {
         const int node = dm.scalar_map[q];
-        const double rho = coef * double(dm.linear[off + q]);
-        es += rho * double(v[node]);
-        adj[node] = Real(rho);
-        if (a.desc) a.desc[static_cast<size_t>(atom) * dm.S + q] = double(v[node]);
+        const Real lin = dm.linear[off + q], vv = v[node];
+        if (sizeof(Real) == 4) csum_add_prod(ehi, elo, float(lin), float(vv));
+        else es64 += double(lin) * double(vv);
+        adj[node] = coef_r * lin;
+        if (a.desc) a.desc[static_cast<size_t>(atom) * dm.S + q] = double(vv);
       }
-      es = warp_sum(es);
-      if (lane == 0) a.site_energy[atom] = dm.species[ti] + dm.shift[ti] + es;
+      const double es = sizeof(Real) == 4 ? warp_csum(ehi, elo) : warp_sum(es64);
+      if (lane == 0) a.site_energy[atom] = dm.species[ti] + dm.shift[ti] + coef * es;
       __syncwarp();
     } else {
       // ---------------- gate reverse: gather hbar, project, load gate values ----------------
@@ -461,8 +512,8 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
           hbar[mu] = s;
         }
       }
-      for (int q = lane; q < M; q += kWarp) {
-        v[q] = a.gmom[(size_t)atom * M + q];
+      for (int q = lane; q <= M; q += kWarp) {
+        v[q] = q < M ? a.gmom[(size_t)atom * M + q] : Real(1);
         adj[q] = Real(0);
       }
       __syncwarp();
@@ -475,8 +526,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
 
     // ---------------- reverse graph and contraction ----------------
-    graph_reverse<Real>(pt, v, adj, lane);
-    contract_reverse<Real>(pt, NB, adj, lane);
+    run_prog<Real>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
     for (int t = lane; t < K * H; t += kWarp) {
       const int b = dm.basic_of[t];
       abar[t] = b >= 0 ? adj[b] : Real(0);
@@ -556,19 +606,27 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         vir[3] -= dx * double(Gy); vir[4] -= dx * double(Gz); vir[5] -= dy * double(Gz);
       }
     }
+    // per-atom virial: lane c < 6 writes component c (FP32 bulk: the compensated warp totals of
+    // all six components in FP32, then one conversion to FP64 for the whole warp)
+    double* vo = a.virial + (size_t)atom * 6;
     if (sizeof(Real) == 4) {
+      float h = 0.f, l = 0.f;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) vir[c] = warp_csum(vhi[c], vlo[c]);
+      for (int c = 0; c < 6; ++c) {
+        warp_csum_pair(vhi[c], vlo[c]);
+        if (lane == c) { h = vhi[c]; l = vlo[c]; }
+      }
+      const double vc = double(h) + double(l);
+      if (lane < 6) vo[lane] = MODE == kModeGateReverse ? vo[lane] + vc : vc;
     } else {
 #pragma unroll
       for (int c = 0; c < 6; ++c) vir[c] = warp_sum(vir[c]);
-    }
-    if (lane == 0) {
-      double* vo = a.virial + (size_t)atom * 6;
-      if (MODE == kModeGateReverse)
-        for (int c = 0; c < 6; ++c) vo[c] += vir[c];
-      else
-        for (int c = 0; c < 6; ++c) vo[c] = vir[c];
+      if (lane == 0) {
+        if (MODE == kModeGateReverse)
+          for (int c = 0; c < 6; ++c) vo[c] += vir[c];
+        else
+          for (int c = 0; c < 6; ++c) vo[c] = vir[c];
+      }
     }
     __syncwarp();
   }

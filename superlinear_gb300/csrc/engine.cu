@@ -3,6 +3,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <map>
@@ -888,6 +889,215 @@ PassOffsets pack_pass(const Model& m, bool gate, Packer& pk) {
   return o;
 }
 
+// ---- per-atom graph program (see GraphProg in device_common.cuh) ----
+struct ProgGroup {
+  int target;
+  std::vector<std::array<int, 2>> ab;
+  std::vector<double> c;
+};
+
+struct HostProg {
+  std::vector<std::array<int, 4>> steps, comb;
+  struct Rec { unsigned ab; int flush; double c; };
+  std::vector<Rec> rows;  // [row][kWarp]
+  int nfwd = 0, max_parts = 0;
+};
+
+// One step: the groups' term lists cut into chunks of about total / 32 terms (at least 4), dealt
+// longest first to the least-loaded lane; lists of several chunks sum through partial slots.
+// Each lane's chunks become one term stream, stored lane-major and padded with zero terms.
+void add_prog_step(HostProg& hp, const std::vector<ProgGroup>& groups, bool reverse, int one) {
+  long long total = 0;
+  for (const auto& g : groups) total += static_cast<long long>(g.ab.size());
+  if (total == 0) return;
+  const int T = std::max(4, static_cast<int>((total + kWarp - 1) / kWarp));
+  struct Ch { int g, tb, te, flush; };
+  std::vector<Ch> chs;
+  const int comb_begin = static_cast<int>(hp.comb.size());
+  int parts = 0;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const int n = static_cast<int>(groups[gi].ab.size());
+    if (!n) continue;
+    if (n <= T) {
+      chs.push_back({static_cast<int>(gi), 0, n, groups[gi].target});
+      continue;
+    }
+    const int k = (n + T - 1) / T, slot0 = parts;
+    for (int j = 0; j < k; ++j) chs.push_back({static_cast<int>(gi), j * n / k, (j + 1) * n / k, -(parts++ + 2)});
+    hp.comb.push_back({groups[gi].target, slot0, parts, 0});
+  }
+  std::vector<int> order(chs.size());
+  for (size_t i = 0; i < chs.size(); ++i) order[i] = static_cast<int>(i);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return chs[x].te - chs[x].tb > chs[y].te - chs[y].tb; });
+  std::vector<int> lane_of(chs.size());
+  long long load[kWarp] = {0};
+  for (int i : order) {
+    int best = 0;
+    for (int l = 1; l < kWarp; ++l)
+      if (load[l] < load[best]) best = l;
+    lane_of[i] = best;
+    load[best] += chs[i].te - chs[i].tb;
+  }
+  // Rows are filled one at a time: each lane takes a term of its current chunk (a chunk's terms
+  // may be summed in any order), choosing the one whose two node reads share a shared-memory
+  // bank (node index mod 32; equal nodes broadcast) with the fewest other lanes' reads of this
+  // row, so that the warp's two loads per row are mostly conflict-free.
+  std::vector<std::vector<int>> lane_chunks(kWarp);
+  for (size_t i = 0; i < chs.size(); ++i) lane_chunks[lane_of[i]].push_back(static_cast<int>(i));
+  std::vector<size_t> next_chunk(kWarp, 0);
+  std::vector<std::vector<int>> pool(kWarp);  // remaining term indices of the lane's current chunk
+  std::vector<int> cur(kWarp, -1);
+  auto refill = [&](int l) {
+    if (next_chunk[l] < lane_chunks[l].size()) {
+      cur[l] = lane_chunks[l][next_chunk[l]++];
+      for (int q = chs[cur[l]].tb; q < chs[cur[l]].te; ++q) pool[l].push_back(q);
+    }
+  };
+  for (int l = 0; l < kWarp; ++l) refill(l);
+  const int first = static_cast<int>(hp.rows.size() / kWarp);
+  const HostProg::Rec pad{static_cast<unsigned>(one) | (static_cast<unsigned>(one) << 16), kProgNoFlush, 0.0};
+  auto seen = [](const std::vector<int>& nodes, int n) { return std::find(nodes.begin(), nodes.end(), n) != nodes.end(); };
+  int len = 0;
+  for (;;) {
+    bool any = false;
+    for (int l = 0; l < kWarp; ++l) any = any || !pool[l].empty();
+    if (!any) break;
+    std::vector<std::vector<int>> bank_a(kWarp), bank_b(kWarp);  // distinct nodes read per bank
+    for (int l = 0; l < kWarp; ++l) {
+      if (pool[l].empty()) { hp.rows.push_back(pad); continue; }
+      const ProgGroup& g = groups[chs[cur[l]].g];
+      size_t best = 0;
+      int best_cost = 1 << 30;
+      for (size_t k = 0; k < pool[l].size(); ++k) {
+        const int a = g.ab[pool[l][k]][0], b = g.ab[pool[l][k]][1];
+        const int c = (seen(bank_a[a % kWarp], a) ? 0 : static_cast<int>(bank_a[a % kWarp].size())) +
+                      (seen(bank_b[b % kWarp], b) ? 0 : static_cast<int>(bank_b[b % kWarp].size()));
+        if (c < best_cost) { best_cost = c; best = k; }
+      }
+      const int q = pool[l][best];
+      pool[l].erase(pool[l].begin() + static_cast<long>(best));
+      const int a = g.ab[q][0], b = g.ab[q][1];
+      if (!seen(bank_a[a % kWarp], a)) bank_a[a % kWarp].push_back(a);
+      if (!seen(bank_b[b % kWarp], b)) bank_b[b % kWarp].push_back(b);
+      const bool last = pool[l].empty();
+      hp.rows.push_back({static_cast<unsigned>(a) | (static_cast<unsigned>(b) << 16), last ? chs[cur[l]].flush : kProgNoFlush,
+                         g.c[q]});
+      if (last) refill(l);
+    }
+    ++len;
+  }
+  hp.steps.push_back({first, len, comb_begin, (static_cast<int>(hp.comb.size()) << 1) | (reverse ? 1 : 0)});
+  hp.max_parts = std::max(hp.max_parts, parts);
+}
+
+// The pass's rank contraction and product graph as a program: forward (contraction, graph levels
+// 1..L), then reverse (graph levels L-1..0, contraction); node M is the constant 1.
+HostProg build_prog(const Model& m, bool gate) {
+  if (m.M + 1 > 65535) throw Error(3, "SUS2 model: too many moment nodes for the per-atom program");
+  HostProg hp;
+  const int one = m.M;
+  const auto& rows = gate ? m.gate_rows : m.outer_rows;
+  const auto& w = gate ? m.gate_w : m.outer_w;
+  const GraphSchedule& g = gate ? m.gate_graph : m.outer_graph;
+  auto weight = [&](const ContractionRow& r) { return r.widx < 0 ? 1.0 : w[r.widx]; };
+  std::vector<int> dsts;
+  for (const auto& r : rows) dsts.push_back(r.dst);
+  std::sort(dsts.begin(), dsts.end());
+  dsts.erase(std::unique(dsts.begin(), dsts.end()), dsts.end());
+  {
+    std::vector<ProgGroup> gs;
+    for (int d : dsts) {
+      ProgGroup pg{d, {}, {}};
+      for (const auto& r : rows)
+        if (r.dst == d) { pg.ab.push_back({r.src, one}); pg.c.push_back(weight(r)); }
+      gs.push_back(std::move(pg));
+    }
+    add_prog_step(hp, gs, false, one);
+  }
+  for (int lv = 0; lv < g.levels; ++lv) {
+    std::vector<ProgGroup> gs;
+    for (int q = g.level_begin[lv]; q < g.level_begin[lv + 1]; ++q) {
+      ProgGroup pg{g.out_nodes[q], {}, {}};
+      for (int p = g.out_begin[q]; p < g.out_begin[q + 1]; ++p) {
+        const Product& pr = m.products[g.fprod[p]];
+        pg.ab.push_back({pr.a, pr.b});
+        pg.c.push_back(pr.c);
+      }
+      gs.push_back(std::move(pg));
+    }
+    add_prog_step(hp, gs, false, one);
+  }
+  hp.nfwd = static_cast<int>(hp.steps.size());
+  for (int lv = static_cast<int>(g.rlevel_begin.size()) - 2; lv >= 0; --lv) {
+    std::vector<ProgGroup> gs;
+    for (int q = g.rlevel_begin[lv]; q < g.rlevel_begin[lv + 1]; ++q) {
+      ProgGroup pg{g.in_nodes[q], {}, {}};
+      for (int e = g.in_begin[q]; e < g.in_begin[q + 1]; ++e) {
+        pg.ab.push_back({g.rprod_out[e], g.rprod_other[e]});
+        pg.c.push_back(g.rprod_c[e]);
+      }
+      gs.push_back(std::move(pg));
+    }
+    add_prog_step(hp, gs, true, one);
+  }
+  {
+    std::vector<ProgGroup> gs;
+    for (int b = 0; b < m.NB; ++b) {
+      ProgGroup pg{b, {}, {}};
+      for (const auto& r : rows)
+        if (r.src == b) { pg.ab.push_back({r.dst, one}); pg.c.push_back(weight(r)); }
+      gs.push_back(std::move(pg));
+    }
+    add_prog_step(hp, gs, true, one);
+  }
+  return hp;
+}
+
+// Serialises the programs of the passes into one 16-byte aligned device image and binds them.
+template <typename Real>
+void upload_progs(const std::vector<const HostProg*>& progs, DevBuf& buf, cudaStream_t s,
+                  std::vector<GraphProg<Real>>& out) {
+  std::vector<unsigned char> img;
+  auto put = [&](const void* p, size_t n) {
+    const size_t o = (img.size() + 15) & ~size_t(15);
+    img.resize(o + n);
+    if (n) std::memcpy(img.data() + o, p, n);
+    return o;
+  };
+  struct Off { size_t steps, comb, rows; };
+  std::vector<Off> offs;
+  for (const HostProg* hp : progs) {
+    Off o{};
+    o.steps = put(hp->steps.data(), sizeof(int4) * hp->steps.size());
+    o.comb = put(hp->comb.data(), sizeof(int4) * hp->comb.size());
+    std::vector<ProgRec<Real>> rows(hp->rows.size());
+    for (size_t q = 0; q < rows.size(); ++q) {
+      rows[q] = ProgRec<Real>{};
+      rows[q].ab = hp->rows[q].ab;
+      rows[q].flush = hp->rows[q].flush;
+      rows[q].c = static_cast<Real>(hp->rows[q].c);
+    }
+    o.rows = put(rows.data(), sizeof(ProgRec<Real>) * rows.size());
+    offs.push_back(o);
+  }
+  if (img.empty()) img.resize(16);
+  buf.ensure(img.size());
+  SUS2G_CUDA(cudaMemcpyAsync(buf.ptr, img.data(), img.size(), cudaMemcpyHostToDevice, s));
+  SUS2G_CUDA(cudaStreamSynchronize(s));
+  const unsigned char* base = static_cast<const unsigned char*>(buf.ptr);
+  out.clear();
+  for (size_t k = 0; k < progs.size(); ++k) {
+    GraphProg<Real> g;
+    g.nsteps = static_cast<int>(progs[k]->steps.size());
+    g.nfwd = progs[k]->nfwd;
+    g.max_parts = progs[k]->max_parts;
+    g.steps = reinterpret_cast<const int4*>(base + offs[k].steps);
+    g.comb = reinterpret_cast<const int4*>(base + offs[k].comb);
+    g.rows = reinterpret_cast<const ProgRec<Real>*>(base + offs[k].rows);
+    out.push_back(g);
+  }
+}
+
 template <typename Real>
 PassTables<Real> bind_pass(const PassOffsets& o, const int* I, const Real* R) {
   PassTables<Real> t{};
@@ -1052,6 +1262,15 @@ void Engine::upload_tables() {
   dm->basic_of = I + o_basic;
   dm->outer = bind_pass<Real>(po, I, R);
   dm->gate = bind_pass<Real>(pg, I, R);
+  {
+    const HostProg prog_outer = build_prog(m, false);
+    const HostProg prog_gate = m.gated ? build_prog(m, true) : HostProg{};
+    std::vector<GraphProg<Real>> bound;
+    upload_progs<Real>({&prog_outer, &prog_gate}, tab_prog_, us, bound);
+    dm->outer.prog = bound[0];
+    dm->gate.prog = m.gated ? bound[1] : bound[0];
+    dm->prog_parts = std::max(bound[0].max_parts, m.gated ? bound[1].max_parts : 0);
+  }
   dm->linear = R + o_lin;
   dm->species = tab_dbl_.as<double>();
   dm->shift = tab_dbl_.as<double>() + m.C;

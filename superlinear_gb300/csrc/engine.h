@@ -208,7 +208,7 @@ class Engine {
   unsigned long long edge_generation_ = 0;
 
   // model tables (both precisions are packed into one buffer each)
-  DevBuf tab_int_, tab_real_, tab_dbl_;
+  DevBuf tab_int_, tab_real_, tab_dbl_, tab_prog_;
   void* dev_model_ = nullptr;  // host copy of DevModel<Real>
 
   // geometry

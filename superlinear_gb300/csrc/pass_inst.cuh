@@ -20,7 +20,7 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
   const auto& dm = a.dm;
   const int H = (L + 1) * (L + 1);
   const size_t smem = sizeof(Real) *
-      (efs_table_size(dm.C, dm.F, dm.B, dm.nblk) + kPassWarps * pass_warp_size<Real>(dm.F, H, dm.M, dm.K));
+      (efs_table_size(dm.C, dm.F, dm.B, dm.nblk) + kPassWarps * pass_warp_size<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts));
   static size_t configured = 0;
   if (smem > configured) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
