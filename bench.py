@@ -456,6 +456,7 @@ def run_profile_effect(args):
     fr = diamond(args.cells, a=3.567, sigma=0.1, seed=4, species=2, type_prob=0.5)
     dev = torch.device("cuda", 0)
     eng = sg.Engine(sg.Model(EFFECT_MODEL), 0, sg.FP32)
+    eng.set_moment_mma(args.moment_mma)
     pos = torch.tensor(fr.positions, device=dev)
     typ = torch.tensor(fr.types, device=dev)
     out = torch.zeros(fr.natoms * 3 + 7, dtype=torch.float64, device=dev)
@@ -543,6 +544,7 @@ def run_ours(args):
         return total / steps, stage_times(eng, steps), launches, clocks
 
     eng32 = make(sg.FP32)
+    eng32.set_moment_mma(args.moment_mma)
     # pass-kernel autotuner on the workload's layout (after one evaluation), as a user would run it
     # (not in the profiling mode, whose ncu launch offsets count the steps' own launches)
     tuned = {}
@@ -741,6 +743,8 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="with --profile-train: eager launches instead of the graph")
     ap.add_argument("--profile-effect", action="store_true",
                     help="only FP32 Effect L4/K8/R2/O3 steps on a --cells diamond (for ncu captures)")
+    ap.add_argument("--moment-mma", action="store_true",
+                    help="with --profile-only / --profile-effect: edge->moment sums on the tensor cores (3xTF32)")
     ap.add_argument("--skip-config5", action="store_true",
                     help="skip the 2,048-frame L5 training loss+gradient and BFGS measurement")
     ap.add_argument("--bfgs-iters", type=int, default=10, help="timed FP32 BFGS iterations on the L5 batch")

@@ -116,6 +116,12 @@ int sus2g_engine_set_step_graph(sus2g_engine engine, int enabled);
  * force gather (after the last pass); 0 = none, -1 = the model's default (Static 1 | 2, Effect 1:
  * the sites that measured faster on GB300).  Results are identical for every mask. */
 int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
+/* FP32 engines: sum each 32-edge batch of the edge->moment accumulation on the tensor cores
+ * (m16n8k8 TF32 mma.sync, operands split into TF32 head and tail, three products per tile) instead
+ * of CUDA-core FMAs (enabled = 1; default 0).  The same sums as the reference's forward_moments
+ * (interfaces/lammps/ML-SUS2/sus2_sl_kernel.cpp:340-354); kept as an option because the CUDA-core
+ * form measured faster on GB300. */
+int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
  * the model runs with both compiled register budgets (3 and 4 resident blocks per SM; basis size 8)
  * over `reps` launches each and keeps the faster for later evaluations (results are identical

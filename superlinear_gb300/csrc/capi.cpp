@@ -168,6 +168,10 @@ int sus2g_engine_copy_edges(sus2g_engine e, long long cap, int* centre, int* nei
   });
 }
 
+int sus2g_engine_set_moment_mma(sus2g_engine e, int enabled) {
+  return guarded([&] { need(e, "engine"); e->engine->set_moment_mma(enabled != 0); });
+}
+
 int sus2g_engine_set_timing(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_timing(enabled != 0); });
 }

@@ -50,6 +50,7 @@ struct PassArgs {
   double* virial;          // [natoms][6] (xx, yy, zz, xy, xz, yz), minus d (x) g
   double* desc;            // [natoms][S] scalar moments (descriptors), or null
   int* error;
+  int moment_mma;          // FP32 engines: 1 = edge->moment batch sums on the tensor cores (3xTF32 mma.sync)
 };
 
 template <typename Real>
@@ -303,6 +304,70 @@ __device__ __forceinline__ void run_prog(const GraphProg<Real>& g, int s0, int s
 }
 
 // ---------------------------------------------------------------------------------------------
+// Edge->moment batch sums on the tensor cores (FP32 engines, optional): the batch's staged rows
+// form the products D[mu][lm] = sum_q u[q][mu] Y[q][lm] (q < 32 edges), computed as m16n8k8 TF32
+// mma.sync tiles with each operand split into a TF32 head and a TF32 tail (3xTF32: head*head +
+// head*tail + tail*head, about FP32 accuracy); the entries with l(mu) = l(lm) are the moment
+// partials, written to part[k][lm].  Rows past the batch are zero; tile columns past F / H read
+// other staged values and are discarded.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned tf32_head(float x) {
+  unsigned h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  return h;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+               "{%0,%1,%2,%3};"
+               : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+template <int L>
+__device__ __forceinline__ void moments_mma_batch(const float* stage, int sw, int yoff, int F, float* part, int lane) {
+  constexpr int Lp = L + 1, H = Lp * Lp;
+  const int g = lane >> 2, t = lane & 3;
+  const int mtiles = (F + 15) / 16;
+  constexpr int ntiles = (H + 7) / 8;
+  for (int mt = 0; mt < mtiles; ++mt) {
+#pragma unroll
+    for (int nt = 0; nt < ntiles; ++nt) {
+      float d[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int ks = 0; ks < kWarp / 8; ++ks) {
+        const float* r0 = stage + (8 * ks + t) * sw;
+        const float* r4 = r0 + 4 * sw;
+        const float av[4] = {r0[16 * mt + g], r0[16 * mt + g + 8], r4[16 * mt + g], r4[16 * mt + g + 8]};
+        const float bv[2] = {r0[yoff + 8 * nt + g], r4[yoff + 8 * nt + g]};
+        unsigned ah[4], al[4], bh[2], bl[2];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          ah[i] = tf32_head(av[i]);
+          al[i] = tf32_head(av[i] - __uint_as_float(ah[i]));
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          bh[i] = tf32_head(bv[i]);
+          bl[i] = tf32_head(bv[i] - __uint_as_float(bh[i]));
+        }
+        mma_tf32(d, al, bh);
+        mma_tf32(d, ah, bl);
+        mma_tf32(d, ah, bh);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int mu = 16 * mt + g + 8 * (i >> 1), lm = 8 * nt + 2 * t + (i & 1);
+        if (mu < F && lm < H) {
+          int l = 0;
+          while ((l + 1) * (l + 1) <= lm) ++l;
+          if (mu % Lp == l) part[(mu / Lp) * H + lm] = d[i];
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------------------------
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
 constexpr int kPassWarps = 4;
@@ -440,12 +505,23 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         Real part[kMaxItems];
 #pragma unroll
         for (int s = 0; s < kMaxItems; ++s) part[s] = Real(0);
-        for (int q = 0; q < nb; ++q) {
-          const Real* sr = stage + q * sw;
+        if (sizeof(Real) == 4 && a.moment_mma) {
+          // tensor-core batch sums into the abar rows (free until the reverse), then each lane
+          // reads its items
+          moments_mma_batch<L>(reinterpret_cast<const float*>(stage), sw, yoff, F, reinterpret_cast<float*>(abar), lane);
 #pragma unroll
           for (int s = 0; s < kMaxItems; ++s) {
-            if (s >= nit) break;  // warp-uniform: only the model's K H items are issued
-            if (it_u[s] >= 0) part[s] += sr[it_u[s]] * sr[it_y[s]];
+            if (s >= nit) break;
+            if (it_u[s] >= 0) part[s] = abar[lane + kWarp * s];
+          }
+        } else {
+          for (int q = 0; q < nb; ++q) {
+            const Real* sr = stage + q * sw;
+#pragma unroll
+            for (int s = 0; s < kMaxItems; ++s) {
+              if (s >= nit) break;  // warp-uniform: only the model's K H items are issued
+              if (it_u[s] >= 0) part[s] += sr[it_u[s]] * sr[it_y[s]];
+            }
           }
         }
 #pragma unroll

@@ -1755,6 +1755,7 @@ PassArgs<Real> Engine::pass_args() {
   vir_atom_.ensure(sizeof(double) * 6 * std::max(1, N));
   PassArgs<Real> a{};
   a.dm = *static_cast<DevModel<Real>*>(dev_model_);
+  a.moment_mma = moment_mma_ ? 1 : 0;
   a.natoms = ncentres_;
   a.types = d_types_;
   a.row = row_.as<int>();

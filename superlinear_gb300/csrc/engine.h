@@ -86,6 +86,13 @@ class Engine {
   // ms_out[2 mode + (budget - 3)] = the timed milliseconds per launch.
   void autotune(int reps, int* blocks_out, double* ms_out);
   void reset_step_graph();
+  // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
+  // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
+  // drops a captured step graph.
+  void set_moment_mma(bool on) {
+    if (on != moment_mma_) reset_step_graph();
+    moment_mma_ = on;
+  }
 
   // --- evaluation ---------------------------------------------------------------------------
   // E / F / virial for the current edges.  Outputs (device, double): per-frame energy [nframes],
@@ -189,6 +196,7 @@ class Engine {
   // step graph (step_frames)
   bool step_graphs_ = true, capturing_ = false;
   int pdl_ = -1;  // set from the model in the constructor
+  bool moment_mma_ = false;
   int urgent_priority_ = 0;  // the device's most urgent stream priority
   cudaGraph_t step_graph_ = nullptr;
   cudaGraphExec_t step_exec_ = nullptr;

@@ -153,6 +153,11 @@ class Engine:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))
 
+    def set_moment_mma(self, on: bool) -> None:
+        """FP32 engines: edge->moment batch sums on the tensor cores (3xTF32 mma.sync) instead of
+        CUDA-core FMAs (off by default)."""
+        check(load().sus2g_engine_set_moment_mma(self._h, 1 if on else 0))
+
     PDL_FILL, PDL_FIRST_PASS, PDL_BETWEEN_PASSES, PDL_GATHER = 1, 2, 4, 8
 
     def set_pdl(self, sites: int = -1) -> None:

@@ -470,3 +470,22 @@ def test_effect_l4k8_13824_atoms_against_oracle(lib, oracle_lib, golden):
     check_fp32(e32[0], f32, e[0], f, fr.natoms)
     check_fp32(e32[0], f32, eo, fo, fr.natoms)
     assert rel_err(v32[0], vo) < 1e-5
+
+
+@pytest.mark.parametrize("name,cells", [("static_l3k4o2", 8), ("effect_l4k8r2o3", 6)])
+def test_moment_mma_option_within_fp32_bars(lib, golden, name, cells):
+    """The optional tensor-core edge->moment sums (3xTF32 mma.sync, sus2g_engine_set_moment_mma)
+    stay within the FP32-bulk force and energy bars of FP64, and switching back restores the
+    CUDA-core results bit for bit."""
+    path = os.path.join(golden, "models", f"{name}.sus2")
+    m, g64, g32 = engines(lib, path)
+    fr = diamond(cells, sigma=0.1, seed=21, species=2 if name.startswith("effect") else 1, type_prob=0.5)
+    e, f, v, s = g64.calc_efs([fr])
+    base = g32.calc_efs([fr])
+    g32.set_moment_mma(True)
+    e32, f32, v32, s32 = g32.calc_efs([fr])
+    check_fp32(e32[0], f32, e[0], f, fr.natoms)
+    g32.set_moment_mma(False)
+    again = g32.calc_efs([fr])
+    for x, y in zip(again, base):
+        assert np.array_equal(x, y)
