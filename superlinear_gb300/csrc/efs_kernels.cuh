@@ -18,8 +18,8 @@
 // x0 x3 R_mu and Y_h in shared memory; lanes then switch to owning (k, lm) moment items and
 // reduce over the staged edges in a fixed order: a plain sum over each batch of <= 32 edges, then a
 // Kahan-compensated add of the batch partial into the atom's moment (FP32 bulk) -- no atomics,
-// deterministic.  The product graph runs level by level over shared-memory node
-// arrays; the reverse graph is a gather per consumed node (no write conflicts).  The adjoint
+// deterministic.  The rank contraction and the product graph, forward and reverse, run as the
+// pass's lane-balanced graph program (GraphProg) over shared-memory node arrays.  The adjoint
 // pass recomputes Y and R per edge instead of storing them and writes g_e per edge; forces are
 // gathered per atom through the reverse-edge permutation by a separate kernel.
 #pragma once
@@ -217,64 +217,17 @@ __device__ __forceinline__ void radial_loop(const DevModel<Real>& dm, const Real
   }
 }
 
-// ---------------------------------------------------------------------------------------------
-// Warp-cooperative per-atom graph helpers on shared-memory node arrays.
-// ---------------------------------------------------------------------------------------------
-template <typename Real>
-__device__ __forceinline__ void contract_forward(const PassTables<Real>& t, Real* v, int lane) {
-  for (int q = lane; q < t.ndst; q += kWarp) {
-    Real s = Real(0);
-    for (int p = t.dst_begin[q]; p < t.dst_begin[q + 1]; ++p) s += t.dst_w[p] * v[t.dst_src[p]];
-    v[t.dst_node[q]] += s;
-  }
-  __syncwarp();
-}
-
-template <typename Real>
-__device__ __forceinline__ void contract_reverse(const PassTables<Real>& t, int NB, Real* adj, int lane) {
-  if (t.ndst == 0) return;
-  for (int b = lane; b < NB; b += kWarp) {
-    Real s = Real(0);
-    for (int p = t.src_begin[b]; p < t.src_begin[b + 1]; ++p) s += t.src_w[p] * adj[t.src_dst[p]];
-    adj[b] += s;
-  }
-  __syncwarp();
-}
-
-template <typename Real>
-__device__ __forceinline__ void graph_forward(const PassTables<Real>& t, Real* v, int lane) {
-  for (int lv = 0; lv < t.levels; ++lv) {
-    for (int q = t.level_begin[lv] + lane; q < t.level_begin[lv + 1]; q += kWarp) {
-      Real s = Real(0);
-      for (int p = t.out_begin[q]; p < t.out_begin[q + 1]; ++p) s += t.fprod_c[p] * v[t.fprod_a[p]] * v[t.fprod_b[p]];
-      v[t.out_nodes[q]] += s;
-    }
-    __syncwarp();
-  }
-}
-
-template <typename Real>
-__device__ __forceinline__ void graph_reverse(const PassTables<Real>& t, const Real* v, Real* adj, int lane) {
-  for (int lv = t.levels - 1; lv >= 0; --lv) {
-    for (int q = t.rlevel_begin[lv] + lane; q < t.rlevel_begin[lv + 1]; q += kWarp) {
-      Real s = Real(0);
-      for (int p = t.in_begin[q]; p < t.in_begin[q + 1]; ++p) s += t.rprod_c[p] * adj[t.rprod_out[p]] * v[t.rprod_other[p]];
-      adj[t.in_nodes[q]] += s;
-    }
-    __syncwarp();
-  }
-}
-
 // Steps [s0, s1) of a pass's graph program (GraphProg, device_common.cuh) on the warp's node
-// arrays: forward steps add into v, reverse steps into adj.  Each lane runs its term stream (one
+// arrays: forward steps add into v, reverse steps into adj (DIR 1 / 2: the range holds forward /
+// reverse steps only).  Each lane runs its term stream (one
 // coalesced row per term), adding chunk sums to their target node or partial slot at the chunk's
 // last term; then the lanes combine the partial slots of lists that were cut into several chunks.
-template <typename Real>
+template <typename Real, int DIR = 0>
 __device__ __forceinline__ void run_prog(const GraphProg<Real>& g, int s0, int s1, Real* v, Real* adj, Real* parts,
                                          int lane) {
   for (int st = s0; st < s1; ++st) {
     const int4 info = g.steps[st];
-    const bool rev = info.w & 1;
+    const bool rev = DIR == 2 || (DIR == 0 && (info.w & 1));
     Real* T = rev ? adj : v;
     const Real* X = rev ? adj : v;
     const ProgRec<Real>* r = g.rows + static_cast<size_t>(info.x) * kWarp + lane;
@@ -543,7 +496,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         }
       }
       __syncwarp();
-      run_prog<Real>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
+      run_prog<Real, 1>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
 
       if (MODE == kModeGateForward) {
         for (int q = lane; q < M; q += kWarp) a.gmom[(size_t)atom * M + q] = v[q];
@@ -602,7 +555,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
 
     // ---------------- reverse graph and contraction ----------------
-    run_prog<Real>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
+    run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
     for (int t = lane; t < K * H; t += kWarp) {
       const int b = dm.basic_of[t];
       abar[t] = b >= 0 ? adj[b] : Real(0);

@@ -805,6 +805,17 @@ void invert3(const double* c, double* inv) {
 // ------------------------------------------------------------------------------------------------
 // model tables
 // ------------------------------------------------------------------------------------------------
+// A pass's graph program on the host (GraphProg, device_common.cuh).  Its structure depends on the
+// model topology only and is built once per engine; each upload fills the coefficients: a fixed
+// product coefficient, or the current rank weight w[widx] of a contraction row.
+struct HostProg {
+  std::vector<std::array<int, 4>> steps, comb;
+  struct Rec { unsigned ab; int flush; int widx; double cfix; };
+  std::vector<Rec> rows;  // [row][kWarp]
+  int nfwd = 0, max_parts = 0;
+  bool gate = false;
+};
+
 namespace {
 
 struct Packer {
@@ -893,14 +904,8 @@ PassOffsets pack_pass(const Model& m, bool gate, Packer& pk) {
 struct ProgGroup {
   int target;
   std::vector<std::array<int, 2>> ab;
-  std::vector<double> c;
-};
-
-struct HostProg {
-  std::vector<std::array<int, 4>> steps, comb;
-  struct Rec { unsigned ab; int flush; double c; };
-  std::vector<Rec> rows;  // [row][kWarp]
-  int nfwd = 0, max_parts = 0;
+  std::vector<double> c;   // fixed coefficient (when widx < 0)
+  std::vector<int> widx;   // rank-weight index, or -1
 };
 
 // One step: the groups' term lists cut into chunks of about total / 32 terms (at least 4), dealt
@@ -955,7 +960,7 @@ void add_prog_step(HostProg& hp, const std::vector<ProgGroup>& groups, bool reve
   };
   for (int l = 0; l < kWarp; ++l) refill(l);
   const int first = static_cast<int>(hp.rows.size() / kWarp);
-  const HostProg::Rec pad{static_cast<unsigned>(one) | (static_cast<unsigned>(one) << 16), kProgNoFlush, 0.0};
+  const HostProg::Rec pad{static_cast<unsigned>(one) | (static_cast<unsigned>(one) << 16), kProgNoFlush, -1, 0.0};
   auto seen = [](const std::vector<int>& nodes, int n) { return std::find(nodes.begin(), nodes.end(), n) != nodes.end(); };
   int len = 0;
   for (;;) {
@@ -981,7 +986,7 @@ void add_prog_step(HostProg& hp, const std::vector<ProgGroup>& groups, bool reve
       if (!seen(bank_b[b % kWarp], b)) bank_b[b % kWarp].push_back(b);
       const bool last = pool[l].empty();
       hp.rows.push_back({static_cast<unsigned>(a) | (static_cast<unsigned>(b) << 16), last ? chs[cur[l]].flush : kProgNoFlush,
-                         g.c[q]});
+                         g.widx[q], g.c[q]});
       if (last) refill(l);
     }
     ++len;
@@ -995,11 +1000,10 @@ void add_prog_step(HostProg& hp, const std::vector<ProgGroup>& groups, bool reve
 HostProg build_prog(const Model& m, bool gate) {
   if (m.M + 1 > 65535) throw Error(3, "SUS2 model: too many moment nodes for the per-atom program");
   HostProg hp;
+  hp.gate = gate;
   const int one = m.M;
   const auto& rows = gate ? m.gate_rows : m.outer_rows;
-  const auto& w = gate ? m.gate_w : m.outer_w;
   const GraphSchedule& g = gate ? m.gate_graph : m.outer_graph;
-  auto weight = [&](const ContractionRow& r) { return r.widx < 0 ? 1.0 : w[r.widx]; };
   std::vector<int> dsts;
   for (const auto& r : rows) dsts.push_back(r.dst);
   std::sort(dsts.begin(), dsts.end());
@@ -1007,9 +1011,9 @@ HostProg build_prog(const Model& m, bool gate) {
   {
     std::vector<ProgGroup> gs;
     for (int d : dsts) {
-      ProgGroup pg{d, {}, {}};
+      ProgGroup pg{d, {}, {}, {}};
       for (const auto& r : rows)
-        if (r.dst == d) { pg.ab.push_back({r.src, one}); pg.c.push_back(weight(r)); }
+        if (r.dst == d) { pg.ab.push_back({r.src, one}); pg.c.push_back(1.0); pg.widx.push_back(r.widx); }
       gs.push_back(std::move(pg));
     }
     add_prog_step(hp, gs, false, one);
@@ -1017,11 +1021,12 @@ HostProg build_prog(const Model& m, bool gate) {
   for (int lv = 0; lv < g.levels; ++lv) {
     std::vector<ProgGroup> gs;
     for (int q = g.level_begin[lv]; q < g.level_begin[lv + 1]; ++q) {
-      ProgGroup pg{g.out_nodes[q], {}, {}};
+      ProgGroup pg{g.out_nodes[q], {}, {}, {}};
       for (int p = g.out_begin[q]; p < g.out_begin[q + 1]; ++p) {
         const Product& pr = m.products[g.fprod[p]];
         pg.ab.push_back({pr.a, pr.b});
         pg.c.push_back(pr.c);
+        pg.widx.push_back(-1);
       }
       gs.push_back(std::move(pg));
     }
@@ -1031,10 +1036,11 @@ HostProg build_prog(const Model& m, bool gate) {
   for (int lv = static_cast<int>(g.rlevel_begin.size()) - 2; lv >= 0; --lv) {
     std::vector<ProgGroup> gs;
     for (int q = g.rlevel_begin[lv]; q < g.rlevel_begin[lv + 1]; ++q) {
-      ProgGroup pg{g.in_nodes[q], {}, {}};
+      ProgGroup pg{g.in_nodes[q], {}, {}, {}};
       for (int e = g.in_begin[q]; e < g.in_begin[q + 1]; ++e) {
         pg.ab.push_back({g.rprod_out[e], g.rprod_other[e]});
         pg.c.push_back(g.rprod_c[e]);
+        pg.widx.push_back(-1);
       }
       gs.push_back(std::move(pg));
     }
@@ -1043,9 +1049,9 @@ HostProg build_prog(const Model& m, bool gate) {
   {
     std::vector<ProgGroup> gs;
     for (int b = 0; b < m.NB; ++b) {
-      ProgGroup pg{b, {}, {}};
+      ProgGroup pg{b, {}, {}, {}};
       for (const auto& r : rows)
-        if (r.src == b) { pg.ab.push_back({r.dst, one}); pg.c.push_back(weight(r)); }
+        if (r.src == b) { pg.ab.push_back({r.dst, one}); pg.c.push_back(1.0); pg.widx.push_back(r.widx); }
       gs.push_back(std::move(pg));
     }
     add_prog_step(hp, gs, true, one);
@@ -1055,7 +1061,7 @@ HostProg build_prog(const Model& m, bool gate) {
 
 // Serialises the programs of the passes into one 16-byte aligned device image and binds them.
 template <typename Real>
-void upload_progs(const std::vector<const HostProg*>& progs, DevBuf& buf, cudaStream_t s,
+void upload_progs(const Model& m, const std::vector<const HostProg*>& progs, DevBuf& buf, cudaStream_t s,
                   std::vector<GraphProg<Real>>& out) {
   std::vector<unsigned char> img;
   auto put = [&](const void* p, size_t n) {
@@ -1070,12 +1076,14 @@ void upload_progs(const std::vector<const HostProg*>& progs, DevBuf& buf, cudaSt
     Off o{};
     o.steps = put(hp->steps.data(), sizeof(int4) * hp->steps.size());
     o.comb = put(hp->comb.data(), sizeof(int4) * hp->comb.size());
+    const std::vector<double>& w = hp->gate ? m.gate_w : m.outer_w;
     std::vector<ProgRec<Real>> rows(hp->rows.size());
     for (size_t q = 0; q < rows.size(); ++q) {
+      const HostProg::Rec& x = hp->rows[q];
       rows[q] = ProgRec<Real>{};
-      rows[q].ab = hp->rows[q].ab;
-      rows[q].flush = hp->rows[q].flush;
-      rows[q].c = static_cast<Real>(hp->rows[q].c);
+      rows[q].ab = x.ab;
+      rows[q].flush = x.flush;
+      rows[q].c = static_cast<Real>(x.widx >= 0 ? w[x.widx] : x.cfix);
     }
     o.rows = put(rows.data(), sizeof(ProgRec<Real>) * rows.size());
     offs.push_back(o);
@@ -1263,10 +1271,13 @@ void Engine::upload_tables() {
   dm->outer = bind_pass<Real>(po, I, R);
   dm->gate = bind_pass<Real>(pg, I, R);
   {
-    const HostProg prog_outer = build_prog(m, false);
-    const HostProg prog_gate = m.gated ? build_prog(m, true) : HostProg{};
+    // the programs' structure is built once per engine; uploads refresh the rank weights
+    if (!prog_[0]) {
+      prog_[0].reset(new HostProg(build_prog(m, false)));
+      prog_[1].reset(new HostProg(m.gated ? build_prog(m, true) : HostProg{}));
+    }
     std::vector<GraphProg<Real>> bound;
-    upload_progs<Real>({&prog_outer, &prog_gate}, tab_prog_, us, bound);
+    upload_progs<Real>(m, {prog_[0].get(), prog_[1].get()}, tab_prog_, us, bound);
     dm->outer.prog = bound[0];
     dm->gate.prog = m.gated ? bound[1] : bound[0];
     dm->prog_parts = std::max(bound[0].max_parts, m.gated ? bound[1].max_parts : 0);

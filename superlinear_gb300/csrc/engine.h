@@ -12,6 +12,7 @@
 namespace sus2g {
 
 template <typename Real> struct PassArgs;  // efs_kernels.cuh
+struct HostProg;                            // engine.cu: a pass's graph program on the host
 
 enum Precision : int { kFP64 = 0, kFP32 = 1 };
 
@@ -217,6 +218,7 @@ class Engine {
 
   // model tables (both precisions are packed into one buffer each)
   DevBuf tab_int_, tab_real_, tab_dbl_, tab_prog_;
+  std::unique_ptr<HostProg> prog_[2];  // outer and gate graph programs (structure built once)
   void* dev_model_ = nullptr;  // host copy of DevModel<Real>
 
   // geometry

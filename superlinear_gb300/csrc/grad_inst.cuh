@@ -42,7 +42,7 @@ GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, in
   cudaGetDevice(&device);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   const size_t table = pass_table_size<Real>(dm.C, dm.F, dm.B, dm.nblk);
-  const size_t per_warp = grad_warp_size<Real>(dm.F, H, dm.M, dm.K);
+  const size_t per_warp = grad_warp_size<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts);
   // the gate forward pass has no per-edge parameter loop
   const int cols = mode == kGradGateForward
                        ? 0

@@ -65,10 +65,13 @@ constexpr int kAccStride = kWarp + 1;
 // Per-warp scratch: staged rows [32][2F + 2H + 1], node values and tangents v, vd [M] each, the
 // node adjoints lam, mu [M] each (in the staged rows when they fit: those are dead once the forward
 // reduction is done, and the per-edge loop recomputes its geometry), abar rows [2][K][H], hbar [2F].
-__host__ __device__ constexpr bool grad_adj_in_stage(int F, int H, int M) { return 2 * M <= kWarp * (2 * F + 2 * H + 1); }
+// (v, vd, lam, mu hold M + 1 entries: node M is the graph program's constant 1, tangent 0; the
+// program's partial slots take two values each)
+__host__ __device__ constexpr bool grad_adj_in_stage(int F, int H, int M) { return 2 * (M + 1) <= kWarp * (2 * F + 2 * H + 1); }
 template <typename Real>
-__host__ __device__ inline int grad_warp_size(int F, int H, int M, int K) {
-  return kWarp * (2 * F + 2 * H + 1) + 2 * M + (grad_adj_in_stage(F, H, M) ? 0 : 2 * M) + 2 * K * H + 2 * F + 4;
+__host__ __device__ inline int grad_warp_size(int F, int H, int M, int K, int parts) {
+  return kWarp * (2 * F + 2 * H + 1) + 2 * (M + 1) + (grad_adj_in_stage(F, H, M) ? 0 : 2 * (M + 1)) + 2 * K * H +
+         2 * F + 2 * parts + 4;
 }
 
 // Accumulator columns per radial index k: Chebyshev coefficients [l][b], species factors [t][l]
@@ -87,83 +90,79 @@ __device__ __forceinline__ void slot_add(double* slot, int idx, Real v, int lane
   if (lane == 0) slot[idx] += double(s);
 }
 
-template <typename Real>
-__device__ __forceinline__ void contract_forward_dual(const PassTables<Real>& t, Real* v, Real* vd, int lane) {
-  for (int q = lane; q < t.ndst; q += kWarp) {
-    Real s = Real(0), sd = Real(0);
-    for (int p = t.dst_begin[q]; p < t.dst_begin[q + 1]; ++p) {
-      s += t.dst_w[p] * v[t.dst_src[p]];
-      sd += t.dst_w[p] * vd[t.dst_src[p]];
-    }
-    v[t.dst_node[q]] += s;
-    vd[t.dst_node[q]] += sd;
-  }
-  __syncwarp();
-}
-
-template <typename Real>
-__device__ __forceinline__ void graph_forward_dual(const PassTables<Real>& t, Real* v, Real* vd, int lane) {
-  for (int lv = 0; lv < t.levels; ++lv) {
-    for (int q = t.level_begin[lv] + lane; q < t.level_begin[lv + 1]; q += kWarp) {
-      Real s = Real(0), sd = Real(0);
-      for (int p = t.out_begin[q]; p < t.out_begin[q + 1]; ++p) {
-        const int x = t.fprod_a[p], y = t.fprod_b[p];
-        const Real c = t.fprod_c[p];
-        s += c * v[x] * v[y];
-        sd += c * (vd[x] * v[y] + v[x] * vd[y]);
+// Steps [s0, s1) of the pass's graph program (run_prog) on values and tangents (DIR 1: the range
+// holds forward steps only, 2: reverse steps only, 0: either -- the kernel compiles only what it
+// runs): forward steps
+//   v[t] += c v[a] v[b],  vd[t] += c (vd[a] v[b] + v[a] vd[b]),
+// reverse steps on the adjoints of values (lam) and tangents (mu):
+//   lam[t] += c (lam[a] v[b] + mu[a] vd[b]),  mu[t] += c mu[a] v[b].
+template <typename Real, int DIR>
+__device__ __forceinline__ void run_prog_dual(const GraphProg<Real>& g, int s0, int s1, Real* v, Real* vd, Real* lam,
+                                              Real* mu, Real* parts, int lane) {
+  for (int st = s0; st < s1; ++st) {
+    const int4 info = g.steps[st];
+    const bool rev = DIR == 2 || (DIR == 0 && (info.w & 1));
+    Real* T = rev ? lam : v;
+    Real* Td = rev ? mu : vd;
+    const ProgRec<Real>* r = g.rows + static_cast<size_t>(info.x) * kWarp + lane;
+    Real acc = Real(0), accd = Real(0);
+    auto flush = [&](int f) {
+      if (f >= 0) { T[f] += acc; Td[f] += accd; }
+      else { parts[2 * (-f - 2)] = acc; parts[2 * (-f - 2) + 1] = accd; }
+      acc = Real(0);
+      accd = Real(0);
+    };
+    if (!rev) {
+#pragma unroll 2
+      for (int i = 0; i < info.y; ++i) {
+        const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+        const int x = p.ab & 0xffffu, y = p.ab >> 16;
+        const Real vx = v[x], vy = v[y];
+        acc += p.c * vx * vy;
+        accd += p.c * (vd[x] * vy + vx * vd[y]);
+        if (p.flush != kProgNoFlush) flush(p.flush);
       }
-      v[t.out_nodes[q]] += s;
-      vd[t.out_nodes[q]] += sd;
+    } else {
+#pragma unroll 2
+      for (int i = 0; i < info.y; ++i) {
+        const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+        const int x = p.ab & 0xffffu, y = p.ab >> 16;
+        const Real vy = v[y], mx = mu[x];
+        acc += p.c * (lam[x] * vy + mx * vd[y]);
+        accd += p.c * mx * vy;
+        if (p.flush != kProgNoFlush) flush(p.flush);
+      }
+    }
+    const int comb_end = info.w >> 1;
+    if (comb_end > info.z) {
+      __syncwarp();
+      for (int q = info.z + lane; q < comb_end; q += kWarp) {
+        const int4 e = g.comb[q];
+        Real s = Real(0), sd = Real(0);
+        for (int p = e.y; p < e.z; ++p) { s += parts[2 * p]; sd += parts[2 * p + 1]; }
+        T[e.x] += s;
+        Td[e.x] += sd;
+      }
     }
     __syncwarp();
   }
 }
 
+// Rank-weight gradients of the contraction (read before the contraction's reverse step changes
+// the basic nodes' adjoints): the per-weight sum of a few products in the compute precision,
+// added to the FP64 slice.
 template <typename Real>
-__device__ __forceinline__ void graph_reverse_dual(const PassTables<Real>& t, const Real* v, const Real* vd, Real* lam,
-                                                   Real* mu, int lane) {
-  for (int lv = t.levels - 1; lv >= 0; --lv) {
-    for (int q = t.rlevel_begin[lv] + lane; q < t.rlevel_begin[lv + 1]; q += kWarp) {
-      Real sl = Real(0), sm = Real(0);
-      for (int p = t.in_begin[q]; p < t.in_begin[q + 1]; ++p) {
-        const int o = t.rprod_out[p], x = t.rprod_other[p];
-        const Real c = t.rprod_c[p];
-        sl += c * (lam[o] * v[x] + mu[o] * vd[x]);
-        sm += c * mu[o] * v[x];
-      }
-      lam[t.in_nodes[q]] += sl;
-      mu[t.in_nodes[q]] += sm;
+__device__ __forceinline__ void rank_weight_grad(const PassGradLayout& gl, const Real* v, const Real* vd,
+                                                 const Real* lam, const Real* mu, double* slot, int lane) {
+  if (gl.rw_off < 0) return;
+  for (int w = lane; w < gl.nw; w += kWarp) {
+    Real s = Real(0);
+    for (int p = gl.w_begin[w]; p < gl.w_begin[w + 1]; ++p) {
+      const int src = gl.w_src[p], dst = gl.w_dst[p];
+      s += lam[dst] * v[src] + mu[dst] * vd[src];
     }
-    __syncwarp();
+    slot[gl.rw_off + w] += double(s);
   }
-}
-
-template <typename Real>
-__device__ __forceinline__ void contract_reverse_dual(const PassTables<Real>& t, const PassGradLayout& gl, int NB,
-                                                      const Real* v, const Real* vd, Real* lam, Real* mu, double* slot,
-                                                      int lane) {
-  if (t.ndst == 0) return;
-  // rank-weight gradients first (they read lam/mu of contraction nodes, which do not change below);
-  // the per-weight sum of a few products in the compute precision, added to the FP64 slice
-  if (gl.rw_off >= 0)
-    for (int w = lane; w < gl.nw; w += kWarp) {
-      Real s = Real(0);
-      for (int p = gl.w_begin[w]; p < gl.w_begin[w + 1]; ++p) {
-        const int src = gl.w_src[p], dst = gl.w_dst[p];
-        s += lam[dst] * v[src] + mu[dst] * vd[src];
-      }
-      slot[gl.rw_off + w] += double(s);
-    }
-  for (int b = lane; b < NB; b += kWarp) {
-    Real sl = Real(0), sm = Real(0);
-    for (int p = t.src_begin[b]; p < t.src_begin[b + 1]; ++p) {
-      sl += t.src_w[p] * lam[t.src_dst[p]];
-      sm += t.src_w[p] * mu[t.src_dst[p]];
-    }
-    lam[b] += sl;
-    mu[b] += sm;
-  }
-  __syncwarp();
 }
 
 template <int L, typename Real, int MODE, bool KAHAN, int BF>
@@ -189,18 +188,19 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
   Real* s_w1 = s_w0 + C * F;
   Real* s_wa = s_w1 + C * F;
   const int ncol = a.acc_cols;
-  Real* wbase = s_wa + C * F + (grad_warp_size<Real>(F, H, M, K) + ncol * kAccStride) * warp;
+  Real* wbase = s_wa + C * F + (grad_warp_size<Real>(F, H, M, K, dm.prog_parts) + ncol * kAccStride) * warp;
   const int sw = 2 * F + 2 * H + 1;
   Real* stage = wbase;
-  Real* v = stage + kWarp * sw;
-  Real* vd = v + M;
+  Real* v = stage + kWarp * sw;    // [M + 1], v[M] = 1
+  Real* vd = v + M + 1;            // [M + 1], vd[M] = 0
   const bool adj_staged = grad_adj_in_stage(F, H, M);
-  Real* lam = adj_staged ? stage : vd + M;
-  Real* mu = lam + M;
-  Real* abl = vd + M + (adj_staged ? 0 : 2 * M);
+  Real* lam = adj_staged ? stage : vd + M + 1;
+  Real* mu = lam + M + 1;
+  Real* abl = vd + M + 1 + (adj_staged ? 0 : 2 * (M + 1));
   Real* abm = abl + K * H;
   Real* hb = abm + K * H;  // [2F]
-  Real* accs = wbase + grad_warp_size<Real>(F, H, M, K);  // [ncol][kAccStride]
+  Real* parts = hb + 2 * F;  // [2 prog_parts]
+  Real* accs = wbase + grad_warp_size<Real>(F, H, M, K, dm.prog_parts);  // [ncol][kAccStride]
   const int nsb = grad_acc_nsb(dm.scaling_mode, Lp);
   const int c_wc = Lp * B, c_scal = c_wc + C * Lp, c_add = c_scal + 2 * nsb * C;
 
@@ -215,6 +215,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
   __syncthreads();
   double* slot = a.slots + static_cast<size_t>(blockIdx.x * warps + warp) * NP;
 
+  const int nit = (K * H + kWarp - 1) / kWarp;  // moment items in use of the kMaxItems slots
   int it_u[kMaxItems], it_y[kMaxItems];
 #pragma unroll
   for (int s = 0; s < kMaxItems; ++s) {
@@ -298,12 +299,14 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
         for (int q = 0; q < nb; ++q) {
           const Real* sr = stage + q * sw;
 #pragma unroll
-          for (int s = 0; s < kMaxItems; ++s)
+          for (int s = 0; s < kMaxItems; ++s) {
+            if (s >= nit) break;  // warp-uniform: only the model's K H items are issued
             if (it_u[s] >= 0) {
               const Real uu = sr[it_u[s]], ud = sr[F + it_u[s]], yy = sr[it_y[s]], yd = sr[it_y[s] + H];
               part[s] += uu * yy;
               partd[s] += ud * yy + uu * yd;
             }
+          }
         }
 #pragma unroll
         for (int s = 0; s < kMaxItems; ++s) {
@@ -312,7 +315,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
         }
         __syncwarp();
       }
-      for (int q = lane; q < M; q += kWarp) { v[q] = Real(0); vd[q] = Real(0); }
+      for (int q = lane; q <= M; q += kWarp) { v[q] = q < M ? Real(0) : Real(1); vd[q] = Real(0); }
       __syncwarp();
 #pragma unroll
       for (int s = 0; s < kMaxItems; ++s) {
@@ -323,8 +326,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
         }
       }
       __syncwarp();
-      contract_forward_dual<Real>(pt, v, vd, lane);
-      graph_forward_dual<Real>(pt, v, vd, lane);
+      run_prog_dual<Real, 1>(pt.prog, 0, pt.prog.nfwd, v, vd, lam, mu, parts, lane);
       if (MODE == kGradGateForward) {
         for (int q = lane; q < M; q += kWarp) {
           a.gmom[static_cast<size_t>(atom) * M + q] = v[q];
@@ -346,7 +348,7 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
       const double ewi = a.ew[atom];
       const double coef = dm.species_readout ? 1.0 : dm.species[ti];
       const int off = dm.species_readout ? ti * dm.S : 0;
-      for (int q = lane; q < M; q += kWarp) { lam[q] = Real(0); mu[q] = Real(0); }
+      for (int q = lane; q <= M; q += kWarp) { lam[q] = Real(0); mu[q] = Real(0); }
       __syncwarp();
       double sp = 0.0;
       for (int q = lane; q < dm.S; q += kWarp) {
@@ -374,9 +376,9 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
         hb[m_] = Real(sd);
         a.lh_atom[static_cast<size_t>(atom) * 2 * F + m_] = sd;
       }
-      for (int q = lane; q < M; q += kWarp) {
-        v[q] = a.gmom[static_cast<size_t>(atom) * M + q];
-        vd[q] = a.gmomd[static_cast<size_t>(atom) * M + q];
+      for (int q = lane; q <= M; q += kWarp) {
+        v[q] = q < M ? a.gmom[static_cast<size_t>(atom) * M + q] : Real(1);
+        vd[q] = q < M ? a.gmomd[static_cast<size_t>(atom) * M + q] : Real(0);
         lam[q] = Real(0);
         mu[q] = Real(0);
       }
@@ -394,8 +396,17 @@ __global__ void grad_pass_kernel(GradArgs<Real> a) {
     }
 
     // ---------------- reverse over values and tangents ----------------
-    graph_reverse_dual<Real>(pt, v, vd, lam, mu, lane);
-    contract_reverse_dual<Real>(pt, gl, NB, v, vd, lam, mu, slot, lane);
+    // the contraction's reverse is the program's last step when the pass has a contraction; the
+    // rank-weight gradients read the adjoints just before it
+    {
+      const int last = pt.ndst > 0 ? pt.prog.nsteps - 1 : pt.prog.nsteps;
+      run_prog_dual<Real, 2>(pt.prog, pt.prog.nfwd, last, v, vd, lam, mu, parts, lane);
+      if (pt.ndst > 0) {
+        rank_weight_grad<Real>(gl, v, vd, lam, mu, slot, lane);
+        __syncwarp();
+        run_prog_dual<Real, 2>(pt.prog, last, pt.prog.nsteps, v, vd, lam, mu, parts, lane);
+      }
+    }
     for (int t = lane; t < K * H; t += kWarp) {
       const int b = dm.basic_of[t];
       abl[t] = b >= 0 ? lam[b] : Real(0);
