@@ -14,20 +14,27 @@ constexpr int kGradMaxWarps = 4;  // warps per block considered by the launch co
 template <typename Real>
 using GradKernel = void (*)(GradArgs<Real>);
 
+// cols: the per-edge parameter contributions go through lane-private shared-memory columns (true)
+// or shuffle trees (false); each kernel contains one of the two forms only (a smaller kernel body
+// keeps the per-edge loop within the instruction cache).  The gate forward pass has neither.
 template <typename Real, int L, int BF>
-GradKernel<Real> kernel_for(int mode) {
+GradKernel<Real> kernel_for(int mode, bool cols) {
   constexpr bool kKahan = sizeof(Real) == 4;
   switch (mode) {
-    case kGradOuter: return grad_pass_kernel<L, Real, kGradOuter, kKahan, BF>;
-    case kGradGateForward: return grad_pass_kernel<L, Real, kGradGateForward, kKahan, BF>;
-    case kGradGateReverse: return grad_pass_kernel<L, Real, kGradGateReverse, kKahan, BF>;
+    case kGradOuter:
+      return cols ? grad_pass_kernel<L, Real, kGradOuter, kKahan, BF, true>
+                  : grad_pass_kernel<L, Real, kGradOuter, kKahan, BF, false>;
+    case kGradGateForward: return grad_pass_kernel<L, Real, kGradGateForward, kKahan, BF, false>;
+    case kGradGateReverse:
+      return cols ? grad_pass_kernel<L, Real, kGradGateReverse, kKahan, BF, true>
+                  : grad_pass_kernel<L, Real, kGradGateReverse, kKahan, BF, false>;
   }
   throw std::runtime_error("unknown gradient mode");
 }
 
 template <typename Real, int L>
-GradKernel<Real> kernel_for(int mode, int B) {
-  return B == 8 ? kernel_for<Real, L, 8>(mode) : kernel_for<Real, L, 0>(mode);
+GradKernel<Real> kernel_for(int mode, int B, bool cols) {
+  return B == 8 ? kernel_for<Real, L, 8>(mode, cols) : kernel_for<Real, L, 0>(mode, cols);
 }
 
 }  // namespace grad_detail
@@ -36,7 +43,6 @@ template <typename Real, int L>
 GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, int sm_count) {
   using namespace grad_detail;
   if (dm.K > kMaxK) throw std::runtime_error("sh_k_max above " + std::to_string(kMaxK) + " is not supported");
-  GradKernel<Real> kern = kernel_for<Real, L>(mode, dm.B);
   constexpr int H = (L + 1) * (L + 1), Lp = L + 1;
   int device = 0, optin = 0;
   cudaGetDevice(&device);
@@ -53,6 +59,7 @@ GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, in
     return sizeof(Real) * (table + warps * (per_warp + static_cast<size_t>(c) * kAccStride));
   };
   if (bytes(1, cols) > static_cast<size_t>(optin)) cfg.acc_cols = 0;  // columns do not fit: shuffle trees
+  GradKernel<Real> kern = kernel_for<Real, L>(mode, dm.B, cfg.acc_cols > 0);
   cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   if (err != cudaSuccess) throw std::runtime_error(std::string("gradient shared memory: ") + cudaGetErrorString(err));
   // warps per block: the most resident warps per SM (registers and shared memory), fewer warps
@@ -78,7 +85,7 @@ GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, in
 template <typename Real, int L>
 int launch_grad_pass_l(int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t s) {
   if (a.natoms == 0) return 0;
-  grad_detail::GradKernel<Real> kern = grad_detail::kernel_for<Real, L>(mode, a.dm.B);
+  grad_detail::GradKernel<Real> kern = grad_detail::kernel_for<Real, L>(mode, a.dm.B, cfg.acc_cols > 0);
   GradArgs<Real> args = a;
   args.acc_cols = cfg.acc_cols;
   kern<<<cfg.grid, cfg.block, cfg.smem, s>>>(args);
