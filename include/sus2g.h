@@ -123,12 +123,19 @@ int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
  * form measured faster on GB300. */
 int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
- * the model runs with both compiled register budgets (3 and 4 resident blocks per SM; basis size 8)
- * over `reps` launches each and keeps the faster for later evaluations (results are identical
- * either way).  blocks4[mode] (may be NULL) = the chosen budgets per pass (0 Static, 1 gate
- * forward, 2 outer, 3 gate reverse; 0 for passes the model does not run), ms8[2 mode + budget - 3]
- * (may be NULL) = milliseconds per launch. */
+ * the model runs in each tile shape -- compiled register budget (3 and 4 resident blocks per SM;
+ * basis size 8), grid shape and centre order (sus2g_engine_pass_shape) -- over `reps` launches
+ * each and keeps the fastest for later evaluations (results are identical in every shape).
+ * blocks4[mode] (may be NULL) = the chosen budgets per pass (0 Static, 1 gate forward, 2 outer,
+ * 3 gate reverse; 0 for passes the model does not run), ms8[2 mode + budget - 3] (may be NULL) =
+ * milliseconds per launch of the budget's fastest shape. */
 int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* ms8);
+/* Tile shape of a per-atom pass (mode 0 Static, 1 gate forward, 2 outer, 3 gate reverse) as the
+ * autotuner left it: shape4 = {register budget in resident blocks per SM (0 = default), grid
+ * (0 all resident blocks, 1 the fewest blocks with the same centres per warp), centre order
+ * (0 grid-strided, 1 contiguous runs per warp), warps per block}.  No counterpart in the
+ * reference (its kernel has no launch shape). */
+int sus2g_engine_pass_shape(sus2g_engine engine, int mode, int* shape4);
 
 /* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
  * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors

@@ -168,6 +168,13 @@ int sus2g_engine_copy_edges(sus2g_engine e, long long cap, int* centre, int* nei
   });
 }
 
+int sus2g_engine_pass_shape(sus2g_engine e, int mode, int* shape4) {
+  return guarded([&] {
+    need(e && shape4 && mode >= 0 && mode < 4, "engine/mode/shape");
+    e->engine->pass_shape(mode, shape4);
+  });
+}
+
 int sus2g_engine_set_moment_mma(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_moment_mma(enabled != 0); });
 }

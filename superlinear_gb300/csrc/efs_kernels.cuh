@@ -51,6 +51,8 @@ struct PassArgs {
   double* desc;            // [natoms][S] scalar moments (descriptors), or null
   int* error;
   int moment_mma;          // FP32 engines: 1 = edge->moment batch sums on the tensor cores (3xTF32 mma.sync)
+  int atom_order;          // 0: warps take centres grid-strided; 1: each warp a contiguous run of centres
+  int grid_mode;           // 0: all resident blocks; 1: the fewest blocks that keep the same atoms per warp
 };
 
 template <typename Real>
@@ -395,7 +397,14 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
   }
 
-  for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
+  // centres of this warp: grid-strided, or one contiguous run (neighbouring centres share their
+  // neighbours' rows in L1)
+  const int gwarp = blockIdx.x * warps + warp, nwarps = gridDim.x * warps;
+  const int per_warp = (a.natoms + nwarps - 1) / nwarps;
+  const int atom_first = a.atom_order ? gwarp * per_warp : gwarp;
+  const int atom_stop = a.atom_order ? min(a.natoms, atom_first + per_warp) : a.natoms;
+  const int atom_step = a.atom_order ? 1 : nwarps;
+  for (int atom = atom_first; atom < atom_stop; atom += atom_step) {
     const int ti = species_of(a.types, atom, C);
     const int e0 = a.row[atom], e1 = a.row_end[atom];
     // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form

@@ -1810,7 +1810,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       if (ghosts)
         SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
       mark_begin(2);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateForward, a, sm_count_, s, pass_blocks_[kModeGateForward], (pdl_ & kPdlFirstPass) != 0);
+      launches_ += launch_pass<Real>(kModeGateForward, a, (pdl_ & kPdlFirstPass) != 0);
       mark_end();
     }
   }
@@ -1819,7 +1819,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
     const int mode = m.gated ? kModeOuter : kModeStatic;
-    launches_ += launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, pass_blocks_[mode], (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
+    launches_ += launch_pass<Real>(mode, a, (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
     mark_end();
     if (m.gated && user_edges_) {
       hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
@@ -1836,7 +1836,7 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) {
       if (user_edges_) a.hbar_atom = hbar_atom_.as<double>();
       mark_begin(3);
-      launches_ += launch_atom_pass<Real>(m.L, kModeGateReverse, a, sm_count_, s, pass_blocks_[kModeGateReverse], (pdl_ & kPdlBetweenPasses) != 0);
+      launches_ += launch_pass<Real>(kModeGateReverse, a, (pdl_ & kPdlBetweenPasses) != 0);
       mark_end();
     }
     wait_reverse();
@@ -2095,11 +2095,22 @@ void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d
   else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
 }
 
+// One per-atom pass in the tile shape chosen for its mode (the defaults until autotune runs).
+template <typename Real>
+int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
+  a.grid_mode = pass_grid_[mode];
+  a.atom_order = pass_order_[mode];
+  return launch_atom_pass<Real>(model_.L, mode, a, sm_count_, stream_, pass_blocks_[mode], pdl);
+}
+
 // Pass-kernel autotuner: on the current layout (the last evaluation's edges), times each pass the
-// model runs with both register budgets (3 and 4 resident blocks per SM), `reps` launches each
-// after one warm-up launch, and keeps the faster budget per pass.  The passes read the state the
-// evaluation before them left (gate signals, node adjoints), so a full evaluation runs first; the
-// gate reverse pass accumulates into the edge gradients, so the next evaluation recomputes them.
+// model runs in every tile shape -- register budget (3 or 4 resident blocks per SM), grid (all
+// resident blocks, or the fewest that keep the same centres per warp) and centre order (grid-
+// strided or contiguous runs per warp) -- `reps` launches each after one warm-up launch, and keeps
+// the fastest shape per pass.  ms_out[2 mode + (budget - 3)] = the best time of each budget.
+// The passes read the state the evaluation before them left (gate signals, node adjoints), so a
+// full evaluation runs first; the gate reverse pass accumulates into the edge gradients, so the
+// next evaluation recomputes them.
 template <typename Real>
 void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
   const Model& m = model_;
@@ -2118,20 +2129,27 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
   for (int k = 0; k < nmodes; ++k) {
     const int mode = modes[k];
     double best = 0.0;
-    int choice = 0;
-    for (int blocks = 3; blocks <= 4; ++blocks) {
-      launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
-      SUS2G_CUDA(cudaEventRecord(e0, s));
-      for (int r = 0; r < reps; ++r) launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
-      SUS2G_CUDA(cudaEventRecord(e1, s));
-      SUS2G_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      const double per = double(ms) / std::max(1, reps);
-      ms_out[2 * mode + (blocks - 3)] = per;
-      if (choice == 0 || per < best) { best = per; choice = blocks; }
-    }
+    int choice = 0, choice_grid = 0, choice_order = 0;
+    for (int blocks = 3; blocks <= 4; ++blocks)
+      for (int grid = 0; grid <= 1; ++grid)
+        for (int order = 0; order <= 1; ++order) {
+          a.grid_mode = grid;
+          a.atom_order = order;
+          launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+          SUS2G_CUDA(cudaEventRecord(e0, s));
+          for (int r = 0; r < reps; ++r) launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+          SUS2G_CUDA(cudaEventRecord(e1, s));
+          SUS2G_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          const double per = double(ms) / std::max(1, reps);
+          double& slot = ms_out[2 * mode + (blocks - 3)];
+          if (slot == 0.0 || per < slot) slot = per;
+          if (choice == 0 || per < best) { best = per; choice = blocks; choice_grid = grid; choice_order = order; }
+        }
     pass_blocks_[mode] = choice;
+    pass_grid_[mode] = choice_grid;
+    pass_order_[mode] = choice_order;
     blocks_out[mode] = choice;
   }
   event_next_ = 0;

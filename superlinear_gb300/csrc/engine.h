@@ -86,6 +86,11 @@ class Engine {
   // register budget (3 or 4 resident blocks per SM; 0 for passes the model does not run),
   // ms_out[2 mode + (budget - 3)] = the timed milliseconds per launch.
   void autotune(int reps, int* blocks_out, double* ms_out);
+  // tile shape of pass `mode` (0 Static, 1 gate forward, 2 outer, 3 gate reverse): register budget
+  // (resident blocks per SM; 0 = default), grid shape, centre order, warps per block
+  void pass_shape(int mode, int* shape4) const {
+    shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode]; shape4[2] = pass_order_[mode]; shape4[3] = 4;
+  }
   void reset_step_graph();
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
@@ -262,6 +267,9 @@ class Engine {
   DevBuf scratch_;
   DevBuf io_[8];
   int pass_blocks_[4] = {0, 0, 0, 0};  // register budget per pass mode (0: the default)
+  int pass_grid_[4] = {0, 0, 0, 0};    // grid shape per pass mode (PassArgs::grid_mode)
+  int pass_order_[4] = {0, 0, 0, 0};   // centre order per pass mode (PassArgs::atom_order)
+  template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
   // second stream for independent work inside a step (reverse edges beside the first pass, the
   // frame reduction beside the force gather)
   cudaStream_t aux_stream_ = nullptr;

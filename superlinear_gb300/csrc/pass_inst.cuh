@@ -31,7 +31,14 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPassWarps * kWarp, smem);
   if (per_sm < 1) throw std::runtime_error("pass kernel does not fit on an SM (shared memory " + std::to_string(smem) + " B)");
   const int need = (a.natoms + kPassWarps - 1) / kPassWarps;
-  const int grid = std::max(1, std::min(need, per_sm * sm_count));
+  const int resident = per_sm * sm_count;
+  int grid = std::max(1, std::min(need, resident));
+  if (a.grid_mode == 1) {
+    // the same number of rounds over the resident warps with the fewest blocks: every warp then
+    // takes the same number of centres (to one)
+    const int rounds = (need + resident - 1) / resident;
+    grid = std::max(1, (need + rounds - 1) / rounds);
+  }
   if (a.natoms == 0) return 0;
   cudaError_t err = launch_kernel(pdl, kern, dim3(grid), dim3(kPassWarps * kWarp), smem, stream, a);
   if (err != cudaSuccess) throw std::runtime_error(std::string("pass launch: ") + cudaGetErrorString(err));

@@ -149,6 +149,20 @@ class Engine:
         check(load().sus2g_engine_autotune(self._h, int(reps), b, ms))
         return {name: (b[q], {3: ms[2 * q], 4: ms[2 * q + 1]}) for q, name in enumerate(self.PASSES) if b[q]}
 
+    def pass_shapes(self):
+        """Tile shape of each pass the model runs: {pass: {"blocks_per_sm", "grid", "order",
+        "warps_per_block"}} (grid "resident" / "balanced", order "strided" / "contiguous")."""
+        out = {}
+        shape = (ctypes.c_int * 4)()
+        passes = ("gate_forward", "outer", "gate_reverse") if self.model.dims["gated"] else ("static",)
+        for q, name in enumerate(self.PASSES):
+            if name not in passes:
+                continue
+            check(load().sus2g_engine_pass_shape(self._h, q, shape))
+            out[name] = {"blocks_per_sm": shape[0], "grid": ("resident", "balanced")[shape[1]],
+                         "order": ("strided", "contiguous")[shape[2]], "warps_per_block": shape[3]}
+        return out
+
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))

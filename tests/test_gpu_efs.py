@@ -170,8 +170,9 @@ def test_mixed_cell_list_and_image_scan_batch(lib, oracle_lib, golden, name):
 
 @pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l4k8r2o3"])
 def test_autotune_keeps_results_and_chooses_budgets(lib, golden, name):
-    """The pass autotuner times both register budgets on the evaluated layout; the chosen kernels
-    compute the same values (bit for bit), before and after, through the step graph too."""
+    """The pass autotuner times every tile shape (register budget, grid, centre order) on the
+    evaluated layout; the chosen kernels compute the same values (bit for bit), before and after,
+    through the step graph too."""
     path = os.path.join(golden, "models", f"{name}.sus2")
     m = lib.Model(path)
     fr = diamond(6, sigma=0.05, seed=9, species=m.dims["C"])
@@ -185,6 +186,11 @@ def test_autotune_keeps_results_and_chooses_budgets(lib, golden, name):
         assert set(choice) == modes
         for blocks, times in choice.values():
             assert blocks in (3, 4) and times[blocks] == min(times.values()) and times[blocks] > 0
+        shapes = g.pass_shapes()
+        assert set(shapes) == modes
+        for name_, sh in shapes.items():
+            assert sh["blocks_per_sm"] == choice[name_][0] and sh["warps_per_block"] == 4
+            assert sh["grid"] in ("resident", "balanced") and sh["order"] in ("strided", "contiguous")
         for _ in range(3):
             after = g.calc_efs([fr])
             for x, y in zip(before, after):
