@@ -337,9 +337,13 @@ def bench_config5(sg, torch, steps, warmup, bfgs_iters, cpu_frames=0):
             t0 = time.perf_counter()
             _, hist = tr.bfgs(p, max_iter=bfgs_iters)
             dt = time.perf_counter() - t0
-            out["bfgs_fp32"] = {"iterations": int(hist.size - 1), "seconds": dt,
-                                "ms_per_iteration": 1e3 * dt / max(1, hist.size - 1),
-                                "loss_first": float(hist[0]), "loss_last": float(hist[-1])}
+            nev = int(tr.bfgs_trials()[0].size)
+            out["bfgs_fp32"] = {"iterations": int(hist.size - 1), "requested": bfgs_iters, "evaluations": nev,
+                                "seconds": dt, "ms_per_iteration": 1e3 * dt / max(1, hist.size - 1),
+                                "loss_first": float(hist[0]), "loss_last": float(hist[-1]),
+                                "line_search": "reference (Linesearch::Iterate)",
+                                "timed_region": "the whole sus2g_trainer_bfgs call from the model's parameters "
+                                                "(every objective evaluation, direction and inverse-Hessian update)"}
         del tr, eng
     out["fp32_over_fp64"] = out["fp64"]["ms_per_step"] / out["fp32"]["ms_per_step"]
     (l32, g32), (l64, g64) = losses["fp32"], losses["fp64"]
@@ -754,7 +758,7 @@ def main():
                     help="with --profile-only / --profile-effect: edge->moment sums on the tensor cores (3xTF32)")
     ap.add_argument("--skip-config5", action="store_true",
                     help="skip the 2,048-frame L5 training loss+gradient and BFGS measurement")
-    ap.add_argument("--bfgs-iters", type=int, default=10, help="timed FP32 BFGS iterations on the L5 batch")
+    ap.add_argument("--bfgs-iters", type=int, default=100, help="timed FP32 BFGS iterations on the L5 batch")
     ap.add_argument("--config5-only", action="store_true",
                     help="only the 2,048-frame L5 training measurement; prints its JSON object")
     args = ap.parse_args()
