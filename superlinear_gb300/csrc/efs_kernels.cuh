@@ -140,7 +140,8 @@ __device__ __forceinline__ EdgeIn<Real> load_edge(const typename Vec4<Real>::typ
   EdgeIn<Real> x;
   x.d = d4[e];
   x.j = nbr[e];
-  x.tj = species_of(types, x.j, C);
+  // one species: no neighbour-type load (it would wait on the neighbour index just loaded)
+  x.tj = C == 1 ? 0 : species_of(types, x.j, C);
   return x;
 }
 
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   const int atom_stop = a.atom_order ? min(a.natoms, atom_first + per_warp) : a.natoms;
   const int atom_step = a.atom_order ? 1 : nwarps;
   for (int atom = atom_first; atom < atom_stop; atom += atom_step) {
-    const int ti = species_of(a.types, atom, C);
+    const int ti = C == 1 ? 0 : species_of(a.types, atom, C);
     const int e0 = a.row[atom], e1 = a.row_end[atom];
     // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form
     double vir[6] = {0, 0, 0, 0, 0, 0};

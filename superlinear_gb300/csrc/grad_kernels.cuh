@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
   }
 
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
-    const int ti = a.types[atom];
+    const int ti = C == 1 ? 0 : a.types[atom];
     const int e0 = a.row[atom], e1 = a.row_end[atom];
     const double* Sw = a.sw + 9 * a.frame_of[atom];
     const Real S00 = Real(Sw[0]), S01 = Real(Sw[1]), S02 = Real(Sw[2]), S10 = Real(Sw[3]), S11 = Real(Sw[4]),
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
                              Real* Yd, bool& ang) {
       const V4 dv = a.d4[e];
       j = a.nbr[e];
-      tj = a.types[j];
+      tj = C == 1 ? 0 : a.types[j];
       r = dv.w;
       const Real ir = Real(1) / r;
       ux = dv.x * ir; uy = dv.y * ir; uz = dv.z * ir;
