@@ -122,6 +122,12 @@ int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
  * (interfaces/lammps/ML-SUS2/sus2_sl_kernel.cpp:340-354); kept as an option because the CUDA-core
  * form measured faster on GB300. */
 int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
+/* FP32 engines, Static models with basis size 8: run the per-atom pass as three kernels -- the
+ * edge->moment forward, the per-atom contraction / graph / readout / adjoint, and the per-edge
+ * adjoint -- through device moment arrays, instead of one fused kernel (enabled = 1; default 0;
+ * the autotuner chooses between the two).  The same arithmetic as the fused pass: results are
+ * bitwise identical.  No counterpart in the reference (a launch-shape choice). */
+int sus2g_engine_set_static_split(sus2g_engine engine, int enabled);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
  * the model runs in each tile shape -- compiled register budget (3 and 4 resident blocks per SM;
  * basis size 8), grid shape and centre order (sus2g_engine_pass_shape) -- over `reps` launches
@@ -133,7 +139,8 @@ int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* m
 /* Tile shape of a per-atom pass (mode 0 Static, 1 gate forward, 2 outer, 3 gate reverse) as the
  * autotuner left it: shape4 = {register budget in resident blocks per SM (0 = default), grid
  * (0 all resident blocks, 1 the fewest blocks with the same centres per warp), centre order
- * (0 grid-strided, 1 contiguous runs per warp), warps per block}.  No counterpart in the
+ * (0 grid-strided, 1 contiguous runs per warp; plus 2 when the Static pass runs as three kernels,
+ * sus2g_engine_set_static_split), warps per block}.  No counterpart in the
  * reference (its kernel has no launch shape). */
 int sus2g_engine_pass_shape(sus2g_engine engine, int mode, int* shape4);
 

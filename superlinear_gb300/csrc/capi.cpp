@@ -175,6 +175,10 @@ int sus2g_engine_pass_shape(sus2g_engine e, int mode, int* shape4) {
   });
 }
 
+int sus2g_engine_set_static_split(sus2g_engine e, int enabled) {
+  return guarded([&] { need(e, "engine"); e->engine->set_static_split(enabled != 0); });
+}
+
 int sus2g_engine_set_moment_mma(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_moment_mma(enabled != 0); });
 }

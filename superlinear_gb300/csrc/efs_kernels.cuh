@@ -29,7 +29,13 @@
 
 namespace sus2g {
 
-enum PassMode : int { kModeStatic = 0, kModeGateForward = 1, kModeOuter = 2, kModeGateReverse = 3 };
+enum PassMode : int {
+  kModeStatic = 0, kModeGateForward = 1, kModeOuter = 2, kModeGateReverse = 3,
+  // the Static pass split at the per-atom boundary into three kernels: the edge->moment forward
+  // (moments to a.mom), the per-atom graph (atom_graph_kernel: readout, adjoint moments to
+  // a.amom) and the per-edge adjoint (from a.amom)
+  kModeStaticFwd = 4, kModeStaticRev = 5
+};
 
 template <typename Real>
 struct PassArgs {
@@ -49,6 +55,8 @@ struct PassArgs {
   double* site_energy;     // [natoms]
   double* virial;          // [natoms][6] (xx, yy, zz, xy, xz, yz), minus d (x) g
   double* desc;            // [natoms][S] scalar moments (descriptors), or null
+  Real* mom;               // [natoms][K H] moments (split Static pass: forward -> graph kernel)
+  Real* amom;              // [natoms][K H] their adjoints (graph kernel -> per-edge adjoint)
   int* error;
   int moment_mma;          // FP32 engines: 1 = edge->moment batch sums on the tensor cores (3xTF32 mma.sync)
   int atom_order;          // 0: warps take centres grid-strided; 1: each warp a contiguous run of centres
@@ -323,6 +331,35 @@ __device__ __forceinline__ void moments_mma_batch(const float* stage, int sw, in
   __syncwarp();
 }
 
+// Readout of one centre and the adjoint seeds: E_i = species + shift + coef sum_q linear_q
+// v[map q] into a.site_energy (the sum in compensated FP32 with exact products for the FP32 bulk
+// form, FP64 otherwise), the scalar moments into a.desc when requested, adj zeroed and seeded with
+// coef linear in Real (the reference's readout, sus2_sl_kernel.cpp:556).
+template <typename Real>
+__device__ __forceinline__ void readout_seeds(const PassArgs<Real>& a, int atom, int ti, const Real* v, Real* adj,
+                                              int lane) {
+  const DevModel<Real>& dm = a.dm;
+  const int M = dm.M;
+  const double coef = dm.species_readout ? 1.0 : dm.species[ti];
+  const Real coef_r = Real(coef);
+  const int off = dm.species_readout ? ti * dm.S : 0;
+  for (int q = lane; q <= M; q += kWarp) adj[q] = Real(0);
+  __syncwarp();
+  double es64 = 0.0;
+  float ehi = 0.f, elo = 0.f;
+  for (int q = lane; q < dm.S; q += kWarp) {
+    const int node = dm.scalar_map[q];
+    const Real lin = dm.linear[off + q], vv = v[node];
+    if (sizeof(Real) == 4) csum_add_prod(ehi, elo, float(lin), float(vv));
+    else es64 += double(lin) * double(vv);
+    adj[node] = coef_r * lin;
+    if (a.desc) a.desc[static_cast<size_t>(atom) * dm.S + q] = double(vv);
+  }
+  const double es = sizeof(Real) == 4 ? warp_csum(ehi, elo) : warp_sum(es64);
+  if (lane == 0) a.site_energy[atom] = dm.species[ti] + dm.shift[ti] + coef * es;
+  __syncwarp();
+}
+
 // ---------------------------------------------------------------------------------------------
 // The pass kernel.
 // ---------------------------------------------------------------------------------------------
@@ -417,9 +454,13 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     EdgeIn<Real> cur{};
     const int nbat = (e1 - e0 + kWarp - 1) / kWarp;
     // the gate reverse pass starts with the per-atom work: its first edge batch loads meanwhile
-    if (MODE == kModeGateReverse && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
+    if ((MODE == kModeGateReverse || MODE == kModeStaticRev) && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
       cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + (nbat - 1) * kWarp + lane, C);
-    if (MODE != kModeGateReverse) {
+    if (MODE == kModeStaticRev) {
+      // ---------------- split pass, per-edge part: adjoint moments from the graph kernel ----------
+      for (int t = lane; t < K * H; t += kWarp) abar[t] = a.amom[static_cast<size_t>(atom) * (K * H) + t];
+      __syncwarp();
+    } else if (MODE != kModeGateReverse) {
       // ---------------- forward moments ----------------
       Real acc[kMaxItems], cmp[kMaxItems];
 #pragma unroll
@@ -495,6 +536,16 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         __syncwarp();
         if (more) cur = nxt;
       }
+      if (MODE == kModeStaticFwd) {
+        // split pass, forward part: the moments go to the graph kernel
+#pragma unroll
+        for (int s = 0; s < kMaxItems; ++s) {
+          if (s >= nit) break;
+          const int t = lane + kWarp * s;
+          if (t < K * H) a.mom[static_cast<size_t>(atom) * (K * H) + t] = acc[s];
+        }
+        continue;
+      }
       for (int q = lane; q <= M; q += kWarp) v[q] = q < M ? Real(0) : Real(1);
       __syncwarp();
 #pragma unroll
@@ -520,26 +571,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
       }
 
       // ---------------- readout and seeds ----------------
-      // E_i = species + shift + coef sum_q linear_q v[map q]: the sum in compensated FP32 (exact
-      // products) for the FP32 bulk form, FP64 otherwise; the seeds adj = coef linear in Real
-      const double coef = dm.species_readout ? 1.0 : dm.species[ti];
-      const Real coef_r = Real(coef);
-      const int off = dm.species_readout ? ti * dm.S : 0;
-      for (int q = lane; q <= M; q += kWarp) adj[q] = Real(0);
-      __syncwarp();
-      double es64 = 0.0;
-      float ehi = 0.f, elo = 0.f;
-      for (int q = lane; q < dm.S; q += kWarp) {
-        const int node = dm.scalar_map[q];
-        const Real lin = dm.linear[off + q], vv = v[node];
-        if (sizeof(Real) == 4) csum_add_prod(ehi, elo, float(lin), float(vv));
-        else es64 += double(lin) * double(vv);
-        adj[node] = coef_r * lin;
-        if (a.desc) a.desc[static_cast<size_t>(atom) * dm.S + q] = double(vv);
-      }
-      const double es = sizeof(Real) == 4 ? warp_csum(ehi, elo) : warp_sum(es64);
-      if (lane == 0) a.site_energy[atom] = dm.species[ti] + dm.shift[ti] + coef * es;
-      __syncwarp();
+      readout_seeds<Real>(a, atom, ti, v, adj, lane);
     } else {
       // ---------------- gate reverse: gather hbar, project, load gate values ----------------
       for (int mu = lane; mu < F; mu += kWarp) {
@@ -565,12 +597,14 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
 
     // ---------------- reverse graph and contraction ----------------
-    run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
-    for (int t = lane; t < K * H; t += kWarp) {
-      const int b = dm.basic_of[t];
-      abar[t] = b >= 0 ? adj[b] : Real(0);
+    if (MODE != kModeStaticRev) {
+      run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
+      for (int t = lane; t < K * H; t += kWarp) {
+        const int b = dm.basic_of[t];
+        abar[t] = b >= 0 ? adj[b] : Real(0);
+      }
+      __syncwarp();
     }
-    __syncwarp();
 
     // ---------------- per-edge adjoint ----------------
     // batches in reverse order, the next one's edge inputs loaded while the current one runs
@@ -666,6 +700,47 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         else
           for (int c = 0; c < 6; ++c) vo[c] = vir[c];
       }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// The per-atom part of the split Static pass: warp per centre, moments a.mom -> the graph
+// program forward -> readout (site energy, descriptors) -> the program's reverse -> adjoint
+// moments a.amom.  Independent of L; several warps of centres in flight per SM hide the
+// program's load latency that the fused pass serialises between its edge phases.
+// ---------------------------------------------------------------------------------------------
+constexpr int kGraphWarps = 4;
+__host__ __device__ inline int graph_warp_size(int M, int parts) { return round4(2 * (M + 1) + parts + 4); }
+
+template <typename Real>
+__global__ void __launch_bounds__(kGraphWarps * kWarp) atom_graph_kernel(PassArgs<Real> a) {
+  const DevModel<Real>& dm = a.dm;
+  const PassTables<Real>& pt = dm.outer;
+  const int M = dm.M, KH = dm.K * dm.H, C = dm.C;
+  const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Real* v = reinterpret_cast<Real*>(smem_raw) + graph_warp_size(M, dm.prog_parts) * warp;
+  Real* adj = v + M + 1;
+  Real* parts = adj + M + 1;
+  pdl_launch_dependents();
+  pdl_wait();
+  for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
+    const int ti = C == 1 ? 0 : species_of(a.types, atom, C);
+    for (int q = lane; q <= M; q += kWarp) v[q] = q < M ? Real(0) : Real(1);
+    __syncwarp();
+    for (int t = lane; t < KH; t += kWarp) {
+      const int b = dm.basic_of[t];
+      if (b >= 0) v[b] = a.mom[static_cast<size_t>(atom) * KH + t];
+    }
+    __syncwarp();
+    run_prog<Real, 1>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
+    readout_seeds<Real>(a, atom, ti, v, adj, lane);
+    run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
+    for (int t = lane; t < KH; t += kWarp) {
+      const int b = dm.basic_of[t];
+      a.amom[static_cast<size_t>(atom) * KH + t] = b >= 0 ? adj[b] : Real(0);
     }
     __syncwarp();
   }

@@ -1819,7 +1819,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
     const int mode = m.gated ? kModeOuter : kModeStatic;
-    launches_ += launch_pass<Real>(mode, a, (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
+    if (!m.gated && use_static_split<Real>()) launches_ += launch_static_split<Real>(a, (pdl_ & kPdlFirstPass) != 0);
+    else launches_ += launch_pass<Real>(mode, a, (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
     mark_end();
     if (m.gated && user_edges_) {
       hbar_atom_.ensure(sizeof(double) * static_cast<size_t>(std::max(1, N)) * m.F);
@@ -2095,6 +2096,28 @@ void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d
   else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
 }
 
+// The Static pass split at the per-atom boundary (FP32 engines, basis size 8): edge->moment
+// forward, per-atom graph kernel, per-edge adjoint -- three launches through device moment
+// arrays; the forward and adjoint kernels take the Static pass's tile shape.
+template <typename Real>
+bool Engine::use_static_split() const {
+  return static_split_ && sizeof(Real) == 4 && model_.B == 8 && !model_.gated;
+}
+template <typename Real>
+int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
+  const size_t n = static_cast<size_t>(std::max(1, ncentres_)) * model_.K * model_.H;
+  mom_.ensure(sizeof(Real) * n);
+  amom_.ensure(sizeof(Real) * n);
+  a.mom = mom_.as<Real>();
+  a.amom = amom_.as<Real>();
+  a.grid_mode = pass_grid_[kModeStatic];
+  a.atom_order = pass_order_[kModeStatic];
+  int k = launch_atom_pass<Real>(model_.L, kModeStaticFwd, a, sm_count_, stream_, pass_blocks_[kModeStatic], pdl);
+  k += launch_atom_graph<Real>(a, sm_count_, stream_);
+  k += launch_atom_pass<Real>(model_.L, kModeStaticRev, a, sm_count_, stream_, pass_blocks_[kModeStatic], false);
+  return k;
+}
+
 // One per-atom pass in the tile shape chosen for its mode (the defaults until autotune runs).
 template <typename Real>
 int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
@@ -2151,6 +2174,18 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
     pass_grid_[mode] = choice_grid;
     pass_order_[mode] = choice_order;
     blocks_out[mode] = choice;
+    if (mode == kModeStatic && sizeof(Real) == 4 && m.B == 8) {
+      // the fused Static pass against its three-kernel split, in the chosen shape
+      static_split_ = true;
+      launch_static_split<Real>(a, false);
+      SUS2G_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r) launch_static_split<Real>(a, false);
+      SUS2G_CUDA(cudaEventRecord(e1, s));
+      SUS2G_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      static_split_ = double(ms) / std::max(1, reps) < best;
+    }
   }
   event_next_ = 0;
   reset_step_graph();  // a captured step holds the previous budgets

@@ -87,14 +87,24 @@ class Engine {
   // ms_out[2 mode + (budget - 3)] = the timed milliseconds per launch.
   void autotune(int reps, int* blocks_out, double* ms_out);
   // tile shape of pass `mode` (0 Static, 1 gate forward, 2 outer, 3 gate reverse): register budget
-  // (resident blocks per SM; 0 = default), grid shape, centre order, warps per block
+  // (resident blocks per SM; 0 = default), grid shape, centre order + 2 x split (Static pass run
+  // as three kernels), warps per block
   void pass_shape(int mode, int* shape4) const {
-    shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode]; shape4[2] = pass_order_[mode]; shape4[3] = 4;
+    shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode];
+    shape4[2] = pass_order_[mode] + (mode == 0 && static_split_ ? 2 : 0); shape4[3] = 4;
   }
   void reset_step_graph();
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
   // drops a captured step graph.
+  // The Static pass as three kernels (edge->moment forward, per-atom graph, per-edge adjoint)
+  // instead of one (FP32 engines, basis size 8; the autotuner also chooses it); a change drops a
+  // captured step graph.
+  void set_static_split(bool on) {
+    if (on != static_split_) reset_step_graph();
+    static_split_ = on;
+  }
+  bool static_split() const { return static_split_; }
   void set_moment_mma(bool on) {
     if (on != moment_mma_) reset_step_graph();
     moment_mma_ = on;
@@ -270,6 +280,10 @@ class Engine {
   int pass_grid_[4] = {0, 0, 0, 0};    // grid shape per pass mode (PassArgs::grid_mode)
   int pass_order_[4] = {0, 0, 0, 0};   // centre order per pass mode (PassArgs::atom_order)
   template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
+  template <typename Real> bool use_static_split() const;
+  template <typename Real> int launch_static_split(PassArgs<Real> a, bool pdl);
+  bool static_split_ = false;   // Static pass as forward / per-atom graph / adjoint kernels
+  DevBuf mom_, amom_;           // the split pass's moments and adjoint moments [N][K H]
   // second stream for independent work inside a step (reverse edges beside the first pass, the
   // frame reduction beside the force gather)
   cudaStream_t aux_stream_ = nullptr;

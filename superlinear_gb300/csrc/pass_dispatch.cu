@@ -1,5 +1,6 @@
 // Run-time selection of the per-L pass and gradient units (instantiated in pass_fp*_l*.cu and
 // grad_fp*_l*.cu); this unit sees only their declarations.
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 
@@ -67,6 +68,30 @@ cudaError_t upload_grad_constants() {
   return cudaSuccess;
 }
 
+template <typename Real>
+int launch_atom_graph(const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+  if (a.natoms == 0) return 0;
+  auto kern = atom_graph_kernel<Real>;
+  const size_t smem = sizeof(Real) * kGraphWarps * static_cast<size_t>(graph_warp_size(a.dm.M, a.dm.prog_parts));
+  static size_t configured = 0;
+  if (smem > configured) {
+    cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (err != cudaSuccess) throw std::runtime_error(std::string("graph kernel shared memory: ") + cudaGetErrorString(err));
+    configured = smem;
+  }
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kGraphWarps * kWarp, smem);
+  if (per_sm < 1) throw std::runtime_error("graph kernel does not fit on an SM");
+  const int need = (a.natoms + kGraphWarps - 1) / kGraphWarps;
+  const int grid = std::max(1, std::min(need, per_sm * sm_count));
+  kern<<<grid, kGraphWarps * kWarp, smem, s>>>(a);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) throw std::runtime_error(std::string("graph kernel launch: ") + cudaGetErrorString(err));
+  return 1;
+}
+
+template int launch_atom_graph<float>(const PassArgs<float>&, int, cudaStream_t);
+template int launch_atom_graph<double>(const PassArgs<double>&, int, cudaStream_t);
 template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t, int, bool);
 template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t, int, bool);
 template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int);

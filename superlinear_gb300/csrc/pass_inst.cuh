@@ -66,6 +66,14 @@ int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cud
     case kModeGateForward: return launch_budget<Real, L, kModeGateForward, BF>(blocks, a, sm_count, s, pdl);
     case kModeOuter: return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s, pdl);
     case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s, pdl);
+    case kModeStaticFwd:
+    case kModeStaticRev:
+      if constexpr (sizeof(Real) == 4) {
+        return mode == kModeStaticFwd ? launch_budget<Real, L, kModeStaticFwd, BF>(blocks, a, sm_count, s, pdl)
+                                      : launch_budget<Real, L, kModeStaticRev, BF>(blocks, a, sm_count, s, pdl);
+      } else {
+        throw std::runtime_error("the split Static pass is compiled for FP32 engines only");
+      }
   }
   throw std::runtime_error("unknown pass mode");
 }

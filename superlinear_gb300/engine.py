@@ -160,12 +160,17 @@ class Engine:
                 continue
             check(load().sus2g_engine_pass_shape(self._h, q, shape))
             out[name] = {"blocks_per_sm": shape[0], "grid": ("resident", "balanced")[shape[1]],
-                         "order": ("strided", "contiguous")[shape[2]], "warps_per_block": shape[3]}
+                         "order": ("strided", "contiguous")[shape[2] & 1], "warps_per_block": shape[3],
+                         "split": bool(shape[2] & 2)}
         return out
 
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))
+
+    def set_static_split(self, on: bool) -> None:
+        """FP32 Static engines: the per-atom pass as forward / per-atom graph / adjoint kernels."""
+        check(load().sus2g_engine_set_static_split(self._h, 1 if on else 0))
 
     def set_moment_mma(self, on: bool) -> None:
         """FP32 engines: edge->moment batch sums on the tensor cores (3xTF32 mma.sync) instead of

@@ -495,3 +495,19 @@ def test_moment_mma_option_within_fp32_bars(lib, golden, name, cells):
     again = g32.calc_efs([fr])
     for x, y in zip(again, base):
         assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("cells", [4, 9])
+def test_static_split_pass_is_bitwise_the_fused_pass(lib, golden, cells):
+    """The Static pass as three kernels (edge->moment forward, per-atom graph, per-edge adjoint;
+    sus2g_engine_set_static_split) gives the fused pass's results bit for bit (FP32), also
+    through the step graph."""
+    path = os.path.join(golden, "models", "static_l3k4o2.sus2")
+    m, g64, g32 = engines(lib, path)
+    fr = diamond(cells, sigma=0.08, seed=41)
+    fused = g32.calc_efs([fr])
+    g32.set_static_split(True)
+    for _ in range(3):
+        split = g32.calc_efs([fr])
+        for x, y in zip(fused, split):
+            assert np.array_equal(x, y)
