@@ -131,7 +131,9 @@ int sus2g_engine_set_static_split(sus2g_engine engine, int enabled);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
  * the model runs in each tile shape -- compiled register budget (3 and 4 resident blocks per SM;
  * basis size 8), grid shape and centre order (sus2g_engine_pass_shape) -- over `reps` launches
- * each and keeps the fastest for later evaluations (results are identical in every shape).
+ * each and keeps the fastest for later evaluations.  Grid shape and centre order never change a
+ * result bit; the two register budgets are separately compiled kernels whose results agree to the
+ * rounding of the precision (the compiler may form multiply-adds differently in each).
  * blocks4[mode] (may be NULL) = the chosen budgets per pass (0 Static, 1 gate forward, 2 outer,
  * 3 gate reverse; 0 for passes the model does not run), ms8[2 mode + budget - 3] (may be NULL) =
  * milliseconds per launch of the budget's fastest shape. */
@@ -139,10 +141,16 @@ int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* m
 /* Tile shape of a per-atom pass (mode 0 Static, 1 gate forward, 2 outer, 3 gate reverse) as the
  * autotuner left it: shape4 = {register budget in resident blocks per SM (0 = default), grid
  * (0 all resident blocks, 1 the fewest blocks with the same centres per warp), centre order
- * (0 grid-strided, 1 contiguous runs per warp; plus 2 when the Static pass runs as three kernels,
- * sus2g_engine_set_static_split), warps per block}.  No counterpart in the
+ * (0 grid-strided, 1 contiguous runs per warp, 2 taken from a device counter as warps finish;
+ * plus 4 when the Static pass runs as three kernels, sus2g_engine_set_static_split), warps per
+ * block}.  No counterpart in the
  * reference (its kernel has no launch shape). */
 int sus2g_engine_pass_shape(sus2g_engine engine, int mode, int* shape4);
+/* Sets the tile shape of a per-atom pass as the autotuner would: blocks = register budget (0
+ * default, 3 or 4), grid 0 / 1 and order 0 / 1 / 2 as in sus2g_engine_pass_shape -- to pin a shape
+ * tuned once for a workload without timing it again (results as under sus2g_engine_autotune).  No
+ * counterpart in the reference. */
+int sus2g_engine_set_pass_shape(sus2g_engine engine, int mode, int blocks, int grid, int order);
 
 /* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
  * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors

@@ -40,6 +40,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
     flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math",
              "-Wno-deprecated-gpu-targets"] + ARCH
+    # objects built with other flags are rebuilt
+    stamp = os.path.join(BUILD, "flags.txt")
+    if not os.path.exists(stamp) or open(stamp).read() != " ".join(flags):
+        for old in glob.glob(os.path.join(BUILD, "*.o")):
+            os.remove(old)
+        with open(stamp, "w") as f:
+            f.write(" ".join(flags))
     jobs_list = []
     objects = []
     for src in sources:

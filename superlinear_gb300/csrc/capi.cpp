@@ -175,6 +175,13 @@ int sus2g_engine_pass_shape(sus2g_engine e, int mode, int* shape4) {
   });
 }
 
+int sus2g_engine_set_pass_shape(sus2g_engine e, int mode, int blocks, int grid, int order) {
+  return guarded([&] {
+    need(e, "engine");
+    e->engine->set_pass_shape(mode, blocks, grid, order);
+  });
+}
+
 int sus2g_engine_set_static_split(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_static_split(enabled != 0); });
 }

@@ -185,19 +185,21 @@ __device__ __forceinline__ T warp_sum(T v) {
 
 // Compensated FP32 accumulation (Knuth two-sum; the running error is kept in lo): sums of FP32
 // terms with close to FP64 accuracy without FP64 arithmetic, which runs at 1/64 of the FP32 rate
-// on this GPU.  No multiplications are involved, so FMA contraction cannot alter the error terms.
+// on this GPU.  Every step is an explicitly rounded operation (__fadd_rn / __fsub_rn / __fmul_rn),
+// which the compiler never fuses with a neighbouring multiply: the sums are the same bits in every
+// kernel instantiation (register budget) that inlines them.
 __device__ __forceinline__ void csum_add(float& hi, float& lo, float x) {
-  const float s = hi + x;
-  const float bb = s - hi;
-  lo += (hi - (s - bb)) + (x - bb);
+  const float s = __fadd_rn(hi, x);
+  const float bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
   hi = s;
 }
 // x * y added exactly (product split by an FMA: p + e == x * y).
 __device__ __forceinline__ void csum_add_prod(float& hi, float& lo, float x, float y) {
-  const float p = x * y;
+  const float p = __fmul_rn(x, y);
   const float e = fmaf(x, y, -p);
   csum_add(hi, lo, p);
-  lo += e;
+  lo = __fadd_rn(lo, e);
 }
 // Warp total of compensated partials (fixed butterfly order), left as (hi, lo) on every lane.
 __device__ __forceinline__ void warp_csum_pair(float& hi, float& lo) {
@@ -205,7 +207,7 @@ __device__ __forceinline__ void warp_csum_pair(float& hi, float& lo) {
   for (int o = 16; o > 0; o >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
     csum_add(hi, lo, oh);
-    lo += ol;
+    lo = __fadd_rn(lo, ol);
   }
 }
 // The same total returned in FP64 on every lane.

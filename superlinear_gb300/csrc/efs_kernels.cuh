@@ -59,7 +59,10 @@ struct PassArgs {
   Real* amom;              // [natoms][K H] their adjoints (graph kernel -> per-edge adjoint)
   int* error;
   int moment_mma;          // FP32 engines: 1 = edge->moment batch sums on the tensor cores (3xTF32 mma.sync)
-  int atom_order;          // 0: warps take centres grid-strided; 1: each warp a contiguous run of centres
+  int atom_order;          // 0: warps take centres grid-strided; 1: each warp a contiguous run of
+                           // centres; 2: warps take the next centre from a device counter (*work,
+                           // zero at launch) as they finish -- dynamic balance for uneven centres
+  int* work;               // the counter of atom_order 2
   int grid_mode;           // 0: all resident blocks; 1: the fewest blocks that keep the same atoms per warp
 };
 
@@ -90,10 +93,16 @@ __host__ __device__ inline int pass_warp_size(int F, int H, int M, int K, int pa
   return round4(kWarp * stage_stride(F, H) + (M + 1) + (adj_in_stage(F, H, M) ? 0 : M + 1) + K * H + F + parts + 4);
 }
 
-// Kahan-compensated accumulation for the FP32 bulk form; plain sums in FP64.
+// Kahan-compensated accumulation for the FP32 bulk form (explicitly rounded steps, never fused
+// with the caller's multiplies); plain sums in FP64.
 template <typename Real, bool KAHAN>
 __device__ __forceinline__ void kadd(Real& s, Real& c, Real x) {
-  if (KAHAN) {
+  if constexpr (KAHAN && sizeof(Real) == 4) {
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  } else if constexpr (KAHAN) {
     const Real y = x - c;
     const Real t = s + y;
     c = (t - s) - y;
@@ -435,14 +444,20 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
   }
 
-  // centres of this warp: grid-strided, or one contiguous run (neighbouring centres share their
-  // neighbours' rows in L1)
+  // centres of this warp: grid-strided, one contiguous run (neighbouring centres share their
+  // neighbours' rows in L1), or taken one at a time from a device counter
   const int gwarp = blockIdx.x * warps + warp, nwarps = gridDim.x * warps;
   const int per_warp = (a.natoms + nwarps - 1) / nwarps;
-  const int atom_first = a.atom_order ? gwarp * per_warp : gwarp;
-  const int atom_stop = a.atom_order ? min(a.natoms, atom_first + per_warp) : a.natoms;
-  const int atom_step = a.atom_order ? 1 : nwarps;
-  for (int atom = atom_first; atom < atom_stop; atom += atom_step) {
+  const bool dynamic = a.atom_order == 2;
+  auto grab = [&]() {
+    int x = 0;
+    if (lane == 0) x = atomicAdd(a.work, 1);
+    return __shfl_sync(0xffffffffu, x, 0);
+  };
+  const int atom_first = dynamic ? grab() : (a.atom_order ? gwarp * per_warp : gwarp);
+  const int atom_stop = a.atom_order == 1 ? min(a.natoms, atom_first + per_warp) : a.natoms;
+  const int atom_step = a.atom_order == 1 ? 1 : nwarps;
+  for (int atom = atom_first; atom < atom_stop; atom = dynamic ? grab() : atom + atom_step) {
     const int ti = C == 1 ? 0 : species_of(a.types, atom, C);
     const int e0 = a.row[atom], e1 = a.row_end[atom];
     // per-atom virial: FP64 for the FP64 form; compensated FP32 (hi, lo) for the FP32 bulk form

@@ -2112,9 +2112,9 @@ int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
   a.amom = amom_.as<Real>();
   a.grid_mode = pass_grid_[kModeStatic];
   a.atom_order = pass_order_[kModeStatic];
-  int k = launch_atom_pass<Real>(model_.L, kModeStaticFwd, a, sm_count_, stream_, pass_blocks_[kModeStatic], pdl);
+  int k = launch_shape<Real>(kModeStaticFwd, a, pass_blocks_[kModeStatic], pdl);
   k += launch_atom_graph<Real>(a, sm_count_, stream_);
-  k += launch_atom_pass<Real>(model_.L, kModeStaticRev, a, sm_count_, stream_, pass_blocks_[kModeStatic], false);
+  k += launch_shape<Real>(kModeStaticRev, a, pass_blocks_[kModeStatic], false);
   return k;
 }
 
@@ -2123,7 +2123,20 @@ template <typename Real>
 int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
   a.grid_mode = pass_grid_[mode];
   a.atom_order = pass_order_[mode];
-  return launch_atom_pass<Real>(model_.L, mode, a, sm_count_, stream_, pass_blocks_[mode], pdl);
+  return launch_shape<Real>(mode, a, pass_blocks_[mode], pdl);
+}
+
+// One pass launch in the shape already set in `a` (budget `blocks`); the dynamic centre order
+// takes its counter, zeroed on the stream before the launch.
+template <typename Real>
+int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
+  if (a.atom_order == 2) {
+    work_.ensure(sizeof(int) * 8);
+    a.work = work_.as<int>() + mode;
+    SUS2G_CUDA(cudaMemsetAsync(a.work, 0, sizeof(int), stream_));
+    pdl = false;  // the memset sits between this launch and its predecessor
+  }
+  return launch_atom_pass<Real>(model_.L, mode, a, sm_count_, stream_, blocks, pdl);
 }
 
 // Pass-kernel autotuner: on the current layout (the last evaluation's edges), times each pass the
@@ -2155,12 +2168,12 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
     int choice = 0, choice_grid = 0, choice_order = 0;
     for (int blocks = 3; blocks <= 4; ++blocks)
       for (int grid = 0; grid <= 1; ++grid)
-        for (int order = 0; order <= 1; ++order) {
+        for (int order = 0; order <= 2; ++order) {
           a.grid_mode = grid;
           a.atom_order = order;
-          launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+          launch_shape<Real>(mode, a, blocks, false);
           SUS2G_CUDA(cudaEventRecord(e0, s));
-          for (int r = 0; r < reps; ++r) launch_atom_pass<Real>(m.L, mode, a, sm_count_, s, blocks);
+          for (int r = 0; r < reps; ++r) launch_shape<Real>(mode, a, blocks, false);
           SUS2G_CUDA(cudaEventRecord(e1, s));
           SUS2G_CUDA(cudaEventSynchronize(e1));
           float ms = 0.f;
@@ -2202,6 +2215,17 @@ void Engine::autotune(int reps, int* blocks_out, double* ms_out) {
   if (precision_ == kFP32) autotune_passes<float>(reps, blocks_out, ms_out);
   else autotune_passes<double>(reps, blocks_out, ms_out);
   check_device_error();
+}
+
+void Engine::set_pass_shape(int mode, int blocks, int grid, int order) {
+  if (mode < 0 || mode > 3) throw Error(1, "pass shape: mode must be 0 .. 3");
+  if (blocks != 0 && blocks != 3 && blocks != 4) throw Error(1, "pass shape: blocks per SM must be 0, 3 or 4");
+  if (grid < 0 || grid > 1 || order < 0 || order > 2) throw Error(1, "pass shape: grid 0 .. 1, order 0 .. 2");
+  pass_blocks_[mode] = blocks;
+  pass_grid_[mode] = grid;
+  pass_order_[mode] = order;
+  reset_step_graph();
+  ++edge_generation_;  // graphs captured by other owners hold the previous shape
 }
 
 void Engine::reset_step_graph() {

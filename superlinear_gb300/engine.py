@@ -151,7 +151,8 @@ class Engine:
 
     def pass_shapes(self):
         """Tile shape of each pass the model runs: {pass: {"blocks_per_sm", "grid", "order",
-        "warps_per_block"}} (grid "resident" / "balanced", order "strided" / "contiguous")."""
+        "warps_per_block", "split"}} (grid "resident" / "balanced", order "strided" / "contiguous" /
+        "dynamic"; split: the Static pass as three kernels)."""
         out = {}
         shape = (ctypes.c_int * 4)()
         passes = ("gate_forward", "outer", "gate_reverse") if self.model.dims["gated"] else ("static",)
@@ -160,9 +161,16 @@ class Engine:
                 continue
             check(load().sus2g_engine_pass_shape(self._h, q, shape))
             out[name] = {"blocks_per_sm": shape[0], "grid": ("resident", "balanced")[shape[1]],
-                         "order": ("strided", "contiguous")[shape[2] & 1], "warps_per_block": shape[3],
-                         "split": bool(shape[2] & 2)}
+                         "order": ("strided", "contiguous", "dynamic")[shape[2] & 3],
+                         "warps_per_block": shape[3], "split": bool(shape[2] & 4)}
         return out
+
+    def set_pass_shape(self, name: str, blocks_per_sm: int = 0, grid: str = "resident",
+                       order: str = "strided") -> None:
+        """Pins the tile shape of one pass (a name of PASSES) as the autotuner would set it."""
+        check(load().sus2g_engine_set_pass_shape(self._h, self.PASSES.index(name), int(blocks_per_sm),
+                                                 ("resident", "balanced").index(grid),
+                                                 ("strided", "contiguous", "dynamic").index(order)))
 
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""

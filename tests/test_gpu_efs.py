@@ -171,8 +171,9 @@ def test_mixed_cell_list_and_image_scan_batch(lib, oracle_lib, golden, name):
 @pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l4k8r2o3"])
 def test_autotune_keeps_results_and_chooses_budgets(lib, golden, name):
     """The pass autotuner times every tile shape (register budget, grid, centre order) on the
-    evaluated layout; the chosen kernels compute the same values (bit for bit), before and after,
-    through the step graph too."""
+    evaluated layout; the chosen kernels compute the same values -- to the rounding of the
+    precision, as the two register budgets are separately compiled kernels -- and repeat them bit
+    for bit through the step graph."""
     path = os.path.join(golden, "models", f"{name}.sus2")
     m = lib.Model(path)
     fr = diamond(6, sigma=0.05, seed=9, species=m.dims["C"])
@@ -190,11 +191,50 @@ def test_autotune_keeps_results_and_chooses_budgets(lib, golden, name):
         assert set(shapes) == modes
         for name_, sh in shapes.items():
             assert sh["blocks_per_sm"] == choice[name_][0] and sh["warps_per_block"] == 4
-            assert sh["grid"] in ("resident", "balanced") and sh["order"] in ("strided", "contiguous")
-        for _ in range(3):
+            assert sh["grid"] in ("resident", "balanced") and sh["order"] in ("strided", "contiguous", "dynamic")
+        tol = SHAPE_TOL[prec == lib.FP32]
+        first = g.calc_efs([fr])
+        for x, y in zip(before, first):
+            assert rel_err(x, y) < tol
+        for _ in range(2):
             after = g.calc_efs([fr])
-            for x, y in zip(before, after):
+            for x, y in zip(first, after):
                 assert np.array_equal(x, y)
+
+
+# the two register budgets of a pass are separate compilations of the same source, whose compiler
+# may form multiply-adds differently: their results agree to the rounding of the precision
+SHAPE_TOL = (1e-13, 2e-6)
+
+
+@pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l4k8r2o3", "effect_l3k4r2o2"])
+def test_every_pass_shape(lib, golden, name):
+    """Each pass in every tile shape: within one register budget, every grid and centre order --
+    the dynamic order included, where warps take centres from a device counter as they finish --
+    gives the same values bit for bit; the other budget agrees to the precision's rounding.  Both
+    precisions, on a two-species frame whose centres have uneven neighbour counts."""
+    m = lib.Model(os.path.join(golden, "models", f"{name}.sus2"))
+    fr = diamond(5, sigma=0.3, seed=13, species=m.dims["C"])
+    passes = ("gate_forward", "outer", "gate_reverse") if m.dims["gated"] else ("static",)
+    for prec in (lib.FP64, lib.FP32):
+        g = lib.Engine(m, 0, prec)
+        ref = g.calc_efs([fr])
+        for p in passes:
+            for blocks in (3, 4):
+                g.set_pass_shape(p, blocks)
+                base = g.calc_efs([fr])
+                for x, y in zip(ref, base):
+                    assert rel_err(x, y) < SHAPE_TOL[prec == lib.FP32], (prec, p, blocks)
+                for grid in ("resident", "balanced"):
+                    for order in ("strided", "contiguous", "dynamic"):
+                        g.set_pass_shape(p, blocks, grid, order)
+                        for _ in range(2):
+                            got = g.calc_efs([fr])
+                            for x, y in zip(base, got):
+                                assert np.array_equal(x, y), (prec, p, blocks, grid, order)
+            g.set_pass_shape(p)
+        with pytest.raises(lib.Sus2Error):
+            g.set_pass_shape(passes[0], 5)
 
 
 def test_bin_capacity_overflow_is_retried(lib, oracle_lib, golden):

@@ -282,8 +282,9 @@ def test_rescale_matches_reference_trainer(sg, golden, path):
 
 
 def test_trainer_after_autotune(sg, golden):
-    """Tuning the engine's passes on the trainer's layout: the trainer captures its graph again and
-    its objective and gradient are unchanged bit for bit."""
+    """Tuning the engine's passes on the trainer's layout: the trainer captures its graph again;
+    its objective and gradient are unchanged to the precision's rounding (the register budgets
+    are separately compiled kernels) and repeat bit for bit."""
     path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
     model = sg.Model(path)
     frames = read_cfg(os.path.join(golden, "frames", "effect_l3k4r2o2__labelled.cfg"))
@@ -294,4 +295,28 @@ def test_trainer_after_autotune(sg, golden):
         choice = eng.autotune(reps=2)
         assert set(choice) == {"gate_forward", "outer", "gate_reverse"}
         l1, g1 = tr.loss_grad(model.params())
-        assert l1 == l0 and np.array_equal(g1, g0)
+        tol = 1e-12 if prec == sg.FP64 else 1e-6
+        assert abs(l1 - l0) <= tol * abs(l0)
+        assert np.max(np.abs(g1 - g0)) <= tol * (1.0 + np.max(np.abs(g0)))
+        l2, g2 = tr.loss_grad(model.params())
+        assert l2 == l1 and np.array_equal(g2, g1)
+
+
+def test_trainer_every_centre_order(sg, golden):
+    """The trainer's objective and gradient in each centre order of its passes (grid-strided,
+    contiguous runs, taken from a device counter) match the default order bit for bit (one
+    register budget: the default)."""
+    path = os.path.join(golden, "models", "effect_l3k4r2o2.sus2")
+    model = sg.Model(path)
+    frames = read_cfg(os.path.join(golden, "frames", "effect_l3k4r2o2__labelled.cfg"))
+    for prec in (sg.FP64, sg.FP32):
+        eng = sg.Engine(model, 0, prec)
+        tr = sg.Trainer(eng, frames)
+        l0, g0 = tr.loss_grad(model.params())
+        for p in ("gate_forward", "outer", "gate_reverse"):
+            for order in ("contiguous", "dynamic"):
+                eng.set_pass_shape(p, 0, "resident", order)
+                for _ in range(2):
+                    l1, g1 = tr.loss_grad(model.params())
+                    assert l1 == l0 and np.array_equal(g1, g0), (prec, p, order)
+            eng.set_pass_shape(p)
