@@ -18,6 +18,7 @@ enum DeviceError : int {
   kErrBadDistance = 4,    // zero or non-finite edge length
   kErrBadPosition = 5,    // a non-finite atom coordinate in a periodic frame
   kErrBadSpecies = 6,     // an atom species index outside [0, C)
+  kErrAsyncCopy = 7,      // a bulk asynchronous copy into shared memory did not complete in time
 };
 
 __device__ __forceinline__ void record_error(int* flag, int code) {
@@ -138,6 +139,53 @@ __device__ __forceinline__ int warp_lane() { return threadIdx.x & (kWarp - 1); }
 // attribute both are no-ops.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// 1-D bulk asynchronous copies (the TMA unit's non-tensor mode) from this GPU's global memory
+// into the CTA's shared memory, completed on an mbarrier with a transaction count.  Addresses on
+// both sides 16-byte aligned, sizes multiples of 16 bytes.  Nothing here uses a cluster peer: the
+// shared::cluster destination is the issuing CTA's own shared memory.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+// one arrival per phase; visible to the async proxy after the fences
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned arrivals) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(arrivals) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// this thread's arrival for the phase, announcing `bytes` of copies that complete it
+__device__ __forceinline__ void mbar_arrive_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// orders this thread's earlier generic shared-memory accesses (and, after a warp barrier, those of
+// the threads it synchronised with) before its later async-proxy operations
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// global -> shared bulk copy, completing `bytes` of the barrier's transaction count
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Waits for the phase of the given parity to complete, for at most about 2^31 clocks (~1 s);
+// false when it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const long long t0 = clock64();
+  for (int it = 0; it < (1 << 26); ++it) {
+    if (mbar_test(bar, parity)) return true;
+    if (clock64() - t0 > (1ll << 31)) break;
+  }
+  return false;
+}
 
 // kernel<<<grid, block, smem, stream>>>(args...), with the programmatic-serialization attribute
 // when pdl is set.  Returns the launch status.

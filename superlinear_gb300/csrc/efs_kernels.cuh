@@ -34,7 +34,10 @@ enum PassMode : int {
   // the Static pass split at the per-atom boundary into three kernels: the edge->moment forward
   // (moments to a.mom), the per-atom graph (atom_graph_kernel: readout, adjoint moments to
   // a.amom) and the per-edge adjoint (from a.amom)
-  kModeStaticFwd = 4, kModeStaticRev = 5
+  kModeStaticFwd = 4, kModeStaticRev = 5,
+  // the Effect outer pass compiled with the neighbours' gate-signal rows h_j brought into shared
+  // memory by 1-D bulk async copies, one 32-edge batch ahead (a kernel variant of kModeOuter)
+  kModeOuterBulk = 6
 };
 
 template <typename Real>
@@ -63,6 +66,7 @@ struct PassArgs {
                            // centres; 2: warps take the next centre from a device counter (*work,
                            // zero at launch) as they finish -- dynamic balance for uneven centres
   int* work;               // the counter of atom_order 2
+  int h_bulk;              // Effect outer pass: neighbours' h_j rows staged by bulk async copies (pass_h_bulk)
   int grid_mode;           // 0: all resident blocks; 1: the fewest blocks that keep the same atoms per warp
 };
 
@@ -91,6 +95,23 @@ __host__ __device__ constexpr bool adj_in_stage(int F, int H, int M) { return M 
 template <typename Real>
 __host__ __device__ inline int pass_warp_size(int F, int H, int M, int K, int parts) {
   return round4(kWarp * stage_stride(F, H) + (M + 1) + (adj_in_stage(F, H, M) ? 0 : M + 1) + K * H + F + parts + 4);
+}
+// Whether the Effect outer pass can stage the neighbours' gate-signal rows h_j with bulk async
+// copies: a row must be a whole number of 16-byte units (the copy's size and alignment rule).
+// The host launches the kModeOuterBulk variant only then, and sizes its scratch by the same test.
+template <typename Real>
+__host__ __device__ constexpr bool h_rows_bulk_ok(int F) {
+  return (F * static_cast<int>(sizeof(Real))) % 16 == 0;
+}
+template <typename Real>
+__host__ __device__ inline bool pass_h_bulk(int mode, int flag, int F) {
+  return (mode == kModeOuter || mode == kModeOuterBulk) && flag != 0 && h_rows_bulk_ok<Real>(F);
+}
+// Per-warp scratch with the h_j staging area appended: 32 rows of F (one per lane, 16-byte
+// aligned) and the warp's mbarrier (4 values, 16 bytes or more).
+template <typename Real>
+__host__ __device__ inline int pass_warp_stride(int F, int H, int M, int K, int parts, bool h_bulk) {
+  return pass_warp_size<Real>(F, H, M, K, parts) + (h_bulk ? kWarp * F + 4 : 0);
 }
 
 // Kahan-compensated accumulation for the FP32 bulk form (explicitly rounded steps, never fused
@@ -379,7 +400,7 @@ constexpr int kPassWarps = 4;
 // otherwise (measured: the L = 4 outer pass spills and runs slower at 128 registers; the FP64
 // kernels spill more).
 __host__ __device__ constexpr int default_min_blocks(int L, bool fp32, int mode) {
-  return (fp32 && (L <= 3 || (L == 4 && mode != kModeOuter))) ? 4 : 3;
+  return (fp32 && (L <= 3 || (L == 4 && mode != kModeOuter && mode != kModeOuterBulk))) ? 4 : 3;
 }
 
 template <int L, typename Real, int MODE, bool KAHAN, int BF, int MINB>
@@ -392,6 +413,11 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   const PassTables<Real>& pt = gate_pass ? dm.gate : dm.outer;
   const int C = dm.C, F = dm.F, B = BF ? BF : dm.B, K = dm.K, M = dm.M, NB = dm.NB;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
+  // Effect outer pass, bulk variant: the neighbours' h_j rows of a 32-edge batch are brought into
+  // hbuf by bulk async copies (one row per lane), issued while the batch before is still being
+  // worked on (a constant false in every other variant)
+  constexpr bool kBulk = MODE == kModeOuterBulk;
+  const bool hb_on = kBulk && h_rows_bulk_ok<Real>(F);
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Real* sm = reinterpret_cast<Real*>(smem_raw);
@@ -399,7 +425,8 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   Real* s_scal = s_coeff + F * B;
   Real* s_pw = s_scal + 2 * dm.nblk * C * C;        // [C^2][F] x0(t_i) x1(t_j)
   Real* s_pa = s_pw + C * C * F;                    // [C^2][F] x0(t_i) wadd(t_j)
-  Real* wbase = sm + efs_table_size(C, F, B, dm.nblk) + pass_warp_size<Real>(F, H, M, K, dm.prog_parts) * warp;
+  const int wsize = pass_warp_size<Real>(F, H, M, K, dm.prog_parts);
+  Real* wbase = sm + efs_table_size(C, F, B, dm.nblk) + pass_warp_stride<Real>(F, H, M, K, dm.prog_parts, hb_on) * warp;
   const int sw = stage_stride(F, H), yoff = stage_yoff(F);
   Real* stage = wbase;                              // [32][sw]: u at [0, F), Y at [yoff, yoff + H)
   Real* v = stage + kWarp * sw;                     // [M + 1], v[M] = 1
@@ -408,6 +435,8 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   Real* abar = v + (M + 1) + (adj_staged ? 0 : M + 1);  // [K][H]
   Real* hbar = abar + K * H;                        // [F]
   Real* parts = hbar + F;                           // [prog_parts]
+  Real* hbuf = wbase + wsize;                       // [32][F] h_j rows of one batch (hb_on)
+  unsigned long long* hb_bar = reinterpret_cast<unsigned long long*>(hbuf + kWarp * F);
 
   // the next kernel may be scheduled as soon as every block has started; the model tables staged
   // here are written only by host uploads, which completed before the launch chain began, so
@@ -423,7 +452,34 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   }
   __syncthreads();
   pdl_wait();
-  const bool effect_outer = MODE == kModeOuter;
+  const bool effect_outer = MODE == kModeOuter || MODE == kModeOuterBulk;
+  // the h_j copies of a batch: lane 0 orders the warp's reads of hbuf before the async writes and
+  // announces the bytes, every lane with an edge copies its row; the caller has synchronised the
+  // warp after its last reads of hbuf
+  unsigned hb_parity = 0;
+  if (hb_on) {
+    if (lane == 0) mbar_init(hb_bar, 1);
+    __syncwarp();
+  }
+  auto hb_issue = [&](bool has_edge, int j, int nedges) {
+    if (lane == 0) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect(hb_bar, static_cast<unsigned>(nedges * F * sizeof(Real)));
+    }
+    __syncwarp();
+    if (has_edge) bulk_copy_g2s(hbuf + lane * F, a.hsig + (size_t)j * F, F * sizeof(Real), hb_bar);
+  };
+  // waits for the batch's rows; on a copy that does not complete (bounded wait) records the error,
+  // waits once more for the copies in flight and returns false: the warp then leaves the kernel
+  auto hb_arrived = [&]() {
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(hb_bar, hb_parity));
+    if (!ok) {
+      if (lane == 0) record_error(a.error, kErrAsyncCopy);
+      mbar_wait_bounded(hb_bar, hb_parity);
+    }
+    hb_parity ^= 1u;
+    return ok;
+  };
 
   // Lane-owned moment items for the forward reduction: item t = lane + 32 s <-> (k, lm); the
   // first nit of the kMaxItems register slots are in use.
@@ -482,11 +538,13 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
       for (int s = 0; s < kMaxItems; ++s) { acc[s] = Real(0); cmp[s] = Real(0); }
       // the next batch's edge inputs are loaded while the current batch is evaluated
       if (e0 + lane < e1) cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + lane, C);
+      if (hb_on && nbat > 0) hb_issue(e0 + lane < e1, cur.j, min(kWarp, e1 - e0));
       for (int base = e0; base < e1; base += kWarp) {
         const int e = base + lane;
         const bool more = base + kWarp < e1;
         EdgeIn<Real> nxt = cur;
         if (more && e + kWarp < e1) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e + kWarp, C);
+        if (hb_on && !hb_arrived()) return;
         Real* row = stage + lane * sw;
         if (e < e1) {
           const V4 dv = cur.d;
@@ -502,13 +560,14 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
           const int pair = ti * C + tj;
           const Real* pw = s_pw + pair * F;
           const Real* pa = s_pa + pair * F;
-          // Effect: the neighbour's gate signal h_j is staged in the row's u slots, each read once
-          // before its u_mu overwrites it
-          if (effect_outer) copy_row<Real>(row, a.hsig + (size_t)j * F, F);
-          else for (int mu = 0; mu < F; ++mu) row[mu] = Real(0);
+          // Effect: the neighbour's gate signal h_j, from the bulk-copied batch rows or staged in
+          // the row's u slots (each read once before its u_mu overwrites it)
+          const Real* hj = hb_on ? hbuf + lane * F : row;
+          if (effect_outer && !hb_on) copy_row<Real>(row, a.hsig + (size_t)j * F, F);
+          else if (!effect_outer) for (int mu = 0; mu < F; ++mu) row[mu] = Real(0);
           radial_loop<L, Real, false, BF>(dm, s_coeff, s_scal, pair, r, [&](int k, int l, int mu, Real R, Real) {
             Real w = pw[mu];
-            if (effect_outer) w += pa[mu] * row[mu];
+            if (effect_outer) w += pa[mu] * hj[mu];
             row[mu] = w * R;
           });
           if (effect_outer && !ang)
@@ -518,6 +577,8 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
           for (int q = 0; q < sw; ++q) row[q] = Real(0);
         }
         __syncwarp();
+        // the next batch's h_j rows travel while this batch is reduced
+        if (hb_on && more) hb_issue(e + kWarp < e1, nxt.j, min(kWarp, e1 - base - kWarp));
         // plain sum over the batch's (<= 32) staged edges, then a compensated add of the batch
         // partial into the atom's running moment
         const int nb = min(kWarp, e1 - base);
@@ -623,48 +684,65 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
 
     // ---------------- per-edge adjoint ----------------
     // batches in reverse order, the next one's edge inputs loaded while the current one runs
+    // (with bulk-copied h_j rows the last forward batch's rows are still in hbuf: the first
+    // adjoint batch uses them, and each batch's copies for the one after are issued mid-batch)
     for (int bt = nbat - 1; bt >= 0; --bt) {
       const int e = e0 + bt * kWarp + lane;
+      const bool valid = e < e1;
       EdgeIn<Real> nxt = cur;
       if (bt > 0) nxt = load_edge<Real>(a.d4, a.nbr, a.types, e - kWarp, C);
-      if (e >= e1) { cur = nxt; continue; }
+      if (hb_on && bt < nbat - 1 && !hb_arrived()) return;
+      if (!hb_on && !valid) { cur = nxt; continue; }
       const V4 dv = cur.d;
       const int j = cur.j;
       const int tj = cur.tj;
       cur = nxt;
-      const Real r = dv.w, ir = Real(1) / r;
-      const Real ux = dv.x * ir, uy = dv.y * ir, uz = dv.z * ir;
-      const bool ang = !(r >= dm.rang);
+      Real r = Real(1), ir = Real(1), ux = Real(0), uy = Real(0), uz = Real(0), s = Real(0);
+      bool ang = false;
       // P[h] = sum_k w R_kl(h) abar[k][h] feeds the angular gradient; the radial-derivative term
       // sum_h Qd[h] Y[h], Qd[h] = sum_k w R'_kl(h) abar[k][h], is summed per (k, l) as
       // w R'_kl S_kl with S_kl = sum_{h in l} abar[k][h] Y[h] (no per-h Qd registers)
-      Real Y[H], P[H];
-      sph_values<L, Real>(ux, uy, uz, Y);
-#pragma unroll
-      for (int h = 0; h < H; ++h) { P[h] = Real(0); if (h > 0 && !ang) Y[h] = Real(0); }
-      // Effect: h_j staged in the lane's row (free after the forward reduction), overwritten in
-      // place by the hbar contributions, which then go out as one row
+      Real P[H];
+      // Effect: the hbar contributions are written to the lane's row (free after the forward
+      // reduction) and go out as one row; h_j comes from the bulk-copied batch rows, or is staged
+      // in that row first (each read before its contribution overwrites it)
       Real* hrow = stage + lane * sw;
-      if (effect_outer) copy_row<Real>(hrow, a.hsig + (size_t)j * F, F);
-      const int pair = ti * C + tj;
-      const Real* pw = s_pw + pair * F;
-      const Real* pa = s_pa + pair * F;
-      Real s = Real(0);
-      radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, pair, r, [&](int k, int l, int mu, Real R, Real Rd) {
-        Real w = pw[mu], wa = Real(0);
-        if (effect_outer) { wa = pa[mu]; w += wa * hrow[mu]; }
-        const Real wR = w * R;
-        const Real* ab = abar + k * H;
-        Real S = Real(0);
+      if (valid) {
+        r = dv.w;
+        ir = Real(1) / r;
+        ux = dv.x * ir; uy = dv.y * ir; uz = dv.z * ir;
+        ang = !(r >= dm.rang);
+        Real Y[H];
+        sph_values<L, Real>(ux, uy, uz, Y);
 #pragma unroll
-        for (int h = l * l; h < (l + 1) * (l + 1); ++h) {
-          const Real av = ab[h];
-          P[h] += wR * av;
-          S += av * Y[h];
-        }
-        s += w * Rd * S;
-        if (effect_outer) hrow[mu] = wa * R * S;
-      });
+        for (int h = 0; h < H; ++h) { P[h] = Real(0); if (h > 0 && !ang) Y[h] = Real(0); }
+        const Real* hj = hb_on ? hbuf + lane * F : hrow;
+        if (effect_outer && !hb_on) copy_row<Real>(hrow, a.hsig + (size_t)j * F, F);
+        const int pair = ti * C + tj;
+        const Real* pw = s_pw + pair * F;
+        const Real* pa = s_pa + pair * F;
+        radial_loop<L, Real, true, BF>(dm, s_coeff, s_scal, pair, r, [&](int k, int l, int mu, Real R, Real Rd) {
+          Real w = pw[mu], wa = Real(0);
+          if (effect_outer) { wa = pa[mu]; w += wa * hj[mu]; }
+          const Real wR = w * R;
+          const Real* ab = abar + k * H;
+          Real S = Real(0);
+#pragma unroll
+          for (int h = l * l; h < (l + 1) * (l + 1); ++h) {
+            const Real av = ab[h];
+            P[h] += wR * av;
+            S += av * Y[h];
+          }
+          s += w * Rd * S;
+          if (effect_outer) hrow[mu] = wa * R * S;
+        });
+      }
+      // the next (earlier, full) batch's h_j rows travel while this one finishes
+      if (hb_on && bt > 0) {
+        __syncwarp();
+        hb_issue(true, cur.j, kWarp);
+      }
+      if (!valid) continue;
       if (effect_outer) {
         if (!ang)
           for (int mu = 0; mu < F; ++mu)

@@ -705,23 +705,26 @@ k_frame_reduce(const FramePlan* plans, int nframes, int S, const double* site, c
   if (threadIdx.x == 0) arrivals[f] = 0u;
 }
 
-// Caller-provided edges (owned centres, LAMMPS layout): count per centre.
-__global__ void k_count_centres(const int* ei, long long n, int* counts, int nowned, int* error) {
+// Caller-provided edges (owned centres, LAMMPS layout): count per centre.  An edge with a centre
+// or neighbour index out of range is flagged and left out here and by the scatter below alike,
+// so that no row keeps an unfilled slot.
+__global__ void k_count_centres(const int* ei, const int* ej, long long n, int* counts, int nowned, int nall,
+                                int* error) {
   const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n) return;
-  const int i = ei[e];
-  if (i < 0 || i >= nowned) { record_error(error, kErrEdgeCapacity); return; }
+  const int i = ei[e], j = ej[e];
+  if (i < 0 || i >= nowned || j < 0 || j >= nall) { record_error(error, kErrEdgeCapacity); return; }
   atomicAdd(counts + i, 1);
 }
 
 template <typename Real>
 __global__ void k_scatter_user_edges(const int* ei, const int* ej, const double* d, long long n, const int* row,
                                      int* cursor, int* nbr, typename Vec4<Real>::type* d4, unsigned long long* key,
-                                     int nall, int* error) {
+                                     int nowned, int nall, int* error) {
   const long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   if (e >= n) return;
   const int i = ei[e], j = ej[e];
-  if (i < 0 || j < 0 || j >= nall) { record_error(error, kErrEdgeCapacity); return; }
+  if (i < 0 || i >= nowned || j < 0 || j >= nall) { record_error(error, kErrEdgeCapacity); return; }
   const double x = d[3 * e], y = d[3 * e + 1], z = d[3 * e + 2];
   const double r2 = x * x + y * y + z * z;
   if (!(r2 > 0) || !isfinite(r2)) record_error(error, kErrBadDistance);
@@ -1397,8 +1400,9 @@ void Engine::check_error_read() {
     static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
                                 "periodic image index outside [-64, 63]", "a directed edge has no reverse partner",
                                 "zero or non-finite edge length", "non-finite atom coordinate",
-                                "atom species index out of range"};
-    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 7 ? msg[h] : "unknown"));
+                                "atom species index out of range",
+                                "a bulk asynchronous copy into shared memory did not complete"};
+    throw Error(20 + h, std::string("device check failed: ") + (h > 0 && h < 8 ? msg[h] : "unknown"));
   }
 }
 
@@ -1722,7 +1726,8 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
   row_.ensure(sizeof(int) * (nall + 1));
   SUS2G_CUDA(cudaMemsetAsync(counts_.ptr, 0, sizeof(int) * (nowned + 1), s));
   if (nedges) {
-    k_count_centres<<<(nedges + 255) / 256, 256, 0, s>>>(d_i, nedges, counts_.as<int>(), nowned, error_.as<int>());
+    k_count_centres<<<(nedges + 255) / 256, 256, 0, s>>>(d_i, d_j, nedges, counts_.as<int>(), nowned, nall,
+                                                         error_.as<int>());
     ++launches_;
   }
   long long total = 0;
@@ -1741,10 +1746,10 @@ void Engine::set_edges(int nowned, int nall, const int* d_types, int nedges, con
   if (nedges) {
     if (precision_ == kFP32)
       k_scatter_user_edges<float><<<(nedges + 255) / 256, 256, 0, s>>>(d_i, d_j, d_d, nedges, row_.as<int>(), cursor.as<int>(),
-          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), tmp_key_.as<unsigned long long>(), nall, error_.as<int>());
+          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeF>(), tmp_key_.as<unsigned long long>(), nowned, nall, error_.as<int>());
     else
       k_scatter_user_edges<double><<<(nedges + 255) / 256, 256, 0, s>>>(d_i, d_j, d_d, nedges, row_.as<int>(), cursor.as<int>(),
-          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), tmp_key_.as<unsigned long long>(), nall, error_.as<int>());
+          tmp_nbr_.as<int>(), tmp_d4_.as<EdgeD>(), tmp_key_.as<unsigned long long>(), nowned, nall, error_.as<int>());
     ++launches_;
   }
   // rows of ghost atoms are empty
@@ -2123,6 +2128,7 @@ template <typename Real>
 int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
   a.grid_mode = pass_grid_[mode];
   a.atom_order = pass_order_[mode];
+  a.h_bulk = pass_stage_[mode];
   return launch_shape<Real>(mode, a, pass_blocks_[mode], pdl);
 }
 
@@ -2141,9 +2147,10 @@ int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
 
 // Pass-kernel autotuner: on the current layout (the last evaluation's edges), times each pass the
 // model runs in every tile shape -- register budget (3 or 4 resident blocks per SM), grid (all
-// resident blocks, or the fewest that keep the same centres per warp) and centre order (grid-
-// strided or contiguous runs per warp) -- `reps` launches each after one warm-up launch, and keeps
-// the fastest shape per pass.  ms_out[2 mode + (budget - 3)] = the best time of each budget.
+// resident blocks, or the fewest that keep the same centres per warp), centre order (grid-
+// strided, contiguous runs per warp, or taken from a device counter) and, for the Effect outer
+// pass, the staging of the neighbours' gate-signal rows (plain loads or bulk async copies) --
+// `reps` launches each after one warm-up launch, and keeps the fastest shape per pass.  ms_out[2 mode + (budget - 3)] = the best time of each budget.
 // The passes read the state the evaluation before them left (gate signals, node adjoints), so a
 // full evaluation runs first; the gate reverse pass accumulates into the edge gradients, so the
 // next evaluation recomputes them.
@@ -2165,27 +2172,36 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
   for (int k = 0; k < nmodes; ++k) {
     const int mode = modes[k];
     double best = 0.0;
-    int choice = 0, choice_grid = 0, choice_order = 0;
+    int choice = 0, choice_grid = 0, choice_order = 0, choice_stage = 0;
+    // h_j staging by bulk copies: the outer pass only (basis size 8), where a row is whole
+    // 16-byte units
+    const int stages = pass_h_bulk<Real>(mode, 1, m.F) && m.B == 8 ? 2 : 1;
     for (int blocks = 3; blocks <= 4; ++blocks)
       for (int grid = 0; grid <= 1; ++grid)
-        for (int order = 0; order <= 2; ++order) {
-          a.grid_mode = grid;
-          a.atom_order = order;
-          launch_shape<Real>(mode, a, blocks, false);
-          SUS2G_CUDA(cudaEventRecord(e0, s));
-          for (int r = 0; r < reps; ++r) launch_shape<Real>(mode, a, blocks, false);
-          SUS2G_CUDA(cudaEventRecord(e1, s));
-          SUS2G_CUDA(cudaEventSynchronize(e1));
-          float ms = 0.f;
-          SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-          const double per = double(ms) / std::max(1, reps);
-          double& slot = ms_out[2 * mode + (blocks - 3)];
-          if (slot == 0.0 || per < slot) slot = per;
-          if (choice == 0 || per < best) { best = per; choice = blocks; choice_grid = grid; choice_order = order; }
-        }
+        for (int order = 0; order <= 2; ++order)
+          for (int stage = 0; stage < stages; ++stage) {
+            a.grid_mode = grid;
+            a.atom_order = order;
+            a.h_bulk = stage;
+            launch_shape<Real>(mode, a, blocks, false);
+            SUS2G_CUDA(cudaEventRecord(e0, s));
+            for (int r = 0; r < reps; ++r) launch_shape<Real>(mode, a, blocks, false);
+            SUS2G_CUDA(cudaEventRecord(e1, s));
+            SUS2G_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            const double per = double(ms) / std::max(1, reps);
+            double& slot = ms_out[2 * mode + (blocks - 3)];
+            if (slot == 0.0 || per < slot) slot = per;
+            if (choice == 0 || per < best) {
+              best = per; choice = blocks; choice_grid = grid; choice_order = order; choice_stage = stage;
+            }
+          }
+    a.h_bulk = 0;
     pass_blocks_[mode] = choice;
     pass_grid_[mode] = choice_grid;
     pass_order_[mode] = choice_order;
+    pass_stage_[mode] = choice_stage;
     blocks_out[mode] = choice;
     if (mode == kModeStatic && sizeof(Real) == 4 && m.B == 8) {
       // the fused Static pass against its three-kernel split, in the chosen shape
@@ -2217,13 +2233,15 @@ void Engine::autotune(int reps, int* blocks_out, double* ms_out) {
   check_device_error();
 }
 
-void Engine::set_pass_shape(int mode, int blocks, int grid, int order) {
+void Engine::set_pass_shape(int mode, int blocks, int grid, int order, int stage) {
   if (mode < 0 || mode > 3) throw Error(1, "pass shape: mode must be 0 .. 3");
   if (blocks != 0 && blocks != 3 && blocks != 4) throw Error(1, "pass shape: blocks per SM must be 0, 3 or 4");
   if (grid < 0 || grid > 1 || order < 0 || order > 2) throw Error(1, "pass shape: grid 0 .. 1, order 0 .. 2");
+  if (stage < 0 || stage > 1) throw Error(1, "pass shape: staging 0 or 1");
   pass_blocks_[mode] = blocks;
   pass_grid_[mode] = grid;
   pass_order_[mode] = order;
+  pass_stage_[mode] = stage;
   reset_step_graph();
   ++edge_generation_;  // graphs captured by other owners hold the previous shape
 }

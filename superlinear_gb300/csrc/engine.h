@@ -88,14 +88,16 @@ class Engine {
   void autotune(int reps, int* blocks_out, double* ms_out);
   // tile shape of pass `mode` (0 Static, 1 gate forward, 2 outer, 3 gate reverse): register budget
   // (resident blocks per SM; 0 = default), grid shape, centre order + 4 x split (Static pass run
-  // as three kernels), warps per block
+  // as three kernels) + 8 x h_j staging by bulk async copies, warps per block
   void pass_shape(int mode, int* shape4) const {
     shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode];
-    shape4[2] = pass_order_[mode] + (mode == 0 && static_split_ ? 4 : 0); shape4[3] = 4;
+    shape4[2] = pass_order_[mode] + (mode == 0 && static_split_ ? 4 : 0) + (pass_stage_[mode] ? 8 : 0);
+    shape4[3] = 4;
   }
   // sets the tile shape of pass `mode` as the autotuner would (blocks 0 = default, 3 or 4; grid 0
-  // or 1; order 0, 1 or 2): for pinning a shape measured elsewhere
-  void set_pass_shape(int mode, int blocks, int grid, int order);
+  // or 1; order 0, 1 or 2; stage 1 = h_j rows by bulk async copies, Effect outer pass): for
+  // pinning a shape measured elsewhere
+  void set_pass_shape(int mode, int blocks, int grid, int order, int stage);
   void reset_step_graph();
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
@@ -282,6 +284,7 @@ class Engine {
   int pass_blocks_[4] = {0, 0, 0, 0};  // register budget per pass mode (0: the default)
   int pass_grid_[4] = {0, 0, 0, 0};    // grid shape per pass mode (PassArgs::grid_mode)
   int pass_order_[4] = {0, 0, 0, 0};   // centre order per pass mode (PassArgs::atom_order)
+  int pass_stage_[4] = {0, 0, 0, 0};   // h_j staging per pass mode (PassArgs::h_bulk; outer pass)
   template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
   template <typename Real> int launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl);
   DevBuf work_;                 // centre counters of the dynamic centre order, one per pass mode

@@ -19,8 +19,9 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
   auto kern = atom_pass_kernel<L, Real, MODE, kKahan, BF, MINB>;
   const auto& dm = a.dm;
   const int H = (L + 1) * (L + 1);
-  const size_t smem = sizeof(Real) *
-      (efs_table_size(dm.C, dm.F, dm.B, dm.nblk) + kPassWarps * pass_warp_size<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts));
+  const bool h_bulk = MODE == kModeOuterBulk && h_rows_bulk_ok<Real>(dm.F);
+  const size_t smem = sizeof(Real) * (efs_table_size(dm.C, dm.F, dm.B, dm.nblk) +
+                                      kPassWarps * pass_warp_stride<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts, h_bulk));
   static size_t configured = 0;
   if (smem > configured) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -64,7 +65,11 @@ int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cud
   switch (mode) {
     case kModeStatic: return launch_budget<Real, L, kModeStatic, BF>(blocks, a, sm_count, s, pdl);
     case kModeGateForward: return launch_budget<Real, L, kModeGateForward, BF>(blocks, a, sm_count, s, pdl);
-    case kModeOuter: return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s, pdl);
+    case kModeOuter:
+      // the bulk-copy variant for basis size 8 where the gate-signal rows allow it
+      if constexpr (BF == 8)
+        if (pass_h_bulk<Real>(mode, a.h_bulk, a.dm.F)) return launch_budget<Real, L, kModeOuterBulk, BF>(blocks, a, sm_count, s, pdl);
+      return launch_budget<Real, L, kModeOuter, BF>(blocks, a, sm_count, s, pdl);
     case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s, pdl);
     case kModeStaticFwd:
     case kModeStaticRev:

@@ -151,8 +151,9 @@ class Engine:
 
     def pass_shapes(self):
         """Tile shape of each pass the model runs: {pass: {"blocks_per_sm", "grid", "order",
-        "warps_per_block", "split"}} (grid "resident" / "balanced", order "strided" / "contiguous" /
-        "dynamic"; split: the Static pass as three kernels)."""
+        "warps_per_block", "split", "bulk_h"}} (grid "resident" / "balanced", order "strided" /
+        "contiguous" / "dynamic"; split: the Static pass as three kernels; bulk_h: the outer pass's
+        gate-signal rows by bulk async copies)."""
         out = {}
         shape = (ctypes.c_int * 4)()
         passes = ("gate_forward", "outer", "gate_reverse") if self.model.dims["gated"] else ("static",)
@@ -162,15 +163,18 @@ class Engine:
             check(load().sus2g_engine_pass_shape(self._h, q, shape))
             out[name] = {"blocks_per_sm": shape[0], "grid": ("resident", "balanced")[shape[1]],
                          "order": ("strided", "contiguous", "dynamic")[shape[2] & 3],
-                         "warps_per_block": shape[3], "split": bool(shape[2] & 4)}
+                         "warps_per_block": shape[3], "split": bool(shape[2] & 4),
+                         "bulk_h": bool(shape[2] & 8)}
         return out
 
     def set_pass_shape(self, name: str, blocks_per_sm: int = 0, grid: str = "resident",
-                       order: str = "strided") -> None:
-        """Pins the tile shape of one pass (a name of PASSES) as the autotuner would set it."""
+                       order: str = "strided", bulk_h: bool = False) -> None:
+        """Pins the tile shape of one pass (a name of PASSES) as the autotuner would set it;
+        bulk_h: the outer pass's gate-signal rows by bulk async copies."""
         check(load().sus2g_engine_set_pass_shape(self._h, self.PASSES.index(name), int(blocks_per_sm),
                                                  ("resident", "balanced").index(grid),
-                                                 ("strided", "contiguous", "dynamic").index(order)))
+                                                 ("strided", "contiguous", "dynamic").index(order),
+                                                 1 if bulk_h else 0))
 
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""

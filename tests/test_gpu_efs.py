@@ -211,7 +211,8 @@ SHAPE_TOL = (1e-13, 2e-6)
 def test_every_pass_shape(lib, golden, name):
     """Each pass in every tile shape: within one register budget, every grid and centre order --
     the dynamic order included, where warps take centres from a device counter as they finish --
-    gives the same values bit for bit; the other budget agrees to the precision's rounding.  Both
+    and, for the Effect outer pass, both ways of bringing in the neighbours' gate-signal rows
+    (plain loads, or bulk async copies one batch ahead) give the same values bit for bit; the other budget agrees to the precision's rounding.  Both
     precisions, on a two-species frame whose centres have uneven neighbour counts."""
     m = lib.Model(os.path.join(golden, "models", f"{name}.sus2"))
     fr = diamond(5, sigma=0.3, seed=13, species=m.dims["C"])
@@ -227,11 +228,12 @@ def test_every_pass_shape(lib, golden, name):
                     assert rel_err(x, y) < SHAPE_TOL[prec == lib.FP32], (prec, p, blocks)
                 for grid in ("resident", "balanced"):
                     for order in ("strided", "contiguous", "dynamic"):
-                        g.set_pass_shape(p, blocks, grid, order)
-                        for _ in range(2):
-                            got = g.calc_efs([fr])
-                            for x, y in zip(base, got):
-                                assert np.array_equal(x, y), (prec, p, blocks, grid, order)
+                        for bulk in ((False, True) if p == "outer" else (False,)):
+                            g.set_pass_shape(p, blocks, grid, order, bulk)
+                            for _ in range(2):
+                                got = g.calc_efs([fr])
+                                for x, y in zip(base, got):
+                                    assert np.array_equal(x, y), (prec, p, blocks, grid, order, bulk)
             g.set_pass_shape(p)
         with pytest.raises(lib.Sus2Error):
             g.set_pass_shape(passes[0], 5)
