@@ -440,6 +440,13 @@ def run_reference(args):
     return 0
 
 
+def pin_order(eng, order):
+    """Pins every pass of the engine's model to one centre order (default budget and grid)."""
+    if order:
+        for p in (("gate_forward", "outer", "gate_reverse") if eng.model.dims["gated"] else ("static",)):
+            eng.set_pass_shape(p, 0, "resident", order)
+
+
 def run_profile_train(args):
     """FP32 trainer steps only (for ncu launch lists of the training workload)."""
     import torch
@@ -447,7 +454,9 @@ def run_profile_train(args):
     import superlinear_gb300 as sg
     frames = training_set(sg)
     model = sg.Model(TRAIN_MODEL)
-    tr = sg.Trainer(sg.Engine(model, 0, sg.FP32), frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
+    eng = sg.Engine(model, 0, sg.FP32)
+    pin_order(eng, args.order)
+    tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
     tr.set_graph(not args.no_graph)
     p = model.params()
     for _ in range(args.warmup + args.steps):
@@ -468,6 +477,7 @@ def run_profile_effect(args):
     dev = torch.device("cuda", 0)
     eng = sg.Engine(sg.Model(EFFECT_MODEL), 0, sg.FP32)
     eng.set_moment_mma(args.moment_mma)
+    pin_order(eng, args.order)
     pos = torch.tensor(fr.positions, device=dev)
     typ = torch.tensor(fr.types, device=dev)
     out = torch.zeros(fr.natoms * 3 + 7, dtype=torch.float64, device=dev)
@@ -556,6 +566,8 @@ def run_ours(args):
 
     eng32 = make(sg.FP32)
     eng32.set_moment_mma(args.moment_mma)
+    if args.profile_only:
+        pin_order(eng32, args.order)
     # pass-kernel autotuner on the workload's layout (after one evaluation), as a user would run it
     # (not in the profiling mode, whose ncu launch offsets count the steps' own launches)
     tuned = {}
@@ -754,6 +766,9 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="with --profile-train: eager launches instead of the graph")
     ap.add_argument("--profile-effect", action="store_true",
                     help="only FP32 Effect L4/K8/R2/O3 steps on a --cells diamond (for ncu captures)")
+    ap.add_argument("--order", choices=("strided", "contiguous", "dynamic"), default=None,
+                    help="with the profiling modes: pin every pass to this centre order (default budgets and "
+                         "grid), as the autotuner's choice would set it, without the autotuner's launches")
     ap.add_argument("--moment-mma", action="store_true",
                     help="with --profile-only / --profile-effect: edge->moment sums on the tensor cores (3xTF32)")
     ap.add_argument("--skip-config5", action="store_true",

@@ -128,6 +128,13 @@ int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
  * the autotuner chooses between the two).  The same arithmetic as the fused pass: results are
  * bitwise identical.  No counterpart in the reference (a launch-shape choice). */
 int sus2g_engine_set_static_split(sus2g_engine engine, int enabled);
+/* The outer and gate reverse parameter-gradient passes (sus2g_engine_combination_grad and the
+ * trainer) as two kernels each -- the per-atom part (forward with tangents, readout seeds, reverse
+ * sweep) writing the moment adjoints, then the per-edge parameter contributions -- instead of one
+ * (enabled = 1, the default; basis size 8).  The per-warp gradient slices then receive their terms
+ * in another order: results agree to the rounding of the precision and repeat bit for bit.  No
+ * counterpart in the reference (a kernel-shape choice). */
+int sus2g_engine_set_grad_split(sus2g_engine engine, int enabled);
 /* Pass-kernel autotuner: on the layout of the engine's last evaluation, times every per-atom pass
  * the model runs in each tile shape -- compiled register budget (3 and 4 resident blocks per SM;
  * basis size 8), grid shape and centre order (sus2g_engine_pass_shape) -- over `reps` launches

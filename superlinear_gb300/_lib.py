@@ -41,6 +41,7 @@ SIGNATURES = {
     "sus2g_engine_set_pdl": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_set_moment_mma": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_set_static_split": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "sus2g_engine_set_grad_split": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_pass_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "sus2g_engine_set_pass_shape": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                    ctypes.c_int]),

@@ -182,6 +182,10 @@ int sus2g_engine_set_pass_shape(sus2g_engine e, int mode, int blocks, int grid, 
   });
 }
 
+int sus2g_engine_set_grad_split(sus2g_engine e, int enabled) {
+  return guarded([&] { need(e, "engine"); e->engine->set_grad_split(enabled != 0); });
+}
+
 int sus2g_engine_set_static_split(sus2g_engine e, int enabled) {
   return guarded([&] { need(e, "engine"); e->engine->set_static_split(enabled != 0); });
 }

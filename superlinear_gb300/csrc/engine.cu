@@ -2004,13 +2004,24 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
   a.sw = sw;
   a.extra_h = extra_h;
   a.error = error_.as<int>();
-  const GradLaunch co = grad_pass_config<Real>(m.L, kGradOuter, dm, ncentres_, sm_count_);
-  GradLaunch cf = co, cr = co;
+  // the outer and gate reverse passes whole, or split into their per-atom and per-edge parts
+  // (basis size 8) through the moment adjoints in gabar_
+  const bool split = grad_split_ && m.B == 8;
+  const int part1 = split ? kGradAtomPart : kGradWhole;
+  const GradLaunch co = grad_pass_config<Real>(m.L, kGradOuter, dm, ncentres_, sm_count_, part1);
+  GradLaunch co2 = co, cf = co, cr = co, cr2 = co;
+  if (split) co2 = grad_pass_config<Real>(m.L, kGradOuter, dm, ncentres_, sm_count_, kGradEdgePart);
   if (m.gated) {
     cf = grad_pass_config<Real>(m.L, kGradGateForward, dm, ncentres_, sm_count_);
-    cr = grad_pass_config<Real>(m.L, kGradGateReverse, dm, ncentres_, sm_count_);
+    cr = grad_pass_config<Real>(m.L, kGradGateReverse, dm, ncentres_, sm_count_, part1);
+    cr2 = split ? grad_pass_config<Real>(m.L, kGradGateReverse, dm, ncentres_, sm_count_, kGradEdgePart) : cr;
   }
-  const int nslots = std::max({co.grid * co.warps, cf.grid * cf.warps, cr.grid * cr.warps});
+  const int nslots = std::max({co.grid * co.warps, co2.grid * co2.warps, cf.grid * cf.warps, cr.grid * cr.warps,
+                               cr2.grid * cr2.warps});
+  if (split) {
+    gabar_.ensure(sizeof(Real) * static_cast<size_t>(std::max(1, ncentres_)) * 2 * m.K * (m.L + 1) * (m.L + 1));
+    a.abar = gabar_.as<Real>();
+  }
   slots_.ensure(sizeof(double) * static_cast<size_t>(nslots) * P);
   SUS2G_CUDA(cudaMemsetAsync(slots_.ptr, 0, sizeof(double) * static_cast<size_t>(nslots) * P, s));
   a.slots = slots_.as<double>();
@@ -2030,7 +2041,9 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
     a.lh_atom = lh_atom_.as<double>();
     launches_ += launch_grad_pass<Real>(m.L, kGradGateForward, a, cf, s);
     launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co, s);
+    if (split) launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co2, s);
     launches_ += launch_grad_pass<Real>(m.L, kGradGateReverse, a, cr, s);
+    if (split) launches_ += launch_grad_pass<Real>(m.L, kGradGateReverse, a, cr2, s);
     const int gw_off = dm.grad.gate_w_off;
     if (N && gw_off >= 0) {
       const int blocks = std::max(1, std::min(nslots, (ncentres_ + kGwChunk - 1) / kGwChunk));
@@ -2046,6 +2059,7 @@ void Engine::run_grad(const double* ew, const double* fw, const double* sw, doub
     }
   } else {
     launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co, s);
+    if (split) launches_ += launch_grad_pass<Real>(m.L, kGradOuter, a, co2, s);
   }
   slot_part_.ensure(sizeof(double) * kSlotGroups * static_cast<size_t>(P));
   k_slot_partial<<<dim3((P + 31) / 32, kSlotGroups), dim3(32, 8), 0, s>>>(slots_.as<double>(), nslots, P,

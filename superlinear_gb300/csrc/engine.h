@@ -110,6 +110,13 @@ class Engine {
     static_split_ = on;
   }
   bool static_split() const { return static_split_; }
+  // The outer and gate reverse parameter-gradient passes as two kernels each (per-atom part,
+  // per-edge part; basis size 8) instead of one; a change drops a captured step graph and makes
+  // graphs captured by other owners (a trainer) be captured again.
+  void set_grad_split(bool on) {
+    if (on != grad_split_) { reset_step_graph(); ++edge_generation_; }
+    grad_split_ = on;
+  }
   void set_moment_mma(bool on) {
     if (on != moment_mma_) reset_step_graph();
     moment_mma_ = on;
@@ -227,6 +234,8 @@ class Engine {
   template <typename Real>
   void run_grad(const double* ew, const double* fw, const double* sw, double* grad, const double* extra_h);
   DevBuf slots_, slot_part_, hsigd_, gmomd_, lhm_, lh_atom_;
+  DevBuf gabar_;                // moment adjoints between the parts of a split gradient pass
+  bool grad_split_ = true;      // gradient passes split at the per-atom boundary (basis size 8)
   void finalize_edges();
 
   Model model_;

@@ -56,6 +56,8 @@ struct GradArgs {
   double* lh_atom;         // [N][2F] gathered per atom (gate reverse)
   const double* extra_h;   // [N][F] additional dJ/dh per atom (objective terms of h), or null
   double* slots;           // [warps in grid][nparams]
+  Real* abar;              // [N][2][K][H] adjoints of the moments (values, tangents): the per-atom part
+                           // of a split pass writes them, its per-edge part reads them
   int* error;
   int acc_cols;            // lane-private accumulator columns per k (0: shuffle-tree reductions)
 };
@@ -73,6 +75,15 @@ __host__ __device__ inline int grad_warp_size(int F, int H, int M, int K, int pa
   return kWarp * (2 * F + 2 * H + 1) + 2 * (M + 1) + (grad_adj_in_stage(F, H, M) ? 0 : 2 * (M + 1)) + 2 * K * H +
          2 * F + 2 * parts + 4;
 }
+
+// Per-warp scratch of the per-edge part of a split pass: the atom's moment adjoints [2][K][H].
+__host__ __device__ inline int grad_edge_warp_size(int K, int H) { return round4(2 * K * H); }
+
+// The parts a pass can run as (GradLaunch::part): the whole pass in one kernel, or split at the
+// per-atom boundary into the per-atom part (forward with tangents, readout seeds, reverse sweep;
+// moment adjoints to GradArgs::abar) and the per-edge part (parameter contributions per edge from
+// those adjoints) -- two smaller kernels whose bodies each fit the instruction cache.
+enum GradPart : int { kGradWhole = 0, kGradAtomPart = 1, kGradEdgePart = 2 };
 
 // Accumulator columns per radial index k: Chebyshev coefficients [l][b], species factors [t][l]
 // (centre and neighbour factors index the same table), warp slope / shift [sb][t][2] (one warp
@@ -167,7 +178,8 @@ __device__ __forceinline__ void rank_weight_grad(const PassGradLayout& gl, const
 
 // (at most 128 threads per block, chosen by the launch configuration; registers capped for three
 // resident blocks, measured 2% faster on the 256-frame training step than the uncapped build)
-template <int L, typename Real, int MODE, bool KAHAN, int BF, bool COLS>
+// PART: GradPart (the gate forward pass runs whole: it has no per-edge parameter loop).
+template <int L, typename Real, int MODE, bool KAHAN, int BF, bool COLS, int PART>
 __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
   constexpr int Lp = L + 1, H = Lp * Lp;
   constexpr int NBM = BF ? BF : kMaxB;
@@ -190,7 +202,8 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
   Real* s_w1 = s_w0 + C * F;
   Real* s_wa = s_w1 + C * F;
   const int ncol = COLS ? a.acc_cols : 0;
-  Real* wbase = s_wa + C * F + (grad_warp_size<Real>(F, H, M, K, dm.prog_parts) + ncol * kAccStride) * warp;
+  const int wsize = PART == kGradEdgePart ? grad_edge_warp_size(K, H) : grad_warp_size<Real>(F, H, M, K, dm.prog_parts);
+  Real* wbase = s_wa + C * F + (wsize + ncol * kAccStride) * warp;
   const int sw = 2 * F + 2 * H + 1;
   Real* stage = wbase;
   Real* v = stage + kWarp * sw;    // [M + 1], v[M] = 1
@@ -198,11 +211,11 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
   const bool adj_staged = grad_adj_in_stage(F, H, M);
   Real* lam = adj_staged ? stage : vd + M + 1;
   Real* mu = lam + M + 1;
-  Real* abl = vd + M + 1 + (adj_staged ? 0 : 2 * (M + 1));
+  Real* abl = PART == kGradEdgePart ? wbase : vd + M + 1 + (adj_staged ? 0 : 2 * (M + 1));
   Real* abm = abl + K * H;
   Real* hb = abm + K * H;  // [2F]
   Real* parts = hb + 2 * F;  // [2 prog_parts]
-  Real* accs = wbase + grad_warp_size<Real>(F, H, M, K, dm.prog_parts);  // [ncol][kAccStride]
+  Real* accs = wbase + wsize;  // [ncol][kAccStride]
   const int nsb = grad_acc_nsb(dm.scaling_mode, Lp);
   const int c_wc = Lp * B, c_scal = c_wc + C * Lp, c_add = c_scal + 2 * nsb * C;
 
@@ -263,6 +276,12 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
         for (int h = 1; h < H; ++h) { Y[h] = Real(0); Yd[h] = Real(0); }
     };
 
+    if constexpr (PART == kGradEdgePart) {
+      // ---------------- the atom's moment adjoints from the per-atom part ----------------
+      const Real* src = a.abar + static_cast<size_t>(atom) * 2 * K * H;
+      for (int t = lane; t < 2 * K * H; t += kWarp) abl[t] = src[t];
+      __syncwarp();
+    } else {
     if (MODE != kGradGateReverse) {
       // ---------------- forward with tangents ----------------
       Real acc[kMaxItems], cmp[kMaxItems], accd[kMaxItems], cmpd[kMaxItems];
@@ -409,12 +428,23 @@ __global__ void __launch_bounds__(128, 3) grad_pass_kernel(GradArgs<Real> a) {
         run_prog_dual<Real, 2>(pt.prog, last, pt.prog.nsteps, v, vd, lam, mu, parts, lane);
       }
     }
+    if constexpr (PART == kGradAtomPart) {
+      Real* dst = a.abar + static_cast<size_t>(atom) * 2 * K * H;
+      for (int t = lane; t < K * H; t += kWarp) {
+        const int b = dm.basic_of[t];
+        dst[t] = b >= 0 ? lam[b] : Real(0);
+        dst[K * H + t] = b >= 0 ? mu[b] : Real(0);
+      }
+      __syncwarp();
+      continue;
+    }
     for (int t = lane; t < K * H; t += kWarp) {
       const int b = dm.basic_of[t];
       abl[t] = b >= 0 ? lam[b] : Real(0);
       abm[t] = b >= 0 ? mu[b] : Real(0);
     }
     __syncwarp();
+    }  // PART != kGradEdgePart
 
     // ---------------- per-edge parameter contributions ----------------
     for (int base = e0; base < e1; base += kWarp) {

@@ -23,14 +23,14 @@ int launch_atom_pass(int L, int mode, const PassArgs<Real>& a, int sm_count, cud
 }
 
 template <typename Real>
-GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count) {
+GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count, int part) {
   switch (L) {
-    case 0: return grad_pass_config_l<Real, 0>(mode, dm, natoms, sm_count);
-    case 1: return grad_pass_config_l<Real, 1>(mode, dm, natoms, sm_count);
-    case 2: return grad_pass_config_l<Real, 2>(mode, dm, natoms, sm_count);
-    case 3: return grad_pass_config_l<Real, 3>(mode, dm, natoms, sm_count);
-    case 4: return grad_pass_config_l<Real, 4>(mode, dm, natoms, sm_count);
-    case 5: return grad_pass_config_l<Real, 5>(mode, dm, natoms, sm_count);
+    case 0: return grad_pass_config_l<Real, 0>(mode, dm, natoms, sm_count, part);
+    case 1: return grad_pass_config_l<Real, 1>(mode, dm, natoms, sm_count, part);
+    case 2: return grad_pass_config_l<Real, 2>(mode, dm, natoms, sm_count, part);
+    case 3: return grad_pass_config_l<Real, 3>(mode, dm, natoms, sm_count, part);
+    case 4: return grad_pass_config_l<Real, 4>(mode, dm, natoms, sm_count, part);
+    case 5: return grad_pass_config_l<Real, 5>(mode, dm, natoms, sm_count, part);
   }
   throw std::runtime_error("sh_l_max above 5 is not supported");
 }
@@ -94,8 +94,8 @@ template int launch_atom_graph<float>(const PassArgs<float>&, int, cudaStream_t)
 template int launch_atom_graph<double>(const PassArgs<double>&, int, cudaStream_t);
 template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t, int, bool);
 template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t, int, bool);
-template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int);
-template GradLaunch grad_pass_config<double>(int, int, const DevModel<double>&, int, int);
+template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int, int);
+template GradLaunch grad_pass_config<double>(int, int, const DevModel<double>&, int, int, int);
 template int launch_grad_pass<float>(int, int, const GradArgs<float>&, const GradLaunch&, cudaStream_t);
 template int launch_grad_pass<double>(int, int, const GradArgs<double>&, const GradLaunch&, cudaStream_t);
 template cudaError_t upload_pass_constants<float>();

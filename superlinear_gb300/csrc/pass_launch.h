@@ -10,12 +10,14 @@ namespace sus2g {
 struct GradLaunch {
   int grid = 0, block = 0, warps = 0;
   int acc_cols = 0;  // lane-private accumulator columns (0: shuffle-tree reductions)
+  int part = 0;      // GradPart: the whole pass, or its per-atom or per-edge part
   size_t smem = 0;
 };
 
-// Launch shape of grad_pass_kernel<L, Real, mode> (grid sized from occupancy x SM count).
+// Launch shape of grad_pass_kernel<L, Real, mode> or of one part of it (GradPart; grid sized from
+// occupancy x SM count).
 template <typename Real>
-GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count);
+GradLaunch grad_pass_config(int L, int mode, const DevModel<Real>& dm, int natoms, int sm_count, int part = 0);
 // Launches it with that shape (a.slots must hold cfg.grid * cfg.warps slices).
 template <typename Real>
 int launch_grad_pass(int L, int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t stream);
@@ -45,7 +47,7 @@ int launch_atom_pass_l(int mode, const PassArgs<Real>& a, int sm_count, cudaStre
 template <typename Real, int L>
 cudaError_t upload_pass_constants_l();
 template <typename Real, int L>
-GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, int sm_count);
+GradLaunch grad_pass_config_l(int mode, const DevModel<Real>& dm, int natoms, int sm_count, int part);
 template <typename Real, int L>
 int launch_grad_pass_l(int mode, const GradArgs<Real>& a, const GradLaunch& cfg, cudaStream_t s);
 template <typename Real, int L>

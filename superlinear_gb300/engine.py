@@ -180,6 +180,11 @@ class Engine:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
         check(load().sus2g_engine_set_step_graph(self._h, 1 if on else 0))
 
+    def set_grad_split(self, on: bool) -> None:
+        """The outer / gate reverse parameter-gradient passes as per-atom + per-edge kernels
+        (default on; basis size 8)."""
+        check(load().sus2g_engine_set_grad_split(self._h, 1 if on else 0))
+
     def set_static_split(self, on: bool) -> None:
         """FP32 Static engines: the per-atom pass as forward / per-atom graph / adjoint kernels."""
         check(load().sus2g_engine_set_static_split(self._h, 1 if on else 0))
