@@ -264,6 +264,23 @@ __device__ __forceinline__ double warp_csum(float hi, float lo) {
   return double(hi) + double(lo);
 }
 
+// p[0] + p[stride] + ... + p[(n - 1) stride], added in that order, with eight loads in flight
+// ahead of the adds (a column of a row-major per-edge array, summed over one centre's edges).
+template <typename Real>
+__device__ __forceinline__ Real column_sum(const Real* p, size_t stride, int n) {
+  Real s = Real(0);
+  int i = 0;
+  for (; i + 8 <= n; i += 8) {
+    Real x[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) x[q] = p[static_cast<size_t>(i + q) * stride];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s += x[q];
+  }
+  for (; i < n; ++i) s += p[static_cast<size_t>(i) * stride];
+  return s;
+}
+
 // Warp index of the scaling block for radial function (k, l) (sus2_sl_kernel.cpp:198).
 __device__ __forceinline__ int scaling_block(int mode, int k, int l, int Lp) {
   return mode == 2 ? k : (mode == 1 ? l : (mode == 0 ? 0 : k * Lp + l));

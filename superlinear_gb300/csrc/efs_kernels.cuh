@@ -654,9 +654,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         if (a.hbar_atom) {
           hbar[mu] = Real(a.hbar_atom[(size_t)atom * F + mu]);
         } else {
-          Real s = Real(0);
-          for (int e = e0; e < e1; ++e) s += a.hcontrib[(size_t)e * F + mu];
-          hbar[mu] = s;
+          hbar[mu] = column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
         }
       }
       for (int q = lane; q <= M; q += kWarp) {

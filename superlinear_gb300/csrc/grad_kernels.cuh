@@ -391,8 +391,7 @@ __global__ void __launch_bounds__(128, PART == kGradWhole ? 3 : 4) grad_pass_ker
     } else {
       // ---------------- gate reverse seeds from dJ/dh, dJ/dhdot ----------------
       for (int m_ = lane; m_ < 2 * F; m_ += kWarp) {
-        Real s = Real(0);
-        for (int e = e0; e < e1; ++e) s += a.lhm[static_cast<size_t>(e) * 2 * F + m_];
+        const Real s = column_sum<Real>(a.lhm + static_cast<size_t>(e0) * 2 * F + m_, 2 * F, e1 - e0);
         double sd = double(s);
         if (a.extra_h && m_ < F) sd += a.extra_h[static_cast<size_t>(atom) * F + m_];
         hb[m_] = Real(sd);
