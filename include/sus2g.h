@@ -122,11 +122,13 @@ int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
  * (interfaces/lammps/ML-SUS2/sus2_sl_kernel.cpp:340-354); kept as an option because the CUDA-core
  * form measured faster on GB300. */
 int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
-/* FP32 engines, Static models with basis size 8: run the per-atom pass as three kernels -- the
- * edge->moment forward, the per-atom contraction / graph / readout / adjoint, and the per-edge
- * adjoint -- through device moment arrays, instead of one fused kernel (enabled = 1; default 0;
- * the autotuner chooses between the two).  The same arithmetic as the fused pass: results are
- * bitwise identical.  No counterpart in the reference (a launch-shape choice). */
+/* FP32 engines, models with basis size 8: run the energy pass (the Static pass, or the Effect
+ * outer pass) as three kernels -- the edge->moment forward, the per-atom contraction / graph /
+ * readout / adjoint, and the per-edge adjoint -- through device moment arrays, instead of one
+ * fused kernel (enabled = 1; default 0; the autotuner chooses between the two).  The same
+ * arithmetic in the same order as the fused pass, in separately compiled kernels: results agree
+ * to FP32 rounding (bit for bit on the Static models tested).  No counterpart in the reference (a
+ * launch-shape choice). */
 int sus2g_engine_set_static_split(sus2g_engine engine, int enabled);
 /* The outer and gate reverse parameter-gradient passes (sus2g_engine_combination_grad and the
  * trainer) as two kernels each -- the per-atom part (forward with tangents, readout seeds, reverse
@@ -146,7 +148,8 @@ int sus2g_engine_set_grad_split(sus2g_engine engine, int enabled);
  * milliseconds per launch of the budget's fastest shape. */
 int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* ms8);
 /* Tile shape of a per-atom pass (mode 0 Static, 1 gate forward, 2 outer, 3 gate reverse) as the
- * autotuner left it: shape4 = {register budget in resident blocks per SM (0 = default), grid
+ * autotuner left it: shape4 = {register budget in resident blocks per SM (0 = default; for a
+ * split pass, that of its per-edge kernels, which the autotuner tunes separately), grid
  * (0 all resident blocks, 1 the fewest blocks with the same centres per warp), centre order
  * (0 grid-strided, 1 contiguous runs per warp, 2 taken from a device counter as warps finish;
  * plus 4 when the Static pass runs as three kernels, sus2g_engine_set_static_split; plus 8 when

@@ -37,7 +37,10 @@ enum PassMode : int {
   kModeStaticFwd = 4, kModeStaticRev = 5,
   // the Effect outer pass compiled with the neighbours' gate-signal rows h_j brought into shared
   // memory by 1-D bulk async copies, one 32-edge batch ahead (a kernel variant of kModeOuter)
-  kModeOuterBulk = 6
+  kModeOuterBulk = 6,
+  // the Effect outer pass split like the Static pass (forward with h_j, per-atom graph kernel,
+  // adjoint writing the hbar contributions)
+  kModeOuterFwd = 7, kModeOuterRev = 8
 };
 
 template <typename Real>
@@ -452,7 +455,11 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   }
   __syncthreads();
   pdl_wait();
-  const bool effect_outer = MODE == kModeOuter || MODE == kModeOuterBulk;
+  const bool effect_outer = MODE == kModeOuter || MODE == kModeOuterBulk || MODE == kModeOuterFwd || MODE == kModeOuterRev;
+  // the two per-edge kernels of a split pass: forward only (moments out), adjoint only (moment
+  // adjoints in)
+  constexpr bool kFwdOnly = MODE == kModeStaticFwd || MODE == kModeOuterFwd;
+  constexpr bool kRevOnly = MODE == kModeStaticRev || MODE == kModeOuterRev;
   // the h_j copies of a batch: lane 0 orders the warp's reads of hbuf before the async writes and
   // announces the bytes, every lane with an edge copies its row; the caller has synchronised the
   // warp after its last reads of hbuf
@@ -525,9 +532,9 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     EdgeIn<Real> cur{};
     const int nbat = (e1 - e0 + kWarp - 1) / kWarp;
     // the gate reverse pass starts with the per-atom work: its first edge batch loads meanwhile
-    if ((MODE == kModeGateReverse || MODE == kModeStaticRev) && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
+    if ((MODE == kModeGateReverse || kRevOnly) && nbat > 0 && e0 + (nbat - 1) * kWarp + lane < e1)
       cur = load_edge<Real>(a.d4, a.nbr, a.types, e0 + (nbat - 1) * kWarp + lane, C);
-    if (MODE == kModeStaticRev) {
+    if (kRevOnly) {
       // ---------------- split pass, per-edge part: adjoint moments from the graph kernel ----------
       for (int t = lane; t < K * H; t += kWarp) abar[t] = a.amom[static_cast<size_t>(atom) * (K * H) + t];
       __syncwarp();
@@ -612,7 +619,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         __syncwarp();
         if (more) cur = nxt;
       }
-      if (MODE == kModeStaticFwd) {
+      if (kFwdOnly) {
         // split pass, forward part: the moments go to the graph kernel
 #pragma unroll
         for (int s = 0; s < kMaxItems; ++s) {
@@ -671,7 +678,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
 
     // ---------------- reverse graph and contraction ----------------
-    if (MODE != kModeStaticRev) {
+    if (!kRevOnly) {
       run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
       for (int t = lane; t < K * H; t += kWarp) {
         const int b = dm.basic_of[t];

@@ -1824,7 +1824,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) wait_reverse();  // the outer pass writes the gate-signal adjoints at reverse edges
     mark_begin(1);
     const int mode = m.gated ? kModeOuter : kModeStatic;
-    if (!m.gated && use_static_split<Real>()) launches_ += launch_static_split<Real>(a, (pdl_ & kPdlFirstPass) != 0);
+    if (use_static_split<Real>())
+      launches_ += launch_static_split<Real>(a, (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
     else launches_ += launch_pass<Real>(mode, a, (pdl_ & (m.gated ? kPdlBetweenPasses : kPdlFirstPass)) != 0);
     mark_end();
     if (m.gated && user_edges_) {
@@ -2115,12 +2116,13 @@ void Engine::efs(double* d_energy, double* d_forces, double* d_virial, double* d
   else run_efs<double>(d_energy, d_forces, d_virial, d_site, kStageAll);
 }
 
-// The Static pass split at the per-atom boundary (FP32 engines, basis size 8): edge->moment
-// forward, per-atom graph kernel, per-edge adjoint -- three launches through device moment
-// arrays; the forward and adjoint kernels take the Static pass's tile shape.
+// The energy pass (Static, or the Effect outer pass) split at the per-atom boundary (FP32
+// engines, basis size 8): edge->moment forward, per-atom graph kernel, per-edge adjoint -- three
+// launches through device moment arrays; the forward and adjoint kernels take the fused pass's
+// tile shape.
 template <typename Real>
 bool Engine::use_static_split() const {
-  return static_split_ && sizeof(Real) == 4 && model_.B == 8 && !model_.gated;
+  return static_split_ && sizeof(Real) == 4 && model_.B == 8;
 }
 template <typename Real>
 int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
@@ -2129,11 +2131,12 @@ int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
   amom_.ensure(sizeof(Real) * n);
   a.mom = mom_.as<Real>();
   a.amom = amom_.as<Real>();
-  a.grid_mode = pass_grid_[kModeStatic];
-  a.atom_order = pass_order_[kModeStatic];
-  int k = launch_shape<Real>(kModeStaticFwd, a, pass_blocks_[kModeStatic], pdl);
+  const int mode = model_.gated ? kModeOuter : kModeStatic;
+  a.grid_mode = pass_grid_[mode];
+  a.atom_order = pass_order_[mode];
+  int k = launch_shape<Real>(model_.gated ? kModeOuterFwd : kModeStaticFwd, a, split_blocks_, pdl);
   k += launch_atom_graph<Real>(a, sm_count_, stream_);
-  k += launch_shape<Real>(kModeStaticRev, a, pass_blocks_[kModeStatic], false);
+  k += launch_shape<Real>(model_.gated ? kModeOuterRev : kModeStaticRev, a, split_blocks_, false);
   return k;
 }
 
@@ -2151,7 +2154,7 @@ int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
 template <typename Real>
 int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
   if (a.atom_order == 2) {
-    work_.ensure(sizeof(int) * 8);
+    work_.ensure(sizeof(int) * 16);  // one counter per pass mode (PassMode values < 16)
     a.work = work_.as<int>() + mode;
     SUS2G_CUDA(cudaMemsetAsync(a.work, 0, sizeof(int), stream_));
     pdl = false;  // the memset sits between this launch and its predecessor
@@ -2217,17 +2220,26 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
     pass_order_[mode] = choice_order;
     pass_stage_[mode] = choice_stage;
     blocks_out[mode] = choice;
-    if (mode == kModeStatic && sizeof(Real) == 4 && m.B == 8) {
-      // the fused Static pass against its three-kernel split, in the chosen shape
+    if ((mode == kModeStatic || mode == kModeOuter) && sizeof(Real) == 4 && m.B == 8) {
+      // the fused energy pass (Static, or Effect outer) against its three-kernel split, in the
+      // chosen grid and centre order, the split kernels with either register budget
       static_split_ = true;
-      launch_static_split<Real>(a, false);
-      SUS2G_CUDA(cudaEventRecord(e0, s));
-      for (int r = 0; r < reps; ++r) launch_static_split<Real>(a, false);
-      SUS2G_CUDA(cudaEventRecord(e1, s));
-      SUS2G_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      static_split_ = double(ms) / std::max(1, reps) < best;
+      double split_best = 0.0;
+      int split_choice = 0;
+      for (int blocks = 3; blocks <= 4; ++blocks) {
+        split_blocks_ = blocks;
+        launch_static_split<Real>(a, false);
+        SUS2G_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) launch_static_split<Real>(a, false);
+        SUS2G_CUDA(cudaEventRecord(e1, s));
+        SUS2G_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        const double per = double(ms) / std::max(1, reps);
+        if (split_choice == 0 || per < split_best) { split_best = per; split_choice = blocks; }
+      }
+      split_blocks_ = split_choice;
+      static_split_ = split_best < best;
     }
   }
   event_next_ = 0;

@@ -91,7 +91,9 @@ class Engine {
   // as three kernels) + 8 x h_j staging by bulk async copies, warps per block
   void pass_shape(int mode, int* shape4) const {
     shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode];
-    shape4[2] = pass_order_[mode] + (mode == 0 && static_split_ ? 4 : 0) + (pass_stage_[mode] ? 8 : 0);
+    const bool split = static_split_ && mode == (model_.gated ? 2 : 0);
+    if (split) shape4[0] = split_blocks_;
+    shape4[2] = pass_order_[mode] + (split ? 4 : 0) + (pass_stage_[mode] ? 8 : 0);
     shape4[3] = 4;
   }
   // sets the tile shape of pass `mode` as the autotuner would (blocks 0 = default, 3 or 4; grid 0
@@ -102,9 +104,9 @@ class Engine {
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
   // drops a captured step graph.
-  // The Static pass as three kernels (edge->moment forward, per-atom graph, per-edge adjoint)
-  // instead of one (FP32 engines, basis size 8; the autotuner also chooses it); a change drops a
-  // captured step graph.
+  // The energy pass -- Static, or the Effect outer pass -- as three kernels (edge->moment forward,
+  // per-atom graph, per-edge adjoint) instead of one (FP32 engines, basis size 8; the autotuner
+  // also chooses it); a change drops a captured step graph.
   void set_static_split(bool on) {
     if (on != static_split_) reset_step_graph();
     static_split_ = on;
@@ -296,10 +298,11 @@ class Engine {
   int pass_stage_[4] = {0, 0, 0, 0};   // h_j staging per pass mode (PassArgs::h_bulk; outer pass)
   template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
   template <typename Real> int launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl);
-  DevBuf work_;                 // centre counters of the dynamic centre order, one per pass mode
+  DevBuf work_;                 // centre counters of the dynamic centre order, one per pass mode (16)
   template <typename Real> bool use_static_split() const;
   template <typename Real> int launch_static_split(PassArgs<Real> a, bool pdl);
-  bool static_split_ = false;   // Static pass as forward / per-atom graph / adjoint kernels
+  bool static_split_ = false;   // energy pass as forward / per-atom graph / adjoint kernels
+  int split_blocks_ = 0;        // register budget of the split's per-edge kernels (0 = default)
   DevBuf mom_, amom_;           // the split pass's moments and adjoint moments [N][K H]
   // second stream for independent work inside a step (reverse edges beside the first pass, the
   // frame reduction beside the force gather)

@@ -73,11 +73,17 @@ int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cud
     case kModeGateReverse: return launch_budget<Real, L, kModeGateReverse, BF>(blocks, a, sm_count, s, pdl);
     case kModeStaticFwd:
     case kModeStaticRev:
-      if constexpr (sizeof(Real) == 4) {
-        return mode == kModeStaticFwd ? launch_budget<Real, L, kModeStaticFwd, BF>(blocks, a, sm_count, s, pdl)
-                                      : launch_budget<Real, L, kModeStaticRev, BF>(blocks, a, sm_count, s, pdl);
+    case kModeOuterFwd:
+    case kModeOuterRev:
+      if constexpr (sizeof(Real) == 4 && BF == 8) {
+        switch (mode) {
+          case kModeStaticFwd: return launch_budget<Real, L, kModeStaticFwd, BF>(blocks, a, sm_count, s, pdl);
+          case kModeStaticRev: return launch_budget<Real, L, kModeStaticRev, BF>(blocks, a, sm_count, s, pdl);
+          case kModeOuterFwd: return launch_budget<Real, L, kModeOuterFwd, BF>(blocks, a, sm_count, s, pdl);
+          default: return launch_budget<Real, L, kModeOuterRev, BF>(blocks, a, sm_count, s, pdl);
+        }
       } else {
-        throw std::runtime_error("the split Static pass is compiled for FP32 engines only");
+        throw std::runtime_error("the split passes are compiled for FP32 engines with basis size 8 only");
       }
   }
   throw std::runtime_error("unknown pass mode");
