@@ -124,8 +124,11 @@ int sus2g_engine_set_pdl(sus2g_engine engine, int sites);
 int sus2g_engine_set_moment_mma(sus2g_engine engine, int enabled);
 /* FP32 engines, models with basis size 8: run the energy pass (the Static pass, or the Effect
  * outer pass) as three kernels -- the edge->moment forward, the per-atom contraction / graph /
- * readout / adjoint, and the per-edge adjoint -- through device moment arrays, instead of one
- * fused kernel (enabled = 1; default 0; the autotuner chooses between the two).  The same
+ * readout / adjoint, and the per-edge adjoint -- through device moment arrays, and the Effect
+ * gate passes as two each (edge->moment forward, then the per-atom gate graph and gate-signal
+ * projection; the per-atom gate-signal adjoint gather and gate graph reverse, then the per-edge
+ * adjoint), instead of one fused kernel per pass (enabled = 1; default 0; the autotuner chooses
+ * per pass).  The same
  * arithmetic in the same order as the fused pass, in separately compiled kernels: results agree
  * to FP32 rounding (bit for bit on the Static models tested).  No counterpart in the reference (a
  * launch-shape choice). */

@@ -40,7 +40,12 @@ enum PassMode : int {
   kModeOuterBulk = 6,
   // the Effect outer pass split like the Static pass (forward with h_j, per-atom graph kernel,
   // adjoint writing the hbar contributions)
-  kModeOuterFwd = 7, kModeOuterRev = 8
+  kModeOuterFwd = 7, kModeOuterRev = 8,
+  // the Effect gate passes split the same way: the gate forward pass's edge->moment part (the
+  // per-atom gate graph and gate-signal projection then run in atom_graph_kernel), and the gate
+  // reverse pass's per-edge adjoint (after atom_graph_kernel gathered the gate-signal adjoint and
+  // ran the gate graph's reverse)
+  kModeGateFwdEdges = 9, kModeGateRevEdges = 10
 };
 
 template <typename Real>
@@ -412,7 +417,10 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   constexpr int kMaxItems = (kMaxK * H + kWarp - 1) / kWarp;
   using V4 = typename Vec4<Real>::type;
   const DevModel<Real>& dm = a.dm;
-  const bool gate_pass = MODE == kModeGateForward || MODE == kModeGateReverse;
+  const bool gate_pass = MODE == kModeGateForward || MODE == kModeGateReverse || MODE == kModeGateFwdEdges ||
+                         MODE == kModeGateRevEdges;
+  // the gate reverse pass adds its edge gradients and virials to the outer pass's
+  constexpr bool kGateRev = MODE == kModeGateReverse || MODE == kModeGateRevEdges;
   const PassTables<Real>& pt = gate_pass ? dm.gate : dm.outer;
   const int C = dm.C, F = dm.F, B = BF ? BF : dm.B, K = dm.K, M = dm.M, NB = dm.NB;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
@@ -458,8 +466,8 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   const bool effect_outer = MODE == kModeOuter || MODE == kModeOuterBulk || MODE == kModeOuterFwd || MODE == kModeOuterRev;
   // the two per-edge kernels of a split pass: forward only (moments out), adjoint only (moment
   // adjoints in)
-  constexpr bool kFwdOnly = MODE == kModeStaticFwd || MODE == kModeOuterFwd;
-  constexpr bool kRevOnly = MODE == kModeStaticRev || MODE == kModeOuterRev;
+  constexpr bool kFwdOnly = MODE == kModeStaticFwd || MODE == kModeOuterFwd || MODE == kModeGateFwdEdges;
+  constexpr bool kRevOnly = MODE == kModeStaticRev || MODE == kModeOuterRev || MODE == kModeGateRevEdges;
   // the h_j copies of a batch: lane 0 orders the warp's reads of hbuf before the async writes and
   // announces the bytes, every lane with an edge copies its row; the caller has synchronised the
   // warp after its last reads of hbuf
@@ -761,7 +769,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
       const Real Gy = uy * s + (gy - uy * ug) * ir;
       const Real Gz = uz * s + (gz - uz * ug) * ir;
       Real* ge = a.g + (size_t)e * 3;
-      if (MODE == kModeGateReverse) {
+      if (kGateRev) {
         ge[0] += Gx; ge[1] += Gy; ge[2] += Gz;
       } else {
         ge[0] = Gx; ge[1] = Gy; ge[2] = Gz;
@@ -788,12 +796,12 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
         if (lane == c) { h = vhi[c]; l = vlo[c]; }
       }
       const double vc = double(h) + double(l);
-      if (lane < 6) vo[lane] = MODE == kModeGateReverse ? vo[lane] + vc : vc;
+      if (lane < 6) vo[lane] = kGateRev ? vo[lane] + vc : vc;
     } else {
 #pragma unroll
       for (int c = 0; c < 6; ++c) vir[c] = warp_sum(vir[c]);
       if (lane == 0) {
-        if (MODE == kModeGateReverse)
+        if (kGateRev)
           for (int c = 0; c < 6; ++c) vo[c] += vir[c];
         else
           for (int c = 0; c < 6; ++c) vo[c] = vir[c];
@@ -810,31 +818,67 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
 // program's load latency that the fused pass serialises between its edge phases.
 // ---------------------------------------------------------------------------------------------
 constexpr int kGraphWarps = 4;
-__host__ __device__ inline int graph_warp_size(int M, int parts) { return round4(2 * (M + 1) + parts + 4); }
+__host__ __device__ inline int graph_warp_size(int M, int parts, int F) { return round4(2 * (M + 1) + parts + F + 4); }
 
-template <typename Real>
+// GM: 0 the energy pass (Static or Effect outer tables: readout, adjoint moments to a.amom);
+// 1 the gate forward pass (gate tables: gate values to a.gmom, gate signals to a.hsig);
+// 2 the gate reverse pass (the gate-signal adjoint gathered per atom, projected onto the gate
+// nodes, the gate graph's reverse, adjoint moments to a.amom).
+
+template <typename Real, int GM>
 __global__ void __launch_bounds__(kGraphWarps * kWarp) atom_graph_kernel(PassArgs<Real> a) {
   const DevModel<Real>& dm = a.dm;
-  const PassTables<Real>& pt = dm.outer;
-  const int M = dm.M, KH = dm.K * dm.H, C = dm.C;
+  const PassTables<Real>& pt = GM == 0 ? dm.outer : dm.gate;
+  const int M = dm.M, KH = dm.K * dm.H, C = dm.C, F = dm.F;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Real* v = reinterpret_cast<Real*>(smem_raw) + graph_warp_size(M, dm.prog_parts) * warp;
+  Real* v = reinterpret_cast<Real*>(smem_raw) + graph_warp_size(M, dm.prog_parts, F) * warp;
   Real* adj = v + M + 1;
   Real* parts = adj + M + 1;
+  Real* hbar = parts + dm.prog_parts;  // [F] (GM 2)
   pdl_launch_dependents();
   pdl_wait();
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
     const int ti = C == 1 ? 0 : species_of(a.types, atom, C);
-    for (int q = lane; q <= M; q += kWarp) v[q] = q < M ? Real(0) : Real(1);
-    __syncwarp();
-    for (int t = lane; t < KH; t += kWarp) {
-      const int b = dm.basic_of[t];
-      if (b >= 0) v[b] = a.mom[static_cast<size_t>(atom) * KH + t];
+    if constexpr (GM == 2) {
+      // the gate-signal adjoint of the atom: summed over its edges' contributions (stored at the
+      // reverse edges by the outer pass), or already summed per atom (caller edges)
+      const int e0 = a.row[atom], e1 = a.row_end[atom];
+      for (int mu = lane; mu < F; mu += kWarp)
+        hbar[mu] = a.hbar_atom ? Real(a.hbar_atom[(size_t)atom * F + mu])
+                               : column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
+      for (int q = lane; q <= M; q += kWarp) {
+        v[q] = q < M ? a.gmom[(size_t)atom * M + q] : Real(1);
+        adj[q] = Real(0);
+      }
+      __syncwarp();
+      for (int q = lane; q < dm.Q; q += kWarp) {
+        Real s = Real(0);
+        for (int mu = 0; mu < F; ++mu) s += hbar[mu] * dm.gate_wmat[mu * dm.Q + q];
+        adj[dm.gate_nodes[q]] += s;
+      }
+      __syncwarp();
+    } else {
+      for (int q = lane; q <= M; q += kWarp) v[q] = q < M ? Real(0) : Real(1);
+      __syncwarp();
+      for (int t = lane; t < KH; t += kWarp) {
+        const int b = dm.basic_of[t];
+        if (b >= 0) v[b] = a.mom[static_cast<size_t>(atom) * KH + t];
+      }
+      __syncwarp();
+      run_prog<Real, 1>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
     }
-    __syncwarp();
-    run_prog<Real, 1>(pt.prog, 0, pt.prog.nfwd, v, adj, parts, lane);
-    readout_seeds<Real>(a, atom, ti, v, adj, lane);
+    if constexpr (GM == 1) {
+      for (int q = lane; q < M; q += kWarp) a.gmom[(size_t)atom * M + q] = v[q];
+      for (int mu = lane; mu < F; mu += kWarp) {
+        Real h = Real(0);
+        for (int q = 0; q < dm.Q; ++q) h += dm.gate_wmat[mu * dm.Q + q] * v[dm.gate_nodes[q]];
+        a.hsig[(size_t)atom * F + mu] = h;
+      }
+      __syncwarp();
+      continue;
+    }
+    if constexpr (GM == 0) readout_seeds<Real>(a, atom, ti, v, adj, lane);
     run_prog<Real, 2>(pt.prog, pt.prog.nfwd, pt.prog.nsteps, v, adj, parts, lane);
     for (int t = lane; t < KH; t += kWarp) {
       const int b = dm.basic_of[t];

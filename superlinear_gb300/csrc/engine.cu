@@ -1815,7 +1815,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
       if (ghosts)
         SUS2G_CUDA(cudaMemsetAsync(hsig_.ptr, 0, sizeof(Real) * static_cast<size_t>(std::max(1, N)) * m.F, s));
       mark_begin(2);
-      launches_ += launch_pass<Real>(kModeGateForward, a, (pdl_ & kPdlFirstPass) != 0);
+      if (use_gate_split<Real>(0)) launches_ += launch_gate_split<Real>(0, a, (pdl_ & kPdlFirstPass) != 0);
+      else launches_ += launch_pass<Real>(kModeGateForward, a, (pdl_ & kPdlFirstPass) != 0);
       mark_end();
     }
   }
@@ -1843,7 +1844,8 @@ void Engine::run_efs(double* d_energy, double* d_forces, double* d_virial, doubl
     if (m.gated) {
       if (user_edges_) a.hbar_atom = hbar_atom_.as<double>();
       mark_begin(3);
-      launches_ += launch_pass<Real>(kModeGateReverse, a, (pdl_ & kPdlBetweenPasses) != 0);
+      if (use_gate_split<Real>(1)) launches_ += launch_gate_split<Real>(1, a, (pdl_ & kPdlBetweenPasses) != 0);
+      else launches_ += launch_pass<Real>(kModeGateReverse, a, (pdl_ & kPdlBetweenPasses) != 0);
       mark_end();
     }
     wait_reverse();
@@ -2140,6 +2142,36 @@ int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
   return k;
 }
 
+// The Effect gate passes split at the per-atom boundary (FP32 engines, basis size 8): which 0 =
+// the gate forward pass (edge->moment kernel, then the per-atom gate graph and gate-signal
+// projection), 1 = the gate reverse pass (per-atom gather / projection / gate graph reverse,
+// then the per-edge adjoint); the per-edge kernels take the fused pass's grid and centre order
+// and their own register budget.
+template <typename Real>
+bool Engine::use_gate_split(int which) const {
+  return gate_split_[which] && sizeof(Real) == 4 && model_.B == 8 && model_.gated;
+}
+template <typename Real>
+int Engine::launch_gate_split(int which, PassArgs<Real> a, bool pdl) {
+  const size_t n = static_cast<size_t>(std::max(1, ncentres_)) * model_.K * model_.H;
+  const int mode = which == 0 ? kModeGateForward : kModeGateReverse;
+  a.grid_mode = pass_grid_[mode];
+  a.atom_order = pass_order_[mode];
+  int k = 0;
+  if (which == 0) {
+    mom_.ensure(sizeof(Real) * n);
+    a.mom = mom_.as<Real>();
+    k += launch_shape<Real>(kModeGateFwdEdges, a, gate_split_blocks_[0], pdl);
+    k += launch_atom_graph<Real>(a, sm_count_, stream_, 1);
+  } else {
+    amom_.ensure(sizeof(Real) * n);
+    a.amom = amom_.as<Real>();
+    k += launch_atom_graph<Real>(a, sm_count_, stream_, 2);
+    k += launch_shape<Real>(kModeGateRevEdges, a, gate_split_blocks_[1], false);
+  }
+  return k;
+}
+
 // One per-atom pass in the tile shape chosen for its mode (the defaults until autotune runs).
 template <typename Real>
 int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
@@ -2240,6 +2272,27 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
       }
       split_blocks_ = split_choice;
       static_split_ = split_best < best;
+    }
+    if ((mode == kModeGateForward || mode == kModeGateReverse) && sizeof(Real) == 4 && m.B == 8) {
+      // each gate pass against its split (per-edge kernel with either budget, per-atom kernel)
+      const int which = mode == kModeGateForward ? 0 : 1;
+      gate_split_[which] = true;
+      double split_best = 0.0;
+      int split_choice = 0;
+      for (int blocks = 3; blocks <= 4; ++blocks) {
+        gate_split_blocks_[which] = blocks;
+        launch_gate_split<Real>(which, a, false);
+        SUS2G_CUDA(cudaEventRecord(e0, s));
+        for (int r = 0; r < reps; ++r) launch_gate_split<Real>(which, a, false);
+        SUS2G_CUDA(cudaEventRecord(e1, s));
+        SUS2G_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        SUS2G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        const double per = double(ms) / std::max(1, reps);
+        if (split_choice == 0 || per < split_best) { split_best = per; split_choice = blocks; }
+      }
+      gate_split_blocks_[which] = split_choice;
+      gate_split_[which] = split_best < best;
     }
   }
   event_next_ = 0;

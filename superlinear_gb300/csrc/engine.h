@@ -91,8 +91,9 @@ class Engine {
   // as three kernels) + 8 x h_j staging by bulk async copies, warps per block
   void pass_shape(int mode, int* shape4) const {
     shape4[0] = pass_blocks_[mode]; shape4[1] = pass_grid_[mode];
-    const bool split = static_split_ && mode == (model_.gated ? 2 : 0);
-    if (split) shape4[0] = split_blocks_;
+    const bool gate_split = model_.gated && (mode == 1 || mode == 3) && gate_split_[mode == 1 ? 0 : 1];
+    const bool split = (static_split_ && mode == (model_.gated ? 2 : 0)) || gate_split;
+    if (split) shape4[0] = gate_split ? gate_split_blocks_[mode == 1 ? 0 : 1] : split_blocks_;
     shape4[2] = pass_order_[mode] + (split ? 4 : 0) + (pass_stage_[mode] ? 8 : 0);
     shape4[3] = 4;
   }
@@ -104,12 +105,13 @@ class Engine {
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
   // drops a captured step graph.
-  // The energy pass -- Static, or the Effect outer pass -- as three kernels (edge->moment forward,
-  // per-atom graph, per-edge adjoint) instead of one (FP32 engines, basis size 8; the autotuner
-  // also chooses it); a change drops a captured step graph.
+  // The per-atom passes split at the per-atom boundary instead of fused (FP32 engines, basis size
+  // 8): the energy pass -- Static, or the Effect outer pass -- as three kernels (edge->moment
+  // forward, per-atom graph, per-edge adjoint), the Effect gate passes as two each; the
+  // autotuner chooses per pass; a change drops a captured step graph.
   void set_static_split(bool on) {
-    if (on != static_split_) reset_step_graph();
-    static_split_ = on;
+    if (on != static_split_ || on != gate_split_[0] || on != gate_split_[1]) reset_step_graph();
+    static_split_ = gate_split_[0] = gate_split_[1] = on;
   }
   bool static_split() const { return static_split_; }
   // The outer and gate reverse parameter-gradient passes as two kernels each (per-atom part,
@@ -300,9 +302,13 @@ class Engine {
   template <typename Real> int launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl);
   DevBuf work_;                 // centre counters of the dynamic centre order, one per pass mode (16)
   template <typename Real> bool use_static_split() const;
+  template <typename Real> bool use_gate_split(int which) const;
+  template <typename Real> int launch_gate_split(int which, PassArgs<Real> a, bool pdl);
   template <typename Real> int launch_static_split(PassArgs<Real> a, bool pdl);
   bool static_split_ = false;   // energy pass as forward / per-atom graph / adjoint kernels
   int split_blocks_ = 0;        // register budget of the split's per-edge kernels (0 = default)
+  bool gate_split_[2] = {false, false};  // Effect gate forward / reverse passes split
+  int gate_split_blocks_[2] = {0, 0};    // their per-edge kernels' register budgets
   DevBuf mom_, amom_;           // the split pass's moments and adjoint moments [N][K H]
   // second stream for independent work inside a step (reverse edges beside the first pass, the
   // frame reduction beside the force gather)

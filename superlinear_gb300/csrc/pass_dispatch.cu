@@ -69,15 +69,17 @@ cudaError_t upload_grad_constants() {
 }
 
 template <typename Real>
-int launch_atom_graph(const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
+int launch_atom_graph(const PassArgs<Real>& a, int sm_count, cudaStream_t s, int gm) {
   if (a.natoms == 0) return 0;
-  auto kern = atom_graph_kernel<Real>;
-  const size_t smem = sizeof(Real) * kGraphWarps * static_cast<size_t>(graph_warp_size(a.dm.M, a.dm.prog_parts));
-  static size_t configured = 0;
-  if (smem > configured) {
+  if (gm < 0 || gm > 2) throw std::runtime_error("graph kernel: unknown pass");
+  auto kern = gm == 0 ? atom_graph_kernel<Real, 0> : gm == 1 ? atom_graph_kernel<Real, 1> : atom_graph_kernel<Real, 2>;
+  const size_t smem =
+      sizeof(Real) * kGraphWarps * static_cast<size_t>(graph_warp_size(a.dm.M, a.dm.prog_parts, a.dm.F));
+  static size_t configured[3] = {0, 0, 0};
+  if (smem > configured[gm]) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (err != cudaSuccess) throw std::runtime_error(std::string("graph kernel shared memory: ") + cudaGetErrorString(err));
-    configured = smem;
+    configured[gm] = smem;
   }
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kGraphWarps * kWarp, smem);
@@ -90,8 +92,8 @@ int launch_atom_graph(const PassArgs<Real>& a, int sm_count, cudaStream_t s) {
   return 1;
 }
 
-template int launch_atom_graph<float>(const PassArgs<float>&, int, cudaStream_t);
-template int launch_atom_graph<double>(const PassArgs<double>&, int, cudaStream_t);
+template int launch_atom_graph<float>(const PassArgs<float>&, int, cudaStream_t, int);
+template int launch_atom_graph<double>(const PassArgs<double>&, int, cudaStream_t, int);
 template int launch_atom_pass<float>(int, int, const PassArgs<float>&, int, cudaStream_t, int, bool);
 template int launch_atom_pass<double>(int, int, const PassArgs<double>&, int, cudaStream_t, int, bool);
 template GradLaunch grad_pass_config<float>(int, int, const DevModel<float>&, int, int, int);

@@ -75,12 +75,16 @@ int launch_mode(int mode, int blocks, const PassArgs<Real>& a, int sm_count, cud
     case kModeStaticRev:
     case kModeOuterFwd:
     case kModeOuterRev:
+    case kModeGateFwdEdges:
+    case kModeGateRevEdges:
       if constexpr (sizeof(Real) == 4 && BF == 8) {
         switch (mode) {
           case kModeStaticFwd: return launch_budget<Real, L, kModeStaticFwd, BF>(blocks, a, sm_count, s, pdl);
           case kModeStaticRev: return launch_budget<Real, L, kModeStaticRev, BF>(blocks, a, sm_count, s, pdl);
           case kModeOuterFwd: return launch_budget<Real, L, kModeOuterFwd, BF>(blocks, a, sm_count, s, pdl);
-          default: return launch_budget<Real, L, kModeOuterRev, BF>(blocks, a, sm_count, s, pdl);
+          case kModeOuterRev: return launch_budget<Real, L, kModeOuterRev, BF>(blocks, a, sm_count, s, pdl);
+          case kModeGateFwdEdges: return launch_budget<Real, L, kModeGateFwdEdges, BF>(blocks, a, sm_count, s, pdl);
+          default: return launch_budget<Real, L, kModeGateRevEdges, BF>(blocks, a, sm_count, s, pdl);
         }
       } else {
         throw std::runtime_error("the split passes are compiled for FP32 engines with basis size 8 only");

@@ -31,9 +31,10 @@ template <typename Real>
 int launch_atom_pass(int L, int mode, const PassArgs<Real>& args, int sm_count, cudaStream_t stream,
                      int blocks = 0, bool pdl = false);
 
-// The per-atom graph kernel of the split Static pass (atom_graph_kernel): returns 1 or throws.
+// The per-atom graph kernel of a split pass (atom_graph_kernel<Real, gm>: 0 energy pass, 1 gate
+// forward, 2 gate reverse): returns 1 or throws.
 template <typename Real>
-int launch_atom_graph(const PassArgs<Real>& args, int sm_count, cudaStream_t stream);
+int launch_atom_graph(const PassArgs<Real>& args, int sm_count, cudaStream_t stream, int gm = 0);
 
 // Per-translation-unit constant-table upload (spherical-harmonic normalisation) of every unit.
 template <typename Real>

@@ -542,17 +542,19 @@ def test_moment_mma_option_within_fp32_bars(lib, golden, name, cells):
 
 
 @pytest.mark.parametrize("name", ["effect_l3k4r2o2", "effect_l4k8r2o3"])
-def test_effect_outer_split_pass(lib, golden, name):
-    """The Effect outer pass as three kernels (forward with the neighbours' gate signals, per-atom
-    graph, adjoint writing the gate-signal adjoint contributions) agrees with the fused pass to
-    FP32 rounding, repeats bit for bit (also through the step graph) and keeps the FP32 bar
-    against FP64; two species, uneven neighbour counts."""
+def test_effect_split_passes(lib, golden, name):
+    """The Effect passes split at the per-atom boundary -- the outer pass as three kernels (forward
+    with the neighbours' gate signals, per-atom graph, adjoint writing the gate-signal adjoint
+    contributions), the gate forward and gate reverse passes as two each (edge->moment kernel and
+    per-atom gate graph; per-atom gather and gate graph reverse, then the per-edge adjoint) --
+    agree with the fused passes to FP32 rounding, repeat bit for bit (also through the step
+    graph) and keep the FP32 bar against FP64; two species, uneven neighbour counts."""
     path = os.path.join(golden, "models", f"{name}.sus2")
     m, g64, g32 = engines(lib, path)
     fr = diamond(5, sigma=0.2, seed=43, species=m.dims["C"])
     fused = g32.calc_efs([fr])
     g32.set_static_split(True)
-    assert g32.pass_shapes()["outer"]["split"]
+    assert all(sh["split"] for sh in g32.pass_shapes().values())
     first = g32.calc_efs([fr])
     for x, y in zip(fused, first):
         assert rel_err(x, y) < SHAPE_TOL[1]
