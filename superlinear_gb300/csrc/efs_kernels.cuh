@@ -71,9 +71,10 @@ struct PassArgs {
   int* error;
   int moment_mma;          // FP32 engines: 1 = edge->moment batch sums on the tensor cores (3xTF32 mma.sync)
   int atom_order;          // 0: warps take centres grid-strided; 1: each warp a contiguous run of
-                           // centres; 2: warps take the next centre from a device counter (*work,
-                           // zero at launch) as they finish -- dynamic balance for uneven centres
-  int* work;               // the counter of atom_order 2
+                           // centres; 2: warps take the next centre from a device counter as they
+                           // finish -- dynamic balance for uneven centres
+  int* work;               // atom_order 2: {next centre, warps done}, zero at launch; the last warp
+                           // to finish zeroes both for the next launch
   int h_bulk;              // Effect outer pass: neighbours' h_j rows staged by bulk async copies (pass_h_bulk)
   int grid_mode;           // 0: all resident blocks; 1: the fewest blocks that keep the same atoms per warp
 };
@@ -528,6 +529,17 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
   const int atom_first = dynamic ? grab() : (a.atom_order ? gwarp * per_warp : gwarp);
   const int atom_stop = a.atom_order == 1 ? min(a.natoms, atom_first + per_warp) : a.natoms;
   const int atom_step = a.atom_order == 1 ? 1 : nwarps;
+  // the dynamic order's reset: every warp counts itself done after its last take (ordered after
+  // it by the fence), and the last one zeroes the pair, when no take of this launch is pending
+  auto finish_dynamic = [&]() {
+    if (dynamic && lane == 0) {
+      __threadfence();
+      if (atomicAdd(a.work + 1, 1) == nwarps - 1) {
+        atomicExch(a.work, 0);
+        atomicExch(a.work + 1, 0);
+      }
+    }
+  };
   for (int atom = atom_first; atom < atom_stop; atom = dynamic ? grab() : atom + atom_step) {
     const int ti = C == 1 ? 0 : species_of(a.types, atom, C);
     const int e0 = a.row[atom], e1 = a.row_end[atom];
@@ -809,6 +821,7 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
     }
     __syncwarp();
   }
+  finish_dynamic();
 }
 
 // ---------------------------------------------------------------------------------------------

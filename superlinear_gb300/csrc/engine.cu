@@ -1152,6 +1152,9 @@ Engine::Engine(const Model& model, int device, int precision) : model_(model), d
   // [0] error code, [1] cell-list edge capacity overflow (largest count), [2] bin capacity overflow
   error_.ensure(3 * sizeof(int));
   SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, 3 * sizeof(int), stream_));
+  // the dynamic centre order's counters: zero now; each launch's last warp zeroes its pair again
+  work_.ensure(sizeof(int) * kWorkInts);
+  SUS2G_CUDA(cudaMemsetAsync(work_.ptr, 0, sizeof(int) * kWorkInts, stream_));
   upload_model();
 }
 
@@ -1397,6 +1400,8 @@ void Engine::check_error_read() {
   }
   if (h) {
     SUS2G_CUDA(cudaMemsetAsync(error_.ptr, 0, sizeof(int), stream_));
+    // a warp that left a pass early (a bounded wait that gave up) did not count itself done
+    SUS2G_CUDA(cudaMemsetAsync(work_.ptr, 0, sizeof(int) * kWorkInts, stream_));
     static const char* msg[] = {"", "neighbour list capacity or centre index out of range",
                                 "periodic image index outside [-64, 63]", "a directed edge has no reverse partner",
                                 "zero or non-finite edge length", "non-finite atom coordinate",
@@ -2185,12 +2190,9 @@ int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
 // takes its counter, zeroed on the stream before the launch.
 template <typename Real>
 int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
-  if (a.atom_order == 2) {
-    work_.ensure(sizeof(int) * 16);  // one counter per pass mode (PassMode values < 16)
-    a.work = work_.as<int>() + mode;
-    SUS2G_CUDA(cudaMemsetAsync(a.work, 0, sizeof(int), stream_));
-    pdl = false;  // the memset sits between this launch and its predecessor
-  }
+  // the dynamic order's counter pair of this mode (zero between launches: the launch's last
+  // warp resets it, so no memset sits between this launch and its predecessor)
+  if (a.atom_order == 2) a.work = work_.as<int>() + 2 * mode;
   return launch_atom_pass<Real>(model_.L, mode, a, sm_count_, stream_, blocks, pdl);
 }
 

@@ -300,7 +300,8 @@ class Engine {
   int pass_stage_[4] = {0, 0, 0, 0};   // h_j staging per pass mode (PassArgs::h_bulk; outer pass)
   template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
   template <typename Real> int launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl);
-  DevBuf work_;                 // centre counters of the dynamic centre order, one per pass mode (16)
+  static constexpr int kWorkInts = 32;  // work_: (next centre, warps done) per pass mode (< 16)
+  DevBuf work_;                 // counters of the dynamic centre order
   template <typename Real> bool use_static_split() const;
   template <typename Real> bool use_gate_split(int which) const;
   template <typename Real> int launch_gate_split(int which, PassArgs<Real> a, bool pdl);
