@@ -221,6 +221,12 @@ int sus2g_stage_finish(sus2g_engine engine, double* energy, double* site_energy,
 int sus2g_efs_combination_grad_host(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
                                     const double* positions, const int* types, const double* ene_w,
                                     const double* frc_w, const double* str_w, double* grad);
+/* The same with positions, types, the weights and grad in device memory (natoms and cells on the
+ * host), on the engine's stream; returns when the gradient is complete (torch's autograd path
+ * for device tensors, superlinear_gb300.autograd.efs_device). */
+int sus2g_efs_combination_grad_device(sus2g_engine engine, int nframes, const int* natoms, const double* cells,
+                                      const double* positions, const int* types, const double* ene_w,
+                                      const double* frc_w, const double* str_w, double* grad);
 
 /* ---- training objective and BFGS --------------------------------------------------------------
  * A trainer holds a fixed set of labelled frames resident on the engine's device (edges built

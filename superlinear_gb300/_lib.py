@@ -57,6 +57,7 @@ SIGNATURES = {
                                             _dp, _dp, _dp]),
     "sus2g_calc_descriptors_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp]),
     "sus2g_efs_combination_grad_host": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _dp]),
+    "sus2g_efs_combination_grad_device": (ctypes.c_int, [_vp, ctypes.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "sus2g_static_efs_noalloc": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp, _vp,
                                                 ctypes.c_longlong, _vp, _vp, _vp, _vp]),
     "sus2g_engine_comm_width": (ctypes.c_int, [_vp, _ip]),

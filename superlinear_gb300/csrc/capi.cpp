@@ -372,6 +372,35 @@ int sus2g_efs_combination_grad_host(sus2g_engine e, int nframes, const int* nato
   });
 }
 
+int sus2g_efs_combination_grad_device(sus2g_engine e, int nframes, const int* natoms, const double* cells,
+                                      const double* positions, const int* types, const double* ene_w,
+                                      const double* frc_w, const double* str_w, double* grad) {
+  return guarded([&] {
+    need(e && nframes >= 0 && (nframes == 0 || (natoms && cells)), "engine/frames");
+    const long long n = total_atoms(nframes, natoms);
+    need(n == 0 || (positions && types && ene_w && frc_w), "positions/types/weights");
+    need(grad && (nframes == 0 || str_w), "grad/stress weights");
+    auto& eng = *e->engine;
+    const int P = eng.model().param_count();
+    cudaStream_t s = eng.stream();
+    cuda(cudaSetDevice(eng.device()), "cudaSetDevice");
+    // the caller's gradient, put back before an attempt repeated after an edge-capacity overflow
+    Slot g0(eng, 5, sizeof(double) * P);
+    cuda(cudaMemcpyAsync(g0.p, grad, sizeof(double) * P, cudaMemcpyDeviceToDevice, s), "grad copy");
+    for (int attempt = 0;; ++attempt) {
+      try {
+        if (attempt) cuda(cudaMemcpyAsync(grad, g0.p, sizeof(double) * P, cudaMemcpyDeviceToDevice, s), "grad copy");
+        eng.build_edges(nframes, natoms, cells, positions, types);
+        if (n) eng.combination_grad(ene_w, frc_w, str_w, grad);
+        eng.check_device_error();
+        break;
+      } catch (const sus2g::EdgeOverflow&) {
+        if (attempt >= 4) throw;  // the capacity has been grown: repeat the evaluation
+      }
+    }
+  });
+}
+
 // Staged evaluation: device staging slots -- 0 types (held from begin to finish), 1..3 edge input
 // at begin and outputs at finish, 4 atom indices and 5 row buffers of the exchanges.
 namespace {

@@ -104,6 +104,7 @@ class Engine:
         check(load().sus2g_engine_create(model._h, int(device), int(precision), ctypes.byref(h)))
         self._h = h
         self.precision = precision
+        self.device = int(device)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -273,6 +274,16 @@ class Engine:
         check(load().sus2g_efs_combination_grad_host(self._h, nf, _i(natoms), _d(cells), _d(pos), _i(types), _d(ew),
                                                      _d(fw), _d(sw), _d(g)))
         return g
+
+    def combination_grad_device(self, natoms, cells, pos_ptr: int, types_ptr: int, ene_w_ptr: int, frc_w_ptr: int,
+                                str_w_ptr: int, grad_ptr: int) -> None:
+        """combination_grad with device pointers (positions, types, weights, grad accumulated
+        into; host natoms / cells), on the engine's stream; returns when the gradient is done."""
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        cells = np.ascontiguousarray(cells, dtype=np.float64)
+        check(load().sus2g_efs_combination_grad_device(self._h, natoms.size, _addr(natoms), _addr(cells),
+                                                       pos_ptr or None, types_ptr or None, ene_w_ptr or None,
+                                                       frc_w_ptr or None, str_w_ptr or None, grad_ptr or None))
 
     # -- caller edge list (pair_style sus2/embedded) --------------------------------------------
     def efs_edges(self, nowned: int, types, ei, ej, d):

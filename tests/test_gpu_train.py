@@ -219,6 +219,43 @@ def test_autograd_function_matches_finite_differences(sg, golden):
     assert abs(fd - g @ d) <= 1e-6 * max(1.0, abs(fd))
 
 
+def test_autograd_device_tensors_match_host_frames(sg, golden):
+    """efs_device: frames as CUDA tensors, every per-atom array kept on the device; the values and
+    the parameter gradient of a scalar objective match the host-frame function (FP64)."""
+    torch = pytest.importorskip("torch")
+    from superlinear_gb300.autograd import efs, efs_device
+    model = sg.Model(os.path.join(golden, "models", "effect_l3k4r2o2.sus2"))
+    eng = sg.Engine(model, 0, sg.FP64)
+    frames = training_frames(3, 8, 40, 3.0, 4.2, 0.1, seed=78, species=2)
+    natoms = np.array([f.natoms for f in frames], dtype=np.int32)
+    cells = np.stack([f.cell for f in frames])
+    dev = torch.device("cuda", 0)
+    pos = torch.tensor(np.concatenate([f.positions for f in frames]), dtype=torch.float64, device=dev)
+    typ = torch.tensor(np.concatenate([f.types for f in frames]), dtype=torch.int32, device=dev)
+    rng = np.random.default_rng(5)
+    n = int(natoms.sum())
+    a = rng.normal(size=len(frames))
+    b = rng.normal(size=(n, 3))
+    c = rng.normal(size=(len(frames), 6))
+
+    p_host = torch.tensor(model.params(), dtype=torch.float64, requires_grad=True)
+    e, f, v = efs(p_host, eng, frames)
+    ((torch.from_numpy(a) * e).sum() + (torch.from_numpy(b) * f).sum() + (torch.from_numpy(c) * v).sum()).backward()
+
+    p_dev = torch.tensor(model.params(), dtype=torch.float64, device=dev, requires_grad=True)
+    ed, fd, vd = efs_device(p_dev, eng, natoms, cells, pos, typ)
+    assert ed.is_cuda and fd.is_cuda and vd.is_cuda
+    ta, tb, tc = (torch.from_numpy(x).to(dev) for x in (a, b, c))
+    ((ta * ed).sum() + (tb * fd).sum() + (tc * vd).sum()).backward()
+    assert p_dev.grad.is_cuda
+    for x, y in ((e, ed), (f, fd), (v, vd)):
+        assert np.allclose(x.detach().numpy(), y.detach().cpu().numpy(), rtol=1e-12, atol=1e-12)
+    g_host, g_dev = p_host.grad.numpy(), p_dev.grad.cpu().numpy()
+    assert np.linalg.norm(g_host - g_dev) <= 1e-12 * np.linalg.norm(g_host)
+    with pytest.raises(ValueError):
+        efs_device(p_dev, eng, natoms, cells, pos.cpu(), typ)
+
+
 def test_trainer_survives_other_use_of_its_engine(sg, golden):
     """Evaluating other geometry on the trainer's engine rebuilds the trainer's edges (and graph)."""
     model = sg.Model(os.path.join(golden, "models", "static_l2k3o2_c2.sus2"))
