@@ -825,10 +825,12 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
 }
 
 // ---------------------------------------------------------------------------------------------
-// The per-atom part of the split Static pass: warp per centre, moments a.mom -> the graph
-// program forward -> readout (site energy, descriptors) -> the program's reverse -> adjoint
-// moments a.amom.  Independent of L; several warps of centres in flight per SM hide the
-// program's load latency that the fused pass serialises between its edge phases.
+// The per-atom part of a split pass, warp per centre: for the energy pass (Static or Effect
+// outer), moments a.mom -> the graph program forward -> readout (site energy, descriptors) -> the
+// program's reverse -> adjoint moments a.amom; for the Effect gate passes, the gate graph forward
+// with the gate-signal projection, or the gate-signal adjoint gather and the gate graph reverse.
+// Independent of L; several warps of centres in flight per SM hide the program's load latency
+// that the fused pass serialises between its edge phases.
 // ---------------------------------------------------------------------------------------------
 constexpr int kGraphWarps = 4;
 __host__ __device__ inline int graph_warp_size(int M, int parts, int F) { return round4(2 * (M + 1) + parts + F + 4); }

@@ -2187,7 +2187,7 @@ int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
 }
 
 // One pass launch in the shape already set in `a` (budget `blocks`); the dynamic centre order
-// takes its counter, zeroed on the stream before the launch.
+// takes its mode's counter pair.
 template <typename Real>
 int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
   // the dynamic order's counter pair of this mode (zero between launches: the launch's last
@@ -2201,7 +2201,10 @@ int Engine::launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl) {
 // resident blocks, or the fewest that keep the same centres per warp), centre order (grid-
 // strided, contiguous runs per warp, or taken from a device counter) and, for the Effect outer
 // pass, the staging of the neighbours' gate-signal rows (plain loads or bulk async copies) --
-// `reps` launches each after one warm-up launch, and keeps the fastest shape per pass.  ms_out[2 mode + (budget - 3)] = the best time of each budget.
+// `reps` launches each after one warm-up launch, and keeps the fastest shape per pass; then, for
+// FP32 models of basis size 8, the pass split at the per-atom boundary in the chosen grid and
+// order with either budget, kept where faster.  ms_out[2 mode + (budget - 3)] = the best time of
+// each budget (fused).
 // The passes read the state the evaluation before them left (gate signals, node adjoints), so a
 // full evaluation runs first; the gate reverse pass accumulates into the edge gradients, so the
 // next evaluation recomputes them.
