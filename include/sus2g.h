@@ -157,15 +157,17 @@ int sus2g_engine_autotune(sus2g_engine engine, int reps, int* blocks4, double* m
  * (0 grid-strided, 1 contiguous runs per warp, 2 taken from a device counter as warps finish;
  * plus 4 when the Static pass runs as three kernels, sus2g_engine_set_static_split; plus 8 when
  * the Effect outer pass brings the neighbours' gate-signal rows into shared memory by 1-D bulk
- * asynchronous copies, one 32-edge batch ahead), warps per block}.  No counterpart in the
+ * asynchronous copies, one 32-edge batch ahead), warps per block (2 or 4 from the autotuner)}.  No counterpart in the
  * reference (its kernel has no launch shape). */
 int sus2g_engine_pass_shape(sus2g_engine engine, int mode, int* shape4);
 /* Sets the tile shape of a per-atom pass as the autotuner would: blocks = register budget (0
  * default, 3 or 4), grid 0 / 1 and order 0 / 1 / 2 as in sus2g_engine_pass_shape, stage 1 = the
  * bulk-copy staging of gate-signal rows (the Effect outer pass, when a row is a whole number of
- * 16-byte units; ignored otherwise) -- to pin a shape tuned once for a workload without timing it
- * again (results as under sus2g_engine_autotune).  No counterpart in the reference. */
-int sus2g_engine_set_pass_shape(sus2g_engine engine, int mode, int blocks, int grid, int order, int stage);
+ * 16-byte units; ignored otherwise), warps = warps per block (1 .. 4; the autotuner tries 2 and
+ * 4) -- to pin a shape tuned once for a workload without timing it again (results as under
+ * sus2g_engine_autotune).  No counterpart in the reference. */
+int sus2g_engine_set_pass_shape(sus2g_engine engine, int mode, int blocks, int grid, int order, int stage,
+                                int warps);
 
 /* Per-atom descriptors of periodic frames: the S scalar moments the readout weighs, desc[N][S]
  * (host), in the order of the model's alpha_moment_mapping -- replaces MLMTPR::CalcDescriptors

@@ -44,7 +44,7 @@ SIGNATURES = {
     "sus2g_engine_set_grad_split": (ctypes.c_int, [_vp, ctypes.c_int]),
     "sus2g_engine_pass_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip]),
     "sus2g_engine_set_pass_shape": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                                   ctypes.c_int]),
+                                                   ctypes.c_int, ctypes.c_int]),
     "sus2g_engine_autotune": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _dp]),
     "sus2g_model_get_scaling": (ctypes.c_int, [_vp, _dp]),
     "sus2g_model_set_scaling": (ctypes.c_int, [_vp, ctypes.c_double]),

@@ -175,10 +175,10 @@ int sus2g_engine_pass_shape(sus2g_engine e, int mode, int* shape4) {
   });
 }
 
-int sus2g_engine_set_pass_shape(sus2g_engine e, int mode, int blocks, int grid, int order, int stage) {
+int sus2g_engine_set_pass_shape(sus2g_engine e, int mode, int blocks, int grid, int order, int stage, int warps) {
   return guarded([&] {
     need(e, "engine");
-    e->engine->set_pass_shape(mode, blocks, grid, order, stage);
+    e->engine->set_pass_shape(mode, blocks, grid, order, stage, warps);
   });
 }
 

@@ -77,6 +77,8 @@ struct PassArgs {
                            // to finish zeroes both for the next launch
   int h_bulk;              // Effect outer pass: neighbours' h_j rows staged by bulk async copies (pass_h_bulk)
   int grid_mode;           // 0: all resident blocks; 1: the fewest blocks that keep the same atoms per warp
+  int block_warps;         // launch shape: warps per block (1 .. kPassWarps; 0 = kPassWarps); the kernel
+                           // reads its block size from blockDim
 };
 
 template <typename Real>

@@ -2141,6 +2141,7 @@ int Engine::launch_static_split(PassArgs<Real> a, bool pdl) {
   const int mode = model_.gated ? kModeOuter : kModeStatic;
   a.grid_mode = pass_grid_[mode];
   a.atom_order = pass_order_[mode];
+  a.block_warps = pass_wpb_[mode];
   int k = launch_shape<Real>(model_.gated ? kModeOuterFwd : kModeStaticFwd, a, split_blocks_, pdl);
   k += launch_atom_graph<Real>(a, sm_count_, stream_);
   k += launch_shape<Real>(model_.gated ? kModeOuterRev : kModeStaticRev, a, split_blocks_, false);
@@ -2162,6 +2163,7 @@ int Engine::launch_gate_split(int which, PassArgs<Real> a, bool pdl) {
   const int mode = which == 0 ? kModeGateForward : kModeGateReverse;
   a.grid_mode = pass_grid_[mode];
   a.atom_order = pass_order_[mode];
+  a.block_warps = pass_wpb_[mode];
   int k = 0;
   if (which == 0) {
     mom_.ensure(sizeof(Real) * n);
@@ -2183,6 +2185,7 @@ int Engine::launch_pass(int mode, PassArgs<Real> a, bool pdl) {
   a.grid_mode = pass_grid_[mode];
   a.atom_order = pass_order_[mode];
   a.h_bulk = pass_stage_[mode];
+  a.block_warps = pass_wpb_[mode];
   return launch_shape<Real>(mode, a, pass_blocks_[mode], pdl);
 }
 
@@ -2226,17 +2229,19 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
   for (int k = 0; k < nmodes; ++k) {
     const int mode = modes[k];
     double best = 0.0;
-    int choice = 0, choice_grid = 0, choice_order = 0, choice_stage = 0;
+    int choice = 0, choice_grid = 0, choice_order = 0, choice_stage = 0, choice_wpb = kPassWarps;
     // h_j staging by bulk copies: the outer pass only (basis size 8), where a row is whole
     // 16-byte units
     const int stages = pass_h_bulk<Real>(mode, 1, m.F) && m.B == 8 ? 2 : 1;
     for (int blocks = 3; blocks <= 4; ++blocks)
       for (int grid = 0; grid <= 1; ++grid)
         for (int order = 0; order <= 2; ++order)
-          for (int stage = 0; stage < stages; ++stage) {
+          for (int stage = 0; stage < stages; ++stage)
+          for (int wpb = 2; wpb <= kPassWarps; wpb += 2) {
             a.grid_mode = grid;
             a.atom_order = order;
             a.h_bulk = stage;
+            a.block_warps = wpb;
             launch_shape<Real>(mode, a, blocks, false);
             SUS2G_CUDA(cudaEventRecord(e0, s));
             for (int r = 0; r < reps; ++r) launch_shape<Real>(mode, a, blocks, false);
@@ -2249,6 +2254,7 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
             if (slot == 0.0 || per < slot) slot = per;
             if (choice == 0 || per < best) {
               best = per; choice = blocks; choice_grid = grid; choice_order = order; choice_stage = stage;
+              choice_wpb = wpb;
             }
           }
     a.h_bulk = 0;
@@ -2256,6 +2262,7 @@ void Engine::autotune_passes(int reps, int* blocks_out, double* ms_out) {
     pass_grid_[mode] = choice_grid;
     pass_order_[mode] = choice_order;
     pass_stage_[mode] = choice_stage;
+    pass_wpb_[mode] = choice_wpb;
     blocks_out[mode] = choice;
     if ((mode == kModeStatic || mode == kModeOuter) && sizeof(Real) == 4 && m.B == 8) {
       // the fused energy pass (Static, or Effect outer) against its three-kernel split, in the
@@ -2317,11 +2324,13 @@ void Engine::autotune(int reps, int* blocks_out, double* ms_out) {
   check_device_error();
 }
 
-void Engine::set_pass_shape(int mode, int blocks, int grid, int order, int stage) {
+void Engine::set_pass_shape(int mode, int blocks, int grid, int order, int stage, int warps) {
   if (mode < 0 || mode > 3) throw Error(1, "pass shape: mode must be 0 .. 3");
   if (blocks != 0 && blocks != 3 && blocks != 4) throw Error(1, "pass shape: blocks per SM must be 0, 3 or 4");
   if (grid < 0 || grid > 1 || order < 0 || order > 2) throw Error(1, "pass shape: grid 0 .. 1, order 0 .. 2");
   if (stage < 0 || stage > 1) throw Error(1, "pass shape: staging 0 or 1");
+  if (warps < 1 || warps > kPassWarps) throw Error(1, "pass shape: warps per block 1 .. 4");
+  pass_wpb_[mode] = warps;
   pass_blocks_[mode] = blocks;
   pass_grid_[mode] = grid;
   pass_order_[mode] = order;

@@ -95,12 +95,12 @@ class Engine {
     const bool split = (static_split_ && mode == (model_.gated ? 2 : 0)) || gate_split;
     if (split) shape4[0] = gate_split ? gate_split_blocks_[mode == 1 ? 0 : 1] : split_blocks_;
     shape4[2] = pass_order_[mode] + (split ? 4 : 0) + (pass_stage_[mode] ? 8 : 0);
-    shape4[3] = 4;
+    shape4[3] = pass_wpb_[mode];
   }
   // sets the tile shape of pass `mode` as the autotuner would (blocks 0 = default, 3 or 4; grid 0
   // or 1; order 0, 1 or 2; stage 1 = h_j rows by bulk async copies, Effect outer pass): for
   // pinning a shape measured elsewhere
-  void set_pass_shape(int mode, int blocks, int grid, int order, int stage);
+  void set_pass_shape(int mode, int blocks, int grid, int order, int stage, int warps);
   void reset_step_graph();
   // Edge->moment batch sums of the FP32 passes on the tensor cores (3xTF32 mma.sync) instead of
   // CUDA-core FMAs; off by default (measured slower on GB300, see the design notes); a change
@@ -298,6 +298,7 @@ class Engine {
   int pass_grid_[4] = {0, 0, 0, 0};    // grid shape per pass mode (PassArgs::grid_mode)
   int pass_order_[4] = {0, 0, 0, 0};   // centre order per pass mode (PassArgs::atom_order)
   int pass_stage_[4] = {0, 0, 0, 0};   // h_j staging per pass mode (PassArgs::h_bulk; outer pass)
+  int pass_wpb_[4] = {4, 4, 4, 4};     // warps per block per pass mode (PassArgs::block_warps)
   template <typename Real> int launch_pass(int mode, PassArgs<Real> a, bool pdl);
   template <typename Real> int launch_shape(int mode, PassArgs<Real> a, int blocks, bool pdl);
   static constexpr int kWorkInts = 32;  // work_: (next centre, warps done) per pass mode (< 16)

@@ -20,8 +20,10 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
   const auto& dm = a.dm;
   const int H = (L + 1) * (L + 1);
   const bool h_bulk = MODE == kModeOuterBulk && h_rows_bulk_ok<Real>(dm.F);
+  // warps per block: at most the compiled launch bound
+  const int wpb = a.block_warps > 0 && a.block_warps < kPassWarps ? a.block_warps : kPassWarps;
   const size_t smem = sizeof(Real) * (efs_table_size(dm.C, dm.F, dm.B, dm.nblk) +
-                                      kPassWarps * pass_warp_stride<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts, h_bulk));
+                                      wpb * pass_warp_stride<Real>(dm.F, H, dm.M, dm.K, dm.prog_parts, h_bulk));
   static size_t configured = 0;
   if (smem > configured) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
@@ -29,9 +31,9 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
     configured = smem;
   }
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPassWarps * kWarp, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, wpb * kWarp, smem);
   if (per_sm < 1) throw std::runtime_error("pass kernel does not fit on an SM (shared memory " + std::to_string(smem) + " B)");
-  const int need = (a.natoms + kPassWarps - 1) / kPassWarps;
+  const int need = (a.natoms + wpb - 1) / wpb;
   const int resident = per_sm * sm_count;
   int grid = std::max(1, std::min(need, resident));
   if (a.grid_mode == 1) {
@@ -41,7 +43,7 @@ int launch_one(const PassArgs<Real>& a, int sm_count, cudaStream_t stream, bool 
     grid = std::max(1, (need + rounds - 1) / rounds);
   }
   if (a.natoms == 0) return 0;
-  cudaError_t err = launch_kernel(pdl, kern, dim3(grid), dim3(kPassWarps * kWarp), smem, stream, a);
+  cudaError_t err = launch_kernel(pdl, kern, dim3(grid), dim3(wpb * kWarp), smem, stream, a);
   if (err != cudaSuccess) throw std::runtime_error(std::string("pass launch: ") + cudaGetErrorString(err));
   return 1;
 }

@@ -169,13 +169,13 @@ class Engine:
         return out
 
     def set_pass_shape(self, name: str, blocks_per_sm: int = 0, grid: str = "resident",
-                       order: str = "strided", bulk_h: bool = False) -> None:
+                       order: str = "strided", bulk_h: bool = False, warps_per_block: int = 4) -> None:
         """Pins the tile shape of one pass (a name of PASSES) as the autotuner would set it;
         bulk_h: the outer pass's gate-signal rows by bulk async copies."""
         check(load().sus2g_engine_set_pass_shape(self._h, self.PASSES.index(name), int(blocks_per_sm),
                                                  ("resident", "balanced").index(grid),
                                                  ("strided", "contiguous", "dynamic").index(order),
-                                                 1 if bulk_h else 0))
+                                                 1 if bulk_h else 0, int(warps_per_block)))
 
     def set_step_graph(self, on: bool) -> None:
         """Replay repeated periodic steps of an unchanged layout as one CUDA graph (default on)."""
