@@ -187,7 +187,9 @@ class Engine:
         check(load().sus2g_engine_set_grad_split(self._h, 1 if on else 0))
 
     def set_static_split(self, on: bool) -> None:
-        """FP32 Static engines: the per-atom pass as forward / per-atom graph / adjoint kernels."""
+        """FP32 engines, basis size 8: every per-atom pass split at the per-atom boundary (the
+        energy pass as forward / per-atom graph / adjoint kernels, the Effect gate passes as two
+        kernels each) instead of fused; the autotuner chooses per pass."""
         check(load().sus2g_engine_set_static_split(self._h, 1 if on else 0))
 
     def set_moment_mma(self, on: bool) -> None:

@@ -66,15 +66,18 @@ def domain_layout(fr, edges, owned):
             "types": fr.types[glob], "ei": np.array(ei), "ej": np.array(ej), "d": np.array(d)}
 
 
-def staged_run(sg, model, precision, fr, edges, parts):
-    """Runs the staged calls on one engine per domain; returns total energy, forces per global
-    atom (owned + ghost contributions), total virial and site energies per global atom."""
+def staged_run(sg, model, precision, fr, edges, parts, split=False):
+    """Runs the staged calls on one engine per domain (with every pass split at the per-atom
+    boundary when split is set); returns total energy, forces per global atom (owned + ghost
+    contributions), total virial and site energies per global atom."""
     doms = [domain_layout(fr, edges, p) for p in parts]
     where = {}
     for k, dom in enumerate(doms):
         for loc, g in enumerate(dom["owned"]):
             where[g] = (k, loc)
     engs = [sg.Engine(model, 0, precision) for _ in doms]
+    for eng in engs:
+        eng.set_static_split(split)
     for eng, dom in zip(engs, doms):
         eng.stage_begin(len(dom["owned"]), dom["types"], dom["ei"], dom["ej"], dom["d"])
     width = engs[0].comm_width()
@@ -157,6 +160,23 @@ def test_staged_fp32_and_determinism(sg, golden):
     e0, f0, v0, s0 = sg.Engine(model, 0, sg.FP64).calc_efs([fr])
     assert np.max(np.abs(f1 - f0)) <= 1e-5
     assert abs(e1 - e0[0]) / fr.natoms <= 1e-6
+
+
+def test_staged_split_passes(sg, golden):
+    """The staged calls with every Effect pass split at the per-atom boundary (gate forward into
+    its edge->moment and per-atom gate graph kernels, the outer pass into three, the gate reverse
+    pass gathering the caller's summed gate-signal adjoints in its per-atom kernel) agree with the
+    fused passes to FP32 rounding and keep the FP32 bar against the periodic FP64 evaluation."""
+    model, fr = frame_and_model(sg, golden, "effect_l3k4r2o2", seed=73)
+    edges = periodic_edges(fr, model.cutoff)
+    parts = np.array_split(np.argsort(fr.positions[:, 2]), 2)
+    fused = staged_run(sg, model, sg.FP32, fr, edges, parts)
+    split = staged_run(sg, model, sg.FP32, fr, edges, parts, split=True)
+    for x, y in zip(fused, split):
+        assert rel_err(x, y) < 2e-6
+    e0, f0, v0, s0 = sg.Engine(model, 0, sg.FP64).calc_efs([fr])
+    assert np.max(np.abs(split[1] - f0)) <= 1e-5
+    assert abs(split[0] - e0[0]) / fr.natoms <= 1e-6
 
 
 def test_staged_order_is_enforced(sg, golden):
