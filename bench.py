@@ -440,8 +440,10 @@ def run_reference(args):
     return 0
 
 
-def pin_order(eng, order):
-    """Pins every pass of the engine's model to one centre order (default budget and grid)."""
+def pin_order(eng, order, split=False):
+    """Pins every pass of the engine's model to one centre order (default budget and grid), and
+    splits the passes when asked."""
+    eng.set_static_split(split)
     if order:
         for p in (("gate_forward", "outer", "gate_reverse") if eng.model.dims["gated"] else ("static",)):
             eng.set_pass_shape(p, 0, "resident", order)
@@ -455,7 +457,7 @@ def run_profile_train(args):
     frames = training_set(sg)
     model = sg.Model(TRAIN_MODEL)
     eng = sg.Engine(model, 0, sg.FP32)
-    pin_order(eng, args.order)
+    pin_order(eng, args.order, args.split)
     tr = sg.Trainer(eng, frames, *TRAIN_WEIGHTS, gate_x_l2=0.0)
     tr.set_graph(not args.no_graph)
     p = model.params()
@@ -477,7 +479,7 @@ def run_profile_effect(args):
     dev = torch.device("cuda", 0)
     eng = sg.Engine(sg.Model(EFFECT_MODEL), 0, sg.FP32)
     eng.set_moment_mma(args.moment_mma)
-    pin_order(eng, args.order)
+    pin_order(eng, args.order, args.split)
     pos = torch.tensor(fr.positions, device=dev)
     typ = torch.tensor(fr.types, device=dev)
     out = torch.zeros(fr.natoms * 3 + 7, dtype=torch.float64, device=dev)
@@ -567,7 +569,7 @@ def run_ours(args):
     eng32 = make(sg.FP32)
     eng32.set_moment_mma(args.moment_mma)
     if args.profile_only:
-        pin_order(eng32, args.order)
+        pin_order(eng32, args.order, args.split)
     # pass-kernel autotuner on the workload's layout (after one evaluation), as a user would run it
     # (not in the profiling mode, whose ncu launch offsets count the steps' own launches)
     tuned = {}
@@ -769,6 +771,8 @@ def main():
     ap.add_argument("--order", choices=("strided", "contiguous", "dynamic"), default=None,
                     help="with the profiling modes: pin every pass to this centre order (default budgets and "
                          "grid), as the autotuner's choice would set it, without the autotuner's launches")
+    ap.add_argument("--split", action="store_true",
+                    help="with the profiling modes: every per-atom pass split at the per-atom boundary")
     ap.add_argument("--moment-mma", action="store_true",
                     help="with --profile-only / --profile-effect: edge->moment sums on the tensor cores (3xTF32)")
     ap.add_argument("--skip-config5", action="store_true",
