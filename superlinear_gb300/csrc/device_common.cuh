@@ -49,6 +49,24 @@ template <> struct __align__(16) ProgRec<double> { unsigned ab; int flush; doubl
 // flush: kProgNoFlush, a node index >= 0, or -(slot + 2) for a partial slot
 constexpr int kProgNoFlush = -1;
 
+// One program record through the read-only data path (the records are written by host uploads
+// only): as a non-coherent load it may be issued ahead of the node stores of earlier records,
+// which a plain load through the generic pointer may not pass.
+template <typename Real>
+__device__ __forceinline__ ProgRec<Real> load_rec(const ProgRec<Real>* p) {
+  const int4 w = __ldg(reinterpret_cast<const int4*>(p));
+  ProgRec<Real> r;
+  r.ab = static_cast<unsigned>(w.x);
+  r.flush = w.y;
+  if constexpr (sizeof(Real) == 4) {
+    r.c = __int_as_float(w.z);
+    r.pad = __int_as_float(w.w);
+  } else {
+    r.c = __hiloint2double(w.w, w.z);
+  }
+  return r;
+}
+
 template <typename Real>
 struct GraphProg {
   int nsteps = 0, nfwd = 0;      // forward steps [0, nfwd), reverse steps [nfwd, nsteps)
@@ -264,21 +282,48 @@ __device__ __forceinline__ double warp_csum(float hi, float lo) {
   return double(hi) + double(lo);
 }
 
-// p[0] + p[stride] + ... + p[(n - 1) stride], added in that order, with eight loads in flight
+// p[0] + p[stride] + ... + p[(n - 1) stride], added in that order, with DEPTH loads in flight
 // ahead of the adds (a column of a row-major per-edge array, summed over one centre's edges).
-template <typename Real>
+template <typename Real, int DEPTH = 8>
 __device__ __forceinline__ Real column_sum(const Real* p, size_t stride, int n) {
   Real s = Real(0);
   int i = 0;
-  for (; i + 8 <= n; i += 8) {
-    Real x[8];
+  for (; i + DEPTH <= n; i += DEPTH) {
+    Real x[DEPTH];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) x[q] = p[static_cast<size_t>(i + q) * stride];
+    for (int q = 0; q < DEPTH; ++q) x[q] = p[static_cast<size_t>(i + q) * stride];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) s += x[q];
+    for (int q = 0; q < DEPTH; ++q) s += x[q];
   }
   for (; i < n; ++i) s += p[static_cast<size_t>(i) * stride];
   return s;
+}
+
+// The F columns of a row-major per-edge array [n][F] (F <= 64) summed over the rows into dst[F]:
+// lane c sums columns c and c + 32 side by side, each row after row in order (the sums of
+// column_sum), sixteen loads in flight.
+template <typename Real>
+__device__ __forceinline__ void column_sums_2(const Real* p, int F, int n, Real* dst, int lane) {
+  const int mu0 = lane, mu1 = lane + 32;
+  const bool on0 = mu0 < F, on1 = mu1 < F;
+  Real s0 = Real(0), s1 = Real(0);
+  int i = 0;
+  for (; i + 8 <= n; i += 8) {
+    Real x0[8], x1[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      x0[q] = on0 ? p[static_cast<size_t>(i + q) * F + mu0] : Real(0);
+      x1[q] = on1 ? p[static_cast<size_t>(i + q) * F + mu1] : Real(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) { s0 += x0[q]; s1 += x1[q]; }
+  }
+  for (; i < n; ++i) {
+    if (on0) s0 += p[static_cast<size_t>(i) * F + mu0];
+    if (on1) s1 += p[static_cast<size_t>(i) * F + mu1];
+  }
+  if (on0) dst[mu0] = s0;
+  if (on1) dst[mu1] = s1;
 }
 
 // Warp index of the scaling block for radial function (k, l) (sus2_sl_kernel.cpp:198).

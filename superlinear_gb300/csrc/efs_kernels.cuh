@@ -286,7 +286,7 @@ __device__ __forceinline__ void run_prog(const GraphProg<Real>& g, int s0, int s
     Real acc = Real(0);
 #pragma unroll 4
     for (int i = 0; i < info.y; ++i) {
-      const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+      const ProgRec<Real> p = load_rec<Real>(r + static_cast<size_t>(i) * kWarp);
       acc += p.c * X[p.ab & 0xffffu] * v[p.ab >> 16];
       if (p.flush != kProgNoFlush) {
         if (p.flush >= 0) T[p.flush] += acc;
@@ -679,11 +679,15 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
       readout_seeds<Real>(a, atom, ti, v, adj, lane);
     } else {
       // ---------------- gate reverse: gather hbar, project, load gate values ----------------
-      for (int mu = lane; mu < F; mu += kWarp) {
-        if (a.hbar_atom) {
-          hbar[mu] = Real(a.hbar_atom[(size_t)atom * F + mu]);
-        } else {
-          hbar[mu] = column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
+      if (!a.hbar_atom && F <= 2 * kWarp) {
+        column_sums_2<Real>(a.hcontrib + (size_t)e0 * F, F, e1 - e0, hbar, lane);
+      } else {
+        for (int mu = lane; mu < F; mu += kWarp) {
+          if (a.hbar_atom) {
+            hbar[mu] = Real(a.hbar_atom[(size_t)atom * F + mu]);
+          } else {
+            hbar[mu] = column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
+          }
         }
       }
       for (int q = lane; q <= M; q += kWarp) {
@@ -861,9 +865,14 @@ __global__ void __launch_bounds__(kGraphWarps * kWarp) atom_graph_kernel(PassArg
       // the gate-signal adjoint of the atom: summed over its edges' contributions (stored at the
       // reverse edges by the outer pass), or already summed per atom (caller edges)
       const int e0 = a.row[atom], e1 = a.row_end[atom];
-      for (int mu = lane; mu < F; mu += kWarp)
-        hbar[mu] = a.hbar_atom ? Real(a.hbar_atom[(size_t)atom * F + mu])
-                               : column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
+      if (!a.hbar_atom && F <= 2 * kWarp) {
+        // both of a lane's columns side by side: the gather is the latency this kernel waits on
+        column_sums_2<Real>(a.hcontrib + (size_t)e0 * F, F, e1 - e0, hbar, lane);
+      } else {
+        for (int mu = lane; mu < F; mu += kWarp)
+          hbar[mu] = a.hbar_atom ? Real(a.hbar_atom[(size_t)atom * F + mu])
+                                 : column_sum<Real>(a.hcontrib + (size_t)e0 * F + mu, F, e1 - e0);
+      }
       for (int q = lane; q <= M; q += kWarp) {
         v[q] = q < M ? a.gmom[(size_t)atom * M + q] : Real(1);
         adj[q] = Real(0);

@@ -126,7 +126,7 @@ __device__ __forceinline__ void run_prog_dual(const GraphProg<Real>& g, int s0, 
     if (!rev) {
 #pragma unroll 2
       for (int i = 0; i < info.y; ++i) {
-        const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+        const ProgRec<Real> p = load_rec<Real>(r + static_cast<size_t>(i) * kWarp);
         const int x = p.ab & 0xffffu, y = p.ab >> 16;
         const Real vx = v[x], vy = v[y];
         acc += p.c * vx * vy;
@@ -136,7 +136,7 @@ __device__ __forceinline__ void run_prog_dual(const GraphProg<Real>& g, int s0, 
     } else {
 #pragma unroll 2
       for (int i = 0; i < info.y; ++i) {
-        const ProgRec<Real> p = r[static_cast<size_t>(i) * kWarp];
+        const ProgRec<Real> p = load_rec<Real>(r + static_cast<size_t>(i) * kWarp);
         const int x = p.ab & 0xffffu, y = p.ab >> 16;
         const Real vy = v[y], mx = mu[x];
         acc += p.c * (lam[x] * vy + mx * vd[y]);
