@@ -666,9 +666,16 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
 
       if (MODE == kModeGateForward) {
         for (int q = lane; q < M; q += kWarp) a.gmom[(size_t)atom * M + q] = v[q];
+        // the gate scalars gathered once into the (here unused) hbar row when they fit, so that
+        // each signal's sum reads its weights and the scalars without a node-index load between
+        const bool staged = dm.Q <= F;
+        if (staged)
+          for (int q = lane; q < dm.Q; q += kWarp) hbar[q] = v[dm.gate_nodes[q]];
+        __syncwarp();
         for (int mu = lane; mu < F; mu += kWarp) {
           Real h = Real(0);
-          for (int q = 0; q < dm.Q; ++q) h += dm.gate_wmat[mu * dm.Q + q] * v[dm.gate_nodes[q]];
+          for (int q = 0; q < dm.Q; ++q)
+            h += dm.gate_wmat[mu * dm.Q + q] * (staged ? hbar[q] : v[dm.gate_nodes[q]]);
           a.hsig[(size_t)atom * F + mu] = h;
         }
         __syncwarp();
@@ -839,7 +846,9 @@ __global__ void __launch_bounds__(kPassWarps * kWarp, MINB) atom_pass_kernel(Pas
 // that the fused pass serialises between its edge phases.
 // ---------------------------------------------------------------------------------------------
 constexpr int kGraphWarps = 4;
-__host__ __device__ inline int graph_warp_size(int M, int parts, int F) { return round4(2 * (M + 1) + parts + F + 4); }
+__host__ __device__ inline int graph_warp_size(int M, int parts, int F, int Q) {
+  return round4(2 * (M + 1) + parts + (F > Q ? F : Q) + 4);
+}
 
 // GM: 0 the energy pass (Static or Effect outer tables: readout, adjoint moments to a.amom);
 // 1 the gate forward pass (gate tables: gate values to a.gmom, gate signals to a.hsig);
@@ -853,10 +862,10 @@ __global__ void __launch_bounds__(kGraphWarps * kWarp) atom_graph_kernel(PassArg
   const int M = dm.M, KH = dm.K * dm.H, C = dm.C, F = dm.F;
   const int warps = blockDim.x / kWarp, warp = threadIdx.x / kWarp, lane = warp_lane();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Real* v = reinterpret_cast<Real*>(smem_raw) + graph_warp_size(M, dm.prog_parts, F) * warp;
+  Real* v = reinterpret_cast<Real*>(smem_raw) + graph_warp_size(M, dm.prog_parts, F, dm.Q) * warp;
   Real* adj = v + M + 1;
   Real* parts = adj + M + 1;
-  Real* hbar = parts + dm.prog_parts;  // [F] (GM 2)
+  Real* hbar = parts + dm.prog_parts;  // [F] (GM 2) or the gate scalars [Q] (GM 1)
   pdl_launch_dependents();
   pdl_wait();
   for (int atom = blockIdx.x * warps + warp; atom < a.natoms; atom += gridDim.x * warps) {
@@ -896,9 +905,14 @@ __global__ void __launch_bounds__(kGraphWarps * kWarp) atom_graph_kernel(PassArg
     }
     if constexpr (GM == 1) {
       for (int q = lane; q < M; q += kWarp) a.gmom[(size_t)atom * M + q] = v[q];
+      // the gate scalars gathered once, so that each signal's sum reads its weights and the
+      // scalars without a node-index load in between
+      Real* gs = hbar;
+      for (int q = lane; q < dm.Q; q += kWarp) gs[q] = v[dm.gate_nodes[q]];
+      __syncwarp();
       for (int mu = lane; mu < F; mu += kWarp) {
         Real h = Real(0);
-        for (int q = 0; q < dm.Q; ++q) h += dm.gate_wmat[mu * dm.Q + q] * v[dm.gate_nodes[q]];
+        for (int q = 0; q < dm.Q; ++q) h += dm.gate_wmat[mu * dm.Q + q] * gs[q];
         a.hsig[(size_t)atom * F + mu] = h;
       }
       __syncwarp();

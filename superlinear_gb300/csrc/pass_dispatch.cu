@@ -74,7 +74,7 @@ int launch_atom_graph(const PassArgs<Real>& a, int sm_count, cudaStream_t s, int
   if (gm < 0 || gm > 2) throw std::runtime_error("graph kernel: unknown pass");
   auto kern = gm == 0 ? atom_graph_kernel<Real, 0> : gm == 1 ? atom_graph_kernel<Real, 1> : atom_graph_kernel<Real, 2>;
   const size_t smem =
-      sizeof(Real) * kGraphWarps * static_cast<size_t>(graph_warp_size(a.dm.M, a.dm.prog_parts, a.dm.F));
+      sizeof(Real) * kGraphWarps * static_cast<size_t>(graph_warp_size(a.dm.M, a.dm.prog_parts, a.dm.F, a.dm.Q));
   static size_t configured[3] = {0, 0, 0};
   if (smem > configured[gm]) {
     cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
