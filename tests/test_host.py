@@ -1,6 +1,8 @@
 """Host-side logic that needs no GPU: the C ABI exports, .sus2 parsing and validation through the
 library's host code, parameter layout, workload generators, and .cfg / .sus2 text round trips."""
 import os
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -153,3 +155,44 @@ def test_model_save_rejects_bad_path(engine_lib, golden):
     m = sg.Model(os.path.join(golden, "models", "static_l3k4o2.sus2"))
     with pytest.raises(sg.Sus2Error):
         m.save("/nonexistent-directory/x.sus2")
+
+
+@pytest.mark.parametrize("name", ["static_l3k4o2", "effect_l4k8r2o3"])
+def test_plain_c_client_of_the_abi(engine_lib, golden, tmp_path, name):
+    """include/sus2g.h compiled as C99 with warnings as errors, linked against libsus2g.so by a C
+    program (tests/c/model_info.c) that loads a model, reads its dimensions, cutoff and
+    parameters and checks the error reporting of a missing file: the same values as the Python
+    binding reads.  Also compiles both headers as C++17.  Needs no GPU."""
+    import superlinear_gb300 as sg
+    from superlinear_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cc is None or cxx is None:
+        pytest.skip("no C / C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    inc = os.path.join(root, "include")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "model_info")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", inc,
+                        os.path.join(root, "tests", "c", "model_info.c"), "-L", libdir, "-lsus2g",
+                        f"-Wl,-rpath,{libdir}", "-lm", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    hpp = tmp_path / "headers.cpp"
+    hpp.write_text('#include "sus2g.h"\n#include "sus2g_kernel.hpp"\nint main() { return 0; }\n')
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-fsyntax-only", "-I", inc, str(hpp)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+    path = os.path.join(golden, "models", f"{name}.sus2")
+    r = subprocess.run([exe, path], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
+    fields = r.stdout.split()
+    assert fields[0] == "INFO"
+    dims = [int(x) for x in fields[1:17]]
+    cutoff, count, abs_sum = float(fields[17]), int(fields[18]), float(fields[19])
+    m = sg.Model(path)
+    p = np.asarray(m.params())
+    assert count == p.size == dims[11]
+    assert cutoff == m.cutoff
+    assert dims == [int(v) for v in m.dims.values()]
+    assert abs(abs_sum - float(np.abs(p).sum())) <= 1e-12 * max(1.0, abs_sum)
