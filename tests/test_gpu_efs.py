@@ -524,6 +524,50 @@ def test_effect_l4k8_13824_atoms_against_oracle(lib, oracle_lib, golden):
     assert rel_err(v32[0], vo) < 1e-5
 
 
+def _rotation(seed):
+    q = np.random.default_rng(seed).normal(size=4)
+    a, b, c, d = q / np.linalg.norm(q)
+    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                     [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                     [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+
+
+def _virial3(v):
+    xx, yy, zz, xy, xz, yz = v
+    return np.array([[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]])
+
+
+def test_full_size_110592_symmetries(lib, golden):
+    """The 110,592-atom configuration itself (24x24x24 diamond cells, Effect L4/K8/R2/O3, two
+    species), through size-independent properties: FP64 plain -- the same edge count, energy and
+    site energies after a rigid rotation of the frame, forces and virial rotating with it, a
+    relabelling of the atoms permuting the per-atom outputs only, zero net force; FP32 bulk on the
+    rotated frame within the FP32 bars of the FP64 result."""
+    path = os.path.join(golden, "models", "effect_l4k8r2o3.sus2")
+    m, g64, g32 = engines(lib, path)
+    fr = diamond(24, a=3.567, sigma=0.1, seed=4, species=2, type_prob=0.5)
+    assert fr.natoms == 110592
+    e, f, v, s = g64.calc_efs([fr])
+    ne = g64.edge_count()
+    scale = 1.0 + np.max(np.abs(f))
+    assert np.max(np.abs(f.sum(axis=0))) <= 1e-8 * scale
+    R = _rotation(11)
+    rot = Frame(fr.cell @ R.T, fr.positions @ R.T, fr.types)
+    er, fr_, vr, sr = g64.calc_efs([rot])
+    assert g64.edge_count() == ne
+    assert abs(er[0] - e[0]) <= 1e-10 * (1.0 + abs(e[0]))
+    assert np.max(np.abs(sr - s)) <= 1e-10 * (1.0 + np.max(np.abs(s)))
+    assert np.max(np.abs(fr_ - f @ R.T)) <= 1e-10 * scale
+    assert np.max(np.abs(_virial3(vr[0]) - R @ _virial3(v[0]) @ R.T)) <= 1e-10 * (1.0 + np.max(np.abs(v)))
+    perm = np.random.default_rng(12).permutation(fr.natoms)
+    ep, fp, vp, sp = g64.calc_efs([Frame(fr.cell, fr.positions[perm], fr.types[perm])])
+    assert abs(ep[0] - e[0]) <= 1e-10 * (1.0 + abs(e[0]))
+    assert np.max(np.abs(fp - f[perm])) <= 1e-10 * scale
+    assert np.max(np.abs(sp - s[perm])) <= 1e-10 * (1.0 + np.max(np.abs(s)))
+    e32, f32, v32, s32 = g32.calc_efs([rot])
+    check_fp32(e32[0], f32, e[0], f @ R.T, fr.natoms)
+
+
 @pytest.mark.parametrize("name,cells", [("static_l3k4o2", 8), ("effect_l4k8r2o3", 6)])
 def test_moment_mma_option_within_fp32_bars(lib, golden, name, cells):
     """The optional tensor-core edge->moment sums (3xTF32 mma.sync, sus2g_engine_set_moment_mma)
