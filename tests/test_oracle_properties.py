@@ -51,3 +51,24 @@ def test_rigid_motion_and_permutation(oracle_lib, golden, name):
     assert np.max(np.abs(fp - f[perm])) <= 1e-10 * scale
     assert np.max(np.abs(sp - s[perm])) <= 1e-10 * (1.0 + np.max(np.abs(s)))
     assert np.max(np.abs(vp - v)) <= 1e-10 * (1.0 + np.max(np.abs(v)))
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_parameter_gradient_is_rotation_invariant(oracle_lib, golden, name):
+    """The combination gradient d/dtheta [sum ew E + sum_e (fw_i - fw_j + S d_e) . dE/dd_e] is the
+    same for a rotated frame when the force weights rotate as vectors and the stress weights as a
+    tensor (S -> R S R^T), and a relabelling of the atoms with their weights leaves it unchanged."""
+    m = oracle_lib.OracleModel(os.path.join(golden, "models", f"{name}.sus2"))
+    fr = training_frames(1, 20, 32, 3.2, 3.8, 0.1, seed=93, species=2)[0]
+    rng = np.random.default_rng(17)
+    ew = rng.normal(size=fr.natoms)
+    fw = rng.normal(size=(fr.natoms, 3))
+    S = rng.normal(size=(3, 3))
+    g = m.grad(fr.cell, fr.positions, fr.types, ew, fw, S)
+    assert np.linalg.norm(g) > 0
+    R = rotation(23)
+    gr = m.grad(fr.cell @ R.T, fr.positions @ R.T, fr.types, ew, fw @ R.T, R @ S @ R.T)
+    assert np.linalg.norm(gr - g) <= 1e-10 * np.linalg.norm(g)
+    perm = np.random.default_rng(29).permutation(fr.natoms)
+    gp = m.grad(fr.cell, fr.positions[perm], fr.types[perm], ew[perm], fw[perm], S)
+    assert np.linalg.norm(gp - g) <= 1e-10 * np.linalg.norm(g)
