@@ -143,8 +143,11 @@ class Engine:
         return ci, cj, d
 
     def autotune(self, reps: int = 5):
-        """Times both register budgets of every pass on the last evaluation's layout and keeps the
-        faster; returns {pass: (chosen blocks per SM, {blocks: ms per launch})}."""
+        """Times every tile shape of every pass on the last evaluation's layout -- register budget,
+        grid, centre order, warps per block, and (FP32, basis size 8) the split at the per-atom
+        boundary and the outer pass's bulk-copy staging -- and keeps the fastest (``pass_shapes()``
+        reports it); returns {pass: (chosen blocks per SM of the fused pass, {blocks: best ms per
+        launch of the fused pass with that budget})}."""
         b = (ctypes.c_int * 4)()
         ms = (ctypes.c_double * 8)()
         check(load().sus2g_engine_autotune(self._h, int(reps), b, ms))
